@@ -1,0 +1,267 @@
+/*
+ * qsm_gpu.h -- C ABI of the GB300 (sm_103a) QSM library.
+ *
+ * One entry point per QSM.m C-MEX gateway on the hot path, with the MEX
+ * gateway's argument order and meaning, so a thin MEX shim (see
+ * qsm.m_gb300/mex/) can forward mxGetData() pointers unchanged:
+ *
+ *   - arrays are MATLAB column-major, x fastest: l = i + nx*j + nx*ny*k;
+ *     vector fields are component-major (component c at offset c*N);
+ *   - masks are uint8 0/1 (MATLAB logical);
+ *   - vsz is double[3] (voxel size);
+ *   - dtype selects float32 or float64, as mxIsSingle(prhs[0]) does;
+ *   - every array pointer may be HOST or DEVICE memory (detected per
+ *     pointer).  Host arrays are copied to the device and results copied
+ *     back inside the call; device arrays are used in place with no copy;
+ *   - "in-place" operator gateways write into their first array argument(s)
+ *     exactly where the MEX file writes (masked variants only where G), so
+ *     other elements keep the caller's contents;
+ *   - solver gateways never modify their inputs and write a separate output.
+ *
+ * Every call is enqueued on the context's stream and returns after the
+ * result is complete (host outputs are copied back; device outputs are
+ * synchronised).  Errors are status codes instead of mexErrMsgTxt; the
+ * message of the last failure is available from qsm_last_error().
+ *
+ * Citations name the reference gateway each function replaces, as
+ * path:line within kamesy/QSM.m.
+ */
+#ifndef QSM_GPU_H
+#define QSM_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QSM_GPU_ABI_VERSION 1
+
+/* Number of blocks of the lane-order reduction (lanes = 256 * QSM_RED_NBLK). */
+#define QSM_RED_NBLK 1024
+
+typedef enum {
+    QSM_OK = 0,
+    QSM_ERR_ARG = 1,        /* null pointer, bad scalar */
+    QSM_ERR_DIMS = 2,       /* unsupported or inconsistent dimensions */
+    QSM_ERR_DTYPE = 3,      /* unsupported dtype */
+    QSM_ERR_NOMEM = 4,      /* device allocation failed */
+    QSM_ERR_CUDA = 5,       /* CUDA runtime error (see qsm_last_error) */
+    QSM_ERR_NONFINITE = 6,  /* a convergence monitor became NaN/Inf */
+    QSM_ERR_DEPTH = 7,      /* nlevels > 16 ("nlevels too large. Increase MAX_DEPTH.") */
+    QSM_ERR_BUSY = 8,       /* session has no free slot / over budget */
+    QSM_ERR_TIMEOUT = 9     /* a bounded device wait gave up */
+} qsm_status;
+
+typedef enum { QSM_F64 = 0, QSM_F32 = 1 } qsm_dtype;
+
+typedef struct qsm_ctx qsm_ctx;
+
+/* ---------------- context ---------------- */
+
+/* Creates a context on `device` with its own non-blocking stream and a
+ * stream-ordered memory pool. */
+qsm_status qsm_ctx_create(int device, qsm_ctx **ctx);
+qsm_status qsm_ctx_destroy(qsm_ctx *ctx);
+/* Use a caller-owned cudaStream_t (passed as void*) instead of the context's. */
+qsm_status qsm_ctx_set_stream(qsm_ctx *ctx, void *cuda_stream);
+void *qsm_ctx_get_stream(qsm_ctx *ctx);
+qsm_status qsm_ctx_set_verbose(qsm_ctx *ctx, int verbose);
+const char *qsm_last_error(const qsm_ctx *ctx);
+const char *qsm_status_string(qsm_status s);
+int qsm_abi_version(void);
+
+/* ---------------- primal-dual inversions ---------------- */
+
+typedef struct {
+    uint32_t iters;        /* iterations run */
+    double monitor_chi;    /* ||chi - chi0|| / ||chi|| at the last check */
+    double monitor_eta;    /* ||eta - eta0|| / ||eta|| at the last check */
+    double seconds;        /* device time of the iteration loop */
+} qsm_pd_info;
+
+/* chi = pd_tgv_mex(d2f, mask, vsz, lam, alpha, tol, maxiter, verbose)
+ * Replaces src/inversion/mex/pd_tgv_mex.c:104-135 (mexFunction) with
+ * mx_pdd/mx_pdf :139-323.  Plain path: one kernel per reference loop nest
+ * (dual, primal, monitor copy, monitor check), no fused multiply-add;
+ * bit-exact with the reference in FP64 and FP32.  info may be NULL. */
+qsm_status qsm_pd_tgv(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3],
+                      const void *d2f, const uint8_t *mask, const double vsz[3],
+                      double lam, double alpha, double tol, uint32_t maxiter,
+                      uint32_t verbose, void *chi, qsm_pd_info *info);
+
+/* chi = pd_tv_mex(d2f, mask, vsz, lam, tol, maxiter, verbose)
+ * Replaces src/inversion/mex/pd_tv_mex.c:100-130 with mx_pdd/mx_pdf :134-306. */
+qsm_status qsm_pd_tv(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3],
+                     const void *d2f, const uint8_t *mask, const double vsz[3],
+                     double lam, double tol, uint32_t maxiter, uint32_t verbose,
+                     void *chi, qsm_pd_info *info);
+
+/* Mixed-precision fused variants of the two gateways above (same arguments
+ * and meaning).  The stencil arithmetic runs in FP32 inside one fused
+ * dual+primal(+extragradient) kernel per iteration; convergence monitors
+ * accumulate in FP64.  Per voxel it evaluates the reference's FP32
+ * expressions (pd_tgv_mex.c:332-485, :659-812) without fused multiply-add,
+ * so chi equals the reference's own single-precision result (mx_pdf).
+ * dtype gives the type of d2f/chi in memory (F64 inputs are rounded to
+ * FP32 on the device, the result widened back). */
+qsm_status qsm_pd_tgv_fused(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3],
+                            const void *d2f, const uint8_t *mask, const double vsz[3],
+                            double lam, double alpha, double tol, uint32_t maxiter,
+                            uint32_t verbose, void *chi, qsm_pd_info *info);
+qsm_status qsm_pd_tv_fused(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3],
+                           const void *d2f, const uint8_t *mask, const double vsz[3],
+                           double lam, double tol, uint32_t maxiter, uint32_t verbose,
+                           void *chi, qsm_pd_info *info);
+
+/* ---------------- finite-difference operators (in place) ---------------- */
+
+/* gradf_mex(dx, dy, dz, u, h): src/utils/fd/mex/gradf_mex.c:13-47 */
+qsm_status qsm_gradf(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3],
+                     void *dx, void *dy, void *dz, const void *u, const double vsz[3]);
+/* gradb_mex: src/utils/fd/mex/gradb_mex.c:13-47 */
+qsm_status qsm_gradb(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3],
+                     void *dx, void *dy, void *dz, const void *u, const double vsz[3]);
+/* gradc_mex: src/utils/fd/mex/gradc_mex.c:13-47 */
+qsm_status qsm_gradc(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3],
+                     void *dx, void *dy, void *dz, const void *u, const double vsz[3]);
+/* gradfm_mex(dx, dy, dz, u, G, h): src/utils/fd/mex/gradfm_mex.c:15-50 */
+qsm_status qsm_gradfm(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3],
+                      void *dx, void *dy, void *dz, const void *u, const uint8_t *G,
+                      const double vsz[3]);
+/* gradbm_mex: src/utils/fd/mex/gradbm_mex.c:15-50 */
+qsm_status qsm_gradbm(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3],
+                      void *dx, void *dy, void *dz, const void *u, const uint8_t *G,
+                      const double vsz[3]);
+/* gradcm_mex: src/utils/fd/mex/gradcm_mex.c:15-50 */
+qsm_status qsm_gradcm(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3],
+                      void *dx, void *dy, void *dz, const void *u, const uint8_t *G,
+                      const double vsz[3]);
+/* gradf_adj_mex(du, x, y, z, h): src/utils/fd/mex/gradf_adj_mex.c:15-49 */
+qsm_status qsm_gradf_adj(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3],
+                         void *du, const void *x, const void *y, const void *z,
+                         const double vsz[3]);
+/* gradb_adj_mex: src/utils/fd/mex/gradb_adj_mex.c:15-49 */
+qsm_status qsm_gradb_adj(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3],
+                         void *du, const void *x, const void *y, const void *z,
+                         const double vsz[3]);
+/* gradfm_adj_mex(du, x, y, z, G, h): src/utils/fd/mex/gradfm_adj_mex.c:15-50 */
+qsm_status qsm_gradfm_adj(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3],
+                          void *du, const void *x, const void *y, const void *z,
+                          const uint8_t *G, const double vsz[3]);
+/* gradbm_adj_mex: src/utils/fd/mex/gradbm_adj_mex.c:15-50 */
+qsm_status qsm_gradbm_adj(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3],
+                          void *du, const void *x, const void *y, const void *z,
+                          const uint8_t *G, const double vsz[3]);
+/* gradfp_mex(dx, dy, dz, u, h): src/inversion/mex/gradfp_mex.c:13-47 */
+qsm_status qsm_gradfp(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3],
+                      void *dx, void *dy, void *dz, const void *u, const double vsz[3]);
+/* gradfp_adj_mex(du, x, y, z, h): src/inversion/mex/gradfp_adj_mex.c:15-49 */
+qsm_status qsm_gradfp_adj(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3],
+                          void *du, const void *x, const void *y, const void *z,
+                          const double vsz[3]);
+/* lap1_mex(d2u, u, G, h) ("lap_mex" in its usage string):
+ * src/utils/fd/mex/lap1_mex.c:29-60 */
+qsm_status qsm_lap1(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3],
+                    void *d2u, const void *u, const uint8_t *G, const double vsz[3]);
+/* lapw_mex(d2u, u, h): src/unwrap/mex/lapw_mex.c:21-51 */
+qsm_status qsm_lapw(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3],
+                    void *d2u, const void *u, const double vsz[3]);
+
+/* ---------------- multigrid pieces (in place) ---------------- */
+
+/* gauss_seidel_mex(v, f, G, h, iter, reverse), red-black build:
+ * src/utils/poisson_solver/mex/gauss_seidel_mex.c:19-49 (+ gauss_seideld :196-311) */
+qsm_status qsm_gauss_seidel(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3],
+                            void *v, const void *f, const uint8_t *G, const double vsz[3],
+                            int32_t iter, int32_t reverse);
+/* residual_mex(r, f, x, G, h): src/utils/poisson_solver/mex/residual_mex.c:17-49 (+ residuald :82-165) */
+qsm_status qsm_residual(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3],
+                        void *r, const void *f, const void *x, const uint8_t *G,
+                        const double vsz[3]);
+/* lapmg_mex(d2u, u, G, h): src/utils/poisson_solver/mex/lapmg_mex.c:17-45 (+ lapmgd :73-154) */
+qsm_status qsm_lapmg(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3],
+                     void *d2u, const void *u, const uint8_t *G, const double vsz[3]);
+/* restrict_mex(x2, x, G2): src/utils/poisson_solver/mex/restrict_mex.c:17-45 (+ restrictd :200-332).
+ * dims2 = size of x2 and G2, dims = size of x. */
+qsm_status qsm_restrict(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims2[3], void *x2,
+                        const size_t dims[3], const void *x, const uint8_t *G2);
+/* prolong_mex(x, x2, G): src/utils/poisson_solver/mex/prolong_mex.c:17-45 (+ prolongd :180-304) */
+qsm_status qsm_prolong(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3], void *x,
+                       const size_t dims2[3], const void *x2, const uint8_t *G);
+/* correct_mex(x, x2, G): src/utils/poisson_solver/mex/correct_mex.c:17-45 (+ correctd :180-304) */
+qsm_status qsm_correct(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3], void *x,
+                       const size_t dims2[3], const void *x2, const uint8_t *G);
+/* coarsen_grid_mex(G2, G): src/utils/poisson_solver/mex/coarsen_grid_mex.c:12-33 (+ coarsen_grid :52-125) */
+qsm_status qsm_coarsen_grid(qsm_ctx *ctx, const size_t dims2[3], uint8_t *G2,
+                            const size_t dims[3], const uint8_t *G);
+/* boundary_mask_mex(B, G): src/utils/poisson_solver/mex/boundary_mask_mex.c:11-29 (+ boundary_mask :46-132) */
+qsm_status qsm_boundary_mask(qsm_ctx *ctx, const size_t dims[3], uint8_t *B, const uint8_t *G);
+/* boundary_mask_l1_mex(B, G, l1): src/utils/poisson_solver/mex/boundary_mask_l1_mex.c:12-32 (+ boundary_mask_l1 :49-117) */
+qsm_status qsm_boundary_mask_l1(qsm_ctx *ctx, const size_t dims[3], uint8_t *B,
+                                const uint8_t *G, uint8_t l1);
+/* p = norm2_mex(x, G): src/utils/poisson_solver/mex/norm2_mex.c:21-51 (+ norm22d :113-131).
+ * Masked 2-norm; *out receives it (as double; FP32 result widened). */
+qsm_status qsm_norm2(qsm_ctx *ctx, qsm_dtype dtype, size_t n, const void *x,
+                     const uint8_t *G, double *out);
+
+/* ---------------- Poisson solvers ---------------- */
+
+typedef struct {
+    int32_t iters;          /* PCG iterations (mgpcg) or cycles run */
+    double resnorm;         /* final ||r||_2 (padded array, as the reference) */
+    double seconds;         /* device time */
+    double *resnorm_hist;   /* optional, caller-owned, >= maxitcg doubles */
+} qsm_mg_info;
+
+/* v = mgpcg_mex(v, f, mask, vsz, tolcg, maxitcg, tolmg, maxitmg, mu, npre,
+ *               npost, nboundary, nlevels, verbose)
+ * Replaces src/utils/poisson_solver/mex/mgpcg_mex.c:73-123 (mx_pcg :126-216,
+ * mx_mg :219-239, mx_cycle :242-279, mx_init :282-332).  Plain path: PCG and
+ * V-cycle in dtype; inner products in lane order (bit-exact with the oracle
+ * built on the project's BLAS shim).  v0 is the initial guess; v_out gets
+ * the solution. */
+qsm_status qsm_mgpcg(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3],
+                     const void *v0, const void *f, const uint8_t *mask, const double vsz[3],
+                     double tolcg, int32_t maxitcg, double tolmg, int32_t maxitmg,
+                     int32_t mu, int32_t npre, int32_t npost, int32_t nboundary,
+                     int32_t nlevels, int32_t verbose, void *v_out, qsm_mg_info *info);
+
+/* Mixed-precision variant: FP64 PCG recurrence (residual update, inner
+ * products, step lengths) preconditioned by an FP32 V-cycle (FP32 smoother,
+ * residual, transfer operators, coarse solve with the reference's FP32
+ * coarse tolerance 1e-4).  v0/f/v_out are FP64.  Same arguments otherwise. */
+qsm_status qsm_mgpcg_mixed(qsm_ctx *ctx, const size_t dims[3],
+                           const double *v0, const double *f, const uint8_t *mask,
+                           const double vsz[3], double tolcg, int32_t maxitcg, double tolmg,
+                           int32_t maxitmg, int32_t mu, int32_t npre, int32_t npost,
+                           int32_t nboundary, int32_t nlevels, int32_t verbose,
+                           double *v_out, qsm_mg_info *info);
+
+/* v = mg_mex(v, f, mask, vsz, tol, maxit, mu, npre, npost, nboundary, nlevels)
+ * Replaces src/utils/poisson_solver/mex/mg_mex.c:55-91. */
+qsm_status qsm_mg(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3],
+                  const void *v0, const void *f, const uint8_t *mask, const double vsz[3],
+                  double tol, int32_t maxit, int32_t mu, int32_t npre, int32_t npost,
+                  int32_t nboundary, int32_t nlevels, void *v_out, qsm_mg_info *info);
+
+/* v = fmg_mex(f, mask, vsz, tol, maxit, mu, npre, npost, nboundary, nlevels)
+ * Replaces src/utils/poisson_solver/mex/fmg_mex.c:54-90. */
+qsm_status qsm_fmg(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3],
+                   const void *f, const uint8_t *mask, const double vsz[3],
+                   double tol, int32_t maxit, int32_t mu, int32_t npre, int32_t npost,
+                   int32_t nboundary, int32_t nlevels, void *v_out, qsm_mg_info *info);
+
+/* ---------------- lane-order inner product (BLAS-1 replacement) ---------------- */
+
+/* *out = x . y in the library's documented lane order (mx_dot,
+ * src/utils/poisson_solver/mex/mx_blas.c:108-131 over MATLAB's ddot/sdot). */
+qsm_status qsm_dot(qsm_ctx *ctx, qsm_dtype dtype, size_t n, const void *x, const void *y,
+                   double *out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QSM_GPU_H */

@@ -1,0 +1,381 @@
+"""GB300-native QSM hot path: Python mirror of QSM.m's C-MEX gateways.
+
+Each function has the name, argument order and meaning of the MEX gateway it
+replaces (``pd_tgv_mex(d2f, mask, vsz, lam, alpha, tol, maxiter, verbose)``,
+``gradf_mex(dx, dy, dz, u, h)`` ...) and forwards to the CUDA library
+``libqsm_gb300.so`` through its C ABI (include/qsm_gpu.h).  There is no CPU
+fallback: if the library cannot be loaded, every call raises.
+
+Arrays follow MATLAB's layout (x fastest, l = i + nx*j + nx*ny*k):
+
+* numpy arrays of shape ``(nx, ny, nz)`` in Fortran order live in host
+  memory; the library copies them to the GPU and results back inside the
+  call;
+* torch CUDA tensors are used in place on the device; a tensor whose strides
+  are Fortran-ordered has dims = shape, a C-contiguous tensor of shape
+  ``(nz, ny, nx)`` has dims = reversed shape.
+
+Masks are uint8/bool 0/1.  In-place gateways write into their first
+argument(s) where the MEX file writes; solvers return a new array of the
+input's kind.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import MgInfo, PdInfo, QsmError, QsmLibraryError, context, lib
+
+__all__ = [
+    "pd_tgv_mex", "pd_tv_mex", "gradf_mex", "gradb_mex", "gradc_mex", "gradfm_mex", "gradbm_mex", "gradcm_mex",
+    "gradf_adj_mex", "gradb_adj_mex", "gradfm_adj_mex", "gradbm_adj_mex", "gradfp_mex", "gradfp_adj_mex",
+    "lap1_mex", "lapw_mex", "gauss_seidel_mex", "residual_mex", "lapmg_mex", "restrict_mex", "prolong_mex",
+    "correct_mex", "coarsen_grid_mex", "boundary_mask_mex", "boundary_mask_l1_mex", "norm2_mex", "mgpcg_mex",
+    "mg_mex", "fmg_mex", "lane_dot", "QsmError", "QsmLibraryError", "context", "lib",
+]
+
+try:  # torch is optional (device-resident callers)
+    import torch as _torch
+except Exception:  # pragma: no cover
+    _torch = None
+
+
+def _is_torch(a) -> bool:
+    return _torch is not None and isinstance(a, _torch.Tensor)
+
+
+_NP_DT = {np.dtype(np.float64): _lib.QSM_F64, np.dtype(np.float32): _lib.QSM_F32}
+
+
+class _Arr:
+    """Pointer, MATLAB dims and dtype code of one argument."""
+
+    def __init__(self, a, *, writable=False, mask=False, ref=None):
+        self.obj = a
+        if _is_torch(a):
+            if not a.is_cuda:
+                raise ValueError("torch tensors must be CUDA tensors (use numpy for host arrays)")
+            if mask and a.dtype == _torch.bool:
+                a = a.to(_torch.uint8)
+                self.obj = a
+            n = a.dim()
+            shp = tuple(a.shape)
+            if a.is_contiguous():
+                self.dims = tuple(reversed(shp))[:3] if n >= 3 else tuple(reversed(shp)) + (1,) * (3 - n)
+            else:
+                st = a.stride()
+                exp, acc = [], 1
+                for s in shp:
+                    exp.append(acc)
+                    acc *= s
+                if list(st) != exp:
+                    raise ValueError("tensor must be contiguous in C or Fortran order")
+                self.dims = shp[:3] + (1,) * (3 - min(3, n))
+            self.ptr = ctypes.c_void_p(a.data_ptr())
+            self.numel = a.numel()
+            if mask:
+                if a.dtype != _torch.uint8:
+                    raise TypeError("masks must be uint8 or bool")
+                self.dt = None
+            else:
+                if a.dtype == _torch.float64:
+                    self.dt = _lib.QSM_F64
+                elif a.dtype == _torch.float32:
+                    self.dt = _lib.QSM_F32
+                else:
+                    raise TypeError(f"unsupported dtype {a.dtype}")
+        else:
+            a = np.asarray(a)
+            if mask:
+                if a.dtype != np.uint8:
+                    a = (a != 0).astype(np.uint8)
+            elif a.dtype not in _NP_DT:
+                raise TypeError(f"unsupported dtype {a.dtype}")
+            if not a.flags.f_contiguous:
+                if writable:
+                    raise ValueError("in-place arguments must be Fortran-ordered numpy arrays")
+                a = np.asfortranarray(a)
+            if writable and not a.flags.writeable:
+                raise ValueError("in-place argument is read-only")
+            self.obj = a
+            self.dims = tuple(a.shape[:3]) + (1,) * (3 - min(3, a.ndim))
+            self.ptr = ctypes.c_void_p(a.ctypes.data)
+            self.numel = a.size
+            self.dt = None if mask else _NP_DT[a.dtype]
+
+    def dims_c(self):
+        return (ctypes.c_size_t * 3)(*self.dims)
+
+
+def _h(vsz):
+    h = np.ascontiguousarray(np.asarray(vsz, dtype=np.float64).reshape(-1))
+    if h.size == 1:
+        h = np.repeat(h, 3)
+    if h.size != 3:
+        raise ValueError("vsz must have 3 entries")
+    return (ctypes.c_double * 3)(*h)
+
+
+def _sync_torch(*arrs):
+    if _torch is not None and any(_is_torch(a.obj) for a in arrs):
+        _torch.cuda.current_stream().synchronize()
+
+
+def _same(arrs):
+    dt = arrs[0].dt
+    for a in arrs[1:]:
+        if a.dt is not None and a.dt != dt:
+            raise TypeError("all floating-point arrays must share one dtype")
+    return dt
+
+
+def _zeros_like(a: _Arr):
+    if _is_torch(a.obj):
+        return _torch.zeros_like(a.obj)
+    return np.zeros(a.obj.shape, dtype=a.obj.dtype, order="F")
+
+
+def _ctx(ctx):
+    return ctx if ctx is not None else context(0)
+
+
+# ---------------------------------------------------------------------------
+# primal-dual inversions (pd_tgv_mex.c, pd_tv_mex.c)
+# ---------------------------------------------------------------------------
+
+def pd_tgv_mex(d2f, mask, vsz, lam, alpha, tol, maxiter, verbose=0, *, fused=False, info=None, ctx=None, out=None):
+    """chi = pd_tgv_mex(d2f, mask, vsz, lam, alpha, tol, maxiter, verbose).
+
+    fused=False: plain path, bit-identical to the reference in d2f's dtype.
+    fused=True: mixed-precision fused FP32 kernel with FP64 monitors (chi
+    equals the reference's FP32 result; FP64 input is rounded, output widened).
+    out: optional preallocated result (same kind, shape and dtype as d2f).
+    """
+    f, m = _Arr(d2f), _Arr(mask, mask=True)
+    out = _zeros_like(f) if out is None else out
+    o = _Arr(out, writable=True)
+    pi = PdInfo()
+    _sync_torch(f, m, o)
+    _ctx(ctx).call("qsm_pd_tgv_fused" if fused else "qsm_pd_tgv", f.dt, f.dims_c(), f.ptr, m.ptr, _h(vsz),
+                   float(lam), float(alpha), float(tol), int(maxiter), int(verbose), o.ptr, ctypes.byref(pi))
+    if info is not None:
+        info.update(iters=pi.iters, monitors=(pi.monitor_chi, pi.monitor_eta), seconds=pi.seconds)
+    return out
+
+
+def pd_tv_mex(d2f, mask, vsz, lam, tol, maxiter, verbose=0, *, fused=False, info=None, ctx=None, out=None):
+    """chi = pd_tv_mex(d2f, mask, vsz, lam, tol, maxiter, verbose)."""
+    f, m = _Arr(d2f), _Arr(mask, mask=True)
+    out = _zeros_like(f) if out is None else out
+    o = _Arr(out, writable=True)
+    pi = PdInfo()
+    _sync_torch(f, m, o)
+    _ctx(ctx).call("qsm_pd_tv_fused" if fused else "qsm_pd_tv", f.dt, f.dims_c(), f.ptr, m.ptr, _h(vsz),
+                   float(lam), float(tol), int(maxiter), int(verbose), o.ptr, ctypes.byref(pi))
+    if info is not None:
+        info.update(iters=pi.iters, monitors=(pi.monitor_chi, pi.monitor_eta), seconds=pi.seconds)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# finite-difference operators (in place)
+# ---------------------------------------------------------------------------
+
+def _grad(name, dx, dy, dz, u, h, G=None, ctx=None):
+    a = [_Arr(dx, writable=True), _Arr(dy, writable=True), _Arr(dz, writable=True), _Arr(u)]
+    dt = _same(a)
+    args = [dt, a[3].dims_c(), a[0].ptr, a[1].ptr, a[2].ptr, a[3].ptr]
+    g = None
+    if G is not None:
+        g = _Arr(G, mask=True)
+        args.append(g.ptr)
+    _sync_torch(*a)
+    _ctx(ctx).call(name, *args, _h(h))
+
+
+def gradf_mex(dx, dy, dz, u, h, *, ctx=None): _grad("qsm_gradf", dx, dy, dz, u, h, ctx=ctx)
+def gradb_mex(dx, dy, dz, u, h, *, ctx=None): _grad("qsm_gradb", dx, dy, dz, u, h, ctx=ctx)
+def gradc_mex(dx, dy, dz, u, h, *, ctx=None): _grad("qsm_gradc", dx, dy, dz, u, h, ctx=ctx)
+def gradfp_mex(dx, dy, dz, u, h, *, ctx=None): _grad("qsm_gradfp", dx, dy, dz, u, h, ctx=ctx)
+def gradfm_mex(dx, dy, dz, u, G, h, *, ctx=None): _grad("qsm_gradfm", dx, dy, dz, u, h, G, ctx=ctx)
+def gradbm_mex(dx, dy, dz, u, G, h, *, ctx=None): _grad("qsm_gradbm", dx, dy, dz, u, h, G, ctx=ctx)
+def gradcm_mex(dx, dy, dz, u, G, h, *, ctx=None): _grad("qsm_gradcm", dx, dy, dz, u, h, G, ctx=ctx)
+
+
+def _adj(name, du, x, y, z, h, G=None, ctx=None):
+    a = [_Arr(du, writable=True), _Arr(x), _Arr(y), _Arr(z)]
+    dt = _same(a)
+    args = [dt, a[0].dims_c(), a[0].ptr, a[1].ptr, a[2].ptr, a[3].ptr]
+    if G is not None:
+        args.append(_Arr(G, mask=True).ptr)
+    _sync_torch(*a)
+    _ctx(ctx).call(name, *args, _h(h))
+
+
+def gradf_adj_mex(du, x, y, z, h, *, ctx=None): _adj("qsm_gradf_adj", du, x, y, z, h, ctx=ctx)
+def gradb_adj_mex(du, x, y, z, h, *, ctx=None): _adj("qsm_gradb_adj", du, x, y, z, h, ctx=ctx)
+def gradfp_adj_mex(du, x, y, z, h, *, ctx=None): _adj("qsm_gradfp_adj", du, x, y, z, h, ctx=ctx)
+def gradfm_adj_mex(du, x, y, z, G, h, *, ctx=None): _adj("qsm_gradfm_adj", du, x, y, z, h, G, ctx=ctx)
+def gradbm_adj_mex(du, x, y, z, G, h, *, ctx=None): _adj("qsm_gradbm_adj", du, x, y, z, h, G, ctx=ctx)
+
+
+def lap1_mex(d2u, u, G, h, *, ctx=None):
+    o, a, g = _Arr(d2u, writable=True), _Arr(u), _Arr(G, mask=True)
+    _sync_torch(o, a)
+    _ctx(ctx).call("qsm_lap1", _same([o, a]), a.dims_c(), o.ptr, a.ptr, g.ptr, _h(h))
+
+
+def lapw_mex(d2u, u, h, *, ctx=None):
+    o, a = _Arr(d2u, writable=True), _Arr(u)
+    _sync_torch(o, a)
+    _ctx(ctx).call("qsm_lapw", _same([o, a]), a.dims_c(), o.ptr, a.ptr, _h(h))
+
+
+# ---------------------------------------------------------------------------
+# multigrid pieces (in place)
+# ---------------------------------------------------------------------------
+
+def gauss_seidel_mex(v, f, G, h, iters, reverse, *, ctx=None):
+    a, b, g = _Arr(v, writable=True), _Arr(f), _Arr(G, mask=True)
+    _sync_torch(a, b)
+    _ctx(ctx).call("qsm_gauss_seidel", _same([a, b]), a.dims_c(), a.ptr, b.ptr, g.ptr, _h(h), int(iters), int(reverse))
+
+
+def residual_mex(r, f, x, G, h, *, ctx=None):
+    a, b, c, g = _Arr(r, writable=True), _Arr(f), _Arr(x), _Arr(G, mask=True)
+    _sync_torch(a, b, c)
+    _ctx(ctx).call("qsm_residual", _same([a, b, c]), a.dims_c(), a.ptr, b.ptr, c.ptr, g.ptr, _h(h))
+
+
+def lapmg_mex(d2u, u, G, h, *, ctx=None):
+    a, b, g = _Arr(d2u, writable=True), _Arr(u), _Arr(G, mask=True)
+    _sync_torch(a, b)
+    _ctx(ctx).call("qsm_lapmg", _same([a, b]), a.dims_c(), a.ptr, b.ptr, g.ptr, _h(h))
+
+
+def restrict_mex(x2, x, G2, *, ctx=None):
+    a, b, g = _Arr(x2, writable=True), _Arr(x), _Arr(G2, mask=True)
+    _sync_torch(a, b)
+    _ctx(ctx).call("qsm_restrict", _same([a, b]), a.dims_c(), a.ptr, b.dims_c(), b.ptr, g.ptr)
+
+
+def prolong_mex(x, x2, G, *, ctx=None):
+    a, b, g = _Arr(x, writable=True), _Arr(x2), _Arr(G, mask=True)
+    _sync_torch(a, b)
+    _ctx(ctx).call("qsm_prolong", _same([a, b]), a.dims_c(), a.ptr, b.dims_c(), b.ptr, g.ptr)
+
+
+def correct_mex(x, x2, G, *, ctx=None):
+    a, b, g = _Arr(x, writable=True), _Arr(x2), _Arr(G, mask=True)
+    _sync_torch(a, b)
+    _ctx(ctx).call("qsm_correct", _same([a, b]), a.dims_c(), a.ptr, b.dims_c(), b.ptr, g.ptr)
+
+
+def coarsen_grid_mex(G2, G, *, ctx=None):
+    a, b = _Arr(G2, writable=True, mask=True), _Arr(G, mask=True)
+    _ctx(ctx).call("qsm_coarsen_grid", a.dims_c(), a.ptr, b.dims_c(), b.ptr)
+    _writeback_mask(G2, a)
+
+
+def boundary_mask_mex(B, G, *, ctx=None):
+    a, b = _Arr(B, writable=True, mask=True), _Arr(G, mask=True)
+    _ctx(ctx).call("qsm_boundary_mask", b.dims_c(), a.ptr, b.ptr)
+    _writeback_mask(B, a)
+
+
+def boundary_mask_l1_mex(B, G, l1, *, ctx=None):
+    a, b = _Arr(B, writable=True, mask=True), _Arr(G, mask=True)
+    _ctx(ctx).call("qsm_boundary_mask_l1", b.dims_c(), a.ptr, b.ptr, int(l1) & 0xFF)
+    _writeback_mask(B, a)
+
+
+def _writeback_mask(orig, a: _Arr):
+    # bool outputs were converted to a uint8 copy; copy the result back
+    if a.obj is not orig:
+        if _is_torch(orig):
+            orig.copy_(a.obj.to(orig.dtype))
+        else:
+            orig[...] = a.obj.astype(orig.dtype)
+
+
+def norm2_mex(x, G, *, ctx=None):
+    a, g = _Arr(x), _Arr(G, mask=True)
+    out = ctypes.c_double(0.0)
+    _sync_torch(a)
+    _ctx(ctx).call("qsm_norm2", a.dt, a.numel, a.ptr, g.ptr, ctypes.byref(out))
+    return out.value
+
+
+def lane_dot(x, y, *, ctx=None):
+    """x . y in the library's lane order (the BLAS-1 dot of the PCG)."""
+    a, b = _Arr(x), _Arr(y)
+    out = ctypes.c_double(0.0)
+    _sync_torch(a, b)
+    _ctx(ctx).call("qsm_dot", _same([a, b]), a.numel, a.ptr, b.ptr, ctypes.byref(out))
+    return out.value
+
+
+# ---------------------------------------------------------------------------
+# Poisson solvers
+# ---------------------------------------------------------------------------
+
+def mgpcg_mex(v, f, mask, vsz, tolcg, maxitcg, tolmg, maxitmg, mu, npre, npost, nboundary, nlevels, verbose=0,
+              *, mixed=False, info=None, ctx=None):
+    """v = mgpcg_mex(v, f, mask, vsz, tolcg, maxitcg, tolmg, maxitmg, mu, npre, npost, nboundary, nlevels, verbose).
+
+    mixed=True runs the FP64 PCG recurrence with an FP32 V-cycle (FP64 arrays only).
+    """
+    fa, m = _Arr(f), _Arr(mask, mask=True)
+    va = _Arr(v) if v is not None else None
+    out = _zeros_like(fa)
+    o = _Arr(out, writable=True)
+    hist = np.zeros(max(1, int(maxitcg)), dtype=np.float64)
+    mi = MgInfo()
+    mi.resnorm_hist = hist.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    _sync_torch(fa, m, o)
+    vp = va.ptr if va is not None else None
+    if mixed:
+        if fa.dt != _lib.QSM_F64:
+            raise TypeError("the mixed-precision solver takes FP64 arrays")
+        _ctx(ctx).call("qsm_mgpcg_mixed", fa.dims_c(), vp, fa.ptr, m.ptr, _h(vsz), float(tolcg), int(maxitcg),
+                       float(tolmg), int(maxitmg), int(mu), int(npre), int(npost), int(nboundary), int(nlevels),
+                       int(verbose), o.ptr, ctypes.byref(mi))
+    else:
+        _ctx(ctx).call("qsm_mgpcg", fa.dt, fa.dims_c(), vp, fa.ptr, m.ptr, _h(vsz), float(tolcg), int(maxitcg),
+                       float(tolmg), int(maxitmg), int(mu), int(npre), int(npost), int(nboundary), int(nlevels),
+                       int(verbose), o.ptr, ctypes.byref(mi))
+    if info is not None:
+        info.update(iters=mi.iters, resnorm=mi.resnorm, seconds=mi.seconds, resnorm_hist=hist[: mi.iters].copy())
+    return out
+
+
+def mg_mex(v, f, mask, vsz, tol, maxit, mu, npre, npost, nboundary, nlevels, *, info=None, ctx=None):
+    """v = mg_mex(v, f, mask, vsz, tol, maxit, mu, npre, npost, nboundary, nlevels)."""
+    fa, m = _Arr(f), _Arr(mask, mask=True)
+    va = _Arr(v) if v is not None else None
+    out = _zeros_like(fa)
+    o = _Arr(out, writable=True)
+    mi = MgInfo()
+    _sync_torch(fa, m, o)
+    _ctx(ctx).call("qsm_mg", fa.dt, fa.dims_c(), va.ptr if va is not None else None, fa.ptr, m.ptr, _h(vsz),
+                   float(tol), int(maxit), int(mu), int(npre), int(npost), int(nboundary), int(nlevels), o.ptr,
+                   ctypes.byref(mi))
+    if info is not None:
+        info.update(cycles=mi.iters, seconds=mi.seconds)
+    return out
+
+
+def fmg_mex(f, mask, vsz, tol, maxit, mu, npre, npost, nboundary, nlevels, *, info=None, ctx=None):
+    """v = fmg_mex(f, mask, vsz, tol, maxit, mu, npre, npost, nboundary, nlevels)."""
+    fa, m = _Arr(f), _Arr(mask, mask=True)
+    out = _zeros_like(fa)
+    o = _Arr(out, writable=True)
+    mi = MgInfo()
+    _sync_torch(fa, m, o)
+    _ctx(ctx).call("qsm_fmg", fa.dt, fa.dims_c(), fa.ptr, m.ptr, _h(vsz), float(tol), int(maxit), int(mu),
+                   int(npre), int(npost), int(nboundary), int(nlevels), o.ptr, ctypes.byref(mi))
+    if info is not None:
+        info.update(cycles=mi.iters, seconds=mi.seconds)
+    return out

@@ -1,0 +1,276 @@
+// Context, staging and lane-order reductions.
+#include <stdarg.h>
+#include <stdlib.h>
+
+#include "common.cuh"
+
+namespace qsm {
+
+void set_error(qsm_ctx *ctx, const char *fmt, ...)
+{
+    if (!ctx) return;
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(ctx->err, sizeof ctx->err, fmt, ap);
+    va_end(ap);
+}
+
+qsm_status dalloc(qsm_ctx *ctx, void **p, size_t bytes)
+{
+    *p = nullptr;
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMallocFromPoolAsync(p, bytes, ctx->pool, ctx->stream);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_error(ctx, "device allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+        *p = nullptr;
+        return QSM_ERR_NOMEM;
+    }
+    return QSM_OK;
+}
+
+qsm_status dfree(qsm_ctx *ctx, void *p)
+{
+    if (!p) return QSM_OK;
+    QSM_CUDA(cudaFreeAsync(p, ctx->stream));
+    return QSM_OK;
+}
+
+bool is_device_ptr(const void *p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+qsm_status stage_in(qsm_ctx *ctx, Staged &s, const void *p, size_t bytes, bool copy_in)
+{
+    s.host = nullptr;
+    s.dev = nullptr;
+    s.bytes = bytes;
+    s.owned = false;
+    if (is_device_ptr(p)) {
+        s.dev = const_cast<void *>(p);
+        return QSM_OK;
+    }
+    s.host = const_cast<void *>(p);
+    QSM_TRY(dalloc(ctx, &s.dev, bytes));
+    s.owned = true;
+    if (copy_in && bytes) QSM_CUDA(cudaMemcpyAsync(s.dev, p, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    return QSM_OK;
+}
+
+qsm_status stage_out(qsm_ctx *ctx, Staged &s, bool copy_out)
+{
+    if (!s.owned) return QSM_OK;
+    if (copy_out && s.bytes) QSM_CUDA(cudaMemcpyAsync(s.host, s.dev, s.bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    qsm_status st = dfree(ctx, s.dev);
+    s.dev = nullptr;
+    s.owned = false;
+    return st;
+}
+
+// ---------------------------------------------------------------------------
+// lane-order dot product
+// ---------------------------------------------------------------------------
+
+template <typename T>
+__device__ __forceinline__ T halve_block(T *sm, int tid, T v)
+{
+    sm[tid] = v;
+    __syncthreads();
+    for (int s = RED_BLOCK / 2; s > 0; s >>= 1) {
+        if (tid < s) sm[tid] = sm[tid] + sm[tid + s];
+        __syncthreads();
+    }
+    return sm[0];
+}
+
+// Final halving over the RED_NBLK block partials by one block of RED_BLOCK
+// threads: level s = 512 is done by each thread for t and t + 256, then the
+// remaining levels in shared memory.
+template <typename T>
+__device__ __forceinline__ T halve_partials(T *sm, int tid, const T *part)
+{
+    static_assert(RED_NBLK == 4 * RED_BLOCK, "lane order layout");
+    T a = __ldcg(part + tid), b = __ldcg(part + tid + 256), c = __ldcg(part + tid + 512), d = __ldcg(part + tid + 768);
+    // s = 512: a[t] += a[t+512] for t < 512
+    sm[tid] = a + c;
+    T hi = b + d;  // element t + 256 after the s = 512 level
+    __syncthreads();
+    // s = 256: a[t] += a[t+256]
+    T v = sm[tid] + hi;
+    __syncthreads();
+    return halve_block(sm, tid, v);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(RED_BLOCK) lane_dot_kernel(const T *__restrict__ x, const T *__restrict__ y,
+                                                             size_t n, T *part, unsigned int *count, double *out)
+{
+    __shared__ T sm[RED_BLOCK];
+    __shared__ bool last;
+    const int tid = threadIdx.x;
+    const size_t t = (size_t)blockIdx.x * RED_BLOCK + tid;
+    T acc = (T)0;
+    for (size_t i = t; i < n; i += RED_LANES) acc = acc + x[i] * y[i];
+    T b = halve_block(sm, tid, acc);
+    if (tid == 0) {
+        part[blockIdx.x] = b;
+        __threadfence();
+        last = atomicAdd(count, 1u) == RED_NBLK - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    T r = halve_partials(sm, tid, part);
+    if (tid == 0) {
+        out[0] = (double)r;
+        *count = 0;
+    }
+}
+
+template <typename T>
+qsm_status lane_dot(qsm_ctx *ctx, const T *x, const T *y, size_t n, double *dout)
+{
+    lane_dot_kernel<T><<<RED_NBLK, RED_BLOCK, 0, ctx->stream>>>(x, y, n, (T *)ctx->red_partial, ctx->red_count, dout);
+    QSM_CUDA(cudaGetLastError());
+    return QSM_OK;
+}
+
+template qsm_status lane_dot<float>(qsm_ctx *, const float *, const float *, size_t, double *);
+template qsm_status lane_dot<double>(qsm_ctx *, const double *, const double *, size_t, double *);
+
+qsm_status read_double(qsm_ctx *ctx, const double *d, double *h)
+{
+    QSM_CUDA(cudaMemcpyAsync(ctx->host_out, d, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+    *h = ctx->host_out[0];
+    return QSM_OK;
+}
+
+}  // namespace qsm
+
+// ---------------------------------------------------------------------------
+// C ABI: context
+// ---------------------------------------------------------------------------
+
+using namespace qsm;
+
+extern "C" {
+
+int qsm_abi_version(void) { return QSM_GPU_ABI_VERSION; }
+
+const char *qsm_status_string(qsm_status s)
+{
+    switch (s) {
+    case QSM_OK: return "ok";
+    case QSM_ERR_ARG: return "invalid argument";
+    case QSM_ERR_DIMS: return "invalid dimensions";
+    case QSM_ERR_DTYPE: return "invalid dtype";
+    case QSM_ERR_NOMEM: return "out of device memory";
+    case QSM_ERR_CUDA: return "CUDA error";
+    case QSM_ERR_NONFINITE: return "non-finite convergence monitor";
+    case QSM_ERR_DEPTH: return "nlevels too large. Increase MAX_DEPTH.";
+    case QSM_ERR_BUSY: return "busy";
+    case QSM_ERR_TIMEOUT: return "timeout";
+    }
+    return "unknown status";
+}
+
+const char *qsm_last_error(const qsm_ctx *ctx) { return ctx ? ctx->err : "no context"; }
+
+qsm_status qsm_ctx_create(int device, qsm_ctx **out)
+{
+    if (!out) return QSM_ERR_ARG;
+    *out = nullptr;
+    qsm_ctx *ctx = (qsm_ctx *)calloc(1, sizeof(qsm_ctx));
+    if (!ctx) return QSM_ERR_NOMEM;
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) {
+        ctx->own_stream = true;
+        cudaMemPoolProps props;
+        memset(&props, 0, sizeof props);
+        props.allocType = cudaMemAllocationTypePinned;
+        props.handleTypes = cudaMemHandleTypeNone;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = device;
+        e = cudaMemPoolCreate(&ctx->pool, &props);
+    }
+    if (e == cudaSuccess) {
+        uint64_t thr = UINT64_MAX;  // keep freed blocks cached in the pool
+        e = cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->red_partial, 4 * RED_NBLK * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->red_out, 8 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->red_count, 8 * sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMemset(ctx->red_count, 0, 8 * sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&ctx->host_out, 8 * sizeof(double));
+    if (e != cudaSuccess) {
+        snprintf(ctx->err, sizeof ctx->err, "context creation failed: %s", cudaGetErrorString(e));
+        fprintf(stderr, "qsm_ctx_create: %s\n", ctx->err);
+        qsm_ctx_destroy(ctx);
+        return QSM_ERR_CUDA;
+    }
+    *out = ctx;
+    return QSM_OK;
+}
+
+qsm_status qsm_ctx_destroy(qsm_ctx *ctx)
+{
+    if (!ctx) return QSM_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->red_partial) cudaFree(ctx->red_partial);
+    if (ctx->red_out) cudaFree(ctx->red_out);
+    if (ctx->red_count) cudaFree(ctx->red_count);
+    if (ctx->host_out) cudaFreeHost(ctx->host_out);
+    if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
+    if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+    free(ctx);
+    return QSM_OK;
+}
+
+qsm_status qsm_ctx_set_stream(qsm_ctx *ctx, void *stream)
+{
+    if (!ctx) return QSM_ERR_ARG;
+    cudaStreamSynchronize(ctx->stream);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    ctx->own_stream = false;
+    ctx->stream = (cudaStream_t)stream;
+    return QSM_OK;
+}
+
+void *qsm_ctx_get_stream(qsm_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+qsm_status qsm_ctx_set_verbose(qsm_ctx *ctx, int verbose)
+{
+    if (!ctx) return QSM_ERR_ARG;
+    ctx->verbose = verbose;
+    return QSM_OK;
+}
+
+qsm_status qsm_dot(qsm_ctx *ctx, qsm_dtype dtype, size_t n, const void *x, const void *y, double *out)
+{
+    if (!ctx || !x || !y || !out) return QSM_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    const size_t es = dtype == QSM_F32 ? 4 : 8;
+    if (dtype != QSM_F32 && dtype != QSM_F64) return QSM_ERR_DTYPE;
+    Staged sx, sy;
+    QSM_TRY(stage_in(ctx, sx, x, n * es, true));
+    QSM_TRY(stage_in(ctx, sy, y, n * es, true));
+    if (dtype == QSM_F32)
+        QSM_TRY(lane_dot<float>(ctx, (const float *)sx.dev, (const float *)sy.dev, n, ctx->red_out));
+    else
+        QSM_TRY(lane_dot<double>(ctx, (const double *)sx.dev, (const double *)sy.dev, n, ctx->red_out));
+    QSM_TRY(stage_out(ctx, sx, false));
+    QSM_TRY(stage_out(ctx, sy, false));
+    return read_double(ctx, ctx->red_out, out);
+}
+
+}  // extern "C"

@@ -1,0 +1,123 @@
+// Shared device/host infrastructure of the GB300 QSM library: status codes,
+// the per-device context (stream + stream-ordered memory pool), staging of
+// caller pointers that may live in host or device memory, launch geometry,
+// and the deterministic "lane order" reductions.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+#include <stdio.h>
+#include <string.h>
+
+#include "../../include/qsm_gpu.h"
+
+namespace qsm {
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+
+void set_error(qsm_ctx *ctx, const char *fmt, ...);
+
+#define QSM_CUDA(call)                                                              \
+    do {                                                                            \
+        cudaError_t e_ = (call);                                                    \
+        if (e_ != cudaSuccess) {                                                    \
+            ::qsm::set_error(ctx, "%s:%d %s: %s", __FILE__, __LINE__, #call,        \
+                             cudaGetErrorString(e_));                               \
+            return QSM_ERR_CUDA;                                                    \
+        }                                                                           \
+    } while (0)
+
+#define QSM_TRY(expr)                                                               \
+    do {                                                                            \
+        qsm_status s_ = (expr);                                                     \
+        if (s_ != QSM_OK) return s_;                                                \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// geometry
+// ---------------------------------------------------------------------------
+
+struct Dims {
+    size_t nx, ny, nz;
+    __host__ __device__ size_t nxny() const { return nx * ny; }
+    __host__ __device__ size_t n() const { return nx * ny * nz; }
+};
+
+static inline Dims make_dims(const size_t *d) { return Dims{d[0], d[1], d[2]}; }
+
+// One thread per voxel: block 32 x 4 x 2 over (x, y, z).
+static inline dim3 vox_block() { return dim3(32, 4, 2); }
+static inline dim3 vox_grid(const Dims &d)
+{
+    return dim3((unsigned)((d.nx + 31) / 32), (unsigned)((d.ny + 3) / 4), (unsigned)((d.nz + 1) / 2));
+}
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+
+}  // namespace qsm
+
+struct qsm_ctx {
+    int device;
+    cudaStream_t stream;
+    bool own_stream;
+    cudaMemPool_t pool;
+    int verbose;
+    char err[512];
+    // lane-order reduction scratch (partials + results), grown on demand
+    double *red_partial;   // 4 * QSM_RED_NBLK doubles
+    double *red_out;       // 8 doubles
+    unsigned int *red_count;
+    double *host_out;      // pinned, 8 doubles
+};
+
+namespace qsm {
+
+// device allocation from the context's pool, ordered on its stream
+qsm_status dalloc(qsm_ctx *ctx, void **p, size_t bytes);
+qsm_status dfree(qsm_ctx *ctx, void *p);
+
+// Where a caller pointer lives.
+bool is_device_ptr(const void *p);
+
+// A caller array that may be host or device memory.  stage_in() gives a
+// device pointer (copying host data in when `copy_in`); stage_out() copies a
+// staged array back to the host buffer and releases the staging copy.
+struct Staged {
+    void *host;      // caller's host pointer (null if caller passed device memory)
+    void *dev;       // device pointer used by kernels
+    size_t bytes;
+    bool owned;
+};
+
+qsm_status stage_in(qsm_ctx *ctx, Staged &s, const void *p, size_t bytes, bool copy_in);
+qsm_status stage_out(qsm_ctx *ctx, Staged &s, bool copy_out);
+
+// ---------------------------------------------------------------------------
+// lane-order reductions
+//
+// Element i of an n-vector goes to lane i mod 2^18; each lane sums its
+// elements in increasing i from +0.0 (no fused multiply-add); lanes form
+// 1024 blocks of 256 reduced by halving (s = 128..1: a[t] += a[t+s]); the
+// 1024 block sums are reduced by the same halving.  The CPU oracle and its
+// BLAS shim use exactly this order, so results agree bit-for-bit.
+// ---------------------------------------------------------------------------
+
+constexpr int RED_BLOCK = 256;
+constexpr int RED_NBLK = QSM_RED_NBLK;
+constexpr size_t RED_LANES = (size_t)RED_BLOCK * RED_NBLK;
+
+// out[0] = dot(x, y) (or sum x*x when y == x) in lane order, on ctx->stream,
+// written to device memory `dout`.  T in {float, double}; FP32 inputs
+// accumulate in FP32 like sdot and the result is widened.
+template <typename T>
+qsm_status lane_dot(qsm_ctx *ctx, const T *x, const T *y, size_t n, double *dout);
+
+// Reads back one device double (synchronises the stream).
+qsm_status read_double(qsm_ctx *ctx, const double *d, double *h);
+
+}  // namespace qsm

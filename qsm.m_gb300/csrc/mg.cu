@@ -1,0 +1,1299 @@
+// Multigrid-preconditioned CG Poisson solver and its pieces:
+//   -Delta u = f in the mask G, u = 0 outside, on a grid padded by one voxel.
+//
+// Kernels evaluate the reference's per-voxel expressions in order without
+// fused multiply-add (bit-identical to src/utils/poisson_solver/mex/*.c in
+// FP32 and FP64).  Inner products and norms use the lane order of
+// common.cu, as does the oracle's BLAS shim, so whole PCG solves are
+// reproducible bit-for-bit.
+//
+//   red-black Gauss-Seidel  one launch per colour pass; a pass only reads the
+//                           other colour, so its voxels are independent
+//   coarsest level          one CTA keeps v, f and G in shared memory and
+//                           runs the reference's <= 1024 x (128 reverse +
+//                           128 forward sweeps + residual + norm) loop,
+//                           including the lane-order norm, with block
+//                           barriers only (no host round trips)
+//   PCG scalars             stay on the device; the host reads ||r|| once
+//                           per iteration for the stopping test
+#include <math.h>
+#include <stdlib.h>
+#include <vector>
+
+#include "common.cuh"
+
+namespace qsm {
+
+template <typename T> struct GsC { T hx, hy, hz, hh; };
+
+template <typename T> static GsC<T> gs_consts(const double *h)
+{
+    // gauss_seidel_mex.c:96-99 / :214-217
+    GsC<T> c;
+    c.hx = (T)(1.0 / (h[0] * h[0]));
+    c.hy = (T)(1.0 / (h[1] * h[1]));
+    c.hz = (T)(1.0 / (h[2] * h[2]));
+    c.hh = (T)(1.0 / (2.0 * (double)(c.hx + c.hy + c.hz)));
+    return c;
+}
+
+template <typename T> struct LapC { T hx, hy, hz, hh; };
+
+template <typename T> static LapC<T> lap_consts(const double *h)
+{
+    // residual_mex.c:98-101 / lapmg_mex.c:87-90
+    LapC<T> c;
+    c.hx = (T)(1.0 / (h[0] * h[0]));
+    c.hy = (T)(1.0 / (h[1] * h[1]));
+    c.hz = (T)(1.0 / (h[2] * h[2]));
+    c.hh = (T)(-2.0 * (c.hx + c.hy + c.hz));
+    return c;
+}
+
+// ---------------------------------------------------------------------------
+// Gauss-Seidel colour pass (gauss_seidel_mex.c:138-190 / :256-308)
+// Pass over voxels with (i + j + k) = par (mod 2) in the interior, except
+// x index skip_i.
+// ---------------------------------------------------------------------------
+
+template <typename T>
+__global__ void gs_color_k(T *v, const T *__restrict__ f, const uint8_t *__restrict__ G, GsC<T> c, Dims d, int par,
+                           size_t skip_i)
+{
+    const size_t j = 1 + (size_t)blockIdx.y * blockDim.y + threadIdx.y;
+    const size_t k = 1 + (size_t)blockIdx.z * blockDim.z + threadIdx.z;
+    if (j + 1 >= d.ny || k + 1 >= d.nz) return;
+    const size_t i = 1 + ((1 + j + k + par) & 1) + 2 * ((size_t)blockIdx.x * blockDim.x + threadIdx.x);
+    if (i + 1 >= d.nx || i == skip_i) return;
+    const size_t nx = d.nx, nxny = d.nxny(), l = i + nx * j + nxny * k;
+    if (!G[l]) return;
+    v[l] = c.hh * (f[l] + (c.hx * (v[l - 1] + v[l + 1]) + c.hy * (v[l - nx] + v[l + nx]) + c.hz * (v[l - nxny] + v[l + nxny])));
+}
+
+template <typename T>
+static qsm_status gauss_seidel(qsm_ctx *ctx, T *v, const T *f, const uint8_t *G, const double *h, const Dims &d,
+                               int32_t iter, bool rev)
+{
+    if (d.nx < 3 || d.ny < 3 || d.nz < 3 || iter <= 0) return QSM_OK;
+    const GsC<T> c = gs_consts<T>(h);
+    const dim3 b(32, 4, 2);
+    const dim3 g((unsigned)(((d.nx - 2 + 1) / 2 + 31) / 32), (unsigned)((d.ny - 2 + 3) / 4), (unsigned)((d.nz - 2 + 1) / 2));
+    const int par0 = rev ? (int)((d.nx + 1) & 1) : 0;
+    const size_t skip = rev ? d.nx - 2 : 1;
+    for (int32_t s = 0; s < iter; ++s) {
+        gs_color_k<T><<<g, b, 0, ctx->stream>>>(v, f, G, c, d, par0, (size_t)-1);
+        gs_color_k<T><<<g, b, 0, ctx->stream>>>(v, f, G, c, d, par0 ^ 1, skip);
+    }
+    QSM_CUDA(cudaGetLastError());
+    return QSM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// residual / Laplacian (residual_mex.c:82-165, lapmg_mex.c:73-154)
+// ---------------------------------------------------------------------------
+
+#define MG_INTERIOR                                                           \
+    const size_t i = 1 + (size_t)blockIdx.x * blockDim.x + threadIdx.x;       \
+    const size_t j = 1 + (size_t)blockIdx.y * blockDim.y + threadIdx.y;       \
+    const size_t k = 1 + (size_t)blockIdx.z * blockDim.z + threadIdx.z;       \
+    if (i + 1 >= d.nx || j + 1 >= d.ny || k + 1 >= d.nz) return;             \
+    const size_t nx = d.nx, nxny = d.nxny(), l = i + nx * j + nxny * k;
+
+template <typename T>
+__global__ void residual_k(T *r, const T *__restrict__ f, const T *__restrict__ x, const uint8_t *__restrict__ G,
+                           LapC<T> c, Dims d)
+{
+    MG_INTERIOR
+    if (!G[l]) return;
+    r[l] = f[l] + (c.hh * x[l] + c.hx * (x[l - 1] + x[l + 1]) + c.hy * (x[l - nx] + x[l + nx]) + c.hz * (x[l - nxny] + x[l + nxny]));
+}
+
+template <typename T>
+__global__ void lapmg_k(T *du, const T *__restrict__ u, const uint8_t *__restrict__ G, LapC<T> c, Dims d)
+{
+    MG_INTERIOR
+    if (!G[l]) return;
+    du[l] = c.hh * u[l] + c.hx * (u[l - 1] + u[l + 1]) + c.hy * (u[l - nx] + u[l + nx]) + c.hz * (u[l - nxny] + u[l + nxny]);
+}
+
+static inline dim3 interior_grid3(const Dims &d)
+{
+    Dims e{d.nx > 2 ? d.nx - 2 : 0, d.ny > 2 ? d.ny - 2 : 0, d.nz > 2 ? d.nz - 2 : 0};
+    return vox_grid(e);
+}
+
+template <typename T>
+static qsm_status residual(qsm_ctx *ctx, T *r, const T *f, const T *x, const uint8_t *G, const double *h, const Dims &d)
+{
+    const dim3 g = interior_grid3(d);
+    if (g.x == 0 || g.y == 0 || g.z == 0) return QSM_OK;
+    residual_k<T><<<g, vox_block(), 0, ctx->stream>>>(r, f, x, G, lap_consts<T>(h), d);
+    QSM_CUDA(cudaGetLastError());
+    return QSM_OK;
+}
+
+template <typename T>
+static qsm_status lapmg(qsm_ctx *ctx, T *du, const T *u, const uint8_t *G, const double *h, const Dims &d)
+{
+    const dim3 g = interior_grid3(d);
+    if (g.x == 0 || g.y == 0 || g.z == 0) return QSM_OK;
+    lapmg_k<T><<<g, vox_block(), 0, ctx->stream>>>(du, u, G, lap_consts<T>(h), d);
+    QSM_CUDA(cudaGetLastError());
+    return QSM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// grid transfer (restrict_mex.c:72-332, prolong/correct_mex.c:73-304)
+// ---------------------------------------------------------------------------
+
+template <typename T>
+__global__ void restrict_k(T *x2, const T *__restrict__ x, const uint8_t *__restrict__ G2, Dims d2, Dims d)
+{
+    const size_t i2 = 1 + (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t j2 = 1 + (size_t)blockIdx.y * blockDim.y + threadIdx.y;
+    const size_t k2 = 1 + (size_t)blockIdx.z * blockDim.z + threadIdx.z;
+    if (i2 + 1 >= d2.nx || j2 + 1 >= d2.ny || k2 + 1 >= d2.nz) return;
+    const size_t l2 = i2 + d2.nx * j2 + d2.nxny() * k2;
+    if (!G2[l2]) {
+        x2[l2] = (T)0;
+        return;
+    }
+    const size_t nx = d.nx, nxny = d.nxny();
+    const size_t l = (2 * i2 - 1) + nx * (2 * j2 - 1) + nxny * (2 * k2 - 1);
+#define X(a, b, c) x[l + (a) + (b) * (ptrdiff_t)nx + (c) * (ptrdiff_t)nxny]
+    const T A = X(-1, -1, -1) + X(1, -1, -1) + X(-1, 1, -1) + X(1, 1, -1) + X(-1, -1, 1) + X(1, -1, 1) + X(-1, 1, 1) + X(1, 1, 1);
+    const T B = X(0, -1, -1) + X(-1, 0, -1) + X(1, 0, -1) + X(0, 1, -1) + X(1, -1, 0) + X(-1, -1, 0) + X(-1, 1, 0) +
+                X(1, 1, 0) + X(0, -1, 1) + X(-1, 0, 1) + X(1, 0, 1) + X(0, 1, 1);
+    const T C = X(0, 0, -1) + X(0, -1, 0) + X(-1, 0, 0) + X(1, 0, 0) + X(0, 1, 0) + X(0, 0, 1);
+#undef X
+    x2[l2] = (T)0.015625 * A + (T)0.03125 * B + (T)0.0625 * C + (T)0.125 * x[l];
+}
+
+// One thread per fine voxel (i, j, k) in [1, 2(n2-2)]^3: coarse parent
+// i2 = (i+1)/2 and offset a = (i+1) mod 2 select the interpolation case.
+template <typename T, bool ADD>
+__global__ void prolong_k(T *x, const T *__restrict__ x2, const uint8_t *__restrict__ G, Dims d, Dims d2)
+{
+    const size_t i = 1 + (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t j = 1 + (size_t)blockIdx.y * blockDim.y + threadIdx.y;
+    const size_t k = 1 + (size_t)blockIdx.z * blockDim.z + threadIdx.z;
+    if (i > 2 * (d2.nx - 2) || j > 2 * (d2.ny - 2) || k > 2 * (d2.nz - 2)) return;
+    const size_t lf = i + d.nx * j + d.nxny() * k;
+    T val = (T)0;
+    if (G[lf]) {
+        const size_t i2 = (i + 1) >> 1, j2 = (j + 1) >> 1, k2 = (k + 1) >> 1;
+        const int a = (int)((i + 1) & 1), b = (int)((j + 1) & 1), c = (int)((k + 1) & 1);
+        const size_t l2 = i2 + d2.nx * j2 + d2.nxny() * k2, ox = 1, oy = d2.nx, oz = d2.nxny();
+        const T c0 = x2[l2];
+        switch (a + 2 * b + 4 * c) {
+        case 0: val = c0; break;
+        case 1: val = (T)0.5 * (c0 + x2[l2 + ox]); break;
+        case 2: val = (T)0.5 * (c0 + x2[l2 + oy]); break;
+        case 4: val = (T)0.5 * (c0 + x2[l2 + oz]); break;
+        case 3: val = (T)0.25 * (c0 + x2[l2 + ox] + x2[l2 + oy] + x2[l2 + ox + oy]); break;
+        case 5: val = (T)0.25 * (c0 + x2[l2 + ox] + x2[l2 + oz] + x2[l2 + ox + oz]); break;
+        case 6: val = (T)0.25 * (c0 + x2[l2 + oy] + x2[l2 + oz] + x2[l2 + oy + oz]); break;
+        default:
+            val = (T)0.125 * (c0 + x2[l2 + ox] + x2[l2 + oy] + x2[l2 + oz] + x2[l2 + ox + oy] + x2[l2 + ox + oz] +
+                              x2[l2 + oy + oz] + x2[l2 + ox + oy + oz]);
+        }
+    }
+    x[lf] = ADD ? x[lf] + val : val;
+}
+
+template <typename T>
+static qsm_status restrict_(qsm_ctx *ctx, T *x2, const T *x, const uint8_t *G2, const Dims &d2, const Dims &d)
+{
+    const dim3 g = interior_grid3(d2);
+    if (g.x == 0 || g.y == 0 || g.z == 0) return QSM_OK;
+    restrict_k<T><<<g, vox_block(), 0, ctx->stream>>>(x2, x, G2, d2, d);
+    QSM_CUDA(cudaGetLastError());
+    return QSM_OK;
+}
+
+template <typename T>
+static qsm_status prolong(qsm_ctx *ctx, T *x, const T *x2, const uint8_t *G, const Dims &d, const Dims &d2, bool add)
+{
+    if (d2.nx < 3 || d2.ny < 3 || d2.nz < 3) return QSM_OK;
+    const Dims e{2 * (d2.nx - 2), 2 * (d2.ny - 2), 2 * (d2.nz - 2)};
+    const dim3 g = vox_grid(e);
+    if (add) prolong_k<T, true><<<g, vox_block(), 0, ctx->stream>>>(x, x2, G, d, d2);
+    else prolong_k<T, false><<<g, vox_block(), 0, ctx->stream>>>(x, x2, G, d, d2);
+    QSM_CUDA(cudaGetLastError());
+    return QSM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// masks (coarsen_grid_mex.c:52-125, boundary_mask_mex.c:46-132,
+// boundary_mask_l1_mex.c:49-117) -- integer, bit-exact
+// ---------------------------------------------------------------------------
+
+__global__ void coarsen_k(uint8_t *G2, const uint8_t *__restrict__ G, Dims d2, Dims d)
+{
+    const size_t i2 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t j2 = (size_t)blockIdx.y * blockDim.y + threadIdx.y;
+    const size_t k2 = (size_t)blockIdx.z * blockDim.z + threadIdx.z;
+    if (i2 >= d2.nx || j2 >= d2.ny || k2 >= d2.nz) return;
+    const size_t l2 = i2 + d2.nx * j2 + d2.nxny() * k2;
+    if (i2 == 0 || j2 == 0 || k2 == 0 || i2 + 1 >= d2.nx || j2 + 1 >= d2.ny || k2 + 1 >= d2.nz) {
+        G2[l2] = 0;
+        return;
+    }
+    const size_t i = 2 * i2 - 1, j = 2 * j2 - 1, k = 2 * k2 - 1;
+    const size_t nx = d.nx, nxny = d.nxny(), l = i + nx * j + nxny * k;
+    const bool bi = !(i < d.nx - 2), bj = !(j < d.ny - 2), bk = !(k < d.nz - 2);
+    G2[l2] = (uint8_t)(G[l] && (bi || G[l + 1]) && (bj || G[l + nx]) && (bk || G[l + nxny]) &&
+                       (bi || bj || G[l + 1 + nx]) && (bi || bk || G[l + 1 + nxny]) && (bj || bk || G[l + nx + nxny]) &&
+                       (bi || bj || bk || G[l + 1 + nx + nxny]));
+}
+
+// b = G on the outermost interior shell and on 2x2x2 blocks (anchored at odd
+// interior indices) that are not wholly inside G; b = 0 elsewhere.
+__global__ void bmask_b_k(uint8_t *b, const uint8_t *__restrict__ G, Dims d)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t j = (size_t)blockIdx.y * blockDim.y + threadIdx.y;
+    const size_t k = (size_t)blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= d.nx || j >= d.ny || k >= d.nz) return;
+    const size_t nx = d.nx, nxny = d.nxny(), l = i + nx * j + nxny * k;
+    uint8_t val = 0;
+    const bool interior = i >= 1 && j >= 1 && k >= 1 && i + 2 <= d.nx && j + 2 <= d.ny && k + 2 <= d.nz;
+    if (interior && (i == 1 || j == 1 || k == 1 || i == d.nx - 2 || j == d.ny - 2 || k == d.nz - 2)) val = G[l];
+    // the block containing (i,j,k): anchor at the odd index <= each coordinate
+    const size_t ai = (i & 1) ? i : i - 1, aj = (j & 1) ? j : j - 1, ak = (k & 1) ? k : k - 1;
+    if (i >= 1 && j >= 1 && k >= 1 && ai + 2 <= d.nx && aj + 2 <= d.ny && ak + 2 <= d.nz) {
+        const size_t la = ai + nx * aj + nxny * ak;
+        const bool full = G[la] && G[la + 1] && G[la + nx] && G[la + nxny] && G[la + 1 + nx] && G[la + 1 + nxny] &&
+                          G[la + nx + nxny] && G[la + 1 + nx + nxny];
+        if (!full) val = G[l];
+    }
+    b[l] = val;
+}
+
+__global__ void bmask_grow_k(uint8_t *B, const uint8_t *__restrict__ b, const uint8_t *__restrict__ G, Dims d)
+{
+    MG_INTERIOR
+    if (G[l]) B[l] = (uint8_t)(b[l - nxny] || b[l - nx] || b[l - 1] || b[l] || b[l + 1] || b[l + nx] || b[l + nxny]);
+}
+
+static qsm_status boundary_mask(qsm_ctx *ctx, uint8_t *B, const uint8_t *G, const Dims &d, uint8_t *scratch)
+{
+    if (d.nx < 3 || d.ny < 3 || d.nz < 3) return QSM_OK;
+    bmask_b_k<<<vox_grid(d), vox_block(), 0, ctx->stream>>>(scratch, G, d);
+    bmask_grow_k<<<interior_grid3(d), vox_block(), 0, ctx->stream>>>(B, scratch, G, d);
+    QSM_CUDA(cudaGetLastError());
+    return QSM_OK;
+}
+
+__global__ void bmask_l1_init_k(uint8_t *B, uint8_t *GL, const uint8_t *__restrict__ G, Dims d)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t j = (size_t)blockIdx.y * blockDim.y + threadIdx.y;
+    const size_t k = (size_t)blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= d.nx || j >= d.ny || k >= d.nz) return;
+    const size_t nx = d.nx, nxny = d.nxny(), l = i + nx * j + nxny * k;
+    uint8_t v;
+    if (i == 0 || j == 0 || k == 0 || i + 1 == d.nx || j + 1 == d.ny || k + 1 == d.nz)
+        v = G[l];
+    else
+        v = (uint8_t)(G[l] && !(G[l - 1] && G[l + 1] && G[l - nx] && G[l + nx] && G[l - nxny] && G[l + nxny]));
+    B[l] = v;
+    GL[l] = v;
+}
+
+// One band step: a voxel that joins (GL: 0 -> L1+1) cannot change another
+// voxel's test in the same step (that test looks for GL == L1), so the
+// step is order-independent.
+__global__ void bmask_l1_step_k(uint8_t *B, uint8_t *GL, const uint8_t *__restrict__ G, Dims d, size_t L1)
+{
+    const size_t i = L1 + (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t j = L1 + (size_t)blockIdx.y * blockDim.y + threadIdx.y;
+    const size_t k = L1 + (size_t)blockIdx.z * blockDim.z + threadIdx.z;
+    if (i + L1 >= d.nx || j + L1 >= d.ny || k + L1 >= d.nz) return;
+    const size_t nx = d.nx, nxny = d.nxny(), l = i + nx * j + nxny * k;
+    if (G[l] && !GL[l] &&
+        (GL[l - 1] == L1 || GL[l + 1] == L1 || GL[l - nx] == L1 || GL[l + nx] == L1 || GL[l - nxny] == L1 ||
+         GL[l + nxny] == L1)) {
+        B[l] = 1;
+        GL[l] = (uint8_t)(L1 + 1);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// pad / unpad / element-wise BLAS-1
+// ---------------------------------------------------------------------------
+
+template <typename T>
+__global__ void pad_k(T *xp, const T *__restrict__ x, Dims d)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t j = (size_t)blockIdx.y * blockDim.y + threadIdx.y;
+    const size_t k = (size_t)blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= d.nx || j >= d.ny || k >= d.nz) return;
+    xp[(i + 1) + (d.nx + 2) * ((j + 1) + (d.ny + 2) * (k + 1))] = x[i + d.nx * (j + d.ny * k)];
+}
+
+template <typename T>
+__global__ void unpad_k(T *x, const T *__restrict__ xp, Dims d)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t j = (size_t)blockIdx.y * blockDim.y + threadIdx.y;
+    const size_t k = (size_t)blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= d.nx || j >= d.ny || k >= d.nz) return;
+    x[i + d.nx * (j + d.ny * k)] = xp[(i + 1) + (d.nx + 2) * ((j + 1) + (d.ny + 2) * (k + 1))];
+}
+
+__global__ void mask01_pad_k(uint8_t *xp, const uint8_t *__restrict__ x, Dims d)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t j = (size_t)blockIdx.y * blockDim.y + threadIdx.y;
+    const size_t k = (size_t)blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= d.nx || j >= d.ny || k >= d.nz) return;
+    xp[(i + 1) + (d.nx + 2) * ((j + 1) + (d.ny + 2) * (k + 1))] = x[i + d.nx * (j + d.ny * k)] != 0;
+}
+
+// Scalar operands of the BLAS-1 kernels live in device memory:
+// sc[idx] (negated when neg) or the immediate `imm` when idx < 0.
+__device__ __forceinline__ double scal_of(const double *sc, int idx, bool neg, double imm)
+{
+    const double a = idx < 0 ? imm : sc[idx];
+    return neg ? -a : a;
+}
+
+// x = a * x (sscal/dscal semantics; FP32 casts a to float)
+template <typename T>
+__global__ void scal_k(T *x, size_t n, const double *sc, int idx, bool neg, double imm)
+{
+    const T a = (T)scal_of(sc, idx, neg, imm);
+    for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) x[l] = a * x[l];
+}
+
+// y = y + a * x (saxpy/daxpy semantics)
+template <typename T>
+__global__ void axpy_k(T *y, const T *__restrict__ x, size_t n, const double *sc, int idx, bool neg, double imm)
+{
+    const T a = (T)scal_of(sc, idx, neg, imm);
+    for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) y[l] = y[l] + a * x[l];
+}
+
+template <typename T, typename S>
+__global__ void cvt_k(T *o, const S *__restrict__ a, size_t n)
+{
+    for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) o[l] = (T)a[l];
+}
+
+// PCG scalar slots
+enum { S_RHO = 0, S_PREV = 1, S_BETA = 2, S_A = 3, S_PQ = 4, S_RES = 5, S_TMP = 6, S_N = 8 };
+
+__global__ void pcg_beta_k(double *sc)
+{
+    // prevrho = rho (done before the V-cycle), beta = rho / prevrho
+    sc[S_BETA] = sc[S_RHO] / sc[S_PREV];
+}
+__global__ void pcg_prev_k(double *sc) { sc[S_PREV] = sc[S_RHO]; }
+__global__ void pcg_alpha_k(double *sc) { sc[S_A] = sc[S_RHO] / sc[S_PQ]; }
+__global__ void sqrt_k(double *dst, const double *src, bool f32)
+{
+    *dst = f32 ? (double)sqrtf((float)*src) : sqrt(*src);
+}
+
+template <typename T>
+static qsm_status scal(qsm_ctx *ctx, T *x, size_t n, const double *sc, int idx, bool neg, double imm = 0.0)
+{
+    scal_k<T><<<1216, 256, 0, ctx->stream>>>(x, n, sc, idx, neg, imm);
+    QSM_CUDA(cudaGetLastError());
+    return QSM_OK;
+}
+
+template <typename T>
+static qsm_status axpy(qsm_ctx *ctx, T *y, const T *x, size_t n, const double *sc, int idx, bool neg, double imm = 0.0)
+{
+    axpy_k<T><<<1216, 256, 0, ctx->stream>>>(y, x, n, sc, idx, neg, imm);
+    QSM_CUDA(cudaGetLastError());
+    return QSM_OK;
+}
+
+// ||x||_2 in lane order into dst (device); FP32 sums in FP32 then sqrtf.
+template <typename T>
+static qsm_status nrm2(qsm_ctx *ctx, const T *x, size_t n, double *dst)
+{
+    QSM_TRY(lane_dot<T>(ctx, x, x, n, dst));
+    sqrt_k<<<1, 1, 0, ctx->stream>>>(dst, dst, sizeof(T) == 4);
+    QSM_CUDA(cudaGetLastError());
+    return QSM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// coarsest level in one CTA (mgpcg_mex.c:265-275)
+// ---------------------------------------------------------------------------
+
+constexpr int CS_THREADS = 1024;
+
+// Lane-order sum of sq[0..n) (n <= 2^18, so lane t holds sq[t] alone):
+// 256-wide halving per block of lanes, then 1024-wide halving of the block
+// sums (blocks past n contribute +0).  sq is clobbered.
+template <typename T>
+__device__ T cta_lane_sum(T *sq, T *blk, int n)
+{
+    const int tid = threadIdx.x;
+    const int nb = (n + RED_BLOCK - 1) / RED_BLOCK;
+    for (int s = RED_BLOCK / 2; s > 0; s >>= 1) {
+        for (int t = tid; t < nb * RED_BLOCK; t += CS_THREADS) {
+            const int o = t % RED_BLOCK;
+            if (o < s) {
+                const int a = t, b = t + s;
+                const T va = a < n ? sq[a] : (T)0, vb = b < n ? sq[b] : (T)0;
+                if (a < n || b < n) sq[a] = va + vb;  // a < n whenever the sum can be non-zero
+            }
+        }
+        __syncthreads();
+    }
+    for (int b = tid; b < RED_NBLK; b += CS_THREADS) blk[b] = b < nb ? (b * RED_BLOCK < n ? sq[b * RED_BLOCK] : (T)0) : (T)0;
+    __syncthreads();
+    for (int s = RED_NBLK / 2; s > 0; s >>= 1) {
+        for (int t = tid; t < s; t += CS_THREADS) blk[t] = blk[t] + blk[t + s];
+        __syncthreads();
+    }
+    return blk[0];
+}
+
+template <typename T>
+__device__ void cta_gs(T *v, const T *f, const uint8_t *G, GsC<T> c, Dims d, int par, int skip_i)
+{
+    const int nx = (int)d.nx, ny = (int)d.ny, nz = (int)d.nz, nxny = nx * ny;
+    const int hx_ = (nx - 2 + 1) / 2, per_k = hx_ * (ny - 2), tot = per_k * (nz - 2);
+    for (int t = threadIdx.x; t < tot; t += CS_THREADS) {
+        const int k = 1 + t / per_k, rem = t % per_k, j = 1 + rem / hx_, ii = rem % hx_;
+        const int i = 1 + ((1 + j + k + par) & 1) + 2 * ii;
+        if (i + 1 >= nx || i == skip_i) continue;
+        const int l = i + nx * j + nxny * k;
+        if (!G[l]) continue;
+        v[l] = c.hh * (f[l] + (c.hx * (v[l - 1] + v[l + 1]) + c.hy * (v[l - nx] + v[l + nx]) + c.hz * (v[l - nxny] + v[l + nxny])));
+    }
+    __syncthreads();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(CS_THREADS) coarse_solve_k(T *gv, const T *__restrict__ gf, const uint8_t *__restrict__ gG,
+                                                             T *gr, Dims d, GsC<T> gc, LapC<T> lc, double tol,
+                                                             int *outer_out)
+{
+    extern __shared__ unsigned char smraw[];
+    const int n = (int)d.n();
+    T *v = (T *)smraw;
+    T *f = v + n;
+    T *sq = f + n;
+    T *blk = sq + n;
+    uint8_t *G = (uint8_t *)(blk + RED_NBLK);
+    const int tid = threadIdx.x;
+    for (int l = tid; l < n; l += CS_THREADS) {
+        v[l] = gv[l];
+        f[l] = gf[l];
+        G[l] = gG[l];
+        sq[l] = f[l] * f[l];
+    }
+    __syncthreads();
+    // reltol = tol * nrm2(f)
+    const T ff = cta_lane_sum<T>(sq, blk, n);
+    const double fn = sizeof(T) == 4 ? (double)sqrtf((float)ff) : sqrt((double)ff);
+    const double reltol = tol * fn;
+    __syncthreads();
+    const int nx = (int)d.nx, ny = (int)d.ny, nz = (int)d.nz, nxny = nx * ny;
+    const int rpar0 = (nx + 1) & 1;
+    int outer = 0;
+    for (int it = 0; it < 1024; ++it) {
+        outer = it + 1;
+        for (int s = 0; s < 128; ++s) {  // reverse sweeps
+            cta_gs<T>(v, f, G, gc, d, rpar0, -1);
+            cta_gs<T>(v, f, G, gc, d, rpar0 ^ 1, nx - 2);
+        }
+        for (int s = 0; s < 128; ++s) {  // forward sweeps
+            cta_gs<T>(v, f, G, gc, d, 0, -1);
+            cta_gs<T>(v, f, G, gc, d, 1, 1);
+        }
+        // residual into r (global copy kept like the reference) and its norm
+        for (int l = tid; l < n; l += CS_THREADS) {
+            const int k = l / nxny, j = (l / nx) % ny, i = l % nx;
+            T r = gr[l];
+            if (i >= 1 && j >= 1 && k >= 1 && i + 1 < nx && j + 1 < ny && k + 1 < nz && G[l]) {
+                r = f[l] + (lc.hh * v[l] + lc.hx * (v[l - 1] + v[l + 1]) + lc.hy * (v[l - nx] + v[l + nx]) +
+                            lc.hz * (v[l - nxny] + v[l + nxny]));
+                gr[l] = r;
+            }
+            sq[l] = r * r;
+        }
+        __syncthreads();
+        const T rr = cta_lane_sum<T>(sq, blk, n);
+        const double rn = sizeof(T) == 4 ? (double)sqrtf((float)rr) : sqrt((double)rr);
+        __syncthreads();
+        if (rn < reltol) break;
+    }
+    for (int l = tid; l < n; l += CS_THREADS) gv[l] = v[l];
+    if (tid == 0 && outer_out) *outer_out += outer;
+}
+
+// ---------------------------------------------------------------------------
+// hierarchy and drivers (mgpcg_mex.c:126-332, mg_mex.c:94-207, fmg_mex.c:93-212)
+// ---------------------------------------------------------------------------
+
+template <typename T>
+struct Level {
+    Dims d;
+    size_t n;
+    T *v, *f, *r;
+    uint8_t *G, *B;
+    double h[3];
+};
+
+template <typename T>
+struct Hier {
+    int nl;
+    Level<T> L[16];
+    void *blk;
+    uint8_t *scratch;    // n(level 0) bytes for boundary-mask construction
+    int *counters;       // device: coarse outer iterations
+    bool coarse_in_smem;
+    size_t coarse_smem;
+};
+
+static inline size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+template <typename T>
+static qsm_status hier_init(qsm_ctx *ctx, Hier<T> &H, int nl, const Dims &dp, const double *h)
+{
+    memset(&H, 0, sizeof H);
+    H.nl = nl;
+    size_t bytes = 0;
+    Dims d = dp;
+    for (int i = 0; i < nl; ++i) {
+        if (i > 0) d = Dims{((d.nx - 2 + 1) >> 1) + 2, ((d.ny - 2 + 1) >> 1) + 2, ((d.nz - 2 + 1) >> 1) + 2};
+        H.L[i].d = d;
+        H.L[i].n = d.n();
+        for (int q = 0; q < 3; ++q) H.L[i].h[q] = i == 0 ? h[q] : H.L[i - 1].h[q] * 2.0;
+        bytes += 3 * al256(d.n() * sizeof(T)) + 2 * al256(d.n());
+    }
+    bytes += al256(dp.n()) + 256;
+    QSM_TRY(dalloc(ctx, &H.blk, bytes));
+    QSM_CUDA(cudaMemsetAsync(H.blk, 0, bytes, ctx->stream));
+    char *c = (char *)H.blk;
+    for (int i = 0; i < nl; ++i) {
+        const size_t n = H.L[i].n;
+        H.L[i].v = (T *)c; c += al256(n * sizeof(T));
+        H.L[i].f = (T *)c; c += al256(n * sizeof(T));
+        H.L[i].r = (T *)c; c += al256(n * sizeof(T));
+        H.L[i].G = (uint8_t *)c; c += al256(n);
+        H.L[i].B = (uint8_t *)c; c += al256(n);
+    }
+    H.scratch = (uint8_t *)c; c += al256(dp.n());
+    H.counters = (int *)c;
+    const size_t nc = H.L[nl - 1].n;
+    H.coarse_smem = nc * (3 * sizeof(T) + 1) + RED_NBLK * sizeof(T) + 64;
+    int maxsm = 0;
+    cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
+    H.coarse_in_smem = H.coarse_smem <= (size_t)maxsm && nc < (1u << 18);
+    if (H.coarse_in_smem)
+        QSM_CUDA(cudaFuncSetAttribute(coarse_solve_k<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)H.coarse_smem));
+    return QSM_OK;
+}
+
+// masks of every level (mx_init): coarsen, boundary masks; FMG restricts f.
+template <typename T>
+static qsm_status hier_masks(qsm_ctx *ctx, Hier<T> &H, bool restrict_f)
+{
+    for (int i = 0; i < H.nl; ++i) {
+        if (i > 0) {
+            coarsen_k<<<vox_grid(H.L[i].d), vox_block(), 0, ctx->stream>>>(H.L[i].G, H.L[i - 1].G, H.L[i].d, H.L[i - 1].d);
+            QSM_CUDA(cudaGetLastError());
+            if (restrict_f) QSM_TRY(restrict_<T>(ctx, H.L[i].f, H.L[i - 1].f, H.L[i].G, H.L[i].d, H.L[i - 1].d));
+        }
+        QSM_TRY(boundary_mask(ctx, H.L[i].B, H.L[i].G, H.L[i].d, H.scratch));
+    }
+    return QSM_OK;
+}
+
+template <typename T>
+static qsm_status coarse_solve(qsm_ctx *ctx, Hier<T> &H, int l, double *scal_dev)
+{
+    Level<T> &L = H.L[l];
+    const double tol = sizeof(T) == 4 ? 1e-4 : 1e-8;
+    if (H.coarse_in_smem) {
+        coarse_solve_k<T><<<1, CS_THREADS, H.coarse_smem, ctx->stream>>>(L.v, L.f, L.G, L.r, L.d, gs_consts<T>(L.h),
+                                                                        lap_consts<T>(L.h), tol, H.counters);
+        QSM_CUDA(cudaGetLastError());
+        return QSM_OK;
+    }
+    // large coarsest grid (e.g. nlevels = 1): the same loop driven from the host
+    double fn, rn;
+    QSM_TRY(nrm2<T>(ctx, L.f, L.n, scal_dev + S_TMP));
+    QSM_TRY(read_double(ctx, scal_dev + S_TMP, &fn));
+    const double reltol = tol * fn;
+    for (int i = 0; i < 1024; ++i) {
+        QSM_TRY(gauss_seidel<T>(ctx, L.v, L.f, L.G, L.h, L.d, 128, true));
+        QSM_TRY(gauss_seidel<T>(ctx, L.v, L.f, L.G, L.h, L.d, 128, false));
+        QSM_TRY(residual<T>(ctx, L.r, L.f, L.v, L.G, L.h, L.d));
+        QSM_TRY(nrm2<T>(ctx, L.r, L.n, scal_dev + S_TMP));
+        QSM_TRY(read_double(ctx, scal_dev + S_TMP, &rn));
+        if (rn < reltol) break;
+    }
+    return QSM_OK;
+}
+
+template <typename T>
+static qsm_status cycle(qsm_ctx *ctx, Hier<T> &H, int l, int mu, int pre, int post, int nb, double *sc)
+{
+    if (l < H.nl - 1) {
+        Level<T> &L = H.L[l], &C = H.L[l + 1];
+        const int32_t bs = (1 << l) * nb;
+        QSM_TRY(gauss_seidel<T>(ctx, L.v, L.f, L.G, L.h, L.d, pre, true));
+        QSM_TRY(gauss_seidel<T>(ctx, L.v, L.f, L.B, L.h, L.d, bs, true));
+        QSM_TRY(residual<T>(ctx, L.r, L.f, L.v, L.G, L.h, L.d));
+        QSM_TRY(restrict_<T>(ctx, C.f, L.r, C.G, C.d, L.d));
+        QSM_CUDA(cudaMemsetAsync(C.v, 0, C.n * sizeof(T), ctx->stream));
+        for (int i = 0; i < mu; ++i) {
+            QSM_TRY(cycle<T>(ctx, H, l + 1, mu, pre, post, nb, sc));
+            if (l + 1 == H.nl - 1) break;
+        }
+        QSM_TRY(prolong<T>(ctx, L.v, C.v, L.G, L.d, C.d, true));
+        QSM_TRY(gauss_seidel<T>(ctx, L.v, L.f, L.B, L.h, L.d, bs, false));
+        QSM_TRY(gauss_seidel<T>(ctx, L.v, L.f, L.G, L.h, L.d, post, false));
+        return QSM_OK;
+    }
+    return coarse_solve<T>(ctx, H, l, sc);
+}
+
+// mx_mg: tol > 0 checks ||r|| < tol ||f|| before each cycle.
+template <typename T>
+static qsm_status mg_run(qsm_ctx *ctx, Hier<T> &H, double tol, int maxit, int mu, int pre, int post, int nb, double *sc,
+                         int *cycles)
+{
+    int cyc = 0;
+    if (tol > 0.0) {
+        double fn, rn;
+        QSM_TRY(nrm2<T>(ctx, H.L[0].f, H.L[0].n, sc + S_TMP));
+        QSM_TRY(read_double(ctx, sc + S_TMP, &fn));
+        const double reltol = tol * fn;
+        for (int i = 0; i < maxit; ++i) {
+            QSM_TRY(residual<T>(ctx, H.L[0].r, H.L[0].f, H.L[0].v, H.L[0].G, H.L[0].h, H.L[0].d));
+            QSM_TRY(nrm2<T>(ctx, H.L[0].r, H.L[0].n, sc + S_TMP));
+            QSM_TRY(read_double(ctx, sc + S_TMP, &rn));
+            if (rn < reltol) break;
+            QSM_TRY(cycle<T>(ctx, H, 0, mu, pre, post, nb, sc));
+            ++cyc;
+        }
+    } else {
+        for (int i = 0; i < maxit; ++i, ++cyc) QSM_TRY(cycle<T>(ctx, H, 0, mu, pre, post, nb, sc));
+    }
+    if (cycles) *cycles = cyc;
+    return QSM_OK;
+}
+
+template <typename T>
+static qsm_status pad(qsm_ctx *ctx, T *xp, const T *x, const Dims &d)
+{
+    pad_k<T><<<vox_grid(d), vox_block(), 0, ctx->stream>>>(xp, x, d);
+    QSM_CUDA(cudaGetLastError());
+    return QSM_OK;
+}
+
+template <typename T>
+static qsm_status unpad(qsm_ctx *ctx, T *x, const T *xp, const Dims &d)
+{
+    unpad_k<T><<<vox_grid(d), vox_block(), 0, ctx->stream>>>(x, xp, d);
+    QSM_CUDA(cudaGetLastError());
+    return QSM_OK;
+}
+
+static qsm_status pad_mask(qsm_ctx *ctx, uint8_t *Gp, const uint8_t *G, const Dims &d)
+{
+    mask01_pad_k<<<vox_grid(d), vox_block(), 0, ctx->stream>>>(Gp, G, d);
+    QSM_CUDA(cudaGetLastError());
+    return QSM_OK;
+}
+
+// PCG (mx_pcg, mgpcg_mex.c:126-216).  TP = PCG precision, TM = V-cycle
+// precision.  With TP == TM the V-cycle's level-0 v/f are the PCG q/r (as in
+// the reference); with TM = float they are FP32 copies converted per call.
+template <typename TP, typename TM>
+static qsm_status pcg(qsm_ctx *ctx, const Dims &d, const TP *v0, const TP *f, const uint8_t *mask, const double *h,
+                      double tolcg, int32_t maxitcg, double tolmg, int32_t maxitmg, int32_t mu, int32_t npre,
+                      int32_t npost, int32_t nb, int32_t nl, int32_t verbose, TP *vout, qsm_mg_info *info)
+{
+    const Dims dp{d.nx + 2, d.ny + 2, d.nz + 2};
+    const size_t n = dp.n();
+    Hier<TM> H;
+    QSM_TRY(hier_init<TM>(ctx, H, nl, dp, h));
+    const bool same = sizeof(TP) == sizeof(TM);
+    // PCG vectors: x, p (and r, q when the V-cycle runs in another precision)
+    void *pv = nullptr;
+    const size_t vb = al256(n * sizeof(TP));
+    QSM_TRY(dalloc(ctx, &pv, (same ? 2 : 4) * vb + S_N * sizeof(double) + 256));
+    QSM_CUDA(cudaMemsetAsync(pv, 0, (same ? 2 : 4) * vb + S_N * sizeof(double) + 256, ctx->stream));
+    TP *x = (TP *)pv, *p = (TP *)((char *)pv + vb);
+    TP *r = same ? (TP *)H.L[0].f : (TP *)((char *)pv + 2 * vb);
+    TP *q = same ? (TP *)H.L[0].v : (TP *)((char *)pv + 3 * vb);
+    double *sc = (double *)((char *)pv + (same ? 2 : 4) * vb);
+
+    QSM_TRY(pad_mask(ctx, H.L[0].G, mask, d));
+    QSM_TRY(hier_masks<TM>(ctx, H, false));
+    if (v0) QSM_TRY(pad<TP>(ctx, x, v0, d));
+    QSM_TRY(pad<TP>(ctx, r, f, d));
+
+    cudaEvent_t e0, e1;
+    QSM_CUDA(cudaEventCreate(&e0));
+    QSM_CUDA(cudaEventCreate(&e1));
+    QSM_CUDA(cudaEventRecord(e0, ctx->stream));
+    QSM_CUDA(cudaMemsetAsync(sc, 0, S_N * sizeof(double), ctx->stream));
+    // rho = 1 initially (mgpcg_mex.c:135-138)
+    const double one = 1.0;
+    QSM_CUDA(cudaMemcpyAsync(sc + S_RHO, &one, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    double res;
+    QSM_TRY(nrm2<TP>(ctx, r, n, sc + S_RES));
+    QSM_TRY(read_double(ctx, sc + S_RES, &res));
+    const double reltol = tolcg * res;
+    QSM_CUDA(cudaMemsetAsync(q, 0, n * sizeof(TP), ctx->stream));
+    QSM_TRY(lapmg<TP>(ctx, q, x, H.L[0].G, h, dp));
+    QSM_TRY(scal<TP>(ctx, q, n, sc, -1, false, -1.0));
+    QSM_TRY(axpy<TP>(ctx, r, q, n, sc, -1, false, -1.0));
+    QSM_TRY(nrm2<TP>(ctx, r, n, sc + S_RES));
+    QSM_TRY(read_double(ctx, sc + S_RES, &res));
+    if (verbose) printf("\niter%6s\tresidual\n", "");
+    int32_t it = 0;
+    for (int32_t i = 0; i < maxitcg; ++i) {
+        if (res <= reltol) break;
+        pcg_prev_k<<<1, 1, 0, ctx->stream>>>(sc);
+        if (same) {
+            QSM_CUDA(cudaMemsetAsync(q, 0, n * sizeof(TP), ctx->stream));
+        } else {
+            cvt_k<TM, TP><<<1216, 256, 0, ctx->stream>>>(H.L[0].f, r, n);
+            QSM_CUDA(cudaMemsetAsync(H.L[0].v, 0, n * sizeof(TM), ctx->stream));
+        }
+        QSM_TRY(mg_run<TM>(ctx, H, tolmg, maxitmg, mu, npre, npost, nb, sc, nullptr));
+        if (!same) cvt_k<TP, TM><<<1216, 256, 0, ctx->stream>>>(q, H.L[0].v, n);
+        QSM_TRY(lane_dot<TP>(ctx, r, q, n, sc + S_RHO));
+        pcg_beta_k<<<1, 1, 0, ctx->stream>>>(sc);
+        QSM_TRY(scal<TP>(ctx, p, n, sc, S_BETA, false));
+        QSM_TRY(axpy<TP>(ctx, p, q, n, sc, -1, false, 1.0));
+        QSM_TRY(lapmg<TP>(ctx, q, p, H.L[0].G, h, dp));
+        QSM_TRY(scal<TP>(ctx, q, n, sc, -1, false, -1.0));
+        QSM_TRY(lane_dot<TP>(ctx, p, q, n, sc + S_PQ));
+        pcg_alpha_k<<<1, 1, 0, ctx->stream>>>(sc);
+        QSM_TRY(axpy<TP>(ctx, x, p, n, sc, S_A, false));
+        QSM_TRY(axpy<TP>(ctx, r, q, n, sc, S_A, true));
+        QSM_TRY(nrm2<TP>(ctx, r, n, sc + S_RES));
+        QSM_TRY(read_double(ctx, sc + S_RES, &res));
+        if (info && info->resnorm_hist) info->resnorm_hist[i] = res;
+        it += 1;
+        if (verbose) printf("%5d/%d\t%1.3e\n", i, maxitcg, res);
+    }
+    if (verbose) printf("\n");
+    QSM_CUDA(cudaEventRecord(e1, ctx->stream));
+    QSM_TRY(unpad<TP>(ctx, vout, x, d));
+    QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (info) {
+        info->iters = it;
+        info->resnorm = res;
+        info->seconds = ms * 1e-3;
+    }
+    QSM_TRY(dfree(ctx, pv));
+    return dfree(ctx, H.blk);
+}
+
+template <typename T>
+static qsm_status mg_solve(qsm_ctx *ctx, const Dims &d, const T *v0, const T *f, const uint8_t *mask, const double *h,
+                           double tol, int32_t maxit, int32_t mu, int32_t npre, int32_t npost, int32_t nb, int32_t nl,
+                           T *vout, qsm_mg_info *info, bool full)
+{
+    const Dims dp{d.nx + 2, d.ny + 2, d.nz + 2};
+    Hier<T> H;
+    QSM_TRY(hier_init<T>(ctx, H, nl, dp, h));
+    void *sv = nullptr;
+    QSM_TRY(dalloc(ctx, &sv, S_N * sizeof(double)));
+    double *sc = (double *)sv;
+    QSM_TRY(pad_mask(ctx, H.L[0].G, mask, d));
+    QSM_TRY(pad<T>(ctx, H.L[0].f, f, d));
+    if (v0) QSM_TRY(pad<T>(ctx, H.L[0].v, v0, d));
+    QSM_TRY(hier_masks<T>(ctx, H, full));
+    cudaEvent_t e0, e1;
+    QSM_CUDA(cudaEventCreate(&e0));
+    QSM_CUDA(cudaEventCreate(&e1));
+    QSM_CUDA(cudaEventRecord(e0, ctx->stream));
+    int cycles = 0;
+    if (!full) {
+        QSM_TRY(mg_run<T>(ctx, H, tol, maxit, mu, npre, npost, nb, sc, &cycles));
+    } else {
+        // mx_fmg (fmg_mex.c:93-119), unrolled from the coarsest level up
+        for (int l = H.nl - 1; l >= 0; --l) {
+            if (l < H.nl - 1) QSM_TRY(prolong<T>(ctx, H.L[l].v, H.L[l + 1].v, H.L[l].G, H.L[l].d, H.L[l + 1].d, false));
+            if (l == 0 && tol > 0.0) {
+                double fn, rn;
+                QSM_TRY(nrm2<T>(ctx, H.L[0].f, H.L[0].n, sc + S_TMP));
+                QSM_TRY(read_double(ctx, sc + S_TMP, &fn));
+                const double reltol = tol * fn;
+                for (int i = 0; i < 1000 * maxit; ++i) {
+                    QSM_TRY(residual<T>(ctx, H.L[0].r, H.L[0].f, H.L[0].v, H.L[0].G, H.L[0].h, H.L[0].d));
+                    QSM_TRY(nrm2<T>(ctx, H.L[0].r, H.L[0].n, sc + S_TMP));
+                    QSM_TRY(read_double(ctx, sc + S_TMP, &rn));
+                    if (rn < reltol) break;
+                    QSM_TRY(cycle<T>(ctx, H, 0, mu, npre, npost, nb, sc));
+                    ++cycles;
+                }
+            } else {
+                for (int i = 0; i < maxit; ++i) QSM_TRY(cycle<T>(ctx, H, l, mu, npre, npost, nb, sc));
+                if (l == 0) cycles += maxit;
+            }
+        }
+    }
+    QSM_CUDA(cudaEventRecord(e1, ctx->stream));
+    QSM_TRY(unpad<T>(ctx, vout, H.L[0].v, d));
+    QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (info) {
+        info->iters = cycles;
+        info->resnorm = 0.0;
+        info->seconds = ms * 1e-3;
+    }
+    QSM_TRY(dfree(ctx, sv));
+    return dfree(ctx, H.blk);
+}
+
+// ---------------------------------------------------------------------------
+// pairwise masked norm (norm2_mex.c:83-131): leaves of <= 128 elements are
+// summed sequentially in parallel, then combined along the same binary tree
+// by one thread.
+// ---------------------------------------------------------------------------
+
+static void leaves(size_t off, size_t n, std::vector<unsigned long long> &out)
+{
+    if (n <= 128) {
+        out.push_back(((unsigned long long)off << 8) | (unsigned long long)n);
+        return;
+    }
+    const size_t m = n >> 1;
+    leaves(off, m, out);
+    leaves(off + m, n - m, out);
+}
+
+template <typename T>
+__global__ void leaf_sum_k(T *out, const unsigned long long *lv, size_t nleaf, const T *__restrict__ x,
+                           const uint8_t *__restrict__ G)
+{
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nleaf) return;
+    const size_t off = lv[t] >> 8, n = lv[t] & 0xFF;
+    T s = G[off] ? x[off] * x[off] : (T)0;
+    for (size_t i = 1; i < n; ++i)
+        if (G[off + i]) s += x[off + i] * x[off + i];
+    out[t] = s;
+}
+
+template <typename T>
+__device__ T tree_combine(const T *leaf, size_t n, size_t &li)
+{
+    // explicit stack: (n, partial, state)
+    struct Fr { size_t n; T a; int st; };
+    Fr stk[64];
+    int sp = 0;
+    stk[0] = {n, (T)0, 0};
+    T ret = (T)0;
+    while (sp >= 0) {
+        Fr &fr = stk[sp];
+        if (fr.n <= 128) {
+            ret = leaf[li++];
+            --sp;
+            continue;
+        }
+        if (fr.st == 0) {
+            fr.st = 1;
+            stk[sp + 1] = {fr.n >> 1, (T)0, 0};
+            ++sp;
+        } else if (fr.st == 1) {
+            fr.a = ret;
+            fr.st = 2;
+            stk[sp + 1] = {fr.n - (fr.n >> 1), (T)0, 0};
+            ++sp;
+        } else {
+            ret = fr.a + ret;
+            --sp;
+        }
+    }
+    return ret;
+}
+
+template <typename T>
+__global__ void tree_k(double *out, const T *leaf, size_t n)
+{
+    size_t li = 0;
+    const T s = tree_combine<T>(leaf, n, li);
+    *out = sizeof(T) == 4 ? (double)sqrtf((float)s) : sqrt((double)s);
+}
+
+}  // namespace qsm
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+
+using namespace qsm;
+
+static bool bad_dt(qsm_dtype dt) { return dt != QSM_F32 && dt != QSM_F64; }
+
+extern "C" {
+
+qsm_status qsm_gauss_seidel(qsm_ctx *ctx, qsm_dtype dt, const size_t dims[3], void *v, const void *f,
+                            const uint8_t *G, const double vsz[3], int32_t iter, int32_t reverse)
+{
+    if (!ctx || !dims || !v || !f || !G || !vsz) return QSM_ERR_ARG;
+    if (bad_dt(dt)) return QSM_ERR_DTYPE;
+    cudaSetDevice(ctx->device);
+    const Dims d = make_dims(dims);
+    const size_t es = dt == QSM_F32 ? 4 : 8;
+    Staged sv, sf, sg;
+    QSM_TRY(stage_in(ctx, sv, v, d.n() * es, true));
+    QSM_TRY(stage_in(ctx, sf, f, d.n() * es, true));
+    QSM_TRY(stage_in(ctx, sg, G, d.n(), true));
+    qsm_status s = dt == QSM_F32 ? gauss_seidel<float>(ctx, (float *)sv.dev, (const float *)sf.dev, (const uint8_t *)sg.dev, vsz, d, iter, reverse != 0)
+                                 : gauss_seidel<double>(ctx, (double *)sv.dev, (const double *)sf.dev, (const uint8_t *)sg.dev, vsz, d, iter, reverse != 0);
+    QSM_TRY(stage_out(ctx, sv, true));
+    QSM_TRY(stage_out(ctx, sf, false));
+    QSM_TRY(stage_out(ctx, sg, false));
+    QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+    return s;
+}
+
+qsm_status qsm_residual(qsm_ctx *ctx, qsm_dtype dt, const size_t dims[3], void *r, const void *f, const void *x,
+                        const uint8_t *G, const double vsz[3])
+{
+    if (!ctx || !dims || !r || !f || !x || !G || !vsz) return QSM_ERR_ARG;
+    if (bad_dt(dt)) return QSM_ERR_DTYPE;
+    cudaSetDevice(ctx->device);
+    const Dims d = make_dims(dims);
+    const size_t es = dt == QSM_F32 ? 4 : 8;
+    Staged sr, sf, sx, sg;
+    QSM_TRY(stage_in(ctx, sr, r, d.n() * es, true));
+    QSM_TRY(stage_in(ctx, sf, f, d.n() * es, true));
+    QSM_TRY(stage_in(ctx, sx, x, d.n() * es, true));
+    QSM_TRY(stage_in(ctx, sg, G, d.n(), true));
+    qsm_status s = dt == QSM_F32 ? residual<float>(ctx, (float *)sr.dev, (const float *)sf.dev, (const float *)sx.dev, (const uint8_t *)sg.dev, vsz, d)
+                                 : residual<double>(ctx, (double *)sr.dev, (const double *)sf.dev, (const double *)sx.dev, (const uint8_t *)sg.dev, vsz, d);
+    QSM_TRY(stage_out(ctx, sr, true));
+    QSM_TRY(stage_out(ctx, sf, false));
+    QSM_TRY(stage_out(ctx, sx, false));
+    QSM_TRY(stage_out(ctx, sg, false));
+    QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+    return s;
+}
+
+qsm_status qsm_lapmg(qsm_ctx *ctx, qsm_dtype dt, const size_t dims[3], void *d2u, const void *u, const uint8_t *G,
+                     const double vsz[3])
+{
+    if (!ctx || !dims || !d2u || !u || !G || !vsz) return QSM_ERR_ARG;
+    if (bad_dt(dt)) return QSM_ERR_DTYPE;
+    cudaSetDevice(ctx->device);
+    const Dims d = make_dims(dims);
+    const size_t es = dt == QSM_F32 ? 4 : 8;
+    Staged so, su, sg;
+    QSM_TRY(stage_in(ctx, so, d2u, d.n() * es, true));
+    QSM_TRY(stage_in(ctx, su, u, d.n() * es, true));
+    QSM_TRY(stage_in(ctx, sg, G, d.n(), true));
+    qsm_status s = dt == QSM_F32 ? lapmg<float>(ctx, (float *)so.dev, (const float *)su.dev, (const uint8_t *)sg.dev, vsz, d)
+                                 : lapmg<double>(ctx, (double *)so.dev, (const double *)su.dev, (const uint8_t *)sg.dev, vsz, d);
+    QSM_TRY(stage_out(ctx, so, true));
+    QSM_TRY(stage_out(ctx, su, false));
+    QSM_TRY(stage_out(ctx, sg, false));
+    QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+    return s;
+}
+
+static bool transfer_dims_ok(const size_t *d2, const size_t *d)
+{
+    for (int q = 0; q < 3; ++q) {
+        if (d2[q] < 2 || d[q] < 1) return false;
+        if (d2[q] >= 3 && 2 * (d2[q] - 2) > d[q] - 1) return false;
+    }
+    return true;
+}
+
+qsm_status qsm_restrict(qsm_ctx *ctx, qsm_dtype dt, const size_t dims2[3], void *x2, const size_t dims[3],
+                        const void *x, const uint8_t *G2)
+{
+    if (!ctx || !dims2 || !dims || !x2 || !x || !G2) return QSM_ERR_ARG;
+    if (bad_dt(dt)) return QSM_ERR_DTYPE;
+    if (!transfer_dims_ok(dims2, dims)) {
+        set_error(ctx, "coarse grid does not fit the fine grid");
+        return QSM_ERR_DIMS;
+    }
+    cudaSetDevice(ctx->device);
+    const Dims d2 = make_dims(dims2), d = make_dims(dims);
+    const size_t es = dt == QSM_F32 ? 4 : 8;
+    Staged s2, s1, sg;
+    QSM_TRY(stage_in(ctx, s2, x2, d2.n() * es, true));
+    QSM_TRY(stage_in(ctx, s1, x, d.n() * es, true));
+    QSM_TRY(stage_in(ctx, sg, G2, d2.n(), true));
+    qsm_status s = dt == QSM_F32 ? restrict_<float>(ctx, (float *)s2.dev, (const float *)s1.dev, (const uint8_t *)sg.dev, d2, d)
+                                 : restrict_<double>(ctx, (double *)s2.dev, (const double *)s1.dev, (const uint8_t *)sg.dev, d2, d);
+    QSM_TRY(stage_out(ctx, s2, true));
+    QSM_TRY(stage_out(ctx, s1, false));
+    QSM_TRY(stage_out(ctx, sg, false));
+    QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+    return s;
+}
+
+static qsm_status prolong_api(qsm_ctx *ctx, qsm_dtype dt, const size_t dims[3], void *x, const size_t dims2[3],
+                              const void *x2, const uint8_t *G, bool add)
+{
+    if (!ctx || !dims2 || !dims || !x2 || !x || !G) return QSM_ERR_ARG;
+    if (bad_dt(dt)) return QSM_ERR_DTYPE;
+    if (!transfer_dims_ok(dims2, dims)) {
+        set_error(ctx, "coarse grid does not fit the fine grid");
+        return QSM_ERR_DIMS;
+    }
+    cudaSetDevice(ctx->device);
+    const Dims d2 = make_dims(dims2), d = make_dims(dims);
+    const size_t es = dt == QSM_F32 ? 4 : 8;
+    Staged s1, s2, sg;
+    QSM_TRY(stage_in(ctx, s1, x, d.n() * es, true));
+    QSM_TRY(stage_in(ctx, s2, x2, d2.n() * es, true));
+    QSM_TRY(stage_in(ctx, sg, G, d.n(), true));
+    qsm_status s = dt == QSM_F32 ? prolong<float>(ctx, (float *)s1.dev, (const float *)s2.dev, (const uint8_t *)sg.dev, d, d2, add)
+                                 : prolong<double>(ctx, (double *)s1.dev, (const double *)s2.dev, (const uint8_t *)sg.dev, d, d2, add);
+    QSM_TRY(stage_out(ctx, s1, true));
+    QSM_TRY(stage_out(ctx, s2, false));
+    QSM_TRY(stage_out(ctx, sg, false));
+    QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+    return s;
+}
+
+qsm_status qsm_prolong(qsm_ctx *ctx, qsm_dtype dt, const size_t dims[3], void *x, const size_t dims2[3], const void *x2,
+                       const uint8_t *G)
+{
+    return prolong_api(ctx, dt, dims, x, dims2, x2, G, false);
+}
+
+qsm_status qsm_correct(qsm_ctx *ctx, qsm_dtype dt, const size_t dims[3], void *x, const size_t dims2[3], const void *x2,
+                       const uint8_t *G)
+{
+    return prolong_api(ctx, dt, dims, x, dims2, x2, G, true);
+}
+
+qsm_status qsm_coarsen_grid(qsm_ctx *ctx, const size_t dims2[3], uint8_t *G2, const size_t dims[3], const uint8_t *G)
+{
+    if (!ctx || !dims2 || !dims || !G2 || !G) return QSM_ERR_ARG;
+    if (!transfer_dims_ok(dims2, dims)) {
+        set_error(ctx, "coarse grid does not fit the fine grid");
+        return QSM_ERR_DIMS;
+    }
+    cudaSetDevice(ctx->device);
+    const Dims d2 = make_dims(dims2), d = make_dims(dims);
+    Staged s2, s1;
+    QSM_TRY(stage_in(ctx, s2, G2, d2.n(), false));
+    QSM_TRY(stage_in(ctx, s1, G, d.n(), true));
+    coarsen_k<<<vox_grid(d2), vox_block(), 0, ctx->stream>>>((uint8_t *)s2.dev, (const uint8_t *)s1.dev, d2, d);
+    QSM_CUDA(cudaGetLastError());
+    QSM_TRY(stage_out(ctx, s2, true));
+    QSM_TRY(stage_out(ctx, s1, false));
+    QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+    return QSM_OK;
+}
+
+qsm_status qsm_boundary_mask(qsm_ctx *ctx, const size_t dims[3], uint8_t *B, const uint8_t *G)
+{
+    if (!ctx || !dims || !B || !G) return QSM_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    const Dims d = make_dims(dims);
+    Staged sb, sg;
+    QSM_TRY(stage_in(ctx, sb, B, d.n(), true));
+    QSM_TRY(stage_in(ctx, sg, G, d.n(), true));
+    void *scr = nullptr;
+    QSM_TRY(dalloc(ctx, &scr, d.n()));
+    qsm_status s = boundary_mask(ctx, (uint8_t *)sb.dev, (const uint8_t *)sg.dev, d, (uint8_t *)scr);
+    QSM_TRY(dfree(ctx, scr));
+    QSM_TRY(stage_out(ctx, sb, true));
+    QSM_TRY(stage_out(ctx, sg, false));
+    QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+    return s;
+}
+
+qsm_status qsm_boundary_mask_l1(qsm_ctx *ctx, const size_t dims[3], uint8_t *B, const uint8_t *G, uint8_t l1)
+{
+    if (!ctx || !dims || !B || !G) return QSM_ERR_ARG;
+    if (dims[0] == 0 || dims[1] == 0 || dims[2] == 0) return QSM_ERR_DIMS;
+    cudaSetDevice(ctx->device);
+    const Dims d = make_dims(dims);
+    Staged sb, sg;
+    QSM_TRY(stage_in(ctx, sb, B, d.n(), true));
+    QSM_TRY(stage_in(ctx, sg, G, d.n(), true));
+    void *gl = nullptr;
+    QSM_TRY(dalloc(ctx, &gl, d.n()));
+    bmask_l1_init_k<<<vox_grid(d), vox_block(), 0, ctx->stream>>>((uint8_t *)sb.dev, (uint8_t *)gl, (const uint8_t *)sg.dev, d);
+    for (size_t L1 = 1; L1 < l1; ++L1) {
+        if (2 * L1 >= d.nx || 2 * L1 >= d.ny || 2 * L1 >= d.nz) break;
+        const Dims e{d.nx - 2 * L1, d.ny - 2 * L1, d.nz - 2 * L1};
+        bmask_l1_step_k<<<vox_grid(e), vox_block(), 0, ctx->stream>>>((uint8_t *)sb.dev, (uint8_t *)gl, (const uint8_t *)sg.dev, d, L1);
+    }
+    QSM_CUDA(cudaGetLastError());
+    QSM_TRY(dfree(ctx, gl));
+    QSM_TRY(stage_out(ctx, sb, true));
+    QSM_TRY(stage_out(ctx, sg, false));
+    QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+    return QSM_OK;
+}
+
+qsm_status qsm_norm2(qsm_ctx *ctx, qsm_dtype dt, size_t n, const void *x, const uint8_t *G, double *out)
+{
+    if (!ctx || !x || !G || !out) return QSM_ERR_ARG;
+    if (bad_dt(dt)) return QSM_ERR_DTYPE;
+    if (n == 0) return QSM_ERR_DIMS;
+    cudaSetDevice(ctx->device);
+    const size_t es = dt == QSM_F32 ? 4 : 8;
+    std::vector<unsigned long long> lv;
+    leaves(0, n, lv);
+    Staged sx, sg;
+    QSM_TRY(stage_in(ctx, sx, x, n * es, true));
+    QSM_TRY(stage_in(ctx, sg, G, n, true));
+    void *buf = nullptr;
+    QSM_TRY(dalloc(ctx, &buf, lv.size() * (8 + es) + 64));
+    unsigned long long *dl = (unsigned long long *)buf;
+    void *leafv = (char *)buf + lv.size() * 8;
+    QSM_CUDA(cudaMemcpyAsync(dl, lv.data(), lv.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+    const unsigned g = (unsigned)((lv.size() + 255) / 256);
+    if (dt == QSM_F32) {
+        leaf_sum_k<float><<<g, 256, 0, ctx->stream>>>((float *)leafv, dl, lv.size(), (const float *)sx.dev, (const uint8_t *)sg.dev);
+        tree_k<float><<<1, 1, 0, ctx->stream>>>(ctx->red_out, (const float *)leafv, n);
+    } else {
+        leaf_sum_k<double><<<g, 256, 0, ctx->stream>>>((double *)leafv, dl, lv.size(), (const double *)sx.dev, (const uint8_t *)sg.dev);
+        tree_k<double><<<1, 1, 0, ctx->stream>>>(ctx->red_out, (const double *)leafv, n);
+    }
+    QSM_CUDA(cudaGetLastError());
+    double r;
+    QSM_TRY(read_double(ctx, ctx->red_out, &r));
+    QSM_TRY(dfree(ctx, buf));
+    QSM_TRY(stage_out(ctx, sx, false));
+    QSM_TRY(stage_out(ctx, sg, false));
+    QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+    *out = r;
+    return QSM_OK;
+}
+
+static qsm_status solver_checks(qsm_ctx *ctx, const size_t *dims, int32_t nl)
+{
+    if (nl > 16) {
+        set_error(ctx, "nlevels too large. Increase MAX_DEPTH.");
+        return QSM_ERR_DEPTH;
+    }
+    if (nl < 1) {
+        set_error(ctx, "nlevels must be >= 1");
+        return QSM_ERR_ARG;
+    }
+    if (dims[0] == 0 || dims[1] == 0 || dims[2] == 0) return QSM_ERR_DIMS;
+    return QSM_OK;
+}
+
+qsm_status qsm_mgpcg(qsm_ctx *ctx, qsm_dtype dt, const size_t dims[3], const void *v0, const void *f,
+                     const uint8_t *mask, const double vsz[3], double tolcg, int32_t maxitcg, double tolmg,
+                     int32_t maxitmg, int32_t mu, int32_t npre, int32_t npost, int32_t nboundary, int32_t nlevels,
+                     int32_t verbose, void *v_out, qsm_mg_info *info)
+{
+    if (!ctx || !dims || !f || !mask || !vsz || !v_out) return QSM_ERR_ARG;
+    if (bad_dt(dt)) return QSM_ERR_DTYPE;
+    QSM_TRY(solver_checks(ctx, dims, nlevels));
+    cudaSetDevice(ctx->device);
+    const Dims d = make_dims(dims);
+    const size_t es = dt == QSM_F32 ? 4 : 8;
+    Staged s0, sf, sm, so;
+    if (v0) QSM_TRY(stage_in(ctx, s0, v0, d.n() * es, true));
+    QSM_TRY(stage_in(ctx, sf, f, d.n() * es, true));
+    QSM_TRY(stage_in(ctx, sm, mask, d.n(), true));
+    QSM_TRY(stage_in(ctx, so, v_out, d.n() * es, false));
+    qsm_status s;
+    if (dt == QSM_F32)
+        s = pcg<float, float>(ctx, d, v0 ? (const float *)s0.dev : nullptr, (const float *)sf.dev, (const uint8_t *)sm.dev, vsz,
+                              tolcg, maxitcg, tolmg, maxitmg, mu, npre, npost, nboundary, nlevels, verbose, (float *)so.dev, info);
+    else
+        s = pcg<double, double>(ctx, d, v0 ? (const double *)s0.dev : nullptr, (const double *)sf.dev, (const uint8_t *)sm.dev,
+                                vsz, tolcg, maxitcg, tolmg, maxitmg, mu, npre, npost, nboundary, nlevels, verbose,
+                                (double *)so.dev, info);
+    if (v0) QSM_TRY(stage_out(ctx, s0, false));
+    QSM_TRY(stage_out(ctx, sf, false));
+    QSM_TRY(stage_out(ctx, sm, false));
+    QSM_TRY(stage_out(ctx, so, s == QSM_OK));
+    QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+    return s;
+}
+
+qsm_status qsm_mgpcg_mixed(qsm_ctx *ctx, const size_t dims[3], const double *v0, const double *f, const uint8_t *mask,
+                           const double vsz[3], double tolcg, int32_t maxitcg, double tolmg, int32_t maxitmg, int32_t mu,
+                           int32_t npre, int32_t npost, int32_t nboundary, int32_t nlevels, int32_t verbose,
+                           double *v_out, qsm_mg_info *info)
+{
+    if (!ctx || !dims || !f || !mask || !vsz || !v_out) return QSM_ERR_ARG;
+    QSM_TRY(solver_checks(ctx, dims, nlevels));
+    cudaSetDevice(ctx->device);
+    const Dims d = make_dims(dims);
+    Staged s0, sf, sm, so;
+    if (v0) QSM_TRY(stage_in(ctx, s0, v0, d.n() * 8, true));
+    QSM_TRY(stage_in(ctx, sf, f, d.n() * 8, true));
+    QSM_TRY(stage_in(ctx, sm, mask, d.n(), true));
+    QSM_TRY(stage_in(ctx, so, v_out, d.n() * 8, false));
+    qsm_status s = pcg<double, float>(ctx, d, v0 ? (const double *)s0.dev : nullptr, (const double *)sf.dev,
+                                      (const uint8_t *)sm.dev, vsz, tolcg, maxitcg, tolmg, maxitmg, mu, npre, npost,
+                                      nboundary, nlevels, verbose, (double *)so.dev, info);
+    if (v0) QSM_TRY(stage_out(ctx, s0, false));
+    QSM_TRY(stage_out(ctx, sf, false));
+    QSM_TRY(stage_out(ctx, sm, false));
+    QSM_TRY(stage_out(ctx, so, s == QSM_OK));
+    QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+    return s;
+}
+
+static qsm_status mg_api(qsm_ctx *ctx, qsm_dtype dt, const size_t *dims, const void *v0, const void *f, const uint8_t *mask,
+                         const double *vsz, double tol, int32_t maxit, int32_t mu, int32_t npre, int32_t npost,
+                         int32_t nb, int32_t nl, void *v_out, qsm_mg_info *info, bool full)
+{
+    if (!ctx || !dims || !f || !mask || !vsz || !v_out) return QSM_ERR_ARG;
+    if (bad_dt(dt)) return QSM_ERR_DTYPE;
+    QSM_TRY(solver_checks(ctx, dims, nl));
+    cudaSetDevice(ctx->device);
+    const Dims d = make_dims(dims);
+    const size_t es = dt == QSM_F32 ? 4 : 8;
+    Staged s0, sf, sm, so;
+    if (v0) QSM_TRY(stage_in(ctx, s0, v0, d.n() * es, true));
+    QSM_TRY(stage_in(ctx, sf, f, d.n() * es, true));
+    QSM_TRY(stage_in(ctx, sm, mask, d.n(), true));
+    QSM_TRY(stage_in(ctx, so, v_out, d.n() * es, false));
+    qsm_status s;
+    if (dt == QSM_F32)
+        s = mg_solve<float>(ctx, d, v0 ? (const float *)s0.dev : nullptr, (const float *)sf.dev, (const uint8_t *)sm.dev, vsz,
+                            tol, maxit, mu, npre, npost, nb, nl, (float *)so.dev, info, full);
+    else
+        s = mg_solve<double>(ctx, d, v0 ? (const double *)s0.dev : nullptr, (const double *)sf.dev, (const uint8_t *)sm.dev,
+                             vsz, tol, maxit, mu, npre, npost, nb, nl, (double *)so.dev, info, full);
+    if (v0) QSM_TRY(stage_out(ctx, s0, false));
+    QSM_TRY(stage_out(ctx, sf, false));
+    QSM_TRY(stage_out(ctx, sm, false));
+    QSM_TRY(stage_out(ctx, so, s == QSM_OK));
+    QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+    return s;
+}
+
+qsm_status qsm_mg(qsm_ctx *ctx, qsm_dtype dt, const size_t dims[3], const void *v0, const void *f, const uint8_t *mask,
+                  const double vsz[3], double tol, int32_t maxit, int32_t mu, int32_t npre, int32_t npost,
+                  int32_t nboundary, int32_t nlevels, void *v_out, qsm_mg_info *info)
+{
+    return mg_api(ctx, dt, dims, v0, f, mask, vsz, tol, maxit, mu, npre, npost, nboundary, nlevels, v_out, info, false);
+}
+
+qsm_status qsm_fmg(qsm_ctx *ctx, qsm_dtype dt, const size_t dims[3], const void *f, const uint8_t *mask,
+                   const double vsz[3], double tol, int32_t maxit, int32_t mu, int32_t npre, int32_t npost,
+                   int32_t nboundary, int32_t nlevels, void *v_out, qsm_mg_info *info)
+{
+    return mg_api(ctx, dt, dims, nullptr, f, mask, vsz, tol, maxit, mu, npre, npost, nboundary, nlevels, v_out, info, true);
+}
+
+}  // extern "C"

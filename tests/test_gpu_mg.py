@@ -1,0 +1,114 @@
+"""GPU multigrid pieces and Poisson solvers against the reference's golden
+outputs and the oracle: bit-for-bit (inner products follow the documented
+lane order on both sides).  The mixed-precision PCG (FP64 recurrence, FP32
+V-cycle) is checked for its error against the FP64 oracle."""
+import numpy as np
+import pytest
+
+from conftest import bits_equal, first_diff
+
+pytestmark = pytest.mark.gpu
+
+
+def _z(shape, dt):
+    return np.zeros(shape, dtype=dt, order="F")
+
+
+@pytest.mark.parametrize("dt", ("float64", "float32"))
+def test_mg_pieces_golden(gpu_ctx, qsm, golden, dt):
+    g = golden("mg_ops")
+    h = g["h"]
+    for si in range(3):
+        tag = f"s{si}_{dt}"
+        v, f, x, G, G2, c2 = (g[f"{tag}_{k}"] for k in ("v", "f", "x", "G", "G2", "c2"))
+        shape, sz2 = v.shape, c2.shape
+        for rev in (0, 1):
+            vv = v.copy(order="F")
+            qsm.gauss_seidel_mex(vv, f, G, h, 3, rev)
+            assert bits_equal(vv, g[f"{tag}_gs{rev}"]), f"gs{rev} {shape} {first_diff(vv, g[f'{tag}_gs{rev}'])}"
+        r = _z(shape, dt)
+        qsm.residual_mex(r, f, x, G, h)
+        assert bits_equal(r, g[f"{tag}_residual"])
+        r = _z(shape, dt)
+        qsm.lapmg_mex(r, x, G, h)
+        assert bits_equal(r, g[f"{tag}_lapmg"])
+        r2 = _z(sz2, dt)
+        qsm.restrict_mex(r2, x, G2)
+        assert bits_equal(r2, g[f"{tag}_restrict"]), first_diff(r2, g[f"{tag}_restrict"])
+        r = v.copy(order="F")
+        qsm.prolong_mex(r, c2, G)
+        assert bits_equal(r, g[f"{tag}_prolong"]), first_diff(r, g[f"{tag}_prolong"])
+        r = v.copy(order="F")
+        qsm.correct_mex(r, c2, G)
+        assert bits_equal(r, g[f"{tag}_correct"])
+
+
+def test_masks_norm_golden(gpu_ctx, qsm, golden):
+    g = golden("mg_ops")
+    for si in range(3):
+        Gb = g[f"s{si}_Gb"]
+        g2 = np.zeros(g[f"s{si}_coarsen"].shape, np.uint8, order="F")
+        qsm.coarsen_grid_mex(g2, Gb)
+        assert bits_equal(g2, g[f"s{si}_coarsen"])
+        B = np.zeros(Gb.shape, np.uint8, order="F")
+        qsm.boundary_mask_mex(B, Gb)
+        assert bits_equal(B, g[f"s{si}_bmask"])
+        for l1 in (1, 2, 3):
+            B = np.zeros(Gb.shape, np.uint8, order="F")
+            qsm.boundary_mask_l1_mex(B, Gb, l1)
+            assert bits_equal(B, g[f"s{si}_bmask_l1_{l1}"]), f"l1={l1}"
+        assert qsm.norm2_mex(g[f"s{si}_xn"], Gb) == float(g[f"s{si}_norm2"])
+
+
+@pytest.mark.parametrize("dt", ("float64", "float32"))
+def test_solvers_golden(gpu_ctx, qsm, golden, dt):
+    g = golden("solvers")
+    for ci, levels in ((0, (1, 2, 3)), (1, (3,))):
+        tag = f"c{ci}_{dt}"
+        f, m = g[f"{tag}_f"], g[f"{tag}_mask"]
+        v0 = np.zeros(f.shape, dtype=dt, order="F")
+        for nl in levels:
+            a = qsm.mgpcg_mex(v0, f, m, [1, 1, 1], 1e-8, 40, -1.0, 1, 1, 1, 1, 2, nl)
+            assert bits_equal(a, g[f"{tag}_mgpcg{nl}"]), f"mgpcg nl={nl} {first_diff(a, g[f'{tag}_mgpcg{nl}'])}"
+            a = qsm.mgpcg_mex(v0, f, m, [1, 1, 1], 1e-8, 40, 1e-3, 3, 1, 2, 2, 2, nl)
+            assert bits_equal(a, g[f"{tag}_mgpcg_mg{nl}"]), f"mgpcg(mg tol) nl={nl}"
+            a = qsm.mg_mex(v0, f, m, [1, 1, 1], 1e-6, 4, 1, 2, 2, 2, nl)
+            assert bits_equal(a, g[f"{tag}_mg{nl}"]), f"mg nl={nl}"
+            a = qsm.fmg_mex(f, m, [1, 1, 1], -1.0, 2, 1, 2, 2, 2, nl)
+            assert bits_equal(a, g[f"{tag}_fmg{nl}"]), f"fmg nl={nl}"
+
+
+def test_lane_dot(gpu_ctx, qsm, port):
+    rng = np.random.default_rng(11)
+    for n in (1, 1000, 262144, 262145, 3_000_001):
+        x, y = rng.standard_normal(n), rng.standard_normal(n)
+        assert qsm.lane_dot(x, y) == port.lane_dot(x, y)
+        xf, yf = x.astype(np.float32), y.astype(np.float32)
+        assert qsm.lane_dot(xf, yf) == port.lane_dot(xf, yf)
+
+
+def test_mgpcg_lbv_options_vs_oracle(gpu_ctx, qsm, port):
+    """LBV's options (mg maxit 2, npre = npost = 2, 5 levels) on a 62^3 problem."""
+    import qsm_gb300.synthetic as S
+
+    f, m, _ = S.poisson_case((62, 62, 62), 4, semi=(20.0, 28.0))
+    v0 = np.zeros(f.shape, order="F")
+    oi, gi = {}, {}
+    b = port.mgpcg_mex(v0, f, m, [1, 1, 1], 1e-8, 100, -1.0, 2, 1, 2, 2, 2, 4, info=oi)
+    a = qsm.mgpcg_mex(v0, f, m, [1, 1, 1], 1e-8, 100, -1.0, 2, 1, 2, 2, 2, 4, info=gi)
+    assert gi["iters"] == oi["iters"]
+    assert bits_equal(a, b), first_diff(a, b)
+    # mixed: FP64 PCG + FP32 V-cycle, same stopping rule
+    mi = {}
+    c = qsm.mgpcg_mex(v0, f, m, [1, 1, 1], 1e-8, 100, -1.0, 2, 1, 2, 2, 2, 4, mixed=True, info=mi)
+    rel = np.linalg.norm(c - b) / np.linalg.norm(b)
+    assert rel < 1e-6, rel
+    assert mi["iters"] <= oi["iters"] + 3
+
+
+def test_mg_errors(gpu_ctx, qsm):
+    f = np.zeros((8, 8, 8), order="F")
+    with pytest.raises(qsm.QsmError, match="DEPTH"):
+        qsm.mgpcg_mex(f, f, np.ones((8, 8, 8), np.uint8), [1, 1, 1], 1e-8, 5, -1.0, 1, 1, 1, 1, 2, 17)
+    with pytest.raises(qsm.QsmError, match="DIMS"):
+        qsm.restrict_mex(np.zeros((9, 9, 9), order="F"), np.zeros((8, 8, 8), order="F"), np.ones((9, 9, 9), np.uint8))

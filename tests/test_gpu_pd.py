@@ -1,0 +1,120 @@
+"""GPU primal-dual TGV / TV against the oracle and the reference's golden
+outputs.  The plain path is bit-exact in FP64 and FP32; the fused
+mixed-precision path is bit-exact with the reference's FP32 result, and its
+error against the FP64 oracle is within the stated 1e-4 relative L2."""
+import hashlib
+
+import numpy as np
+import pytest
+
+from conftest import bits_equal, first_diff
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("dt", ("float64", "float32"))
+@pytest.mark.parametrize("case", [0, 1, 2])
+def test_pd_golden_plain(gpu_ctx, qsm, golden, dt, case):
+    g = golden("pd")
+    tag = f"c{case}_{dt}"
+    d2f, m, h = g[f"{tag}_d2f"], g[f"{tag}_mask"], g[f"{tag}_h"]
+    lam, alpha, tol, iters = g[f"{tag}_args"]
+    chi = qsm.pd_tgv_mex(d2f, m, h, lam, alpha, tol, int(iters))
+    assert bits_equal(chi, g[f"{tag}_tgv"]), first_diff(chi, g[f"{tag}_tgv"])
+    chi = qsm.pd_tv_mex(d2f, m, h, lam, tol, int(iters))
+    assert bits_equal(chi, g[f"{tag}_tv"]), first_diff(chi, g[f"{tag}_tv"])
+
+
+@pytest.mark.parametrize("case", [0, 1, 2])
+def test_pd_golden_fused_fp32(gpu_ctx, qsm, golden, case):
+    """The fused kernel reproduces the reference's single-precision chi."""
+    g = golden("pd")
+    tag = f"c{case}_float32"
+    d2f, m, h = g[f"{tag}_d2f"], g[f"{tag}_mask"], g[f"{tag}_h"]
+    lam, alpha, tol, iters = g[f"{tag}_args"]
+    chi = qsm.pd_tgv_mex(d2f, m, h, lam, alpha, tol, int(iters), fused=True)
+    assert bits_equal(chi, g[f"{tag}_tgv"]), first_diff(chi, g[f"{tag}_tgv"])
+    chi = qsm.pd_tv_mex(d2f, m, h, lam, tol, int(iters), fused=True)
+    assert bits_equal(chi, g[f"{tag}_tv"]), first_diff(chi, g[f"{tag}_tv"])
+
+
+def test_config0_fp64_bitexact(gpu_ctx, qsm, golden):
+    """64^3, 1000 iterations, FP64 plain path == reference (SHA-256)."""
+    g = golden("config0_tgv")
+    lam, alpha, tol, iters = g["args"]
+    info = {}
+    chi = qsm.pd_tgv_mex(g["d2f"], g["mask"], [1, 1, 1], lam, alpha, tol, int(iters), info=info)
+    assert info["iters"] == 1000
+    digest = np.frombuffer(hashlib.sha256(np.asfortranarray(chi).tobytes(order="F")).digest(), dtype=np.uint8)
+    assert np.array_equal(digest, g["chi_sha256"]), first_diff(chi[::7, ::5, ::3], g["chi_samples"])
+
+
+def test_config0_fused_error(gpu_ctx, qsm, port, golden):
+    """Mixed path (FP32 fused, FP64 input/output) vs the FP64 oracle: rel-L2 <= 1e-4,
+    and bit-identical to the FP32 oracle."""
+    g = golden("config0_tgv")
+    lam, alpha, tol, iters = g["args"]
+    d2f, m = g["d2f"], g["mask"]
+    chi_mixed = qsm.pd_tgv_mex(d2f, m, [1, 1, 1], lam, alpha, tol, int(iters), fused=True)
+    chi64 = port.pd_tgv_mex(d2f, m, [1, 1, 1], lam, alpha, tol, int(iters))
+    rel = np.linalg.norm(chi_mixed - chi64) / np.linalg.norm(chi64)
+    assert rel <= 1e-4, rel
+    chi32 = port.pd_tgv_mex(np.asfortranarray(d2f.astype(np.float32)), m, [1, 1, 1], lam, alpha, tol, int(iters))
+    assert bits_equal(chi_mixed.astype(np.float32), chi32)
+
+
+@pytest.mark.parametrize("shape", [(37, 70, 19), (3, 3, 3), (5, 4, 130)])
+@pytest.mark.parametrize("dt", ("float64", "float32"))
+def test_pd_vs_oracle_shapes(gpu_ctx, qsm, port, shape, dt):
+    rng = np.random.default_rng(7)
+    d2f = np.asfortranarray((rng.standard_normal(shape) * 0.05).astype(dt))
+    m = np.asfortranarray((rng.random(shape) > 0.15).astype(np.uint8))
+    h = [1.0, 0.9, 1.2]
+    for fused in (False, True):
+        if fused and dt == "float64":
+            continue
+        a = qsm.pd_tgv_mex(d2f, m, h, 0.003, 2.0, 0.0, 30, fused=fused)
+        b = port.pd_tgv_mex(d2f, m, h, 0.003, 2.0, 0.0, 30)
+        assert bits_equal(a, b), f"tgv fused={fused} {first_diff(a, b)}"
+        a = qsm.pd_tv_mex(d2f, m, h, 0.003, 0.0, 30, fused=fused)
+        b = port.pd_tv_mex(d2f, m, h, 0.003, 0.0, 30)
+        assert bits_equal(a, b), f"tv fused={fused} {first_diff(a, b)}"
+
+
+def test_pd_stopping_rule(gpu_ctx, qsm, port):
+    """tol > 0: both paths stop at the oracle's iteration (checked every 10)."""
+    rng = np.random.default_rng(3)
+    shape = (24, 22, 20)
+    d2f = np.asfortranarray(rng.standard_normal(shape) * 0.01)
+    g = np.indices(shape).astype(float)
+    m = np.asfortranarray((sum((g[i] - 11) ** 2 for i in range(3)) < 64).astype(np.uint8))
+    oi, pi_, fi = {}, {}, {}
+    b = port.pd_tgv_mex(d2f, m, [1, 1, 1], 0.003, 2.0, 5e-3, 2000, info=oi)
+    a = qsm.pd_tgv_mex(d2f, m, [1, 1, 1], 0.003, 2.0, 5e-3, 2000, info=pi_)
+    assert oi["iters"] < 2000 and oi["iters"] % 10 == 0
+    assert pi_["iters"] == oi["iters"]
+    assert bits_equal(a, b)
+    assert pi_["monitors"] == oi["monitors"]  # lane-order monitors are bit-identical
+    b32 = port.pd_tgv_mex(d2f.astype(np.float32), m, [1, 1, 1], 0.003, 2.0, 5e-3, 2000, info=oi)
+    a32 = qsm.pd_tgv_mex(d2f.astype(np.float32), m, [1, 1, 1], 0.003, 2.0, 5e-3, 2000, fused=True, info=fi)
+    assert fi["iters"] == oi["iters"]
+    assert bits_equal(a32, b32)
+
+
+def test_pd_empty_mask_and_device_tensors(gpu_ctx, qsm):
+    torch = pytest.importorskip("torch")
+    shape = (16, 12, 10)
+    d2f = torch.randn(shape[::-1], dtype=torch.float64, device="cuda")
+    m = torch.zeros(shape[::-1], dtype=torch.uint8, device="cuda")
+    chi = qsm.pd_tgv_mex(d2f, m, [1, 1, 1], 0.003, 2.0, 0.0, 20)
+    assert chi.is_cuda and float(chi.abs().max()) == 0.0
+    chi = qsm.pd_tv_mex(d2f.float(), m, [1, 1, 1], 0.003, 0.0, 20, fused=True)
+    assert float(chi.abs().max()) == 0.0
+
+
+def test_pd_errors(gpu_ctx, qsm):
+    a = np.zeros((0, 4, 4), order="F")
+    with pytest.raises(qsm.QsmError, match="DIMS"):
+        qsm.pd_tgv_mex(a, np.zeros((0, 4, 4), np.uint8), [1, 1, 1], 0.003, 2.0, 0.0, 5)
+    with pytest.raises(TypeError):
+        qsm.pd_tgv_mex(np.zeros((4, 4, 4), np.int32), np.ones((4, 4, 4), np.uint8), [1, 1, 1], 0.003, 2.0, 0.0, 5)
