@@ -121,10 +121,15 @@ class ClockSampler:
                 "samples": len(rows)}
 
 
-def _case():
+def _case(shape=None):
     import qsm_gb300.synthetic as S
 
-    d2f, mask, chi_true = S.config2(seed=2)
+    if shape is None:
+        d2f, mask, _ = S.config2(seed=2)
+    else:  # reduced volume for profiler captures, same recipe scaled
+        semi = tuple(0.42 * n for n in shape)
+        d2f, mask, _ = S.tgv_case(shape, 2, n_ell=60, chi=(-0.15, 0.15), noise=0.02,
+                                  mask=S.ellipsoid_mask(shape, semi))
     return d2f, mask
 
 
@@ -189,7 +194,8 @@ def run_ours(args):
 
     ctx = qsm_gb300.context(local)
     stream = torch.cuda.ExternalStream(qsm_gb300.lib().qsm_ctx_get_stream(ctx.handle))
-    d2f, mask = _case()
+    ITERS = args.iters
+    d2f, mask = _case(tuple(int(v) for v in args.shape.split(",")) if args.shape else None)
     N = d2f.size
     shape_c = d2f.shape[::-1]
     # device-resident inputs (C-order (nz, ny, nx) tensors == MATLAB x-fastest)
@@ -229,6 +235,11 @@ def run_ours(args):
         ms, chi_mixed = timed(mixed_step, args.steps)
     loop_s = info["seconds"]
     value = ws * N * ITERS * args.steps / (ms * 1e-3)
+    if args.only == "fused":
+        if rank == 0:
+            print(json.dumps({"profile_run": True, "value": value, "unit": "voxel-iter/s", "shape": list(d2f.shape),
+                              "iters": ITERS, "loop_s": loop_s}))
+        return
 
     # fused-kernel roofline: average launch time from the library's loop events
     peak, peak_kind = _peaks()
@@ -276,7 +287,7 @@ def run_ours(args):
         if dist is not None:
             dist.destroy_process_group()
         return
-    cb = cpu_baseline(d2f, mask) if ws == 1 or rank == 0 else None
+    cb = cpu_baseline(d2f, mask) if (ws == 1 or rank == 0) and not args.no_cpu else None
     line = {
         "metric": METRIC, "value": value, "unit": "voxel-iter/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -305,6 +316,11 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    # profiling aids (the reported configuration uses the defaults)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--shape", default="", help="nx,ny,nz of a reduced volume (profiler captures)")
+    ap.add_argument("--iters", type=int, default=ITERS, help="iterations per inversion (profiler captures)")
+    ap.add_argument("--only", default="all", choices=["all", "fused"], help="run only the fused arm")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
