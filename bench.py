@@ -238,13 +238,15 @@ def run_ours(args):
     if args.only == "fused":
         if rank == 0:
             print(json.dumps({"profile_run": True, "value": value, "unit": "voxel-iter/s", "shape": list(d2f.shape),
-                              "iters": ITERS, "loop_s": loop_s}))
+                              "iters": ITERS, "loop_s": loop_s, "tile": list(info["tile"]),
+                              "active_voxels": int(info["active_voxels"])}))
         return
 
     # fused-kernel roofline: average launch time from the library's loop events
     peak, peak_kind = _peaks()
     t_launch = loop_s / info["iters"]
-    achieved = ALG_BYTES_FP32 * N / t_launch / 1e9
+    active = int(info["active_voxels"])  # voxels of the launched (mask-holding) tiles
+    achieved = ALG_BYTES_FP32 * active / t_launch / 1e9
 
     # plain FP64 path (reference structure, bit-exact with the reference MEX)
     d2f64_dev = d2f_dev
@@ -298,7 +300,9 @@ def run_ours(args):
         "speedup_vs_fp64": value / value64, "rel_l2_vs_fp64": rel,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": None, "kernel": "tgv_fused_k", "bytes_per_voxel_iter": ALG_BYTES_FP32,
-                     "avg_launch_us": t_launch * 1e6, "peak_source": peak_kind},
+                     "avg_launch_us": t_launch * 1e6, "peak_source": peak_kind, "active_voxels": active,
+                     "tile": list(info["tile"]),
+                     "dense_voxels": N},
         "cpu_baseline": cb,
         "e2e": {"value": e2e_value, "unit": "voxel-iter/s", "h2d_bytes_per_step": int(N * 8 + N),
                 "d2h_bytes_per_step": int(N * 8)},

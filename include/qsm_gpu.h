@@ -79,6 +79,10 @@ typedef struct {
     double monitor_chi;    /* ||chi - chi0|| / ||chi|| at the last check */
     double monitor_eta;    /* ||eta - eta0|| / ||eta|| at the last check */
     double seconds;        /* device time of the iteration loop */
+    uint64_t active_voxels;/* voxels the iteration kernels visit: the interior for the
+                              plain path, the interior of the tiles holding mask voxels
+                              for the fused path (outside them nothing changes) */
+    uint32_t tile[3];      /* fused path: the tile shape used (x, y, z); 0 for the plain path */
 } qsm_pd_info;
 
 /* chi = pd_tgv_mex(d2f, mask, vsz, lam, alpha, tol, maxiter, verbose)

@@ -16,3 +16,4 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]);
 
 void mexErrMsgTxt(const char *msg);
 int mexPrintf(const char *fmt, ...);
+int mexAtExit(void (*fn)(void));

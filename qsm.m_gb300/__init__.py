@@ -161,7 +161,8 @@ def pd_tgv_mex(d2f, mask, vsz, lam, alpha, tol, maxiter, verbose=0, *, fused=Fal
     _ctx(ctx).call("qsm_pd_tgv_fused" if fused else "qsm_pd_tgv", f.dt, f.dims_c(), f.ptr, m.ptr, _h(vsz),
                    float(lam), float(alpha), float(tol), int(maxiter), int(verbose), o.ptr, ctypes.byref(pi))
     if info is not None:
-        info.update(iters=pi.iters, monitors=(pi.monitor_chi, pi.monitor_eta), seconds=pi.seconds)
+        info.update(iters=pi.iters, monitors=(pi.monitor_chi, pi.monitor_eta), seconds=pi.seconds,
+                    active_voxels=pi.active_voxels, tile=tuple(pi.tile))
     return out
 
 
@@ -175,7 +176,8 @@ def pd_tv_mex(d2f, mask, vsz, lam, tol, maxiter, verbose=0, *, fused=False, info
     _ctx(ctx).call("qsm_pd_tv_fused" if fused else "qsm_pd_tv", f.dt, f.dims_c(), f.ptr, m.ptr, _h(vsz),
                    float(lam), float(tol), int(maxiter), int(verbose), o.ptr, ctypes.byref(pi))
     if info is not None:
-        info.update(iters=pi.iters, monitors=(pi.monitor_chi, pi.monitor_eta), seconds=pi.seconds)
+        info.update(iters=pi.iters, monitors=(pi.monitor_chi, pi.monitor_eta), seconds=pi.seconds,
+                    active_voxels=pi.active_voxels, tile=tuple(pi.tile))
     return out
 
 

@@ -42,7 +42,8 @@ class QsmError(RuntimeError):
 
 class PdInfo(ctypes.Structure):
     _fields_ = [("iters", ctypes.c_uint32), ("monitor_chi", ctypes.c_double),
-                ("monitor_eta", ctypes.c_double), ("seconds", ctypes.c_double)]
+                ("monitor_eta", ctypes.c_double), ("seconds", ctypes.c_double),
+                ("active_voxels", ctypes.c_uint64), ("tile", ctypes.c_uint32 * 3)]
 
 
 class MgInfo(ctypes.Structure):

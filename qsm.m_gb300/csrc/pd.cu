@@ -433,6 +433,8 @@ static qsm_status pd_plain(qsm_ctx *ctx, bool tgv, const Dims &d, const void *d2
         info->monitor_chi = hctl.checks ? hctl.n1 : 1.0;
         info->monitor_eta = hctl.checks ? hctl.n2 : 1.0;
         info->seconds = ms * 1e-3;
+        info->active_voxels = (uint64_t)(d.nx > 2 ? d.nx - 2 : 0) * (d.ny > 2 ? d.ny - 2 : 0) * (d.nz > 2 ? d.nz - 2 : 0);
+        info->tile[0] = info->tile[1] = info->tile[2] = 0;
     }
     QSM_TRY(dfree(ctx, blk));
     return QSM_OK;
