@@ -210,6 +210,26 @@ qsm_status qsm_boundary_mask_l1(qsm_ctx *ctx, const size_t dims[3], uint8_t *B,
 qsm_status qsm_norm2(qsm_ctx *ctx, qsm_dtype dtype, size_t n, const void *x,
                      const uint8_t *G, double *out);
 
+/* Largest n accepted by qsm_norm2_noalloc (2^25 elements). */
+#define QSM_NORM2_NOALLOC_MAX_N ((size_t)1 << 25)
+
+/* Masked pairwise 2-norm of qsm_norm2 that allocates no memory.  No
+ * counterpart in the reference: it exists for callers that cannot let a
+ * library allocate device memory (a MATLAB session that hands MEX files its
+ * own gpuArray memory; pipelines that allocate everything once at start-up,
+ * since cudaMalloc/cudaFree synchronise the device mid-run).
+ *   - x (n values of dtype), G (n bytes) and out (one double) are DEVICE
+ *     pointers; the work is enqueued on `stream` (a cudaStream_t, NULL for
+ *     the default stream) and *out is written when it completes;
+ *   - no context is needed; scratch is a fixed device array inside the
+ *     library (4 MiB per GPU that loads it, held until exit), so n must be
+ *     1..QSM_NORM2_NOALLOC_MAX_N, otherwise QSM_ERR_DIMS;
+ *   - all calls share that array: calls that overlap on the GPU race;
+ *   - the first call on each device looks up the array's address with that
+ *     device current; make that first call before any stream capture. */
+qsm_status qsm_norm2_noalloc(qsm_dtype dtype, size_t n, const void *x, const uint8_t *G,
+                             double *out, void *stream);
+
 /* ---------------- Poisson solvers ---------------- */
 
 typedef struct {

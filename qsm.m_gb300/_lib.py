@@ -113,6 +113,8 @@ def lib() -> ctypes.CDLL:
     L.qsm_status_string.restype = ctypes.c_char_p
     L.qsm_abi_version.argtypes = []
     L.qsm_abi_version.restype = ctypes.c_int
+    L.qsm_norm2_noalloc.argtypes = [I32, ctypes.c_size_t, P, U8, P, P]
+    L.qsm_norm2_noalloc.restype = STATUS
     for name, args in SIGNATURES.items():
         fn = getattr(L, name)
         fn.argtypes = [CTX] + args
@@ -125,7 +127,7 @@ def exported_symbols() -> list[str]:
     """Names of every function include/qsm_gpu.h declares."""
     return sorted(list(SIGNATURES) + ["qsm_ctx_create", "qsm_ctx_destroy", "qsm_ctx_set_stream",
                                       "qsm_ctx_get_stream", "qsm_ctx_set_verbose", "qsm_last_error",
-                                      "qsm_status_string", "qsm_abi_version"])
+                                      "qsm_status_string", "qsm_abi_version", "qsm_norm2_noalloc"])
 
 
 class Context:
