@@ -155,6 +155,39 @@ def cpu_baseline(d2f, mask, budget_s=15.0):
             "sample": f"{iters} FP64 iterations of the same 224x224x128 TGV inversion (CPU oracle, OpenMP)"}
 
 
+def poisson_arm(qsm_gb300, ctx, torch):
+    """256^3 MG-PCG Poisson solve with LBV's options (src/bgremove/lbv.m:58-75):
+    FP64 PCG with an FP64 V-cycle (bit-identical to the oracle) beside FP64 PCG
+    with an FP32 V-cycle; iterations, device time, error of the mixed solution
+    against the FP64 one."""
+    import qsm_gb300.synthetic as S
+
+    f, mask, _ = S.config1(seed=1)
+    n = f.size
+    f_dev = torch.from_numpy(np.ascontiguousarray(f.transpose(2, 1, 0))).cuda()
+    m_dev = torch.from_numpy(np.ascontiguousarray(mask.transpose(2, 1, 0))).cuda()
+    v0 = torch.zeros_like(f_dev)
+    maxit = int(np.ceil(np.sqrt(n)))
+    out = {"workload": "MG-PCG 256^3 FP64, rtol 1e-8, mg maxit 2, npre=npost=2, nboundary 2, mu 1, 5 levels"}
+    sols = {}
+    for mixed in (False, True):
+        info = {}
+        qsm_gb300.mgpcg_mex(v0, f_dev, m_dev, [1, 1, 1], 1e-8, maxit, -1.0, 2, 1, 2, 2, 2, 5, mixed=mixed, ctx=ctx)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        v = qsm_gb300.mgpcg_mex(v0, f_dev, m_dev, [1, 1, 1], 1e-8, maxit, -1.0, 2, 1, 2, 2, 2, 5, mixed=mixed,
+                                info=info, ctx=ctx)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        key = "fp32_vcycle" if mixed else "fp64"
+        sols[key] = v
+        out[key] = {"iters": info["iters"], "seconds": info["seconds"], "wall_s": wall, "resnorm": info["resnorm"]}
+    out["rel_l2_fp32_vcycle_vs_fp64"] = float(torch.linalg.vector_norm(sols["fp32_vcycle"] - sols["fp64"]) /
+                                              torch.linalg.vector_norm(sols["fp64"]))
+    out["speedup_fp32_vcycle"] = out["fp64"]["seconds"] / out["fp32_vcycle"]["seconds"]
+    return out
+
+
 def run_reference(args):
     ws, rank, _ = _dist()
     if rank != 0:
@@ -285,6 +318,8 @@ def run_ours(args):
         e2e_s = float(t.item())
     e2e_value = ws * N * ITERS * args.steps / e2e_s
 
+    poisson = None if args.no_poisson else poisson_arm(qsm_gb300, ctx, torch)
+
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
@@ -306,6 +341,7 @@ def run_ours(args):
         "cpu_baseline": cb,
         "e2e": {"value": e2e_value, "unit": "voxel-iter/s", "h2d_bytes_per_step": int(N * 8 + N),
                 "d2h_bytes_per_step": int(N * 8)},
+        "poisson": poisson,
         "gpu_launches": int(args.steps * (ITERS + 5)),
         "clocks": clk.summary(),
     }
@@ -322,6 +358,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     # profiling aids (the reported configuration uses the defaults)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-poisson", action="store_true", help="skip the MG-PCG arm")
     ap.add_argument("--shape", default="", help="nx,ny,nz of a reduced volume (profiler captures)")
     ap.add_argument("--iters", type=int, default=ITERS, help="iterations per inversion (profiler captures)")
     ap.add_argument("--only", default="all", choices=["all", "fused"], help="run only the fused arm")

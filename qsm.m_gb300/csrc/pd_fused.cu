@@ -50,6 +50,7 @@
 
 #include "common.cuh"
 #include "pd.cuh"
+#include "pd_fused.cuh"
 
 namespace qsm {
 
@@ -74,77 +75,6 @@ __global__ void tile_flags_k(uint8_t *flag, const uint8_t *__restrict__ mm, Dims
     }
     any = __syncthreads_or(any);
     if (threadIdx.x == 0) flag[t] = (uint8_t)any;
-}
-
-struct FusedArgs {
-    const float *Pc[5];     // chi^n, eta^n, w1^n, w2^n, w3^n (TV: chi, eta)
-    const float *Pp[5];     // iterate n-1
-    float *Pn[5];           // iterate n+1 (written)
-    const float *Dc[10];    // nu, p1..3, q1..6 at n (TV: nu, p1..3)
-    float *Dn[10];          // at n+1 (written)
-    const float *f;
-    const uint8_t *mm;
-    double *part;           // 4 x gridDim.x partial monitor sums
-    unsigned int *count;
-    PdCtl *ctl;
-    const unsigned *tiles;  // active tile indices (x fastest), one per block
-    unsigned gx, gy;        // tiles per row / per plane
-};
-
-// extragradient point (pd_tgv_mex.c:804-810): x_ = x^n + 1*(x^n - x^(n-1))
-__device__ __forceinline__ float xbar(const float *__restrict__ c, const float *__restrict__ p, size_t l)
-{
-    const float cn = __ldg(c + l);
-    return cn + 1.0f * (cn - __ldg(p + l));
-}
-
-// Monitor sums of one block, then the last block folds the partials in
-// block order and applies the stopping test.  red aliases dynamic shared
-// memory (4 x THREADS doubles) that is free once the primal has finished.
-template <int THREADS>
-__device__ __forceinline__ void monitor_reduce(const FusedArgs &s, double *red, const double *acc, double tol,
-                                               uint32_t it)
-{
-    __shared__ bool last;
-    const int tid = threadIdx.x;
-    const unsigned int nblk = gridDim.x, bid = blockIdx.x;
-    __syncthreads();  // everyone is done reading the dual from shared memory
-#pragma unroll
-    for (int q = 0; q < 4; ++q) red[q * THREADS + tid] = acc[q];
-    __syncthreads();
-    for (int st = THREADS / 2; st > 0; st >>= 1) {
-        if (tid < st)
-#pragma unroll
-            for (int q = 0; q < 4; ++q) red[q * THREADS + tid] += red[q * THREADS + tid + st];
-        __syncthreads();
-    }
-    if (tid == 0) {
-#pragma unroll
-        for (int q = 0; q < 4; ++q) s.part[(size_t)q * nblk + bid] = red[q * THREADS];
-        __threadfence();
-        last = atomicAdd(s.count, 1u) == nblk - 1;
-    }
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        double a = 0.0;
-        for (unsigned int b2 = tid; b2 < nblk; b2 += THREADS) a += __ldcg(s.part + (size_t)q * nblk + b2);
-        red[q * THREADS + tid] = a;
-    }
-    __syncthreads();
-    for (int st = THREADS / 2; st > 0; st >>= 1) {
-        if (tid < st)
-#pragma unroll
-            for (int q = 0; q < 4; ++q) red[q * THREADS + tid] += red[q * THREADS + tid + st];
-        __syncthreads();
-    }
-    if (tid == 0) {
-        double r[4] = {red[0], red[THREADS], red[2 * THREADS], red[3 * THREADS]};
-        pd_finish(s.ctl, r, tol, it);
-        *s.count = 0;
-    }
 }
 
 // ---------------------------------------------------------------------------
@@ -367,14 +297,17 @@ tv_fused_k(FusedArgs s, DualC<float> dc, PrimalC<float> pc, Dims d, double tol, 
 // ---------------------------------------------------------------------------
 
 struct Variant {
-    int tx, ty, tz;
+    int tx, ty, tz;   // tile of interior voxels (z: chunk of planes for the streaming kernel)
+    bool stream;      // pd_stream.cu column-streaming kernel, else the 3-D tile kernel here
 };
-// (x, y, z) tile of interior voxels; threads = tx * ty
-static const Variant kVariants[] = {{32, 8, 4}, {32, 8, 2}, {32, 4, 4}, {32, 16, 2}};
+// 3-D tiles: threads = tx * ty; streaming: threads = (tx + 4) * (ty + 4)
+static const Variant kVariants[] = {{32, 8, 4, false}, {32, 8, 2, false}, {32, 4, 4, false}, {32, 16, 2, false},
+                                    {28, 12, 8, true},   {28, 12, 16, true},  {28, 12, 32, true},  {28, 12, 64, true}};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
 static size_t smem_bytes(const Variant &v, bool tgv)
 {
+    if (v.stream) return stream_smem(v.tx, v.ty, tgv);
     const size_t bn = (size_t)(v.tx + 2) * (v.ty + 2) * (v.tz + 2);
     const size_t dual = (tgv ? 10 : 4) * bn * sizeof(float);
     const size_t red = 4 * (size_t)v.tx * v.ty * sizeof(double);
@@ -408,11 +341,14 @@ static qsm_status launch_variant(qsm_ctx *ctx, int v, bool tgv, bool chk, unsign
                                  const DualC<float> &dc, const PrimalC<float> &pc, const Dims &d, double tol, uint32_t it)
 {
     const size_t sm = smem_bytes(kVariants[v], tgv);
+    if (kVariants[v].stream)
+        return stream_launch(ctx, kVariants[v].tx, kVariants[v].ty, kVariants[v].tz, tgv, chk, nact, s, dc, pc, d, tol, it);
     switch (v) {
     case 0: launch_t<32, 8, 4, 2>(ctx, tgv, chk, nact, s, dc, pc, d, tol, it, sm); break;
     case 1: launch_t<32, 8, 2, 3>(ctx, tgv, chk, nact, s, dc, pc, d, tol, it, sm); break;
     case 2: launch_t<32, 4, 4, 4>(ctx, tgv, chk, nact, s, dc, pc, d, tol, it, sm); break;
-    default: launch_t<32, 16, 2, 1>(ctx, tgv, chk, nact, s, dc, pc, d, tol, it, sm); break;
+    case 3: launch_t<32, 16, 2, 1>(ctx, tgv, chk, nact, s, dc, pc, d, tol, it, sm); break;
+    default: return QSM_ERR_ARG;
     }
     QSM_CUDA(cudaGetLastError());
     return QSM_OK;
@@ -424,7 +360,7 @@ static qsm_status set_all_smem(qsm_ctx *ctx)
     QSM_TRY((set_smem_t<32, 8, 2, 3>(ctx, smem_bytes(kVariants[1], true), smem_bytes(kVariants[1], false))));
     QSM_TRY((set_smem_t<32, 4, 4, 4>(ctx, smem_bytes(kVariants[2], true), smem_bytes(kVariants[2], false))));
     QSM_TRY((set_smem_t<32, 16, 2, 1>(ctx, smem_bytes(kVariants[3], true), smem_bytes(kVariants[3], false))));
-    return QSM_OK;
+    return stream_set_smem(ctx);
 }
 
 // process-wide tuning table: (tgv, nx, ny, nz) -> variant

@@ -36,14 +36,14 @@ def dipole_kernel(shape, vsz=(1.0, 1.0, 1.0), bdir=(0.0, 0.0, 1.0)) -> np.ndarra
 
 def sphere_mask(shape, radius, centre=None) -> np.ndarray:
     c = [(n - 1) / 2 for n in shape] if centre is None else centre
-    g = np.indices(shape, dtype=np.float64)
+    g = np.ogrid[0:shape[0], 0:shape[1], 0:shape[2]]
     r2 = sum((g[i] - c[i]) ** 2 for i in range(3))
     return np.asfortranarray(r2 <= radius * radius).astype(np.uint8, order="F")
 
 
 def ellipsoid_mask(shape, semi, centre=None) -> np.ndarray:
     c = [(n - 1) / 2 for n in shape] if centre is None else centre
-    g = np.indices(shape, dtype=np.float64)
+    g = np.ogrid[0:shape[0], 0:shape[1], 0:shape[2]]
     q = sum(((g[i] - c[i]) / semi[i]) ** 2 for i in range(3))
     return np.asfortranarray(q <= 1.0).astype(np.uint8, order="F")
 
@@ -151,13 +151,17 @@ def poisson_case(shape, seed, *, n_gauss=40, sigma=(5.0, 30.0), semi=(80.0, 120.
     f = -Delta_h u on the mask."""
     rng = np.random.default_rng(seed)
     g = [np.arange(n, dtype=np.float64) for n in shape]
-    u = np.zeros(shape, dtype=np.float64, order="F")
-    for _ in range(n_gauss):
+    ex = [np.empty((n_gauss, n)) for n in shape]
+    for t in range(n_gauss):
         c = [rng.uniform(0, n - 1) for n in shape]
         s = rng.uniform(sigma[0], sigma[1])
         a = rng.uniform(-1.0, 1.0)
-        ex = [np.exp(-((g[i] - c[i]) ** 2) / (2 * s * s)) for i in range(3)]
-        u += a * ex[0][:, None, None] * ex[1][None, :, None] * ex[2][None, None, :]
+        for i in range(3):
+            ex[i][t] = np.exp(-((g[i] - c[i]) ** 2) / (2 * s * s))
+        ex[0][t] *= a
+    # u[i,j,k] = sum_t ex0[t,i] ex1[t,j] ex2[t,k], as one contraction
+    xy = np.einsum("ti,tj->tji", ex[0], ex[1]).reshape(n_gauss, -1)   # (t, j*nx + i)
+    u = np.asfortranarray((ex[2].T @ xy).reshape(shape[2], shape[1], shape[0]).transpose(2, 1, 0))
     ctr = [(n - 1) / 2 + rng.uniform(-jitter, jitter) for n in shape]
     sa = [min(rng.uniform(semi[0], semi[1]), (n - 1) / 2 - 2) for n in shape]
     mask = ellipsoid_mask(shape, sa, centre=ctr)

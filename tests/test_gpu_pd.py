@@ -120,21 +120,24 @@ def test_pd_errors(gpu_ctx, qsm):
         qsm.pd_tgv_mex(np.zeros((4, 4, 4), np.int32), np.ones((4, 4, 4), np.uint8), [1, 1, 1], 0.003, 2.0, 0.0, 5)
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3])
-def test_fused_tile_variants_bitexact(gpu_ctx, qsm, port, variant, monkeypatch):
-    """Every compiled tile shape gives the reference's FP32 result (partial
-    tiles, odd extents, a mask that leaves whole tiles inactive)."""
+@pytest.mark.parametrize("shape", [(77, 41, 23), (70, 30, 75)])
+@pytest.mark.parametrize("variant", list(range(8)))
+def test_fused_tile_variants_bitexact(gpu_ctx, qsm, port, variant, shape, monkeypatch):
+    """Every compiled tile shape (3-D tiles 0-3, z-streaming column tiles 4-7)
+    gives the reference's FP32 result (partial tiles and chunks, odd extents,
+    a mask that leaves whole tiles inactive)."""
     monkeypatch.setenv("QSM_FUSED_VARIANT", str(variant))
     rng = np.random.default_rng(40 + variant)
-    shape = (77, 41, 23)
     d2f = np.asfortranarray((rng.standard_normal(shape) * 0.05).astype(np.float32))
     g = np.indices(shape).astype(float)
-    m = np.asfortranarray((((g[0] - 30) / 25) ** 2 + ((g[1] - 20) / 15) ** 2 + ((g[2] - 11) / 8) ** 2 <= 1).astype(np.uint8))
+    c = [(n - 1) / 2 for n in shape]
+    m = np.asfortranarray(((((g[0] - c[0]) / (0.42 * shape[0])) ** 2 + ((g[1] - c[1]) / (0.42 * shape[1])) ** 2 +
+                            ((g[2] - c[2]) / (0.42 * shape[2])) ** 2) <= 1).astype(np.uint8))
     info = {}
     a = qsm.pd_tgv_mex(d2f, m, [1, 1, 1], 0.003, 2.0, 0.0, 30, fused=True, info=info)
     b = port.pd_tgv_mex(d2f, m, [1, 1, 1], 0.003, 2.0, 0.0, 30)
     assert bits_equal(a, b), first_diff(a, b)
-    assert info["active_voxels"] < 75 * 39 * 21  # inactive tiles were skipped
+    assert info["active_voxels"] < (shape[0] - 2) * (shape[1] - 2) * (shape[2] - 2)  # inactive tiles skipped
     a = qsm.pd_tv_mex(d2f, m, [1, 1, 1], 0.003, 0.0, 30, fused=True)
     b = port.pd_tv_mex(d2f, m, [1, 1, 1], 0.003, 0.0, 30)
     assert bits_equal(a, b), first_diff(a, b)
@@ -152,4 +155,5 @@ def test_autotuned_solve_is_reset(gpu_ctx, qsm, port, monkeypatch):
     a = qsm.pd_tgv_mex(d2f, m, [1, 1, 1], 0.003, 2.0, 0.0, 40, fused=True, info=info)
     b = port.pd_tgv_mex(d2f, m, [1, 1, 1], 0.003, 2.0, 0.0, 40)
     assert bits_equal(a, b), first_diff(a, b)
-    assert tuple(info["tile"]) in {(32, 8, 4), (32, 8, 2), (32, 4, 4), (32, 16, 2)}
+    assert tuple(info["tile"]) in {(32, 8, 4), (32, 8, 2), (32, 4, 4), (32, 16, 2), (28, 12, 8), (28, 12, 16),
+                                   (28, 12, 32), (28, 12, 64)}
