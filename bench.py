@@ -188,6 +188,118 @@ def poisson_arm(qsm_gb300, ctx, torch):
     return out
 
 
+def _batch_case(b, shape):
+    """Volume b of the batched configuration: the 64^3 recipe (12 ellipsoids,
+    semi-axes U[4,16], chi U[-0.1,0.1] ppm, noise 0.01 ppm) at this size, in
+    an inscribed ellipsoidal mask (semi-axes 0.42 x extent)."""
+    import qsm_gb300.synthetic as S
+
+    mask = S.ellipsoid_mask(shape, [0.42 * n for n in shape])
+    d2f, mask, _ = S.tgv_case(shape, 3000 + b, n_ell=12, chi=(-0.1, 0.1), noise=0.01, mask=mask)
+    return np.asfortranarray(d2f.astype(np.float32)), mask
+
+
+def batch_arm(qsm_gb300, ctx, torch, count=32, iters=500):
+    """Batched TV: 32 volumes of uneven size (each axis from {96..256} x
+    {96..256} x {64..176} in steps of 16), lam 1e-3, 500 iterations each,
+    FP32 stencils with FP64 monitors, all volumes in one persistent launch
+    per tile shape and iteration replayed from a captured CUDA graph.  The
+    tile shape per grid size comes from the autotuner (a short batch of the
+    same sizes runs first and fills its table).  Against: the same volumes
+    solved one after another through the one-volume fused call."""
+    import qsm_gb300.synthetic as S
+
+    sizes = S.config3_sizes(seed=3, count=count)
+    t0 = time.perf_counter()
+    cases = [_batch_case(b, s) for b, s in enumerate(sizes)]
+    gen_s = time.perf_counter() - t0
+    d2fs = [torch.from_numpy(np.ascontiguousarray(c[0].transpose(2, 1, 0))).cuda() for c in cases]
+    masks = [torch.from_numpy(np.ascontiguousarray(c[1].transpose(2, 1, 0))).cuda() for c in cases]
+    outs = [torch.empty_like(d) for d in d2fs]
+    qsm_gb300.pd_tv_batch(d2fs, masks, [1, 1, 1], 1e-3, 0.0, 20, ctx=ctx, outs=outs)  # tunes every grid size
+    infos = []
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    qsm_gb300.pd_tv_batch(d2fs, masks, [1, 1, 1], 1e-3, 0.0, iters, ctx=ctx, outs=outs, infos=infos)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    dev_s = infos[0]["seconds"]
+    vox = sum(int(np.prod(s)) for s in sizes)
+    active = sum(int(i["active_voxels"]) for i in infos)
+    # the same volumes one after another (device time of each solve's loop)
+    seq_s, same = 0.0, True
+    for b in range(count):
+        inf = {}
+        chi = qsm_gb300.pd_tv_mex(d2fs[b], masks[b], [1, 1, 1], 1e-3, 0.0, iters, fused=True, info=inf, ctx=ctx)
+        seq_s += inf["seconds"]
+        same = same and bool(torch.equal(chi, outs[b]))
+    tiles = sorted({tuple(i["tile"]) for i in infos})
+    return {"workload": f"{count} TV volumes, sizes from {{96..256}}x{{96..256}}x{{64..176}} step 16, lam 1e-3, "
+                        f"{iters} iterations, tol 0",
+            "voxels": vox, "active_voxels": active, "iterations": iters,
+            "value": vox * iters / dev_s, "unit": "voxel-iter/s",
+            "device_s": dev_s, "wall_s": wall,
+            "hbm_gbs": 70 * active * iters / dev_s / 1e9, "bytes_per_voxel_iter": 70,
+            "one_by_one_device_s": seq_s, "speedup_vs_one_by_one": seq_s / dev_s,
+            "same_as_one_by_one": same, "tiles": [list(t) for t in tiles], "input_generation_s": gen_s,
+            "gpu_launches_per_iteration": len(tiles)}
+
+
+def serve_arm(qsm_gb300, ctx, seconds=30.0, rate=4.0, per_kind=6, budget=160 * 10**9):
+    """Served reconstructions: Poisson arrivals at `rate`/s for `seconds`, 40%
+    Poisson (LBV options), 30% TV (lam 1e-3, 500 iterations), 30% TGV (lam
+    0.003, alpha 2, 1000 iterations), sizes as the batched configuration, a
+    pool of `per_kind` seeded cases per kind, FIFO admission against a
+    160 GB device budget.  Every case is first solved alone (which also tunes
+    its grid size); every served result must equal its case's alone result
+    bit for bit.  Errors: FP32 results against the FP64 plain GPU path (bit-
+    identical to the FP64 oracle)."""
+    from qsm_gb300 import serve
+
+    t0 = time.perf_counter()
+    pool = serve.make_pool(per_kind, seed=4)
+    gen_s = time.perf_counter() - t0
+    alone, err = {}, {k: [] for k in serve.KINDS}
+    for kind in serve.KINDS:
+        for c, case in enumerate(pool[kind]):
+            if kind == "poisson":
+                a = serve.lbv_args(case["shape"])
+                args = (None, case["f"], case["mask"], [1, 1, 1], a["tolcg"], a["maxitcg"], a["tolmg"], a["maxitmg"],
+                        a["mu"], a["npre"], a["npost"], a["nboundary"], a["nlevels"])
+                out = qsm_gb300.mgpcg_mex(*args, mixed=True, ctx=ctx)
+                ref = qsm_gb300.mgpcg_mex(*args, mixed=False, ctx=ctx)
+            elif kind == "tv":
+                a = serve.TV_ARGS
+                out = qsm_gb300.pd_tv_mex(case["d2f"], case["mask"], [1, 1, 1], a["lam"], a["tol"], a["maxiter"],
+                                          fused=True, ctx=ctx)
+                ref = qsm_gb300.pd_tv_mex(case["d2f"].astype(np.float64), case["mask"], [1, 1, 1], a["lam"], a["tol"],
+                                          a["maxiter"], ctx=ctx)
+            else:
+                a = serve.TGV_ARGS
+                out = qsm_gb300.pd_tgv_mex(case["d2f"], case["mask"], [1, 1, 1], a["lam"], a["alpha"], a["tol"],
+                                           a["maxiter"], fused=True, ctx=ctx)
+                ref = qsm_gb300.pd_tgv_mex(case["d2f"].astype(np.float64), case["mask"], [1, 1, 1], a["lam"],
+                                           a["alpha"], a["tol"], a["maxiter"], ctx=ctx)
+            alone[(kind, c)] = serve.digest(out)
+            err[kind].append(float(np.linalg.norm(out.astype(np.float64) - ref) / max(np.linalg.norm(ref), 1e-300)))
+    reqs = serve.arrivals(rate, seconds, seed=4, pool_size=per_kind)
+    with qsm_gb300.Session(budget_bytes=budget, poisson_workers=2, ctx=ctx) as sess:
+        loop = serve.ServeLoop(sess, pool)
+        recs = loop.run(reqs)
+    summ = serve.summarize(recs, seconds)
+    mism = [r.rid for r in recs if r.digest != alone[(r.kind, r.case)]]
+    summ.update({
+        "workload": f"Poisson arrivals {rate}/s for {seconds:.0f} s (seed 4), 40% Poisson / 30% TV / 30% TGV, "
+                    f"sizes from {{96..256}}x{{96..256}}x{{64..176}}, {per_kind} seeded cases per kind, "
+                    f"budget {budget / 1e9:.0f} GB",
+        "arrived": len(reqs), "rejected": len(loop.rejected), "budget_refusals": loop.refusals,
+        "max_resident": loop.max_resident, "max_queue": loop.max_queue, "steps": loop.steps,
+        "same_alone_vs_mix": not mism, "mismatches": mism[:10],
+        "rel_l2_vs_fp64_max": {k: (max(v) if v else None) for k, v in err.items()},
+        "input_generation_s": gen_s})
+    return summ
+
+
 def run_reference(args):
     ws, rank, _ = _dist()
     if rank != 0:
@@ -319,6 +431,8 @@ def run_ours(args):
     e2e_value = ws * N * ITERS * args.steps / e2e_s
 
     poisson = None if args.no_poisson else poisson_arm(qsm_gb300, ctx, torch)
+    batch = None if args.no_batch else batch_arm(qsm_gb300, ctx, torch)
+    served = None if args.no_serve else serve_arm(qsm_gb300, ctx, seconds=args.serve_seconds)
 
     if rank != 0:
         if dist is not None:
@@ -334,7 +448,9 @@ def run_ours(args):
         "fp64_plain": {"value": value64, "unit": "voxel-iter/s", "ms_per_step": ms64 / max(1, min(2, args.steps))},
         "speedup_vs_fp64": value / value64, "rel_l2_vs_fp64": rel,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "kernel": "tgv_fused_k", "bytes_per_voxel_iter": ALG_BYTES_FP32,
+                     "traffic": None,
+                     "kernel": "stream_k<28,12,TGV>" if info["tile"][0] == 28 else "tgv_fused_k<%d,%d,%d>" % tuple(info["tile"]),
+                     "bytes_per_voxel_iter": ALG_BYTES_FP32,
                      "avg_launch_us": t_launch * 1e6, "peak_source": peak_kind, "active_voxels": active,
                      "tile": list(info["tile"]),
                      "dense_voxels": N},
@@ -342,6 +458,8 @@ def run_ours(args):
         "e2e": {"value": e2e_value, "unit": "voxel-iter/s", "h2d_bytes_per_step": int(N * 8 + N),
                 "d2h_bytes_per_step": int(N * 8)},
         "poisson": poisson,
+        "batch": batch,
+        "served": served,
         "gpu_launches": int(args.steps * (ITERS + 5)),
         "clocks": clk.summary(),
     }
@@ -359,6 +477,9 @@ def main():
     # profiling aids (the reported configuration uses the defaults)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-poisson", action="store_true", help="skip the MG-PCG arm")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched TV arm")
+    ap.add_argument("--no-serve", action="store_true", help="skip the served-requests arm")
+    ap.add_argument("--serve-seconds", type=float, default=30.0, help="arrival window of the served arm")
     ap.add_argument("--shape", default="", help="nx,ny,nz of a reduced volume (profiler captures)")
     ap.add_argument("--iters", type=int, default=ITERS, help="iterations per inversion (profiler captures)")
     ap.add_argument("--only", default="all", choices=["all", "fused"], help="run only the fused arm")

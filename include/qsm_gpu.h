@@ -277,6 +277,81 @@ qsm_status qsm_fmg(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3],
                    double tol, int32_t maxit, int32_t mu, int32_t npre, int32_t npost,
                    int32_t nboundary, int32_t nlevels, void *v_out, qsm_mg_info *info);
 
+/* ---------------- many-volume batches and resident sessions ----------------
+ *
+ * No counterpart in the reference: QSM.m solves one volume per MEX call and
+ * loops over echoes/volumes in MATLAB (src/inversion/sstgv.m:68-71,
+ * src/bgremove/lbv.m:97-100).  These entry points keep many solves resident
+ * on one GPU and advance them together.
+ */
+
+/* Batched fused primal-dual solves: `count` volumes, volume b of size
+ * dims[3b..3b+2] with arrays d2f[b], mask[b] and output chi[b] (host or
+ * device, dtype as in qsm_pd_tv_fused).  vsz, lam, alpha, tol and maxiter
+ * are shared.  All volumes advance in one persistent launch per tile shape
+ * and iteration, replayed from a captured CUDA graph; each chi[b] equals
+ * qsm_pd_tv_fused / qsm_pd_tgv_fused of that volume alone.  info may be
+ * NULL or hold `count` entries (seconds = device time of the whole batch). */
+qsm_status qsm_pd_tv_batch(qsm_ctx *ctx, qsm_dtype dtype, uint32_t count, const size_t *dims,
+                           const void *const *d2f, const uint8_t *const *mask, const double vsz[3],
+                           double lam, double tol, uint32_t maxiter, void *const *chi,
+                           qsm_pd_info *info);
+qsm_status qsm_pd_tgv_batch(qsm_ctx *ctx, qsm_dtype dtype, uint32_t count, const size_t *dims,
+                            const void *const *d2f, const uint8_t *const *mask, const double vsz[3],
+                            double lam, double alpha, double tol, uint32_t maxiter,
+                            void *const *chi, qsm_pd_info *info);
+
+/* A session holds admitted solves resident in device memory until their
+ * results are fetched.  Primal-dual solves advance together in
+ * qsm_session_step (the batched launches above); Poisson solves run whole on
+ * `poisson_workers` host threads, each with its own stream, concurrently
+ * with the steps.  Admission: a submit whose footprint
+ * (qsm_session_footprint) does not fit in budget_bytes minus the bytes in
+ * use fails with QSM_ERR_BUSY and changes nothing (budget 0 = no limit).
+ * A session is driven from one host thread. */
+typedef struct qsm_session qsm_session;
+typedef enum {
+    QSM_JOB_TV = 0,        /* pd_tv (fused, FP32 state) */
+    QSM_JOB_TGV = 1,       /* pd_tgv (fused, FP32 state) */
+    QSM_JOB_MGPCG = 2,     /* mgpcg, FP64 PCG + FP32 V-cycle */
+    QSM_JOB_MGPCG_F64 = 3  /* mgpcg, FP64 throughout */
+} qsm_job_kind;
+
+qsm_status qsm_session_create(qsm_ctx *ctx, size_t budget_bytes, int32_t poisson_workers,
+                              qsm_session **session);
+qsm_status qsm_session_destroy(qsm_session *session);
+/* Device bytes a job of this kind and size holds while resident. */
+size_t qsm_session_footprint(int32_t kind, const size_t dims[3], int32_t nlevels);
+size_t qsm_session_bytes_in_use(const qsm_session *session);
+/* Admits a TV (tgv = 0, alpha unused) or TGV solve with pd_tv_mex /
+ * pd_tgv_mex arguments.  Inputs are copied; the call returns once the
+ * solve's state is initialised (and, for a new grid size, its tile shape
+ * tuned). */
+qsm_status qsm_session_submit_pd(qsm_session *session, int32_t tgv, qsm_dtype dtype,
+                                 const size_t dims[3], const void *d2f, const uint8_t *mask,
+                                 const double vsz[3], double lam, double alpha, double tol,
+                                 uint32_t maxiter, uint64_t *id);
+/* Admits an mgpcg_mex solve (FP64 arrays; v0 may be NULL for zeros; mixed
+ * selects the FP32 V-cycle).  It runs on the next free Poisson worker. */
+qsm_status qsm_session_submit_mgpcg(qsm_session *session, const size_t dims[3], const double *v0,
+                                    const double *f, const uint8_t *mask, const double vsz[3],
+                                    double tolcg, int32_t maxitcg, double tolmg, int32_t maxitmg,
+                                    int32_t mu, int32_t npre, int32_t npost, int32_t nboundary,
+                                    int32_t nlevels, int32_t mixed, uint64_t *id);
+/* Advances every running primal-dual solve by `iters` iterations (rounded up
+ * to a multiple of 30; solves stop at their own maxiter or tolerance) and
+ * returns when they are done. */
+qsm_status qsm_session_step(qsm_session *session, uint32_t iters);
+/* *finished = 1 once the job's result can be fetched.  pd_info / mg_info
+ * (either may be NULL) receive the job's statistics. */
+qsm_status qsm_session_poll(qsm_session *session, uint64_t id, int32_t *finished,
+                            qsm_pd_info *pd_info, qsm_mg_info *mg_info);
+/* Copies a finished job's result (chi in the submit dtype, or the FP64
+ * Poisson solution) to `out` (host or device) and releases its state. */
+qsm_status qsm_session_fetch(qsm_session *session, uint64_t id, void *out);
+/* Jobs admitted and not yet finished. */
+uint32_t qsm_session_running(const qsm_session *session);
+
 /* ---------------- lane-order inner product (BLAS-1 replacement) ---------------- */
 
 /* *out = x . y in the library's documented lane order (mx_dot,

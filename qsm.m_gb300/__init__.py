@@ -33,7 +33,8 @@ __all__ = [
     "gradf_adj_mex", "gradb_adj_mex", "gradfm_adj_mex", "gradbm_adj_mex", "gradfp_mex", "gradfp_adj_mex",
     "lap1_mex", "lapw_mex", "gauss_seidel_mex", "residual_mex", "lapmg_mex", "restrict_mex", "prolong_mex",
     "correct_mex", "coarsen_grid_mex", "boundary_mask_mex", "boundary_mask_l1_mex", "norm2_mex", "mgpcg_mex",
-    "mg_mex", "fmg_mex", "lane_dot", "QsmError", "QsmLibraryError", "context", "lib",
+    "mg_mex", "fmg_mex", "lane_dot", "pd_tv_batch", "pd_tgv_batch", "Session", "footprint", "QsmError",
+    "QsmLibraryError", "context", "lib",
 ]
 
 try:  # torch is optional (device-resident callers)
@@ -381,3 +382,150 @@ def fmg_mex(f, mask, vsz, tol, maxit, mu, npre, npost, nboundary, nlevels, *, in
     if info is not None:
         info.update(cycles=mi.iters, seconds=mi.seconds)
     return out
+
+
+# ---------------------------------------------------------------------------
+# many-volume batches and resident sessions (no reference counterpart: QSM.m
+# loops over volumes in MATLAB, src/inversion/sstgv.m:68-71)
+# ---------------------------------------------------------------------------
+
+def _pd_info_dict(pi: PdInfo) -> dict:
+    return dict(iters=pi.iters, monitors=(pi.monitor_chi, pi.monitor_eta), seconds=pi.seconds,
+                active_voxels=pi.active_voxels, tile=tuple(pi.tile))
+
+
+def _pd_batch(name, d2fs, masks, vsz, scalars, *, infos, ctx, outs):
+    fs = [_Arr(a) for a in d2fs]
+    ms = [_Arr(a, mask=True) for a in masks]
+    if len(fs) != len(ms):
+        raise ValueError("one mask per volume")
+    dt = _same(fs) if fs else _lib.QSM_F32
+    outs = [_zeros_like(f) for f in fs] if outs is None else list(outs)
+    os_ = [_Arr(o, writable=True) for o in outs]
+    n = len(fs)
+    dims = (ctypes.c_size_t * (3 * max(n, 1)))(*[x for f in fs for x in f.dims])
+    pf = (ctypes.c_void_p * max(n, 1))(*[f.ptr.value for f in fs])
+    pm = (ctypes.c_void_p * max(n, 1))(*[m.ptr.value for m in ms])
+    po = (ctypes.c_void_p * max(n, 1))(*[o.ptr.value for o in os_])
+    pis = (PdInfo * max(n, 1))()
+    _sync_torch(*(fs + ms + os_))
+    _ctx(ctx).call(name, dt, n, dims, pf, pm, _h(vsz), *scalars[:-1], int(scalars[-1]), po, pis)
+    if infos is not None:
+        infos[:] = [_pd_info_dict(pis[b]) for b in range(n)]
+    return outs
+
+
+def pd_tv_batch(d2fs, masks, vsz, lam, tol, maxiter, *, infos=None, ctx=None, outs=None):
+    """[chi_b] = pd_tv_mex(d2f_b, mask_b, vsz, lam, tol, maxiter) for every volume b, advanced together
+    (fused FP32 path, one persistent launch per tile shape and iteration, CUDA-graph replays)."""
+    return _pd_batch("qsm_pd_tv_batch", d2fs, masks, vsz, (float(lam), float(tol), maxiter), infos=infos, ctx=ctx,
+                     outs=outs)
+
+
+def pd_tgv_batch(d2fs, masks, vsz, lam, alpha, tol, maxiter, *, infos=None, ctx=None, outs=None):
+    """[chi_b] = pd_tgv_mex(d2f_b, mask_b, vsz, lam, alpha, tol, maxiter) for every volume b, advanced together."""
+    return _pd_batch("qsm_pd_tgv_batch", d2fs, masks, vsz, (float(lam), float(alpha), float(tol), maxiter),
+                     infos=infos, ctx=ctx, outs=outs)
+
+
+def footprint(kind: str, dims, nlevels: int = 5) -> int:
+    """Device bytes a resident job holds: kind in {"tv", "tgv", "mgpcg", "mgpcg_f64"}."""
+    k = {"tv": _lib.QSM_JOB_TV, "tgv": _lib.QSM_JOB_TGV, "mgpcg": _lib.QSM_JOB_MGPCG,
+         "mgpcg_f64": _lib.QSM_JOB_MGPCG_F64}[kind]
+    return int(lib().qsm_session_footprint(k, (ctypes.c_size_t * 3)(*dims), int(nlevels)))
+
+
+class Session:
+    """Resident solves on one GPU (qsm_session_* in include/qsm_gpu.h).
+
+    Primal-dual solves advance together in :meth:`step`; Poisson solves run
+    on ``poisson_workers`` worker streams concurrently.  A submit that does
+    not fit in ``budget_bytes`` raises :class:`QsmError` with status
+    QSM_ERR_BUSY and leaves the session unchanged.
+    """
+
+    def __init__(self, budget_bytes: int = 0, poisson_workers: int = 2, *, ctx=None):
+        self.ctx = _ctx(ctx)
+        h = _lib.SES()
+        self._check(lib().qsm_session_create(self.ctx.handle, int(budget_bytes), int(poisson_workers),
+                                             ctypes.byref(h)), "qsm_session_create")
+        self.handle = h
+        self._meta = {}
+
+    def _check(self, st, name):
+        if st != 0:
+            msg = lib().qsm_last_error(self.ctx.handle) or b""
+            raise QsmError(st, f"{name}: {msg.decode(errors='replace')}")
+
+    def submit_pd(self, d2f, mask, vsz, lam, alpha, tol, maxiter, *, tgv=True) -> int:
+        f, m = _Arr(d2f), _Arr(mask, mask=True)
+        _sync_torch(f, m)
+        jid = ctypes.c_uint64()
+        self._check(lib().qsm_session_submit_pd(self.handle, 1 if tgv else 0, f.dt, f.dims_c(), f.ptr, m.ptr,
+                                                _h(vsz), float(lam), float(alpha), float(tol), int(maxiter),
+                                                ctypes.byref(jid)), "qsm_session_submit_pd")
+        self._meta[jid.value] = ("pd", f)
+        return jid.value
+
+    def submit_mgpcg(self, v, f, mask, vsz, tolcg, maxitcg, tolmg, maxitmg, mu, npre, npost, nboundary, nlevels,
+                     *, mixed=True) -> int:
+        fa, m = _Arr(f), _Arr(mask, mask=True)
+        if fa.dt != _lib.QSM_F64:
+            raise TypeError("session Poisson solves take FP64 arrays")
+        va = _Arr(v) if v is not None else None
+        _sync_torch(fa, m)
+        jid = ctypes.c_uint64()
+        self._check(lib().qsm_session_submit_mgpcg(
+            self.handle, fa.dims_c(), va.ptr if va is not None else None, fa.ptr, m.ptr, _h(vsz), float(tolcg),
+            int(maxitcg), float(tolmg), int(maxitmg), int(mu), int(npre), int(npost), int(nboundary), int(nlevels),
+            1 if mixed else 0, ctypes.byref(jid)), "qsm_session_submit_mgpcg")
+        self._meta[jid.value] = ("mg", fa)
+        return jid.value
+
+    def step(self, iters: int = 30):
+        self._check(lib().qsm_session_step(self.handle, int(iters)), "qsm_session_step")
+
+    def poll(self, jid: int):
+        """(finished, info dict)"""
+        fin = ctypes.c_int32()
+        pi, mi = PdInfo(), MgInfo()
+        self._check(lib().qsm_session_poll(self.handle, int(jid), ctypes.byref(fin), ctypes.byref(pi),
+                                           ctypes.byref(mi)), "qsm_session_poll")
+        kind = self._meta[jid][0] if jid in self._meta else "pd"
+        if kind == "pd":
+            return bool(fin.value), _pd_info_dict(pi)
+        return bool(fin.value), dict(iters=mi.iters, resnorm=mi.resnorm, seconds=mi.seconds)
+
+    def fetch(self, jid: int, out=None):
+        if jid not in self._meta:
+            raise QsmError(1, f"qsm_session_fetch: unknown session job id {jid}")
+        kind, a = self._meta[jid]
+        out = _zeros_like(a) if out is None else out
+        o = _Arr(out, writable=True)
+        _sync_torch(o)
+        self._check(lib().qsm_session_fetch(self.handle, int(jid), o.ptr), "qsm_session_fetch")
+        del self._meta[jid]
+        return out
+
+    def running(self) -> int:
+        return int(lib().qsm_session_running(self.handle))
+
+    def bytes_in_use(self) -> int:
+        return int(lib().qsm_session_bytes_in_use(self.handle))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().qsm_session_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

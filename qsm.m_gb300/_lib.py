@@ -82,7 +82,30 @@ SIGNATURES = {
     "qsm_mgpcg_mixed": [SZ3, P, P, U8, D3, DBL, I32, DBL, I32, I32, I32, I32, I32, I32, I32, P, ctypes.POINTER(MgInfo)],
     "qsm_mg": [I32, SZ3, P, P, U8, D3, DBL, I32, I32, I32, I32, I32, I32, P, ctypes.POINTER(MgInfo)],
     "qsm_fmg": [I32, SZ3, P, U8, D3, DBL, I32, I32, I32, I32, I32, I32, P, ctypes.POINTER(MgInfo)],
+    # count volumes: dims (size_t[3*count]), arrays of d2f / mask / chi pointers
+    "qsm_pd_tv_batch": [I32, U32, P, P, P, D3, DBL, DBL, U32, P, P],
+    "qsm_pd_tgv_batch": [I32, U32, P, P, P, D3, DBL, DBL, DBL, U32, P, P],
 }
+
+SES = ctypes.c_void_p
+U64P = ctypes.POINTER(ctypes.c_uint64)
+# session functions: name -> (argtypes, restype)
+SESSION_SIGNATURES = {
+    "qsm_session_create": ([CTX, ctypes.c_size_t, I32, ctypes.POINTER(SES)], STATUS),
+    "qsm_session_destroy": ([SES], STATUS),
+    "qsm_session_footprint": ([I32, SZ3, I32], ctypes.c_size_t),
+    "qsm_session_bytes_in_use": ([SES], ctypes.c_size_t),
+    "qsm_session_submit_pd": ([SES, I32, I32, SZ3, P, U8, D3, DBL, DBL, DBL, U32, U64P], STATUS),
+    "qsm_session_submit_mgpcg": ([SES, SZ3, P, P, U8, D3, DBL, I32, DBL, I32, I32, I32, I32, I32, I32, I32, U64P],
+                                 STATUS),
+    "qsm_session_step": ([SES, U32], STATUS),
+    "qsm_session_poll": ([SES, ctypes.c_uint64, ctypes.POINTER(I32), ctypes.POINTER(PdInfo), ctypes.POINTER(MgInfo)],
+                         STATUS),
+    "qsm_session_fetch": ([SES, ctypes.c_uint64, P], STATUS),
+    "qsm_session_running": ([SES], U32),
+}
+
+QSM_JOB_TV, QSM_JOB_TGV, QSM_JOB_MGPCG, QSM_JOB_MGPCG_F64 = 0, 1, 2, 3
 
 _lib = None
 
@@ -119,13 +142,17 @@ def lib() -> ctypes.CDLL:
         fn = getattr(L, name)
         fn.argtypes = [CTX] + args
         fn.restype = STATUS
+    for name, (args, res) in SESSION_SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
     _lib = L
     return L
 
 
 def exported_symbols() -> list[str]:
     """Names of every function include/qsm_gpu.h declares."""
-    return sorted(list(SIGNATURES) + ["qsm_ctx_create", "qsm_ctx_destroy", "qsm_ctx_set_stream",
+    return sorted(list(SIGNATURES) + list(SESSION_SIGNATURES) + ["qsm_ctx_create", "qsm_ctx_destroy", "qsm_ctx_set_stream",
                                       "qsm_ctx_get_stream", "qsm_ctx_set_verbose", "qsm_last_error",
                                       "qsm_status_string", "qsm_abi_version", "qsm_norm2_noalloc"])
 

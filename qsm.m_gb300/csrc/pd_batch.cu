@@ -1,0 +1,847 @@
+// Resident many-volume sessions: batched primal-dual TV/TGV and concurrent
+// MG-PCG Poisson solves on one GPU.
+//
+// The reference solves one volume per MEX call (echo and volume loops are
+// serial MATLAB: src/inversion/sstgv.m:68-71, src/bgremove/lbv.m:97-100).
+// Here a session keeps every admitted solve's state resident in HBM and
+// advances all primal-dual solves together:
+//
+//   * one persistent kernel per (tile variant, TV|TGV) group and iteration
+//     walks a work list of (volume, active tile) items that spans every
+//     resident volume of that group; CTAs take items from a device counter
+//     (dynamic load balance over uneven volumes) and run the same tile /
+//     column body as the one-volume fused kernels (pd_tile.cuh), so each
+//     volume's chi is bit-identical to its one-volume fused solve;
+//   * per-volume descriptors (state pointers for each of the 6 buffer
+//     rotations, constants, iteration window, monitor scratch) live in a
+//     device table; a CTA copies its item's descriptor into shared memory;
+//   * 30 iterations (the period of the 3-buffer primal / 2-buffer dual
+//     rotation and of the every-10th-iteration monitor) are captured once
+//     into a CUDA graph with one launch chain per group on its own stream
+//     (groups touch disjoint volumes, so their chains overlap), then
+//     replayed; the graph is re-captured only when the resident set changes;
+//   * a volume admitted between replays starts at the session's iteration
+//     base (a multiple of 30), so its buffer phase and monitor iterations
+//     are the graph's; a volume whose monitors met tol, or that reached its
+//     maxiter, is skipped by every later item of its own;
+//   * Poisson solves (mgpcg) run whole on worker threads, each with its own
+//     stream and context, concurrently with the primal-dual replays.
+//
+// Admission is by device footprint against the session's byte budget.
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <atomic>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "common.cuh"
+#include "pd.cuh"
+#include "pd_fused.cuh"
+#include "pd_tile.cuh"
+
+namespace qsm {
+
+constexpr uint32_t kGraphIters = 30;  // lcm(3, 2, 10)
+constexpr int kPhases = 6;            // lcm(3, 2)
+
+// One volume, one buffer rotation.
+struct BatchVol {
+    FusedArgs a;        // tiles unused; part/count/ctl are the volume's own
+    DualC<float> dc;
+    PrimalC<float> pc;
+    Dims d;
+    double tol;
+    uint32_t maxiter;   // iterations of this solve
+    uint32_t start;     // session iteration at which it started (multiple of kGraphIters)
+    uint32_t item0;     // first work item of this volume in its group's list
+    uint32_t nitems;    // its active tiles
+};
+
+// Persistent loop over the work items of one group.  items[w] = (volume,
+// tile); sched[0] hands out items, sched[1] counts exited CTAs (the last
+// one re-arms both for the next launch).
+template <int THREADS, typename Work>
+__device__ __forceinline__ void batch_loop(const BatchVol *__restrict__ vols, const uint2 *__restrict__ items,
+                                           uint32_t nitems, uint32_t g, unsigned *sched, bool check, double *red,
+                                           BatchVol &sv, Work work)
+{
+    __shared__ unsigned sw;
+    __shared__ int sskip;
+    uint32_t loaded = 0xffffffffu;
+    for (;;) {
+        __syncthreads();  // the previous item is done with shared memory
+        if (threadIdx.x == 0) sw = atomicAdd(sched, 1u);
+        __syncthreads();
+        const unsigned w = sw;
+        if (w >= nitems) break;
+        const uint2 it = items[w];
+        if (it.x != loaded) {
+            const uint32_t *src = (const uint32_t *)(vols + it.x);
+            uint32_t *dst = (uint32_t *)&sv;
+            for (int k = threadIdx.x; k < (int)(sizeof(BatchVol) / 4); k += THREADS) dst[k] = src[k];
+            loaded = it.x;
+            __syncthreads();
+        }
+        if (threadIdx.x == 0)
+            sskip = (g - sv.start >= sv.maxiter) || *(volatile uint32_t *)&sv.a.ctl->done;
+        __syncthreads();
+        if (sskip) continue;
+        double acc[4] = {0.0, 0.0, 0.0, 0.0};
+        work(sv, it.y, acc);
+        if (check)
+            monitor_fold<THREADS>(sv.a.part, sv.a.count, sv.a.ctl, sv.nitems, w - sv.item0, red, acc, sv.tol,
+                                  g - sv.start + 1);
+    }
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(sched + 1, 1u) == gridDim.x - 1) {
+            sched[0] = 0;
+            sched[1] = 0;
+        }
+    }
+}
+
+template <int TX, int TY, int TZ, int MINB, bool TGV, bool CHECK>
+__global__ void __launch_bounds__(TX * TY, MINB)
+batch_tile_k(const BatchVol *vols, const uint2 *items, uint32_t nitems, const uint32_t *gbase, uint32_t i,
+             unsigned *sched)
+{
+    extern __shared__ double smem_raw[];
+    __shared__ BatchVol sv;
+    const uint32_t g = *gbase + i;
+    batch_loop<TX * TY>(vols, items, nitems, g, sched, CHECK, smem_raw, sv,
+                        [&](const BatchVol &v, unsigned tile, double *acc) {
+                            if (TGV) tile_tgv<TX, TY, TZ>(v.a, v.dc, v.pc, v.d, tile, CHECK, (float *)smem_raw, acc);
+                            else tile_tv<TX, TY, TZ>(v.a, v.dc, v.pc, v.d, tile, CHECK, (float *)smem_raw, acc);
+                        });
+}
+
+template <int TX, int TY, bool TGV, bool CHECK>
+__global__ void __launch_bounds__((TX + 4) * (TY + 4), 1)
+batch_column_k(const BatchVol *vols, const uint2 *items, uint32_t nitems, const uint32_t *gbase, uint32_t i,
+               unsigned *sched, int cz)
+{
+    extern __shared__ double smem_raw[];
+    __shared__ BatchVol sv;
+    const uint32_t g = *gbase + i;
+    batch_loop<(TX + 4) * (TY + 4)>(vols, items, nitems, g, sched, CHECK, smem_raw, sv,
+                                    [&](const BatchVol &v, unsigned tile, double *acc) {
+                                        column_pd<TX, TY, TGV>(v.a, v.dc, v.pc, v.d, cz, tile, CHECK,
+                                                               (float *)smem_raw, acc);
+                                    });
+}
+
+__global__ void advance_k(uint32_t *gbase, uint32_t n) { *gbase += n; }
+
+// ---------------------------------------------------------------------------
+// kernel table
+// ---------------------------------------------------------------------------
+
+using BatchFn = void (*)(const BatchVol *, const uint2 *, uint32_t, const uint32_t *, uint32_t, unsigned *);
+using ColumnFn = void (*)(const BatchVol *, const uint2 *, uint32_t, const uint32_t *, uint32_t, unsigned *, int);
+
+struct BatchKernel {
+    const void *fn[2];  // [check]
+    bool column;
+};
+
+template <int TX, int TY, int TZ, int MINB, bool TGV>
+static BatchKernel tile_kernel()
+{
+    return {{(const void *)batch_tile_k<TX, TY, TZ, MINB, TGV, false>, (const void *)batch_tile_k<TX, TY, TZ, MINB, TGV, true>},
+            false};
+}
+
+template <int TX, int TY, bool TGV>
+static BatchKernel column_kernel()
+{
+    return {{(const void *)batch_column_k<TX, TY, TGV, false>, (const void *)batch_column_k<TX, TY, TGV, true>}, true};
+}
+
+// Kernels of variant v (the same tile shapes as the one-volume path).
+static BatchKernel batch_kernel(int v, bool tgv)
+{
+    switch (v) {
+    case 0: return tgv ? tile_kernel<32, 8, 4, 2, true>() : tile_kernel<32, 8, 4, 2, false>();
+    case 1: return tgv ? tile_kernel<32, 8, 2, 3, true>() : tile_kernel<32, 8, 2, 3, false>();
+    case 2: return tgv ? tile_kernel<32, 4, 4, 4, true>() : tile_kernel<32, 4, 4, 4, false>();
+    case 3: return tgv ? tile_kernel<32, 16, 2, 1, true>() : tile_kernel<32, 16, 2, 1, false>();
+    default: return tgv ? column_kernel<28, 12, true>() : column_kernel<28, 12, false>();
+    }
+}
+
+}  // namespace qsm
+
+using namespace qsm;
+
+// ---------------------------------------------------------------------------
+// session
+// ---------------------------------------------------------------------------
+
+namespace {
+
+struct PdJob {
+    uint64_t id = 0;
+    PdVolume v;
+    qsm_dtype dt = QSM_F32;
+    double tol = 0.0;
+    uint32_t maxiter = 0, start = 0, iters = 0;
+    bool finished = false;
+    PdCtl ctl{};
+    double seconds = 0.0;
+    size_t bytes = 0;
+    std::vector<unsigned> tiles;  // active tiles of the chosen variant (host copy)
+};
+
+struct MgJob {
+    uint64_t id = 0;
+    Dims d{};
+    size_t dims[3] = {0, 0, 0};
+    double vsz[3] = {1, 1, 1};
+    double tolcg = 0, tolmg = 0;
+    int32_t maxitcg = 0, maxitmg = 0, mu = 1, npre = 1, npost = 1, nb = 0, nl = 1;
+    bool mixed = true, has_v0 = false;
+    void *blk = nullptr;  // device: v0 | f | out | mask
+    double *v0 = nullptr, *f = nullptr, *out = nullptr;
+    uint8_t *mask = nullptr;
+    std::atomic<int> state{0};  // 0 queued, 1 running, 2 finished
+    qsm_status st = QSM_OK;
+    char err[256] = {0};
+    qsm_mg_info info{};
+    size_t bytes = 0;
+};
+
+struct Group {
+    int var = 0;
+    bool tgv = false;
+    std::vector<uint2> items;
+    uint2 *d_items = nullptr;     // inside the session's item buffer
+    unsigned *d_sched = nullptr;  // 2 counters
+    unsigned grid = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+};
+
+}  // namespace
+
+struct qsm_session {
+    qsm_ctx *ctx = nullptr;
+    size_t budget = 0, used = 0;
+    uint64_t next_id = 1;
+    std::map<uint64_t, std::unique_ptr<PdJob>> pd;
+    std::map<uint64_t, std::unique_ptr<MgJob>> mg;
+
+    // iteration base: host mirror and device copy
+    uint32_t gbase = 0;
+    void *dev_blk = nullptr;  // gbase + sched counters
+    uint32_t *d_gbase = nullptr;
+    unsigned *d_sched = nullptr;
+
+    // batched work of the resident running primal-dual solves
+    bool dirty = true;
+    std::vector<PdJob *> running;
+    BatchVol *d_vols = nullptr;
+    size_t vols_cap = 0;
+    uint2 *d_items = nullptr;
+    size_t items_cap = 0;
+    std::vector<Group> groups;
+    cudaStream_t gstream[2 * kNumVariants] = {};
+    cudaEvent_t gdone[2 * kNumVariants] = {};
+    cudaEvent_t fork = nullptr, ev0 = nullptr, ev1 = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    PdCtl *h_ctl = nullptr;  // pinned
+    size_t h_ctl_cap = 0;
+
+    // Poisson workers
+    std::vector<std::thread> workers;
+    std::vector<qsm_ctx *> wctx;
+    std::mutex mu;
+    std::condition_variable cv;
+    std::deque<MgJob *> queue;
+    bool stop = false;
+};
+
+namespace {
+
+qsm_status fail(qsm_session *s, qsm_status st, const char *msg)
+{
+    set_error(s->ctx, "%s", msg);
+    return st;
+}
+
+size_t mg_footprint(const Dims &d, int nl, bool mixed)
+{
+    // hierarchy (v, f, r + G, B per level, scratch) + PCG vectors + staged inputs/outputs
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const Dims dp{d.nx + 2, d.ny + 2, d.nz + 2};
+    const size_t tm = mixed ? 4 : 8;
+    size_t bytes = 0;
+    Dims l = dp;
+    for (int i = 0; i < nl; ++i) {
+        if (i > 0) l = Dims{((l.nx - 2 + 1) >> 1) + 2, ((l.ny - 2 + 1) >> 1) + 2, ((l.nz - 2 + 1) >> 1) + 2};
+        bytes += 3 * al(l.n() * tm) + 2 * al(l.n());
+    }
+    bytes += al(dp.n()) + 256;
+    bytes += (mixed ? 4 : 2) * al(dp.n() * 8) + 4096;
+    bytes += 3 * al(d.n() * 8) + al(d.n()) + 1024;  // v0, f, out, mask
+    return bytes;
+}
+
+void worker_main(qsm_session *s, int w)
+{
+    qsm_ctx *ctx = s->wctx[w];
+    cudaSetDevice(ctx->device);
+    for (;;) {
+        MgJob *j = nullptr;
+        {
+            std::unique_lock<std::mutex> lock(s->mu);
+            s->cv.wait(lock, [&] { return s->stop || !s->queue.empty(); });
+            if (s->stop && s->queue.empty()) return;
+            j = s->queue.front();
+            s->queue.pop_front();
+        }
+        j->state.store(1);
+        qsm_status st;
+        if (j->mixed)
+            st = qsm_mgpcg_mixed(ctx, j->dims, j->has_v0 ? j->v0 : nullptr, j->f, j->mask, j->vsz, j->tolcg,
+                                 j->maxitcg, j->tolmg, j->maxitmg, j->mu, j->npre, j->npost, j->nb, j->nl, 0, j->out,
+                                 &j->info);
+        else
+            st = qsm_mgpcg(ctx, QSM_F64, j->dims, j->has_v0 ? j->v0 : nullptr, j->f, j->mask, j->vsz, j->tolcg,
+                           j->maxitcg, j->tolmg, j->maxitmg, j->mu, j->npre, j->npost, j->nb, j->nl, 0, j->out,
+                           &j->info);
+        j->st = st;
+        if (st != QSM_OK) snprintf(j->err, sizeof j->err, "%s", qsm_last_error(ctx));
+        j->state.store(2);
+    }
+}
+
+// Rebuilds the device work lists and re-captures the 30-iteration graph.
+qsm_status rebuild(qsm_session *s)
+{
+    qsm_ctx *ctx = s->ctx;
+    s->running.clear();
+    for (auto &kv : s->pd)
+        if (!kv.second->finished) s->running.push_back(kv.second.get());
+    if (s->exec) {
+        cudaGraphExecDestroy(s->exec);
+        s->exec = nullptr;
+    }
+    s->groups.clear();
+    const size_t nv = s->running.size();
+    s->dirty = false;
+    if (nv == 0) return QSM_OK;
+
+    // groups by (variant, kind); items in volume order, tiles ascending
+    std::map<std::pair<int, int>, size_t> gi;
+    std::vector<BatchVol> hv(kPhases * nv);
+    std::vector<uint32_t> item0(nv), gidx(nv);
+    for (size_t k = 0; k < nv; ++k) {
+        PdJob *j = s->running[k];
+        const auto key = std::make_pair(j->v.var, (int)j->v.tgv);
+        auto it = gi.find(key);
+        if (it == gi.end()) {
+            it = gi.emplace(key, s->groups.size()).first;
+            Group g;
+            g.var = j->v.var;
+            g.tgv = j->v.tgv;
+            s->groups.push_back(g);
+        }
+        Group &g = s->groups[it->second];
+        gidx[k] = (uint32_t)it->second;
+        item0[k] = (uint32_t)g.items.size();
+        for (unsigned t : j->tiles) g.items.push_back(make_uint2((unsigned)k, t));
+    }
+    for (size_t k = 0; k < nv; ++k) {
+        PdJob *j = s->running[k];
+        for (int p = 0; p < kPhases; ++p) {
+            BatchVol &b = hv[p * nv + k];
+            memset(&b, 0, sizeof b);
+            b.a = pd_volume_args(j->v, j->v.var, (uint32_t)p);
+            b.a.tiles = nullptr;
+            b.dc = j->v.dc;
+            b.pc = j->v.pc;
+            b.d = j->v.d;
+            b.tol = j->tol;
+            b.maxiter = j->maxiter;
+            b.start = j->start;
+            b.item0 = item0[k];
+            b.nitems = (uint32_t)j->tiles.size();
+        }
+    }
+    size_t nitems = 0;
+    for (auto &g : s->groups) nitems += g.items.size();
+    if (hv.size() > s->vols_cap) {
+        if (s->d_vols) QSM_TRY(dfree(ctx, s->d_vols));
+        s->d_vols = nullptr;
+        s->vols_cap = std::max(hv.size(), 2 * s->vols_cap);
+        QSM_TRY(dalloc(ctx, (void **)&s->d_vols, s->vols_cap * sizeof(BatchVol)));
+    }
+    if (nitems > s->items_cap) {
+        if (s->d_items) QSM_TRY(dfree(ctx, s->d_items));
+        s->d_items = nullptr;
+        s->items_cap = std::max(nitems, 2 * s->items_cap);
+        QSM_TRY(dalloc(ctx, (void **)&s->d_items, s->items_cap * sizeof(uint2)));
+    }
+    QSM_CUDA(cudaMemcpyAsync(s->d_vols, hv.data(), hv.size() * sizeof(BatchVol), cudaMemcpyHostToDevice, ctx->stream));
+    size_t off = 0;
+    int sm = 0;
+    QSM_CUDA(cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, ctx->device));
+    for (size_t q = 0; q < s->groups.size(); ++q) {
+        Group &g = s->groups[q];
+        g.d_items = s->d_items + off;
+        g.d_sched = s->d_sched + 2 * q;
+        QSM_CUDA(cudaMemcpyAsync(g.d_items, g.items.data(), g.items.size() * sizeof(uint2), cudaMemcpyHostToDevice,
+                                 ctx->stream));
+        off += g.items.size();
+        const BatchKernel bk = batch_kernel(g.var, g.tgv);
+        const int threads = variant_threads(g.var);
+        const size_t smem = variant_smem(g.var, g.tgv);
+        int occ = 0;
+        QSM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bk.fn[0], threads, smem));
+        occ = std::max(occ, 1);
+        g.grid = (unsigned)std::min<size_t>(g.items.size(), (size_t)sm * occ);
+        g.stream = s->gstream[q];
+        g.done = s->gdone[q];
+    }
+    QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+
+    // capture kGraphIters iterations: one launch chain per group, forked from
+    // and joined back into the session stream, then the base advance
+    cudaGraph_t graph = nullptr;
+    QSM_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t ce = cudaEventRecord(s->fork, ctx->stream);
+    for (size_t q = 0; q < s->groups.size() && ce == cudaSuccess; ++q) {
+        Group &g = s->groups[q];
+        ce = cudaStreamWaitEvent(g.stream, s->fork, 0);
+        const BatchKernel bk = batch_kernel(g.var, g.tgv);
+        const int threads = variant_threads(g.var);
+        const size_t smem = variant_smem(g.var, g.tgv);
+        uint32_t n = (uint32_t)g.items.size();
+        for (uint32_t i = 0; i < kGraphIters && ce == cudaSuccess; ++i) {
+            const bool chk = ((i + 1) % 10) == 0;
+            const BatchVol *vp = s->d_vols + (size_t)(i % kPhases) * nv;
+            if (bk.column) {
+                int cz = variant(g.var).tz;
+                void *args[] = {(void *)&vp, (void *)&g.d_items, (void *)&n, (void *)&s->d_gbase, (void *)&i,
+                                (void *)&g.d_sched, (void *)&cz};
+                ce = cudaLaunchKernel(bk.fn[chk], dim3(g.grid), dim3(threads), args, smem, g.stream);
+            } else {
+                void *args[] = {(void *)&vp, (void *)&g.d_items, (void *)&n, (void *)&s->d_gbase, (void *)&i,
+                                (void *)&g.d_sched};
+                ce = cudaLaunchKernel(bk.fn[chk], dim3(g.grid), dim3(threads), args, smem, g.stream);
+            }
+        }
+        if (ce == cudaSuccess) ce = cudaEventRecord(g.done, g.stream);
+        if (ce == cudaSuccess) ce = cudaStreamWaitEvent(ctx->stream, g.done, 0);
+    }
+    if (ce == cudaSuccess) {
+        advance_k<<<1, 1, 0, ctx->stream>>>(s->d_gbase, kGraphIters);
+        ce = cudaGetLastError();
+    }
+    cudaError_t ee = cudaStreamEndCapture(ctx->stream, &graph);
+    if (ce != cudaSuccess || ee != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        s->dirty = true;
+        set_error(ctx, "graph capture failed: %s", cudaGetErrorString(ce != cudaSuccess ? ce : ee));
+        return QSM_ERR_CUDA;
+    }
+    ce = cudaGraphInstantiate(&s->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) {
+        s->exec = nullptr;
+        s->dirty = true;
+        set_error(ctx, "graph instantiation failed: %s", cudaGetErrorString(ce));
+        return QSM_ERR_CUDA;
+    }
+    return QSM_OK;
+}
+
+qsm_status set_batch_smem(qsm_ctx *ctx)
+{
+    for (int v = 0; v < kNumVariants; ++v)
+        for (int tg = 0; tg < 2; ++tg) {
+            const BatchKernel bk = batch_kernel(v, tg != 0);
+            const int sm = (int)variant_smem(v, tg != 0);
+            for (int c = 0; c < 2; ++c)
+                QSM_CUDA(cudaFuncSetAttribute(bk.fn[c], cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+        }
+    return QSM_OK;
+}
+
+void fill_pd_info(const PdJob &j, qsm_pd_info *info)
+{
+    if (!info) return;
+    info->iters = j.iters;
+    info->monitor_chi = j.ctl.checks ? j.ctl.n1 : 1.0;
+    info->monitor_eta = j.ctl.checks ? j.ctl.n2 : 1.0;
+    info->seconds = j.seconds;
+    info->active_voxels = j.v.tl[j.v.var].active_vox;
+    info->tile[0] = (uint32_t)variant(j.v.var).tx;
+    info->tile[1] = (uint32_t)variant(j.v.var).ty;
+    info->tile[2] = (uint32_t)variant(j.v.var).tz;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+
+extern "C" {
+
+qsm_status qsm_session_create(qsm_ctx *ctx, size_t budget_bytes, int32_t poisson_workers, qsm_session **out)
+{
+    if (!ctx || !out || poisson_workers < 0 || poisson_workers > 16) return QSM_ERR_ARG;
+    *out = nullptr;
+    cudaSetDevice(ctx->device);
+    std::unique_ptr<qsm_session> s(new qsm_session());
+    s->ctx = ctx;
+    s->budget = budget_bytes;
+    QSM_TRY(set_batch_smem(ctx));
+    // gbase + 2 scheduler counters per possible group
+    const size_t blk = 256 + 2 * (2 * kNumVariants) * sizeof(unsigned);
+    QSM_TRY(dalloc(ctx, &s->dev_blk, blk));
+    QSM_CUDA(cudaMemsetAsync(s->dev_blk, 0, blk, ctx->stream));
+    s->d_gbase = (uint32_t *)s->dev_blk;
+    s->d_sched = (unsigned *)((char *)s->dev_blk + 256);
+    for (int q = 0; q < 2 * kNumVariants; ++q) {
+        QSM_CUDA(cudaStreamCreateWithFlags(&s->gstream[q], cudaStreamNonBlocking));
+        QSM_CUDA(cudaEventCreateWithFlags(&s->gdone[q], cudaEventDisableTiming));
+    }
+    QSM_CUDA(cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming));
+    QSM_CUDA(cudaEventCreate(&s->ev0));
+    QSM_CUDA(cudaEventCreate(&s->ev1));
+    QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+    s->groups.reserve(2 * kNumVariants);
+    for (int w = 0; w < poisson_workers; ++w) {
+        qsm_ctx *wc = nullptr;
+        qsm_status st = qsm_ctx_create(ctx->device, &wc);
+        if (st != QSM_OK) {
+            qsm_session_destroy(s.release());
+            return st;
+        }
+        s->wctx.push_back(wc);
+    }
+    qsm_session *raw = s.release();
+    for (int w = 0; w < poisson_workers; ++w) raw->workers.emplace_back(worker_main, raw, w);
+    *out = raw;
+    return QSM_OK;
+}
+
+qsm_status qsm_session_destroy(qsm_session *s)
+{
+    if (!s) return QSM_OK;
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        s->stop = true;
+    }
+    s->cv.notify_all();
+    for (auto &t : s->workers) t.join();
+    for (auto *wc : s->wctx) qsm_ctx_destroy(wc);
+    qsm_ctx *ctx = s->ctx;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (auto &kv : s->pd) pd_volume_free(ctx, &kv.second->v);
+    for (auto &kv : s->mg)
+        if (kv.second->blk) dfree(ctx, kv.second->blk);
+    if (s->exec) cudaGraphExecDestroy(s->exec);
+    if (s->d_vols) dfree(ctx, s->d_vols);
+    if (s->d_items) dfree(ctx, s->d_items);
+    if (s->dev_blk) dfree(ctx, s->dev_blk);
+    for (int q = 0; q < 2 * kNumVariants; ++q) {
+        if (s->gstream[q]) cudaStreamDestroy(s->gstream[q]);
+        if (s->gdone[q]) cudaEventDestroy(s->gdone[q]);
+    }
+    if (s->fork) cudaEventDestroy(s->fork);
+    if (s->ev0) cudaEventDestroy(s->ev0);
+    if (s->ev1) cudaEventDestroy(s->ev1);
+    if (s->h_ctl) cudaFreeHost(s->h_ctl);
+    cudaStreamSynchronize(ctx->stream);
+    delete s;
+    return QSM_OK;
+}
+
+size_t qsm_session_footprint(int32_t kind, const size_t dims[3], int32_t nlevels)
+{
+    if (!dims) return 0;
+    const Dims d = make_dims(dims);
+    switch (kind) {
+    case QSM_JOB_TV: return pd_volume_bytes(false, d);
+    case QSM_JOB_TGV: return pd_volume_bytes(true, d);
+    case QSM_JOB_MGPCG: return mg_footprint(d, std::max(1, std::min(nlevels, 16)), true);
+    case QSM_JOB_MGPCG_F64: return mg_footprint(d, std::max(1, std::min(nlevels, 16)), false);
+    default: return 0;
+    }
+}
+
+size_t qsm_session_bytes_in_use(const qsm_session *s) { return s ? s->used : 0; }
+
+qsm_status qsm_session_submit_pd(qsm_session *s, int32_t tgv, qsm_dtype dt, const size_t dims[3], const void *d2f,
+                                 const uint8_t *mask, const double vsz[3], double lam, double alpha, double tol,
+                                 uint32_t maxiter, uint64_t *id)
+{
+    if (!s || !dims || !d2f || !mask || !vsz || !id) return QSM_ERR_ARG;
+    if (dt != QSM_F32 && dt != QSM_F64) return QSM_ERR_DTYPE;
+    qsm_ctx *ctx = s->ctx;
+    cudaSetDevice(ctx->device);
+    const Dims d = make_dims(dims);
+    if (d.n() == 0) return fail(s, QSM_ERR_DIMS, "empty volume");
+    if (d.n() > 0xffffffffull) return fail(s, QSM_ERR_DIMS, "volume above 2^32 voxels");
+    const size_t bytes = pd_volume_bytes(tgv != 0, d);
+    if (s->budget && s->used + bytes > s->budget) return fail(s, QSM_ERR_BUSY, "session byte budget exceeded");
+    const size_t es = dt == QSM_F32 ? 4 : 8;
+    Staged sf, sm;
+    QSM_TRY(stage_in(ctx, sf, d2f, d.n() * es, true));
+    QSM_TRY(stage_in(ctx, sm, mask, d.n(), true));
+    std::unique_ptr<PdJob> j(new PdJob());
+    qsm_status st = pd_volume_init(ctx, &j->v, tgv != 0, d, dt, sf.dev, (const uint8_t *)sm.dev, vsz, lam, alpha);
+    if (st == QSM_OK) st = pd_volume_tune(ctx, &j->v, maxiter);
+    stage_out(ctx, sf, false);
+    stage_out(ctx, sm, false);
+    if (st != QSM_OK) {
+        pd_volume_free(ctx, &j->v);
+        return st;
+    }
+    const TileList &tl = j->v.tl[j->v.var];
+    j->tiles.resize(tl.nact);
+    if (tl.nact)
+        QSM_CUDA(cudaMemcpyAsync(j->tiles.data(), tl.dev, tl.nact * sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+    QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+    j->id = s->next_id++;
+    j->dt = dt;
+    j->tol = tol;
+    j->maxiter = maxiter;
+    j->start = s->gbase;
+    j->bytes = bytes;
+    if (maxiter == 0 || tl.nact == 0) {
+        // nothing to iterate: chi stays 0 (as the one-volume path)
+        j->finished = true;
+        j->iters = maxiter;
+    }
+    *id = j->id;
+    s->used += bytes;
+    s->pd.emplace(j->id, std::move(j));
+    s->dirty = true;
+    return QSM_OK;
+}
+
+qsm_status qsm_session_submit_mgpcg(qsm_session *s, const size_t dims[3], const double *v0, const double *f,
+                                    const uint8_t *mask, const double vsz[3], double tolcg, int32_t maxitcg,
+                                    double tolmg, int32_t maxitmg, int32_t mu, int32_t npre, int32_t npost,
+                                    int32_t nboundary, int32_t nlevels, int32_t mixed, uint64_t *id)
+{
+    if (!s || !dims || !f || !mask || !vsz || !id) return QSM_ERR_ARG;
+    if (s->workers.empty()) return fail(s, QSM_ERR_ARG, "session has no Poisson workers");
+    if (nlevels < 1) return QSM_ERR_ARG;
+    if (nlevels > 16) return QSM_ERR_DEPTH;
+    qsm_ctx *ctx = s->ctx;
+    cudaSetDevice(ctx->device);
+    const Dims d = make_dims(dims);
+    if (d.n() == 0) return fail(s, QSM_ERR_DIMS, "empty volume");
+    const size_t bytes = mg_footprint(d, nlevels, mixed != 0);
+    if (s->budget && s->used + bytes > s->budget) return fail(s, QSM_ERR_BUSY, "session byte budget exceeded");
+    std::unique_ptr<MgJob> j(new MgJob());
+    const size_t vb = (d.n() * 8 + 255) & ~(size_t)255;
+    QSM_TRY(dalloc(ctx, &j->blk, 3 * vb + d.n()));
+    char *c = (char *)j->blk;
+    j->v0 = (double *)c;
+    j->f = (double *)(c + vb);
+    j->out = (double *)(c + 2 * vb);
+    j->mask = (uint8_t *)(c + 3 * vb);
+    if (v0) QSM_CUDA(cudaMemcpyAsync(j->v0, v0, d.n() * 8, cudaMemcpyDefault, ctx->stream));
+    QSM_CUDA(cudaMemcpyAsync(j->f, f, d.n() * 8, cudaMemcpyDefault, ctx->stream));
+    QSM_CUDA(cudaMemcpyAsync(j->mask, mask, d.n(), cudaMemcpyDefault, ctx->stream));
+    QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+    j->id = s->next_id++;
+    j->d = d;
+    for (int q = 0; q < 3; ++q) {
+        j->dims[q] = dims[q];
+        j->vsz[q] = vsz[q];
+    }
+    j->tolcg = tolcg;
+    j->maxitcg = maxitcg;
+    j->tolmg = tolmg;
+    j->maxitmg = maxitmg;
+    j->mu = mu;
+    j->npre = npre;
+    j->npost = npost;
+    j->nb = nboundary;
+    j->nl = nlevels;
+    j->mixed = mixed != 0;
+    j->has_v0 = v0 != nullptr;
+    j->bytes = bytes;
+    *id = j->id;
+    s->used += bytes;
+    MgJob *raw = j.get();
+    s->mg.emplace(j->id, std::move(j));
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        s->queue.push_back(raw);
+    }
+    s->cv.notify_one();
+    return QSM_OK;
+}
+
+qsm_status qsm_session_step(qsm_session *s, uint32_t iters)
+{
+    if (!s) return QSM_ERR_ARG;
+    qsm_ctx *ctx = s->ctx;
+    cudaSetDevice(ctx->device);
+    if (s->dirty) QSM_TRY(rebuild(s));
+    if (s->running.empty()) return QSM_OK;
+    const uint32_t reps = std::max<uint32_t>(1, (iters + kGraphIters - 1) / kGraphIters);
+    QSM_CUDA(cudaEventRecord(s->ev0, ctx->stream));
+    for (uint32_t r = 0; r < reps; ++r) QSM_CUDA(cudaGraphLaunch(s->exec, ctx->stream));
+    QSM_CUDA(cudaEventRecord(s->ev1, ctx->stream));
+    s->gbase += reps * kGraphIters;
+    const size_t nv = s->running.size();
+    if (nv > s->h_ctl_cap) {
+        if (s->h_ctl) cudaFreeHost(s->h_ctl);
+        s->h_ctl = nullptr;
+        s->h_ctl_cap = std::max(nv, 2 * s->h_ctl_cap);
+        QSM_CUDA(cudaMallocHost((void **)&s->h_ctl, s->h_ctl_cap * sizeof(PdCtl)));
+    }
+    for (size_t k = 0; k < nv; ++k)
+        QSM_CUDA(cudaMemcpyAsync(s->h_ctl + k, s->running[k]->v.ctl, sizeof(PdCtl), cudaMemcpyDeviceToHost, ctx->stream));
+    QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+    for (size_t k = 0; k < nv; ++k) {
+        PdJob *j = s->running[k];
+        j->ctl = s->h_ctl[k];
+        j->seconds += ms * 1e-3;
+        const uint32_t done_it = s->gbase - j->start;
+        if (j->ctl.done) {
+            j->finished = true;
+            j->iters = j->ctl.iters;
+        } else if (done_it >= j->maxiter) {
+            j->finished = true;
+            j->iters = j->maxiter;
+        }
+        if (j->finished) s->dirty = true;
+    }
+    return QSM_OK;
+}
+
+qsm_status qsm_session_poll(qsm_session *s, uint64_t id, int32_t *finished, qsm_pd_info *pd_info,
+                            qsm_mg_info *mg_info)
+{
+    if (!s || !finished) return QSM_ERR_ARG;
+    auto ip = s->pd.find(id);
+    if (ip != s->pd.end()) {
+        *finished = ip->second->finished ? 1 : 0;
+        fill_pd_info(*ip->second, pd_info);
+        return QSM_OK;
+    }
+    auto im = s->mg.find(id);
+    if (im != s->mg.end()) {
+        MgJob &j = *im->second;
+        *finished = j.state.load() == 2 ? 1 : 0;
+        if (*finished && mg_info) {
+            double *hist = mg_info->resnorm_hist;
+            *mg_info = j.info;
+            mg_info->resnorm_hist = hist;
+        }
+        if (*finished && j.st != QSM_OK) return fail(s, j.st, j.err);
+        return QSM_OK;
+    }
+    return fail(s, QSM_ERR_ARG, "unknown session job id");
+}
+
+qsm_status qsm_session_fetch(qsm_session *s, uint64_t id, void *out)
+{
+    if (!s || !out) return QSM_ERR_ARG;
+    qsm_ctx *ctx = s->ctx;
+    cudaSetDevice(ctx->device);
+    auto ip = s->pd.find(id);
+    if (ip != s->pd.end()) {
+        PdJob &j = *ip->second;
+        if (!j.finished) return fail(s, QSM_ERR_BUSY, "job still running");
+        const size_t es = j.dt == QSM_F32 ? 4 : 8;
+        Staged so;
+        QSM_TRY(stage_in(ctx, so, out, j.v.d.n() * es, false));
+        QSM_TRY(pd_volume_result(ctx, j.v, j.iters, j.dt, so.dev));
+        QSM_TRY(stage_out(ctx, so, true));
+        QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+        QSM_TRY(pd_volume_free(ctx, &j.v));
+        s->used -= j.bytes;
+        s->pd.erase(ip);
+        return QSM_OK;
+    }
+    auto im = s->mg.find(id);
+    if (im != s->mg.end()) {
+        MgJob &j = *im->second;
+        if (j.state.load() != 2) return fail(s, QSM_ERR_BUSY, "job still running");
+        qsm_status st = j.st;
+        if (st == QSM_OK) {
+            QSM_CUDA(cudaMemcpyAsync(out, j.out, j.d.n() * 8, cudaMemcpyDefault, ctx->stream));
+            QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+        }
+        QSM_TRY(dfree(ctx, j.blk));
+        s->used -= j.bytes;
+        s->mg.erase(im);
+        return st;
+    }
+    return fail(s, QSM_ERR_ARG, "unknown session job id");
+}
+
+uint32_t qsm_session_running(const qsm_session *s)
+{
+    if (!s) return 0;
+    uint32_t n = 0;
+    for (auto &kv : s->pd) n += kv.second->finished ? 0 : 1;
+    for (auto &kv : s->mg) n += kv.second->state.load() == 2 ? 0 : 1;
+    return n;
+}
+
+static qsm_status pd_batch(qsm_ctx *ctx, bool tgv, qsm_dtype dt, uint32_t count, const size_t *dims,
+                           const void *const *d2f, const uint8_t *const *mask, const double vsz[3], double lam,
+                           double alpha, double tol, uint32_t maxiter, void *const *chi, qsm_pd_info *info)
+{
+    if (!ctx || !dims || !d2f || !mask || !vsz || !chi) return QSM_ERR_ARG;
+    if (dt != QSM_F32 && dt != QSM_F64) return QSM_ERR_DTYPE;
+    qsm_session *s = nullptr;
+    QSM_TRY(qsm_session_create(ctx, 0, 0, &s));
+    std::vector<uint64_t> ids(count);
+    qsm_status st = QSM_OK;
+    for (uint32_t b = 0; b < count && st == QSM_OK; ++b)
+        st = qsm_session_submit_pd(s, tgv ? 1 : 0, dt, dims + 3 * b, d2f[b], mask[b], vsz, lam, alpha, tol, maxiter,
+                                   &ids[b]);
+    // advance until every solve stopped (check the monitors every 90 iterations)
+    while (st == QSM_OK && qsm_session_running(s) > 0) st = qsm_session_step(s, 3 * kGraphIters);
+    for (uint32_t b = 0; b < count && st == QSM_OK; ++b) {
+        int32_t fin = 0;
+        st = qsm_session_poll(s, ids[b], &fin, info ? info + b : nullptr, nullptr);
+        if (st == QSM_OK) st = qsm_session_fetch(s, ids[b], chi[b]);
+    }
+    if (st != QSM_OK) {
+        qsm_session_destroy(s);
+        return st;
+    }
+    return qsm_session_destroy(s);
+}
+
+qsm_status qsm_pd_tv_batch(qsm_ctx *ctx, qsm_dtype dt, uint32_t count, const size_t *dims, const void *const *d2f,
+                           const uint8_t *const *mask, const double vsz[3], double lam, double tol, uint32_t maxiter,
+                           void *const *chi, qsm_pd_info *info)
+{
+    return pd_batch(ctx, false, dt, count, dims, d2f, mask, vsz, lam, 0.0, tol, maxiter, chi, info);
+}
+
+qsm_status qsm_pd_tgv_batch(qsm_ctx *ctx, qsm_dtype dt, uint32_t count, const size_t *dims, const void *const *d2f,
+                            const uint8_t *const *mask, const double vsz[3], double lam, double alpha, double tol,
+                            uint32_t maxiter, void *const *chi, qsm_pd_info *info)
+{
+    return pd_batch(ctx, true, dt, count, dims, d2f, mask, vsz, lam, alpha, tol, maxiter, chi, info);
+}
+
+}  // extern "C"

@@ -29,16 +29,18 @@ __device__ __forceinline__ float xbar(const float *__restrict__ c, const float *
     return cn + 1.0f * (cn - __ldg(p + l));
 }
 
-// Monitor sums of one block, then the last block folds the partials in
-// block order and applies the stopping test.  red aliases dynamic shared
-// memory (4 x THREADS doubles) that is free once the primal has finished.
+// Monitor sums of one tile (block), then the last of the nblk tiles folds
+// the partials in tile order and applies the stopping test.  red aliases
+// dynamic shared memory (4 x THREADS doubles) that is free once the primal
+// has finished.  After the call the shared memory is free again only after
+// the next __syncthreads.
 template <int THREADS>
-__device__ __forceinline__ void monitor_reduce(const FusedArgs &s, double *red, const double *acc, double tol,
-                                               uint32_t it)
+__device__ __forceinline__ void monitor_fold(double *part, unsigned int *count, PdCtl *ctl, unsigned int nblk,
+                                             unsigned int bid, double *red, const double *acc, double tol,
+                                             uint32_t it)
 {
     __shared__ bool last;
     const int tid = threadIdx.x;
-    const unsigned int nblk = gridDim.x, bid = blockIdx.x;
     __syncthreads();  // everyone is done reading the dual from shared memory
 #pragma unroll
     for (int q = 0; q < 4; ++q) red[q * THREADS + tid] = acc[q];
@@ -51,9 +53,9 @@ __device__ __forceinline__ void monitor_reduce(const FusedArgs &s, double *red, 
     }
     if (tid == 0) {
 #pragma unroll
-        for (int q = 0; q < 4; ++q) s.part[(size_t)q * nblk + bid] = red[q * THREADS];
+        for (int q = 0; q < 4; ++q) part[(size_t)q * nblk + bid] = red[q * THREADS];
         __threadfence();
-        last = atomicAdd(s.count, 1u) == nblk - 1;
+        last = atomicAdd(count, 1u) == nblk - 1;
     }
     __syncthreads();
     if (!last) return;
@@ -61,7 +63,7 @@ __device__ __forceinline__ void monitor_reduce(const FusedArgs &s, double *red, 
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         double a = 0.0;
-        for (unsigned int b2 = tid; b2 < nblk; b2 += THREADS) a += __ldcg(s.part + (size_t)q * nblk + b2);
+        for (unsigned int b2 = tid; b2 < nblk; b2 += THREADS) a += __ldcg(part + (size_t)q * nblk + b2);
         red[q * THREADS + tid] = a;
     }
     __syncthreads();
@@ -73,15 +75,78 @@ __device__ __forceinline__ void monitor_reduce(const FusedArgs &s, double *red, 
     }
     if (tid == 0) {
         double r[4] = {red[0], red[THREADS], red[2 * THREADS], red[3 * THREADS]};
-        pd_finish(s.ctl, r, tol, it);
-        *s.count = 0;
+        pd_finish(ctl, r, tol, it);
+        *count = 0;
     }
 }
 
+// one block per active tile
+template <int THREADS>
+__device__ __forceinline__ void monitor_reduce(const FusedArgs &s, double *red, const double *acc, double tol,
+                                               uint32_t it)
+{
+    monitor_fold<THREADS>(s.part, s.count, s.ctl, gridDim.x, blockIdx.x, red, acc, tol, it);
+}
 
 size_t stream_smem(int tx, int ty, bool tgv);
 qsm_status stream_set_smem(qsm_ctx *ctx);
 qsm_status stream_launch(qsm_ctx *ctx, int tx, int ty, int cz, bool tgv, bool chk, unsigned nact, const FusedArgs &s,
                          const DualC<float> &dc, const PrimalC<float> &pc, const Dims &d, double tol, uint32_t it);
+
+// ---------------------------------------------------------------------------
+// Tile variants and the device state of one fused solve (pd_fused.cu), shared
+// with the many-volume session (pd_batch.cu).
+// ---------------------------------------------------------------------------
+
+struct Variant {
+    int tx, ty, tz;   // tile of interior voxels (z: chunk of planes for the column kernel)
+    bool stream;      // column-streaming kernel, else the 3-D tile kernel
+};
+constexpr int kNumVariants = 8;
+const Variant &variant(int v);
+size_t variant_smem(int v, bool tgv);
+int variant_threads(int v);
+
+struct TileList {
+    unsigned gx = 0, gy = 0, gz = 0, nact = 0;
+    unsigned *dev = nullptr;  // active tile indices, ascending (inside the state block)
+    uint64_t active_vox = 0;  // interior voxels covered by the active tiles
+};
+
+// Device state of one solve: triple-buffered primal, double-buffered dual,
+// scaled data, masks, the active-tile lists of every variant and the monitor
+// scratch, in one allocation.
+struct PdVolume {
+    bool tgv = false;
+    Dims d{};
+    int np = 0, nd = 0;
+    void *blk = nullptr;
+    float *P[3][5] = {};
+    float *D[2][10] = {};
+    float *f = nullptr;
+    uint8_t *mm = nullptr;       // bit 0 m, bit 1 mi
+    TileList tl[kNumVariants];
+    double *part = nullptr;      // 4 x (max tiles) monitor partials
+    unsigned *count = nullptr;   // arrival counter of the monitor fold
+    PdCtl *ctl = nullptr;
+    size_t state_bytes = 0;      // primal + dual buffers (from P[0][0])
+    DualC<float> dc{};
+    PrimalC<float> pc{};
+    int var = 0;                 // chosen tile variant
+};
+
+// Device bytes one solve holds (the allocation pd_volume_init makes).
+size_t pd_volume_bytes(bool tgv, const Dims &d);
+// Allocates and initialises the state from device d2f (dtype dt) and mask.
+qsm_status pd_volume_init(qsm_ctx *ctx, PdVolume *v, bool tgv, const Dims &d, qsm_dtype dt, const void *d2f,
+                          const uint8_t *mask, const double *h, double lam, double alpha);
+// Kernel arguments of variant var for the iteration that reads iterate `it`.
+FusedArgs pd_volume_args(const PdVolume &v, int var, uint32_t it);
+// Picks v->var: QSM_FUSED_VARIANT, the tuning table, or timing each variant
+// on this volume for a few iterations (the state is zeroed again after).
+qsm_status pd_volume_tune(qsm_ctx *ctx, PdVolume *v, uint32_t maxiter);
+// chi after `iters` iterations, converted to dt.
+qsm_status pd_volume_result(qsm_ctx *ctx, const PdVolume &v, uint32_t iters, qsm_dtype dt, void *chi);
+qsm_status pd_volume_free(qsm_ctx *ctx, PdVolume *v);
 
 }  // namespace qsm

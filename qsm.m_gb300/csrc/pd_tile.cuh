@@ -1,0 +1,467 @@
+// Device bodies of the fused mixed-precision TGV/TV iteration, shared by the
+// one-volume kernels (pd_fused.cu: 3-D tiles; pd_stream.cu: z-streaming
+// columns) and the persistent many-volume kernels (pd_batch.cu).
+//
+// 3-D tile (tile_tgv / tile_tv, TX x TY threads):
+//   1. the dual (nu, p, q) is evaluated on the tile plus the one-voxel layer
+//      on its low side (which the primal's backward differences read) and
+//      nu alone on the high-side faces (the primal's Laplacian reads them),
+//      into shared memory; halo points are recomputed by every tile that
+//      needs them, with identical arithmetic, instead of synchronising the
+//      grid;
+//   2. the primal (chi, eta, w) of the tile reads the dual from shared
+//      memory and writes the next iterate.
+//
+// Column (column_pd, (TX+4) x (TY+4) threads): each thread walks its column
+// upwards one plane per step:
+//
+//   step j:  (a) read the primal iterates n and n-1 at plane j+1 of its own
+//                column and form the extragradient point (chi_, eta_, w_);
+//                keep it in registers (z-neighbours) and publish it in
+//                shared memory (x/y-neighbours of plane j+1)
+//            (b) the dual at plane j (threads of the one-voxel ring and the
+//                tile) from registers (z) and shared memory (x, y): written
+//                to shared memory, and to HBM by the owning threads
+//            (c) the primal + extragradient at plane j-1 (tile threads), from
+//                the dual of planes j-2 (registers), j-1 (shared memory, x/y
+//                neighbours) and j (own value)
+//            one __syncthreads
+//
+// so every input value of a plane is read from HBM once per CTA (the ring
+// re-reads neighbouring tiles' edges, mostly from L2) and the dual is
+// evaluated once per plane and column (plus the ring), not on a 3-D halo.
+// Only the two planes below a chunk are recomputed.
+//
+// Both skip voxels outside the mask (their state is identically 0).  Per
+// voxel the FP32 expressions are those of update_dualf / update_primalf
+// (pd_tgv_mex.c:332-485, :659-812; TV: pd_tv_mex.c:314-412, :524-622) in the
+// reference's association order; the files are built without fused
+// multiply-add, so chi is bit-identical to the reference's mx_pdf.
+#pragma once
+
+#include <math.h>
+
+#include "common.cuh"
+#include "pd.cuh"
+#include "pd_fused.cuh"
+
+namespace qsm {
+
+// One 3-D tile of the fused TGV iteration; shd holds 10 x (TX+2)(TY+2)(TZ+2)
+// floats; acc receives this thread's FP64 monitor terms when check is set.
+template <int TX, int TY, int TZ>
+__device__ __forceinline__ void tile_tgv(const FusedArgs &s, const DualC<float> &dc, const PrimalC<float> &pc,
+                                         const Dims &d, unsigned tile, bool check, float *shd, double *acc)
+{
+    constexpr int BX = TX + 2, BY = TY + 2, BZ = TZ + 2, BN = BX * BY * BZ, THREADS = TX * TY;
+    const size_t nx = d.nx, nxny = d.nxny();
+    const size_t x0 = 1 + (size_t)(tile % s.gx) * TX, y0 = 1 + (size_t)((tile / s.gx) % s.gy) * TY,
+                 z0 = 1 + (size_t)(tile / (s.gx * s.gy)) * TZ;
+    const int tid = threadIdx.x;
+
+    // ---- 1. dual on the box [x0-1, x0+TX] x ... (low layer + tile + high faces)
+    for (int p = tid; p < BN; p += THREADS) {
+        const int bx = p % BX, by = (p / BX) % BY, bz = p / (BX * BY);
+        const size_t x = x0 - 1 + bx, y = y0 - 1 + by, z = z0 - 1 + bz;
+        const int nhigh = (int)(bx == BX - 1) + (int)(by == BY - 1) + (int)(bz == BZ - 1);
+        float v[10];
+#pragma unroll
+        for (int q = 0; q < 10; ++q) v[q] = 0.0f;
+        if (nhigh <= 1 && x < d.nx && y < d.ny && z < d.nz) {
+            const size_t l = x + nx * y + nxny * z;
+            // mi: all six neighbours in the mask (never true on a face); the dual is 0 outside it
+            const bool inside = (__ldg(s.mm + l) & 2) != 0;
+            if (inside) {
+                const float c0 = xbar(s.Pc[0], s.Pp[0], l);
+                const float cxm = xbar(s.Pc[0], s.Pp[0], l - 1), cxp = xbar(s.Pc[0], s.Pp[0], l + 1);
+                const float cym = xbar(s.Pc[0], s.Pp[0], l - nx), cyp = xbar(s.Pc[0], s.Pp[0], l + nx);
+                const float czm = xbar(s.Pc[0], s.Pp[0], l - nxny), czp = xbar(s.Pc[0], s.Pp[0], l + nxny);
+                const float lap = dc.lhh * xbar(s.Pc[1], s.Pp[1], l) +
+                                  dc.lhx * (xbar(s.Pc[1], s.Pp[1], l - 1) + xbar(s.Pc[1], s.Pp[1], l + 1)) +
+                                  dc.lhy * (xbar(s.Pc[1], s.Pp[1], l - nx) + xbar(s.Pc[1], s.Pp[1], l + nx)) +
+                                  dc.lhz * (xbar(s.Pc[1], s.Pp[1], l - nxny) + xbar(s.Pc[1], s.Pp[1], l + nxny));
+                const float wav = dc.whh * c0 + dc.whx * (cxm + cxp) + dc.why * (cym + cyp) + dc.whz * (czm + czp);
+                v[0] = __ldg(s.Dc[0] + l) + ((lap - wav) + __ldg(s.f + l));
+                if (nhigh == 0) {
+#pragma unroll
+                    for (int q = 1; q < 10; ++q) v[q] = __ldg(s.Dc[q] + l);
+                    const float w1 = xbar(s.Pc[2], s.Pp[2], l), w2 = xbar(s.Pc[3], s.Pp[3], l), w3 = xbar(s.Pc[4], s.Pp[4], l);
+                    float a1 = v[1] + dc.hx * (cxp - c0) - dc.sg * w1;
+                    float a2 = v[2] + dc.hy * (cyp - c0) - dc.sg * w2;
+                    float a3 = v[3] + dc.hz * (czp - c0) - dc.sg * w3;
+                    float t = a1 * a1 + a2 * a2 + a3 * a3;
+                    if (t > dc.alp12) {
+                        t = dc.alp1 / sqrtf(t);
+                        a1 = a1 * t; a2 = a2 * t; a3 = a3 * t;
+                    }
+                    v[1] = a1; v[2] = a2; v[3] = a3;
+                    const float w1x = xbar(s.Pc[2], s.Pp[2], l + 1), w1y = xbar(s.Pc[2], s.Pp[2], l + nx), w1z = xbar(s.Pc[2], s.Pp[2], l + nxny);
+                    const float w2x = xbar(s.Pc[3], s.Pp[3], l + 1), w2y = xbar(s.Pc[3], s.Pp[3], l + nx), w2z = xbar(s.Pc[3], s.Pp[3], l + nxny);
+                    const float w3x = xbar(s.Pc[4], s.Pp[4], l + 1), w3y = xbar(s.Pc[4], s.Pp[4], l + nx), w3z = xbar(s.Pc[4], s.Pp[4], l + nxny);
+                    float b1 = v[4] + dc.hx * (w1x - w1);
+                    float b2 = v[5] + dc.hx2 * (w2x - w2) + dc.hy2 * (w1y - w1);
+                    float b3 = v[6] + dc.hx2 * (w3x - w3) + dc.hz2 * (w1z - w1);
+                    float b4 = v[7] + dc.hy * (w2y - w2);
+                    float b5 = v[8] + dc.hy2 * (w3y - w3) + dc.hz2 * (w2z - w2);
+                    float b6 = v[9] + dc.hz * (w3z - w3);
+                    t = b1 * b1 + b4 * b4 + b6 * b6 + 2.0f * (b2 * b2 + b3 * b3 + b5 * b5);
+                    if (t > dc.alp02) {
+                        t = dc.alp0 / sqrtf(t);
+                        b1 = b1 * t; b2 = b2 * t; b3 = b3 * t; b4 = b4 * t; b5 = b5 * t; b6 = b6 * t;
+                    }
+                    v[4] = b1; v[5] = b2; v[6] = b3; v[7] = b4; v[8] = b5; v[9] = b6;
+                    // the owning tile stores the new dual
+                    if (bx >= 1 && by >= 1 && bz >= 1) {
+#pragma unroll
+                        for (int q = 0; q < 10; ++q) s.Dn[q][l] = v[q];
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 10; ++q) shd[q * BN + p] = v[q];
+    }
+    __syncthreads();
+
+    // ---- 2. primal + extragradient on the tile
+    const int tx = tid % TX, ty = tid / TX;
+    const size_t x = x0 + tx, y = y0 + ty;
+    if (x + 1 < d.nx && y + 1 < d.ny) {
+#pragma unroll 1
+        for (int tz = 0; tz < TZ; ++tz) {
+            const size_t z = z0 + tz;
+            if (z + 1 >= d.nz) break;
+            const size_t l = x + nx * y + nxny * z;
+            if (!(__ldg(s.mm + l) & 1)) continue;
+            const int b = (tx + 1) + BX * ((ty + 1) + BY * (tz + 1));
+            constexpr int sx = 1, sy = BX, sz = BX * BY;
+#define SH(q, o) shd[(q) * BN + b + (o)]
+            const float nu0 = SH(0, 0);
+            const float xs = SH(0, -sx) + SH(0, sx);
+            const float ys = SH(0, -sy) + SH(0, sy);
+            const float zs = SH(0, -sz) + SH(0, sz);
+            const float en = __ldg(s.Pc[1] + l), cn = __ldg(s.Pc[0] + l);
+            const float w1n = __ldg(s.Pc[2] + l), w2n = __ldg(s.Pc[3] + l), w3n = __ldg(s.Pc[4] + l);
+            const float e1 = pc.tau1 * (en - pc.lhh * nu0 - pc.lhx * xs - pc.lhy * ys - pc.lhz * zs);
+            const float c1 = cn + (pc.hx * (SH(1, 0) - SH(1, -sx)) + pc.hy * (SH(2, 0) - SH(2, -sy)) +
+                                   pc.hz * (SH(3, 0) - SH(3, -sz)) + (pc.whh * nu0 + pc.whx * xs + pc.why * ys + pc.whz * zs));
+            const float u1 = w1n + (pc.tt * SH(1, 0) + pc.hx * (SH(4, 0) - SH(4, -sx) + SH(5, 0) - SH(5, -sy) + SH(6, 0) - SH(6, -sz)));
+            const float u2 = w2n + (pc.tt * SH(2, 0) + pc.hy * (SH(5, 0) - SH(5, -sx) + SH(7, 0) - SH(7, -sy) + SH(8, 0) - SH(8, -sz)));
+            const float u3 = w3n + (pc.tt * SH(3, 0) + pc.hz * (SH(6, 0) - SH(6, -sx) + SH(8, 0) - SH(8, -sy) + SH(9, 0) - SH(9, -sz)));
+#undef SH
+            s.Pn[0][l] = c1;
+            s.Pn[1][l] = e1;
+            s.Pn[2][l] = u1;
+            s.Pn[3][l] = u2;
+            s.Pn[4][l] = u3;
+            if (check) {
+                double a, bb, c, e;
+                mon_terms(c1, cn, e1, en, a, bb, c, e);
+                acc[0] += a; acc[1] += bb; acc[2] += c; acc[3] += e;
+            }
+        }
+    }
+    (void)THREADS;
+}
+
+// One 3-D tile of the fused TV iteration; shd holds 4 x (TX+2)(TY+2)(TZ+2) floats.
+template <int TX, int TY, int TZ>
+__device__ __forceinline__ void tile_tv(const FusedArgs &s, const DualC<float> &dc, const PrimalC<float> &pc,
+                                        const Dims &d, unsigned tile, bool check, float *shd, double *acc)
+{
+    constexpr int BX = TX + 2, BY = TY + 2, BZ = TZ + 2, BN = BX * BY * BZ, THREADS = TX * TY;
+    const size_t nx = d.nx, nxny = d.nxny();
+    const size_t x0 = 1 + (size_t)(tile % s.gx) * TX, y0 = 1 + (size_t)((tile / s.gx) % s.gy) * TY,
+                 z0 = 1 + (size_t)(tile / (s.gx * s.gy)) * TZ;
+    const int tid = threadIdx.x;
+    for (int p = tid; p < BN; p += THREADS) {
+        const int bx = p % BX, by = (p / BX) % BY, bz = p / (BX * BY);
+        const size_t x = x0 - 1 + bx, y = y0 - 1 + by, z = z0 - 1 + bz;
+        const int nhigh = (int)(bx == BX - 1) + (int)(by == BY - 1) + (int)(bz == BZ - 1);
+        float v[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        if (nhigh <= 1 && x < d.nx && y < d.ny && z < d.nz) {
+            const size_t l = x + nx * y + nxny * z;
+            const bool inside = (__ldg(s.mm + l) & 2) != 0;  // the dual is 0 outside mi
+            if (inside) {
+                const float c0 = xbar(s.Pc[0], s.Pp[0], l);
+                const float cxm = xbar(s.Pc[0], s.Pp[0], l - 1), cxp = xbar(s.Pc[0], s.Pp[0], l + 1);
+                const float cym = xbar(s.Pc[0], s.Pp[0], l - nx), cyp = xbar(s.Pc[0], s.Pp[0], l + nx);
+                const float czm = xbar(s.Pc[0], s.Pp[0], l - nxny), czp = xbar(s.Pc[0], s.Pp[0], l + nxny);
+                const float lap = dc.lhh * xbar(s.Pc[1], s.Pp[1], l) +
+                                  dc.lhx * (xbar(s.Pc[1], s.Pp[1], l - 1) + xbar(s.Pc[1], s.Pp[1], l + 1)) +
+                                  dc.lhy * (xbar(s.Pc[1], s.Pp[1], l - nx) + xbar(s.Pc[1], s.Pp[1], l + nx)) +
+                                  dc.lhz * (xbar(s.Pc[1], s.Pp[1], l - nxny) + xbar(s.Pc[1], s.Pp[1], l + nxny));
+                const float wav = dc.whh * c0 + dc.whx * (cxm + cxp) + dc.why * (cym + cyp) + dc.whz * (czm + czp);
+                v[0] = __ldg(s.Dc[0] + l) + ((lap - wav) + __ldg(s.f + l));
+                if (nhigh == 0) {
+                    float a1 = __ldg(s.Dc[1] + l) + dc.hx * (cxp - c0);
+                    float a2 = __ldg(s.Dc[2] + l) + dc.hy * (cyp - c0);
+                    float a3 = __ldg(s.Dc[3] + l) + dc.hz * (czp - c0);
+                    float t = a1 * a1 + a2 * a2 + a3 * a3;
+                    if (t > dc.alp12) {
+                        t = dc.alp1 / sqrtf(t);
+                        a1 = a1 * t; a2 = a2 * t; a3 = a3 * t;
+                    }
+                    v[1] = a1; v[2] = a2; v[3] = a3;
+                    if (bx >= 1 && by >= 1 && bz >= 1) {
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) s.Dn[q][l] = v[q];
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) shd[q * BN + p] = v[q];
+    }
+    __syncthreads();
+
+    const int tx = tid % TX, ty = tid / TX;
+    const size_t x = x0 + tx, y = y0 + ty;
+    if (x + 1 < d.nx && y + 1 < d.ny) {
+#pragma unroll 1
+        for (int tz = 0; tz < TZ; ++tz) {
+            const size_t z = z0 + tz;
+            if (z + 1 >= d.nz) break;
+            const size_t l = x + nx * y + nxny * z;
+            if (!(__ldg(s.mm + l) & 1)) continue;
+            const int b = (tx + 1) + BX * ((ty + 1) + BY * (tz + 1));
+            constexpr int sx = 1, sy = BX, sz = BX * BY;
+            const float nu0 = shd[b];
+            const float xs = shd[b - sx] + shd[b + sx];
+            const float ys = shd[b - sy] + shd[b + sy];
+            const float zs = shd[b - sz] + shd[b + sz];
+            const float en = __ldg(s.Pc[1] + l), cn = __ldg(s.Pc[0] + l);
+            const float e1 = pc.tau1 * (en - pc.lhh * nu0 - pc.lhx * xs - pc.lhy * ys - pc.lhz * zs);
+            const float c1 = cn + (pc.hx * (shd[BN + b] - shd[BN + b - sx]) + pc.hy * (shd[2 * BN + b] - shd[2 * BN + b - sy]) +
+                                   pc.hz * (shd[3 * BN + b] - shd[3 * BN + b - sz]) +
+                                   (pc.whh * nu0 + pc.whx * xs + pc.why * ys + pc.whz * zs));
+            s.Pn[0][l] = c1;
+            s.Pn[1][l] = e1;
+            if (check) {
+                double a, bb, c, e;
+                mon_terms(c1, cn, e1, en, a, bb, c, e);
+                acc[0] += a; acc[1] += bb; acc[2] += c; acc[3] += e;
+            }
+        }
+    }
+    (void)THREADS;
+}
+
+// One TX x TY column tile, planes [zs, zs + cz) of the interior, of the
+// fused TGV (TGV) or TV iteration with (TX+4)(TY+4) threads; smem holds
+// 2 x (NB + ND) planes of (TX+4)(TY+4) floats.  acc receives this thread's
+// FP64 monitor terms when check is set.
+template <int TX, int TY, bool TGV>
+__device__ __forceinline__ void column_pd(const FusedArgs &s, const DualC<float> &dc, const PrimalC<float> &pc,
+                                          const Dims &d, int cz, unsigned tile, bool check, float *smem, double *acc)
+{
+    constexpr int WX = TX + 4, WY = TY + 4, NT = WX * WY;
+    constexpr int NB = TGV ? 5 : 2;   // extragradient arrays: chi_, eta_, w1_, w2_, w3_
+    constexpr int ND = TGV ? 10 : 4;  // dual arrays: nu, p1..3, q1..6
+    float *B = smem;                  // [2][NB][NT]  extragradient point of one plane
+    float *S = B + 2 * NB * NT;       // [2][ND][NT]  dual of one plane
+    const long x0 = 1 + (long)(tile % s.gx) * TX, y0 = 1 + (long)((tile / s.gx) % s.gy) * TY;
+    const long zs = 1 + (long)(tile / (s.gx * s.gy)) * cz;
+    const long ze = min(zs + (long)cz, (long)d.nz - 1);
+    const int tid = threadIdx.x, tx = tid % WX, ty = tid / WX;
+    const long x = x0 - 2 + tx, y = y0 - 2 + ty;
+    const bool valid = x >= 0 && y >= 0 && x < (long)d.nx && y < (long)d.ny;
+    const bool ring1 = tx >= 1 && tx <= TX + 2 && ty >= 1 && ty <= TY + 2;  // dual is evaluated here
+    const bool owned = tx >= 2 && tx <= TX + 1 && ty >= 2 && ty <= TY + 1 && x + 1 < (long)d.nx && y + 1 < (long)d.ny;
+    const size_t nxny = d.nxny();
+    const size_t col = valid ? (size_t)x + d.nx * (size_t)y : 0;
+    const long nz = (long)d.nz;
+
+    // Every global input is fetched one plane step before it is used, so the
+    // memory latency of a plane overlaps the arithmetic of the previous one.
+    //   raw iterates n, n-1 (+ mask bit m) of the own column, plane j+2
+    float rc[NB], rp[NB];
+    bool rm = false;
+    auto fetch_bars = [&](long z) {
+        rm = valid && z >= 0 && z < nz && (__ldg(s.mm + col + nxny * (size_t)z) & 1);
+        const size_t l = col + nxny * (size_t)(rm ? z : 0);  // an in-bounds address even when unused
+#pragma unroll
+        for (int q = 0; q < NB; ++q) {
+            rc[q] = rm ? __ldg(s.Pc[q] + l) : 0.0f;
+            rp[q] = rm ? __ldg(s.Pp[q] + l) : 0.0f;
+        }
+    };
+    auto make_bars = [&](float *v) {
+#pragma unroll
+        for (int q = 0; q < NB; ++q) v[q] = rm ? rc[q] + 1.0f * (rc[q] - rp[q]) : 0.0f;
+    };
+    //   dual state n and f at plane j+1 (ring threads inside mi)
+    float rd[ND], rf = 0.0f;
+    bool rmi = false;
+    auto fetch_dual = [&](long z) {
+        rmi = ring1 && valid && z >= 1 && z + 1 < nz && (__ldg(s.mm + col + nxny * (size_t)z) & 2);
+        const size_t l = col + nxny * (size_t)(rmi ? z : 0);
+#pragma unroll
+        for (int q = 0; q < ND; ++q) rd[q] = rmi ? __ldg(s.Dc[q] + l) : 0.0f;
+        rf = rmi ? __ldg(s.f + l) : 0.0f;
+    };
+    //   iterate n at plane j (primal of the next step), owned threads inside m
+    float rpc[NB];
+    bool rpm = false;
+    auto fetch_primal = [&](long z) {
+        rpm = owned && z >= zs && z < ze && (__ldg(s.mm + col + nxny * (size_t)z) & 1);
+        const size_t l = col + nxny * (size_t)(rpm ? z : 0);
+#pragma unroll
+        for (int q = 0; q < NB; ++q) rpc[q] = rpm ? __ldg(s.Pc[q] + l) : 0.0f;
+    };
+
+    // registers: extragradient point of planes j-1, j, j+1 (own column)
+    float bm[NB], b0[NB], bp[NB];
+    fetch_bars(zs - 2);
+    make_bars(bm);
+    fetch_bars(zs - 1);
+    make_bars(b0);
+    {
+        float *Bw = B + ((zs - 1) & 1) * NB * NT;
+#pragma unroll
+        for (int q = 0; q < NB; ++q) Bw[q * NT + tid] = b0[q];
+    }
+    fetch_bars(zs);
+    fetch_dual(zs - 1);
+    // own dual of plane j-2 (read by the primal at j-1 through its z-1 neighbour)
+    float nu_m2 = 0.f, p3_m2 = 0.f, q3_m2 = 0.f, q5_m2 = 0.f, q6_m2 = 0.f;
+    __syncthreads();
+
+    for (long j = zs - 1; j <= ze; ++j) {
+        float *Bj = B + (j & 1) * NB * NT;              // extragradient of plane j (written last step)
+        float *Bn = B + ((j + 1) & 1) * NB * NT;        // plane j+1 (written now)
+        float *Sj = S + (j & 1) * ND * NT;              // dual of plane j (written now; held plane j-2)
+        const float *Sm = S + ((j + 1) & 1) * ND * NT;  // dual of plane j-1
+
+        // own dual values of plane j-2 before plane j overwrites them
+        if (owned && j - 1 >= zs) {
+            nu_m2 = Sj[tid];
+            p3_m2 = Sj[3 * NT + tid];
+            if (TGV) {
+                q3_m2 = Sj[6 * NT + tid];
+                q5_m2 = Sj[8 * NT + tid];
+                q6_m2 = Sj[9 * NT + tid];
+            }
+        }
+
+        // (a) extragradient point of plane j+1 (fetched last step); fetch plane j+2
+        make_bars(bp);
+#pragma unroll
+        for (int q = 0; q < NB; ++q) Bn[q * NT + tid] = bp[q];
+        fetch_bars(j + 2);
+
+        // (b) dual at plane j from the state fetched last step; fetch plane j+1
+        float v[ND];
+        const bool do_dual = rmi;
+        float dcur[ND], fcur = rf;
+#pragma unroll
+        for (int q = 0; q < ND; ++q) dcur[q] = rd[q];
+        // the primal's iterate of plane j-1 (fetched last step)
+        float pcur[NB];
+        const bool do_primal = rpm;
+#pragma unroll
+        for (int q = 0; q < NB; ++q) pcur[q] = rpc[q];
+        fetch_dual(j + 1);
+        fetch_primal(j);
+#pragma unroll
+        for (int q = 0; q < ND; ++q) v[q] = 0.0f;
+        if (do_dual) {
+            const size_t l = col + nxny * (size_t)j;
+            const float c0 = b0[0];
+            const float cxm = Bj[tid - 1], cxp = Bj[tid + 1], cym = Bj[tid - WX], cyp = Bj[tid + WX];
+            const float czm = bm[0], czp = bp[0];
+            const float *E = Bj + NT;
+            const float lap = dc.lhh * b0[1] + dc.lhx * (E[tid - 1] + E[tid + 1]) +
+                              dc.lhy * (E[tid - WX] + E[tid + WX]) + dc.lhz * (bm[1] + bp[1]);
+            const float wav = dc.whh * c0 + dc.whx * (cxm + cxp) + dc.why * (cym + cyp) + dc.whz * (czm + czp);
+            v[0] = dcur[0] + ((lap - wav) + fcur);
+            if (TGV) {
+                const float w1 = b0[2], w2 = b0[3], w3 = b0[4];
+                float a1 = dcur[1] + dc.hx * (cxp - c0) - dc.sg * w1;
+                float a2 = dcur[2] + dc.hy * (cyp - c0) - dc.sg * w2;
+                float a3 = dcur[3] + dc.hz * (czp - c0) - dc.sg * w3;
+                float t = a1 * a1 + a2 * a2 + a3 * a3;
+                if (t > dc.alp12) {
+                    t = dc.alp1 / sqrtf(t);
+                    a1 = a1 * t; a2 = a2 * t; a3 = a3 * t;
+                }
+                v[1] = a1; v[2] = a2; v[3] = a3;
+                const float *W1 = Bj + 2 * NT, *W2 = Bj + 3 * NT, *W3 = Bj + 4 * NT;
+                const float w1x = W1[tid + 1], w1y = W1[tid + WX], w1z = bp[2];
+                const float w2x = W2[tid + 1], w2y = W2[tid + WX], w2z = bp[3];
+                const float w3x = W3[tid + 1], w3y = W3[tid + WX], w3z = bp[4];
+                float r1 = dcur[4] + dc.hx * (w1x - w1);
+                float r2 = dcur[5] + dc.hx2 * (w2x - w2) + dc.hy2 * (w1y - w1);
+                float r3 = dcur[6] + dc.hx2 * (w3x - w3) + dc.hz2 * (w1z - w1);
+                float r4 = dcur[7] + dc.hy * (w2y - w2);
+                float r5 = dcur[8] + dc.hy2 * (w3y - w3) + dc.hz2 * (w2z - w2);
+                float r6 = dcur[9] + dc.hz * (w3z - w3);
+                t = r1 * r1 + r4 * r4 + r6 * r6 + 2.0f * (r2 * r2 + r3 * r3 + r5 * r5);
+                if (t > dc.alp02) {
+                    t = dc.alp0 / sqrtf(t);
+                    r1 = r1 * t; r2 = r2 * t; r3 = r3 * t; r4 = r4 * t; r5 = r5 * t; r6 = r6 * t;
+                }
+                v[4] = r1; v[5] = r2; v[6] = r3; v[7] = r4; v[8] = r5; v[9] = r6;
+            } else {
+                float a1 = dcur[1] + dc.hx * (cxp - c0);
+                float a2 = dcur[2] + dc.hy * (cyp - c0);
+                float a3 = dcur[3] + dc.hz * (czp - c0);
+                float t = a1 * a1 + a2 * a2 + a3 * a3;
+                if (t > dc.alp12) {
+                    t = dc.alp1 / sqrtf(t);
+                    a1 = a1 * t; a2 = a2 * t; a3 = a3 * t;
+                }
+                v[1] = a1; v[2] = a2; v[3] = a3;
+            }
+            if (owned && j >= zs && j < ze) {
+#pragma unroll
+                for (int q = 0; q < ND; ++q) s.Dn[q][l] = v[q];
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < ND; ++q) Sj[q * NT + tid] = v[q];
+
+        // (c) primal + extragradient at plane j-1
+        if (do_primal) {
+            const size_t l = col + nxny * (size_t)(j - 1);
+            const float nu0 = Sm[tid];
+            const float xs = Sm[tid - 1] + Sm[tid + 1];
+            const float ys = Sm[tid - WX] + Sm[tid + WX];
+            const float zs_ = nu_m2 + v[0];
+            const float cn = pcur[0], en = pcur[1];
+            const float e1 = pc.tau1 * (en - pc.lhh * nu0 - pc.lhx * xs - pc.lhy * ys - pc.lhz * zs_);
+            const float *P1 = Sm + NT, *P2 = Sm + 2 * NT, *P3 = Sm + 3 * NT;
+            const float c1 = cn + (pc.hx * (P1[tid] - P1[tid - 1]) + pc.hy * (P2[tid] - P2[tid - WX]) +
+                                   pc.hz * (P3[tid] - p3_m2) +
+                                   (pc.whh * nu0 + pc.whx * xs + pc.why * ys + pc.whz * zs_));
+            s.Pn[0][l] = c1;
+            s.Pn[1][l] = e1;
+            if (TGV) {
+                const float *Q1 = Sm + 4 * NT, *Q2 = Sm + 5 * NT, *Q3 = Sm + 6 * NT, *Q4 = Sm + 7 * NT,
+                            *Q5 = Sm + 8 * NT, *Q6 = Sm + 9 * NT;
+                const float u1 = pcur[2] + (pc.tt * P1[tid] + pc.hx * (Q1[tid] - Q1[tid - 1] + Q2[tid] - Q2[tid - WX] +
+                                                                        Q3[tid] - q3_m2));
+                const float u2 = pcur[3] + (pc.tt * P2[tid] + pc.hy * (Q2[tid] - Q2[tid - 1] + Q4[tid] - Q4[tid - WX] +
+                                                                        Q5[tid] - q5_m2));
+                const float u3 = pcur[4] + (pc.tt * P3[tid] + pc.hz * (Q3[tid] - Q3[tid - 1] + Q5[tid] - Q5[tid - WX] +
+                                                                        Q6[tid] - q6_m2));
+                s.Pn[2][l] = u1;
+                s.Pn[3][l] = u2;
+                s.Pn[4][l] = u3;
+            }
+            if (check) {
+                double a, b, c, e;
+                mon_terms(c1, cn, e1, en, a, b, c, e);
+                acc[0] += a; acc[1] += b; acc[2] += c; acc[3] += e;
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < NB; ++q) {
+            bm[q] = b0[q];
+            b0[q] = bp[q];
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace qsm
