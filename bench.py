@@ -188,6 +188,17 @@ def poisson_arm(qsm_gb300, ctx, torch):
     return out
 
 
+def _generate(fn, *cols):
+    """fn over the argument columns in spawned worker processes (input
+    generation only; spawn is safe after CUDA initialisation)."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+
+    workers = max(1, min(16, (os.cpu_count() or 1) - 1, len(cols[0])))
+    with cf.ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+        return list(ex.map(fn, *cols))
+
+
 def _batch_case(b, shape):
     """Volume b of the batched configuration: the 64^3 recipe (12 ellipsoids,
     semi-axes U[4,16], chi U[-0.1,0.1] ppm, noise 0.01 ppm) at this size, in
@@ -211,7 +222,7 @@ def batch_arm(qsm_gb300, ctx, torch, count=32, iters=500):
 
     sizes = S.config3_sizes(seed=3, count=count)
     t0 = time.perf_counter()
-    cases = [_batch_case(b, s) for b, s in enumerate(sizes)]
+    cases = _generate(_batch_case, list(range(count)), sizes)
     gen_s = time.perf_counter() - t0
     d2fs = [torch.from_numpy(np.ascontiguousarray(c[0].transpose(2, 1, 0))).cuda() for c in cases]
     masks = [torch.from_numpy(np.ascontiguousarray(c[1].transpose(2, 1, 0))).cuda() for c in cases]
@@ -257,7 +268,7 @@ def serve_arm(qsm_gb300, ctx, seconds=30.0, rate=4.0, per_kind=6, budget=160 * 1
     from qsm_gb300 import serve
 
     t0 = time.perf_counter()
-    pool = serve.make_pool(per_kind, seed=4)
+    pool = serve.make_pool(per_kind, seed=4, workers=max(1, min(16, (os.cpu_count() or 1) - 1)))
     gen_s = time.perf_counter() - t0
     alone, err = {}, {k: [] for k in serve.KINDS}
     for kind in serve.KINDS:

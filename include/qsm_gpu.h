@@ -119,6 +119,29 @@ qsm_status qsm_pd_tv_fused(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3],
                            double lam, double tol, uint32_t maxiter, uint32_t verbose,
                            void *chi, qsm_pd_info *info);
 
+/* ---------------- FFT total-variation inversion (ADMM) ---------------- */
+
+typedef struct {
+    uint32_t iters;        /* ADMM iterations run */
+    double rho;            /* final penalty parameter */
+    double nr, eps_pri;    /* primal residual and its tolerance at the last iteration */
+    double ns, eps_dual;   /* dual residual and its tolerance */
+    double seconds;        /* device time of the iterations */
+} qsm_tv_info;
+
+/* x = tv(f, mask, vsz, bdir, opts) for one 3-D volume:
+ * src/inversion/tv.m:101-277 (tv_), dipole kernel dipoleKernel.m:56-65, Laplace
+ * symbol laplaceKernel.m / tv.m:140-142; opts as tv.m:38-82 (defaults mu 7.5e3,
+ * tv 1 anisotropic | 2 isotropic, rtol 0.1, atol 1e-4, maxit 20, rho 9, alpha 1.5,
+ * rtau 0.7, stau 100, gamma 3).  Arithmetic in dtype (FP64 as MATLAB's default
+ * class), reductions in FP64; cuFFT R2C/C2R with a fused k-space multiply.
+ * Every dimension must be >= 3.  info may be NULL. */
+qsm_status qsm_tv_admm(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3], const void *f,
+                       const uint8_t *mask, const double vsz[3], const double bdir[3], double mu,
+                       int32_t tv, double rtol, double atol, int32_t maxit, double rho,
+                       double alpha, double rtau, double stau, double gamma, int32_t verbose,
+                       void *x, qsm_tv_info *info);
+
 /* ---------------- finite-difference operators (in place) ---------------- */
 
 /* gradf_mex(dx, dy, dz, u, h): src/utils/fd/mex/gradf_mex.c:13-47 */

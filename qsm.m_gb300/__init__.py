@@ -26,14 +26,14 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from ._lib import MgInfo, PdInfo, QsmError, QsmLibraryError, context, lib
+from ._lib import MgInfo, PdInfo, QsmError, QsmLibraryError, TvInfo, context, lib
 
 __all__ = [
     "pd_tgv_mex", "pd_tv_mex", "gradf_mex", "gradb_mex", "gradc_mex", "gradfm_mex", "gradbm_mex", "gradcm_mex",
     "gradf_adj_mex", "gradb_adj_mex", "gradfm_adj_mex", "gradbm_adj_mex", "gradfp_mex", "gradfp_adj_mex",
     "lap1_mex", "lapw_mex", "gauss_seidel_mex", "residual_mex", "lapmg_mex", "restrict_mex", "prolong_mex",
     "correct_mex", "coarsen_grid_mex", "boundary_mask_mex", "boundary_mask_l1_mex", "norm2_mex", "mgpcg_mex",
-    "mg_mex", "fmg_mex", "lane_dot", "pd_tv_batch", "pd_tgv_batch", "Session", "footprint", "QsmError",
+    "mg_mex", "fmg_mex", "lane_dot", "tv", "pd_tv_batch", "pd_tgv_batch", "Session", "footprint", "QsmError",
     "QsmLibraryError", "context", "lib",
 ]
 
@@ -381,6 +381,48 @@ def fmg_mex(f, mask, vsz, tol, maxit, mu, npre, npost, nboundary, nlevels, *, in
                    int(npre), int(npost), int(nboundary), int(nlevels), o.ptr, ctypes.byref(mi))
     if info is not None:
         info.update(cycles=mi.iters, seconds=mi.seconds)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# FFT total-variation inversion (src/inversion/tv.m)
+# ---------------------------------------------------------------------------
+
+TV_DEFAULTS = dict(mu=7.5e3, tv=1, rtol=1e-1, atol=1e-4, maxit=20, verbose=0, rho=9.0, alpha=1.5, rtau=0.7,
+                   stau=1e2, gamma=3.0)  # tv.m:38-82
+
+
+def tv(f, mask, vsz, bdir=(0.0, 0.0, 1.0), opts=None, *, info=None, ctx=None):
+    """x = tv(f, mask, vsz, bdir, opts): ADMM total-variation dipole inversion
+    with the k-space data term (tv.m).  f is 3-D, or 4-D with echoes along the
+    last axis (each echo solved in turn, tv.m:87-95).  Computes in f's dtype."""
+    o = dict(TV_DEFAULTS)
+    if opts:
+        o.update({k: v for k, v in dict(opts).items() if v is not None})
+    b = np.asarray(bdir, dtype=np.float64).reshape(3)
+    bd = (ctypes.c_double * 3)(*b)
+    if not _is_torch(f) and np.ndim(f) == 4:
+        f4 = np.asarray(f)
+        out = np.zeros(f4.shape, dtype=f4.dtype, order="F")
+        infos = []
+        for t in range(f4.shape[3]):
+            it = {}
+            out[..., t] = tv(np.asfortranarray(f4[..., t]), mask, vsz, bdir, o, info=it, ctx=ctx)
+            infos.append(it)
+        if info is not None:
+            info.update(echoes=infos)
+        return out
+    fa, m = _Arr(f), _Arr(mask, mask=True)
+    out = _zeros_like(fa)
+    oa = _Arr(out, writable=True)
+    ti = TvInfo()
+    _sync_torch(fa, m, oa)
+    _ctx(ctx).call("qsm_tv_admm", fa.dt, fa.dims_c(), fa.ptr, m.ptr, _h(vsz), bd, float(o["mu"]), int(o["tv"]),
+                   float(o["rtol"]), float(o["atol"]), int(o["maxit"]), float(o["rho"]), float(o["alpha"]),
+                   float(o["rtau"]), float(o["stau"]), float(o["gamma"]), int(o["verbose"]), oa.ptr, ctypes.byref(ti))
+    if info is not None:
+        info.update(iters=ti.iters, rho=ti.rho, nr=ti.nr, eps_pri=ti.eps_pri, ns=ti.ns, eps_dual=ti.eps_dual,
+                    seconds=ti.seconds)
     return out
 
 

@@ -46,6 +46,12 @@ class PdInfo(ctypes.Structure):
                 ("active_voxels", ctypes.c_uint64), ("tile", ctypes.c_uint32 * 3)]
 
 
+class TvInfo(ctypes.Structure):
+    _fields_ = [("iters", ctypes.c_uint32), ("rho", ctypes.c_double), ("nr", ctypes.c_double),
+                ("eps_pri", ctypes.c_double), ("ns", ctypes.c_double), ("eps_dual", ctypes.c_double),
+                ("seconds", ctypes.c_double)]
+
+
 class MgInfo(ctypes.Structure):
     _fields_ = [("iters", ctypes.c_int32), ("resnorm", ctypes.c_double), ("seconds", ctypes.c_double),
                 ("resnorm_hist", ctypes.POINTER(ctypes.c_double))]
@@ -82,6 +88,8 @@ SIGNATURES = {
     "qsm_mgpcg_mixed": [SZ3, P, P, U8, D3, DBL, I32, DBL, I32, I32, I32, I32, I32, I32, I32, P, ctypes.POINTER(MgInfo)],
     "qsm_mg": [I32, SZ3, P, P, U8, D3, DBL, I32, I32, I32, I32, I32, I32, P, ctypes.POINTER(MgInfo)],
     "qsm_fmg": [I32, SZ3, P, U8, D3, DBL, I32, I32, I32, I32, I32, I32, P, ctypes.POINTER(MgInfo)],
+    "qsm_tv_admm": [I32, SZ3, P, U8, D3, D3, DBL, I32, DBL, DBL, I32, DBL, DBL, DBL, DBL, DBL, I32, P,
+                    ctypes.POINTER(TvInfo)],
     # count volumes: dims (size_t[3*count]), arrays of d2f / mask / chi pointers
     "qsm_pd_tv_batch": [I32, U32, P, P, P, D3, DBL, DBL, U32, P, P],
     "qsm_pd_tgv_batch": [I32, U32, P, P, P, D3, DBL, DBL, DBL, U32, P, P],

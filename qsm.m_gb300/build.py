@@ -25,7 +25,7 @@ NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "--prec-div=true", "--prec-sqrt=true",
     "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "-Xptxas", "-O3",
 ]
-SOURCES = ["common.cu", "fd.cu", "pd.cu", "pd_fused.cu", "pd_stream.cu", "pd_batch.cu", "mg.cu", "noalloc.cu"]
+SOURCES = ["common.cu", "fd.cu", "pd.cu", "pd_fused.cu", "pd_stream.cu", "pd_batch.cu", "tv_admm.cu", "mg.cu", "noalloc.cu"]
 
 
 def nvcc() -> str:
@@ -65,7 +65,7 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(lambda s: _compile(s, extra), SOURCES))
     tmp = LIB + ".tmp"
-    cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
+    cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-lcufft"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -18,6 +18,8 @@
 //                           per iteration for the stopping test
 #include <math.h>
 #include <stdlib.h>
+#include <mutex>
+#include <set>
 #include <vector>
 
 #include "common.cuh"
@@ -558,6 +560,21 @@ struct Hier {
 
 static inline size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
 
+// The coarse solver's dynamic shared-memory limit is a process-wide function
+// attribute: raise it once per device to the opt-in maximum, so concurrent
+// solves on several host threads never lower it under each other's launch.
+template <typename T>
+static qsm_status coarse_smem_limit(qsm_ctx *ctx, int maxsm)
+{
+    static std::mutex mu;
+    static std::set<int> done;
+    std::lock_guard<std::mutex> lock(mu);
+    if (done.count(ctx->device)) return QSM_OK;
+    QSM_CUDA(cudaFuncSetAttribute(coarse_solve_k<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm));
+    done.insert(ctx->device);
+    return QSM_OK;
+}
+
 template <typename T>
 static qsm_status hier_init(qsm_ctx *ctx, Hier<T> &H, int nl, const Dims &dp, const double *h)
 {
@@ -591,8 +608,7 @@ static qsm_status hier_init(qsm_ctx *ctx, Hier<T> &H, int nl, const Dims &dp, co
     int maxsm = 0;
     cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
     H.coarse_in_smem = H.coarse_smem <= (size_t)maxsm && nc < (1u << 18);
-    if (H.coarse_in_smem)
-        QSM_CUDA(cudaFuncSetAttribute(coarse_solve_k<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)H.coarse_smem));
+    if (H.coarse_in_smem) QSM_TRY(coarse_smem_limit<T>(ctx, maxsm));
     return QSM_OK;
 }
 

@@ -1,0 +1,497 @@
+// FFT total-variation inversion (ADMM) of src/inversion/tv.m:101-277 on the
+// GPU: the data term's solve u = real(ifft3(iA .* (F + fft3(r)))) runs as a
+// cuFFT R2C, one fused pointwise k-space kernel, and a cuFFT C2R; the
+// gradient, shrinkage, multiplier update and residual norms are fused
+// stencil kernels.  Only the five convergence scalars per iteration go to
+// the host, which applies tv.m's stopping test and rho update (:226-268).
+//
+// k-space terms are evaluated where they are used, from the grid indices:
+//   D(k) = 1/3 - (k.b)^2/|k|^2, D(0) = 0, k_a = fftfreq(n_a, h_a)
+//        (dipoleKernel.m:56-65, ifftshifted so DC is first);
+//   L(k) = sum_a (2/h_a^2)(1 - cos(2 pi i_a/n_a)), the symbol of the negated
+//        7-point Laplacian (laplaceKernel.m, tv.m:140-142);
+//   iA   = 1/(mu D^2 + rho L), 0 where not finite (tv.m:144-145);
+// so no N-sized iA, K or L array is stored or re-read, and a rho update
+// costs nothing.  u = real(ifft3(X)) equals the C2R of the Hermitian part
+// of X; the stored half spectrum therefore carries, on planes where index
+// negation is not frequency negation (even-size Nyquist planes) and B0 is
+// oblique, the average of the multipliers at k and at the negated index.
+//
+// FP64 (the MATLAB default class) or FP32 arithmetic by dtype; every
+// reduction accumulates in FP64 with a fixed order (block partials folded
+// in block order), so results are run-to-run deterministic.
+#include <cufft.h>
+#include <math.h>
+#include <stdio.h>
+
+#include <algorithm>
+
+#include "common.cuh"
+
+namespace qsm {
+
+template <typename T> struct CxT;
+template <> struct CxT<double> { using type = cufftDoubleComplex; };
+template <> struct CxT<float> { using type = cufftComplex; };
+
+constexpr int TV_BLOCK = 256;
+constexpr int TV_GRID = 4 * 152;   // grid-stride reductions: fixed block count
+constexpr int TV_NSUM = 5;         // nr, na, nb, ||s||^2, ||rho grad' l||^2
+
+struct TvK {
+    int nx, ny, nz, nxh;   // real dims, half-spectrum x extent
+    double hx, hy, hz;     // voxel size
+    double bx, by, bz;     // unit B0 direction
+    double mu;
+    bool oblique;          // B0 has two or more non-zero components
+};
+
+__device__ __forceinline__ double fftfreq(int i, int n, double h) { return (double)(i <= (n - 1) / 2 ? i : i - n) / (n * h); }
+
+// D and L at half-spectrum index (i, j, k) with signs s of the frequencies
+__device__ __forceinline__ void dl_at(const TvK &K, double fx, double fy, double fz, int i, int j, int k, double &D,
+                                      double &L)
+{
+    const double kb = K.bx * fx + K.by * fy + K.bz * fz;
+    const double k2 = fx * fx + fy * fy + fz * fz;
+    D = (i == 0 && j == 0 && k == 0) ? 0.0 : 1.0 / 3.0 - (kb * kb) / k2;
+    L = (2.0 / (K.hx * K.hx)) * (1.0 - cospi(2.0 * i / K.nx)) + (2.0 / (K.hy * K.hy)) * (1.0 - cospi(2.0 * j / K.ny)) +
+        (2.0 / (K.hz * K.hz)) * (1.0 - cospi(2.0 * k / K.nz));
+}
+
+__device__ __forceinline__ double inv_a(double K, double L, double rho)
+{
+    const double a = 1.0 / (K + rho * L);
+    return isfinite(a) ? a : 0.0;
+}
+
+// X = iA .* (mu D .* fhat + R) / N in place of R (tv.m:172-175)
+template <typename T>
+__global__ void kmul_k(typename CxT<T>::type *R, const typename CxT<T>::type *__restrict__ fhat, TvK K, double rho,
+                       double invn)
+{
+    const size_t nh = (size_t)K.nxh * K.ny * K.nz;
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < nh; q += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(q % K.nxh), j = (int)((q / K.nxh) % K.ny), k = (int)(q / ((size_t)K.nxh * K.ny));
+        const double fx = fftfreq(i, K.nx, K.hx), fy = fftfreq(j, K.ny, K.hy), fz = fftfreq(k, K.nz, K.hz);
+        double D, L;
+        dl_at(K, fx, fy, fz, i, j, k, D, L);
+        double a = inv_a(K.mu * D * D, L, rho), ad = a * (K.mu * D);
+        const bool nyq = (2 * i == K.nx) || (2 * j == K.ny) || (2 * k == K.nz);
+        if (K.oblique && nyq) {
+            // the negated index keeps Nyquist frequencies and flips the others
+            const double gx = 2 * i == K.nx ? fx : -fx, gy = 2 * j == K.ny ? fy : -fy, gz = 2 * k == K.nz ? fz : -fz;
+            double D2, L2;
+            dl_at(K, gx, gy, gz, i, j, k, D2, L2);
+            const double a2 = inv_a(K.mu * D2 * D2, L2, rho);
+            ad = 0.5 * (ad + a2 * (K.mu * D2));
+            a = 0.5 * (a + a2);
+        }
+        const typename CxT<T>::type fh = fhat[q], r = R[q];
+        typename CxT<T>::type o;
+        o.x = (T)((ad * (double)fh.x + a * (double)r.x) * invn);
+        o.y = (T)((ad * (double)fh.y + a * (double)r.y) * invn);
+        R[q] = o;
+    }
+}
+
+struct Vox {
+    size_t l, NX, NY, NZ;
+    int i, j, k;
+};
+
+__device__ __forceinline__ Vox vox_at(size_t l, const Dims &d)
+{
+    Vox v;
+    v.l = l;
+    v.i = (int)(l % d.nx);
+    v.j = (int)((l / d.nx) % d.ny);
+    v.k = (int)(l / d.nxny());
+    v.NX = d.nx - 1;
+    v.NY = d.nx * (d.ny - 1);
+    v.NZ = d.nxny() * (d.nz - 1);
+    return v;
+}
+
+// gradfp_adj_mex.c:156-257 of the field g_c(l) (h holds -1/h), with the
+// reference's association order of the three axis terms.
+template <typename T, typename G>
+__device__ __forceinline__ T adj_at(const Vox &v, const Dims &d, const T *ih, G g)
+{
+    const size_t l = v.l;
+    const T a = ih[0] * (g(0, l) - g(0, v.i > 0 ? l - 1 : l + v.NX));
+    const T b = ih[1] * (g(1, l) - g(1, v.j > 0 ? l - d.nx : l + v.NY));
+    const T c = ih[2] * (g(2, l) - g(2, v.k > 0 ? l - d.nxny() : l + v.NZ));
+    return v.k == 0 ? (a + b) + c : v.j == 0 ? (c + a) + b : (c + b) + a;
+}
+
+// r = gradfp_adj(rho v - l) (tv.m:166-170)
+template <typename T>
+__global__ void adj_rhs_k(T *r, const T *__restrict__ v, const T *__restrict__ lm, Dims d, T nx_, T ny_, T nz_, T rho)
+{
+    const size_t N = d.n();
+    const T ih[3] = {nx_, ny_, nz_};
+    for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < N; l += (size_t)gridDim.x * blockDim.x) {
+        const Vox vx = vox_at(l, d);
+        r[l] = adj_at<T>(vx, d, ih, [&](int c, size_t m) { return rho * v[c * N + m] - lm[c * N + m]; });
+    }
+}
+
+template <int NS>
+__device__ __forceinline__ void block_sums(double *part, double (&acc)[NS])
+{
+    __shared__ double red[NS][TV_BLOCK];
+    const int t = threadIdx.x;
+#pragma unroll
+    for (int q = 0; q < NS; ++q) red[q][t] = acc[q];
+    __syncthreads();
+    for (int s = TV_BLOCK / 2; s > 0; s >>= 1) {
+        if (t < s)
+#pragma unroll
+            for (int q = 0; q < NS; ++q) red[q][t] += red[q][t + s];
+        __syncthreads();
+    }
+    if (t == 0)
+#pragma unroll
+        for (int q = 0; q < NS; ++q) part[q * gridDim.x + blockIdx.x] = red[q][0];
+}
+
+// grad, over-relaxation, shrinkage, multiplier update and the primal
+// residual sums of one ADMM iteration (tv.m:185-221, :227-234)
+template <typename T, bool ISO>
+__global__ void __launch_bounds__(TV_BLOCK)
+grad_shrink_k(T *vn, const T *__restrict__ vo, T *lm, const T *__restrict__ u, Dims d, T hx, T hy, T hz, T alpha,
+              T rho, T irho, double *part)
+{
+    const size_t N = d.n();
+    double acc[3] = {0.0, 0.0, 0.0};  // nr, na, nb
+    for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < N; l += (size_t)gridDim.x * blockDim.x) {
+        const Vox v = vox_at(l, d);
+        const T u0 = u[l];
+        T dd[3];
+        dd[0] = hx * ((v.i + 1 < (int)d.nx ? u[l + 1] : u[l - v.NX]) - u0);
+        dd[1] = hy * ((v.j + 1 < (int)d.ny ? u[l + d.nx] : u[l - v.NY]) - u0);
+        dd[2] = hz * ((v.k + 1 < (int)d.nz ? u[l + d.nxny()] : u[l - v.NZ]) - u0);
+        T d1[3], r[3], w[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            d1[c] = alpha * dd[c] + ((T)1 - alpha) * vo[c * N + l];
+            r[c] = d1[c] + irho * lm[c * N + l];
+        }
+        if (ISO) {
+            T s = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+            s = (s - irho) * (T)(s > irho) / s;
+            if (!isfinite(s)) s = (T)0;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) w[c] = r[c] * s;
+        } else {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const T m = fabs(r[c]) - irho;
+                const T sg = r[c] > (T)0 ? (T)1 : r[c] < (T)0 ? (T)-1 : (T)0;
+                w[c] = (m > (T)0 ? m : (T)0) * sg;
+            }
+        }
+        double e2 = 0.0, a2 = 0.0, b2 = 0.0;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            vn[c * N + l] = w[c];
+            lm[c * N + l] = lm[c * N + l] + rho * (d1[c] - w[c]);
+            const T e = dd[c] - w[c];
+            e2 += (double)(e * e);
+            a2 += (double)(dd[c] * dd[c]);
+            b2 += (double)(w[c] * w[c]);
+        }
+        acc[0] += sqrt(e2);
+        acc[1] += sqrt(a2);
+        acc[2] += sqrt(b2);
+    }
+    block_sums<3>(part, acc);
+}
+
+// ||rho gradfp_adj(v - v_)||^2 and ||rho gradfp_adj(l)||^2 (tv.m:230, :239)
+template <typename T>
+__global__ void __launch_bounds__(TV_BLOCK)
+adj_norms_k(const T *__restrict__ vn, const T *__restrict__ vo, const T *__restrict__ lm, Dims d, T nx_, T ny_, T nz_,
+            T rho, double *part)
+{
+    const size_t N = d.n();
+    const T ih[3] = {nx_, ny_, nz_};
+    double acc[2] = {0.0, 0.0};
+    for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < N; l += (size_t)gridDim.x * blockDim.x) {
+        const Vox v = vox_at(l, d);
+        const T s = rho * adj_at<T>(v, d, ih, [&](int c, size_t m) { return vn[c * N + m] - vo[c * N + m]; });
+        const T t = rho * adj_at<T>(v, d, ih, [&](int c, size_t m) { return lm[c * N + m]; });
+        acc[0] += (double)(s * s);
+        acc[1] += (double)(t * t);
+    }
+    block_sums<2>(part, acc);
+}
+
+// initial v = grad(u), nr = sum |v| (tv.m:150-152)
+template <typename T>
+__global__ void __launch_bounds__(TV_BLOCK)
+grad_init_k(T *v, const T *__restrict__ u, Dims d, T hx, T hy, T hz, double *part)
+{
+    const size_t N = d.n();
+    double acc[1] = {0.0};
+    for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < N; l += (size_t)gridDim.x * blockDim.x) {
+        const Vox x = vox_at(l, d);
+        const T u0 = u[l];
+        const T a = hx * ((x.i + 1 < (int)d.nx ? u[l + 1] : u[l - x.NX]) - u0);
+        const T b = hy * ((x.j + 1 < (int)d.ny ? u[l + d.nx] : u[l - x.NY]) - u0);
+        const T c = hz * ((x.k + 1 < (int)d.nz ? u[l + d.nxny()] : u[l - x.NZ]) - u0);
+        v[l] = a;
+        v[N + l] = b;
+        v[2 * N + l] = c;
+        acc[0] += sqrt((double)(a * a + b * b + c * c));
+    }
+    block_sums<1>(part, acc);
+}
+
+// fold the block partials of `ns` sums in block order
+__global__ void fold_k(double *out, const double *__restrict__ part, int ns, int nblk)
+{
+    const int q = threadIdx.x;
+    if (q >= ns) return;
+    double s = 0.0;
+    for (int b = 0; b < nblk; ++b) s += part[q * nblk + b];
+    out[q] = s;
+}
+
+template <typename T, typename S>
+__global__ void cvt_in_k(T *o, const S *__restrict__ a, size_t n)
+{
+    for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x)
+        o[l] = (T)a[l];
+}
+
+// x = mask .* u (tv.m:275)
+template <typename T, typename S>
+__global__ void mask_out_k(S *x, const T *__restrict__ u, const uint8_t *__restrict__ m, size_t n)
+{
+    for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x)
+        x[l] = (S)((m[l] ? (T)1 : (T)0) * u[l]);
+}
+
+static const char *cufft_str(cufftResult r)
+{
+    switch (r) {
+    case CUFFT_SUCCESS: return "CUFFT_SUCCESS";
+    case CUFFT_ALLOC_FAILED: return "CUFFT_ALLOC_FAILED";
+    case CUFFT_INVALID_VALUE: return "CUFFT_INVALID_VALUE";
+    case CUFFT_INVALID_SIZE: return "CUFFT_INVALID_SIZE";
+    case CUFFT_EXEC_FAILED: return "CUFFT_EXEC_FAILED";
+    default: return "cuFFT error";
+    }
+}
+
+#define QSM_FFT(call)                                                                           \
+    do {                                                                                        \
+        cufftResult r_ = (call);                                                                \
+        if (r_ != CUFFT_SUCCESS) {                                                              \
+            ::qsm::set_error(ctx, "%s:%d %s: %s", __FILE__, __LINE__, #call, cufft_str(r_));    \
+            st = r_ == CUFFT_ALLOC_FAILED ? QSM_ERR_NOMEM : QSM_ERR_CUDA;                      \
+            goto done;                                                                          \
+        }                                                                                       \
+    } while (0)
+
+#define QSM_STEP(expr)           \
+    do {                         \
+        st = (expr);             \
+        if (st != QSM_OK) goto done; \
+    } while (0)
+
+static qsm_status cuda_st(qsm_ctx *ctx, cudaError_t e, const char *what)
+{
+    if (e == cudaSuccess) return QSM_OK;
+    set_error(ctx, "%s: %s", what, cudaGetErrorString(e));
+    return QSM_ERR_CUDA;
+}
+
+struct TvOpts {
+    double mu, rtol, atol, rho, alpha, rtau, stau, gamma;
+    int tv, maxit, verbose;
+};
+
+template <typename T, typename S>
+static qsm_status tv_run(qsm_ctx *ctx, const Dims &d, const S *f, const uint8_t *mask, const double *h,
+                         const double *bdir, TvOpts o, S *xout, qsm_tv_info *info)
+{
+    using C = typename CxT<T>::type;
+    const size_t N = d.n();
+    const int nxh = (int)(d.nx / 2 + 1);
+    const size_t nh = (size_t)nxh * d.ny * d.nz;
+    // u, r, v[2] (3 components each, N apart), l (3); fhat, R; partials + sums
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t rb = al(N * sizeof(T)), vb = al(3 * N * sizeof(T)), cb = al(nh * sizeof(C));
+    const size_t bytes = 2 * rb + 3 * vb + 2 * cb + (TV_NSUM * TV_GRID + 64) * sizeof(double);
+    void *blk = nullptr;
+    QSM_TRY(dalloc(ctx, &blk, bytes));
+    char *c = (char *)blk;
+    T *u = (T *)c; c += rb;
+    T *r = (T *)c; c += rb;
+    T *v[2];
+    v[0] = (T *)c; c += vb;
+    v[1] = (T *)c; c += vb;
+    T *lm = (T *)c; c += vb;
+    C *fhat = (C *)c; c += cb;
+    C *R = (C *)c; c += cb;
+    double *part = (double *)c;
+    double *sums = part + TV_NSUM * TV_GRID;
+
+    qsm_status st = QSM_OK;
+    cufftHandle pf = 0, pi = 0;
+    bool havef = false, havei = false;
+    const cufftType tf = sizeof(T) == 8 ? CUFFT_D2Z : CUFFT_R2C, ti = sizeof(T) == 8 ? CUFFT_Z2D : CUFFT_C2R;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    double hs[TV_NSUM];
+    double nr = 0.0, nr_, ns = 0.0, na, nb, ep = 0.0, ed = 0.0, rho = o.rho, irho = 1.0 / o.rho;
+    int flag = 0, cur = 0;
+    uint32_t it = 0;
+    const double atolp = sqrt(3.0 * (double)N) * o.atol, atold = sqrt((double)N) * o.atol;
+    TvK K;
+    K.nx = (int)d.nx; K.ny = (int)d.ny; K.nz = (int)d.nz; K.nxh = nxh;
+    K.hx = h[0]; K.hy = h[1]; K.hz = h[2];
+    {
+        const double bn = sqrt(bdir[0] * bdir[0] + bdir[1] * bdir[1] + bdir[2] * bdir[2]);
+        K.bx = bdir[0] / bn; K.by = bdir[1] / bn; K.bz = bdir[2] / bn;
+        K.oblique = ((bdir[0] != 0.0) + (bdir[1] != 0.0) + (bdir[2] != 0.0)) > 1;
+    }
+    K.mu = o.mu;
+    const T ihx = (T)(1.0 / h[0]), ihy = (T)(1.0 / h[1]), ihz = (T)(1.0 / h[2]);
+    const dim3 g(TV_GRID), b(TV_BLOCK);
+    const unsigned gk = (unsigned)std::min<size_t>((nh + TV_BLOCK - 1) / TV_BLOCK, 8 * 152);
+
+    QSM_STEP(cuda_st(ctx, cudaMemsetAsync(lm, 0, 3 * N * sizeof(T), ctx->stream), "memset"));
+    QSM_FFT(cufftPlan3d(&pf, (int)d.nz, (int)d.ny, (int)d.nx, tf));
+    havef = true;
+    QSM_FFT(cufftPlan3d(&pi, (int)d.nz, (int)d.ny, (int)d.nx, ti));
+    havei = true;
+    QSM_FFT(cufftSetStream(pf, ctx->stream));
+    QSM_FFT(cufftSetStream(pi, ctx->stream));
+    QSM_STEP(cuda_st(ctx, cudaEventCreate(&e0), "event"));
+    QSM_STEP(cuda_st(ctx, cudaEventCreate(&e1), "event"));
+    QSM_STEP(cuda_st(ctx, cudaEventRecord(e0, ctx->stream), "event"));
+
+    // u = f; fhat = fft3(f) (F = mu conj(D) fhat is formed in kmul_k)
+    cvt_in_k<T, S><<<g, b, 0, ctx->stream>>>(u, f, N);
+    if (sizeof(T) == 8) QSM_FFT(cufftExecD2Z(pf, (cufftDoubleReal *)u, (cufftDoubleComplex *)fhat));
+    else QSM_FFT(cufftExecR2C(pf, (cufftReal *)u, (cufftComplex *)fhat));
+    grad_init_k<T><<<g, b, 0, ctx->stream>>>(v[0], u, d, ihx, ihy, ihz, part);
+    fold_k<<<1, 32, 0, ctx->stream>>>(sums, part, 1, TV_GRID);
+    QSM_STEP(cuda_st(ctx, cudaMemcpyAsync(hs, sums, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "copy"));
+    QSM_STEP(cuda_st(ctx, cudaStreamSynchronize(ctx->stream), "sync"));
+    nr = hs[0];
+    if (o.verbose) printf("\niter\t\t||r||\t\teps_pri\t\t||s||\t\teps_dual\n");
+
+    for (int ii = 1; ii <= o.maxit; ++ii) {
+        it = (uint32_t)ii;
+        const int nxt = cur ^ 1;
+        // u-subproblem
+        adj_rhs_k<T><<<g, b, 0, ctx->stream>>>(r, v[cur], lm, d, -ihx, -ihy, -ihz, (T)rho);
+        if (sizeof(T) == 8) QSM_FFT(cufftExecD2Z(pf, (cufftDoubleReal *)r, (cufftDoubleComplex *)R));
+        else QSM_FFT(cufftExecR2C(pf, (cufftReal *)r, (cufftComplex *)R));
+        kmul_k<T><<<gk, TV_BLOCK, 0, ctx->stream>>>(R, fhat, K, rho, 1.0 / (double)N);
+        if (sizeof(T) == 8) QSM_FFT(cufftExecZ2D(pi, (cufftDoubleComplex *)R, (cufftDoubleReal *)u));
+        else QSM_FFT(cufftExecC2R(pi, (cufftComplex *)R, (cufftReal *)u));
+        // v-subproblem, multipliers, residuals
+        if (o.tv == 1)
+            grad_shrink_k<T, false><<<g, b, 0, ctx->stream>>>(v[nxt], v[cur], lm, u, d, ihx, ihy, ihz, (T)o.alpha,
+                                                              (T)rho, (T)irho, part);
+        else
+            grad_shrink_k<T, true><<<g, b, 0, ctx->stream>>>(v[nxt], v[cur], lm, u, d, ihx, ihy, ihz, (T)o.alpha,
+                                                             (T)rho, (T)irho, part);
+        adj_norms_k<T><<<g, b, 0, ctx->stream>>>(v[nxt], v[cur], lm, d, -ihx, -ihy, -ihz, (T)rho, part + 3 * TV_GRID);
+        fold_k<<<1, 32, 0, ctx->stream>>>(sums, part, TV_NSUM, TV_GRID);
+        QSM_STEP(cuda_st(ctx, cudaGetLastError(), "launch"));
+        QSM_STEP(cuda_st(ctx, cudaMemcpyAsync(hs, sums, TV_NSUM * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "copy"));
+        QSM_STEP(cuda_st(ctx, cudaStreamSynchronize(ctx->stream), "sync"));
+        cur = nxt;
+        nr_ = nr;
+        nr = hs[0];
+        na = hs[1];
+        nb = hs[2];
+        ns = sqrt(hs[3]);
+        ep = atolp + o.rtol * std::max(na, nb);
+        ed = atold + o.rtol * sqrt(hs[4]);
+        if (o.verbose) printf("%3d/%d\t\t%.4e\t%.4e\t%.4e\t%.4e\n", ii, o.maxit, nr, ep, ns, ed);
+        if (nr < ep && ns < ed) break;
+        // rho update (tv.m:247-268)
+        if (nr > o.stau * ns || (nr > o.rtau * nr_ && flag < 3)) {
+            rho = o.gamma * rho;
+            irho = 1.0 / rho;
+            if (flag > 5) flag = 0;
+        } else if (nr < ns / o.stau) {
+            rho = rho / (o.gamma * o.gamma);
+            irho = 1.0 / rho;
+            flag = flag + 1;
+        }
+    }
+    if (o.verbose) printf("\n");
+    QSM_STEP(cuda_st(ctx, cudaEventRecord(e1, ctx->stream), "event"));
+    mask_out_k<T, S><<<g, b, 0, ctx->stream>>>(xout, u, mask, N);
+    QSM_STEP(cuda_st(ctx, cudaGetLastError(), "launch"));
+    QSM_STEP(cuda_st(ctx, cudaStreamSynchronize(ctx->stream), "sync"));
+    if (info) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        info->iters = it;
+        info->rho = rho;
+        info->nr = nr;
+        info->eps_pri = ep;
+        info->ns = ns;
+        info->eps_dual = ed;
+        info->seconds = ms * 1e-3;
+    }
+done:
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (havef) cufftDestroy(pf);
+    if (havei) cufftDestroy(pi);
+    qsm_status st2 = dfree(ctx, blk);
+    return st != QSM_OK ? st : st2;
+}
+
+}  // namespace qsm
+
+using namespace qsm;
+
+extern "C" qsm_status qsm_tv_admm(qsm_ctx *ctx, qsm_dtype dt, const size_t dims[3], const void *f, const uint8_t *mask,
+                                  const double vsz[3], const double bdir[3], double mu, int32_t tv, double rtol,
+                                  double atol, int32_t maxit, double rho, double alpha, double rtau, double stau,
+                                  double gamma, int32_t verbose, void *x, qsm_tv_info *info)
+{
+    if (!ctx || !dims || !f || !mask || !vsz || !bdir || !x) return QSM_ERR_ARG;
+    if (dt != QSM_F32 && dt != QSM_F64) return QSM_ERR_DTYPE;
+    if (tv != 1 && tv != 2) return QSM_ERR_ARG;
+    if (maxit < 0 || !(rho > 0.0)) return QSM_ERR_ARG;
+    if (bdir[0] == 0.0 && bdir[1] == 0.0 && bdir[2] == 0.0) return QSM_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    const Dims d = make_dims(dims);
+    if (d.nx < 3 || d.ny < 3 || d.nz < 3) {
+        set_error(ctx, "tv: every dimension must be >= 3 (padarray of the 3x3x3 Laplace kernel)");
+        return QSM_ERR_DIMS;
+    }
+    if (d.nx > 0x7fffffff || d.ny > 0x7fffffff || d.nz > 0x7fffffff) return QSM_ERR_DIMS;
+    const size_t es = dt == QSM_F32 ? 4 : 8;
+    Staged sf, sm, sx;
+    QSM_TRY(stage_in(ctx, sf, f, d.n() * es, true));
+    QSM_TRY(stage_in(ctx, sm, mask, d.n(), true));
+    QSM_TRY(stage_in(ctx, sx, x, d.n() * es, false));
+    TvOpts o{mu, rtol, atol, rho, alpha, rtau, stau, gamma, tv, maxit, verbose};
+    qsm_status st;
+    if (dt == QSM_F64)
+        st = tv_run<double, double>(ctx, d, (const double *)sf.dev, (const uint8_t *)sm.dev, vsz, bdir, o,
+                                    (double *)sx.dev, info);
+    else
+        st = tv_run<float, float>(ctx, d, (const float *)sf.dev, (const uint8_t *)sm.dev, vsz, bdir, o,
+                                  (float *)sx.dev, info);
+    stage_out(ctx, sf, false);
+    stage_out(ctx, sm, false);
+    if (st != QSM_OK) {
+        stage_out(ctx, sx, false);
+        return st;
+    }
+    return stage_out(ctx, sx, true);
+}

@@ -84,27 +84,44 @@ def arrivals(rate: float, duration: float, seed: int, mix=(0.4, 0.3, 0.3), pool_
         out.append(Request(len(out), float(t), kind, int(rng.integers(pool_size))))
 
 
-def make_pool(per_kind: int, seed: int, sizes=None) -> dict:
+def pool_case(kind: str, shape, case_seed: int) -> dict:
+    """One seeded input case (see make_pool)."""
+    from . import synthetic
+
+    shape = tuple(int(n) for n in shape)
+    if kind == "poisson":
+        f, m, _ = synthetic.poisson_case(shape, case_seed, semi=(0.3 * min(shape), 0.45 * min(shape)))
+        return dict(shape=shape, f=f, mask=m)
+    mask = synthetic.ellipsoid_mask(shape, [0.42 * n for n in shape])
+    d2f, mask, _ = synthetic.tgv_case(shape, case_seed, n_ell=12, chi=(-0.1, 0.1), noise=0.01, mask=mask)
+    return dict(shape=shape, d2f=d2f.astype(np.float32, order="F"), mask=mask)
+
+
+def make_pool(per_kind: int, seed: int, sizes=None, workers: int = 1) -> dict:
     """Seeded inputs: per kind `per_kind` cases with volume sizes drawn as in
     the batched configuration (each axis from {96..256}x{96..256}x{64..176}
     in steps of 16).  PD cases: an ellipsoid phantom and its field as in the
-    64^3 configuration (noise 0.01 ppm); Poisson cases: the 256^3 Poisson
-    recipe at that size."""
+    64^3 configuration (noise 0.01 ppm) in an inscribed ellipsoidal mask;
+    Poisson cases: the 256^3 Poisson recipe at that size.  workers > 1
+    generates in spawned processes (safe after CUDA initialisation)."""
     from . import synthetic
 
-    pool = {k: [] for k in KINDS}
+    jobs = []
     for ki, kind in enumerate(KINDS):
         shp = sizes or synthetic.config3_sizes(seed=seed + 10 * ki, count=per_kind)
         for c in range(per_kind):
-            shape = tuple(shp[c % len(shp)])
-            cs = seed * 1000 + ki * 100 + c
-            if kind == "poisson":
-                f, m, _ = synthetic.poisson_case(shape, cs, semi=(0.3 * min(shape), 0.45 * min(shape)))
-                pool[kind].append(dict(shape=shape, f=f, mask=m))
-            else:
-                mask = synthetic.ellipsoid_mask(shape, [0.42 * n for n in shape])
-                d2f, mask, _ = synthetic.tgv_case(shape, cs, n_ell=12, chi=(-0.1, 0.1), noise=0.01, mask=mask)
-                pool[kind].append(dict(shape=shape, d2f=d2f.astype(np.float32, order="F"), mask=mask))
+            jobs.append((kind, tuple(shp[c % len(shp)]), seed * 1000 + ki * 100 + c))
+    if workers > 1:
+        import concurrent.futures as cf
+        import multiprocessing as mp
+
+        with cf.ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+            cases = list(ex.map(pool_case, *zip(*jobs)))
+    else:
+        cases = [pool_case(*j) for j in jobs]
+    pool = {k: [] for k in KINDS}
+    for (kind, _, _), case in zip(jobs, cases):
+        pool[kind].append(case)
     return pool
 
 

@@ -167,3 +167,18 @@ def test_session_admission_budget(gpu_ctx, qsm):
             s.submit_mgpcg(None, np.zeros((8, 8, 8)), np.ones((8, 8, 8), np.uint8), [1, 1, 1], *MG_ARGS)
     ref = qsm.pd_tv_mex(b[0], b[1], [1, 1, 1], 0.003, 0.0, 30, fused=True)
     assert bits_equal(chi, ref)
+
+
+def test_session_concurrent_poisson_sizes(gpu_ctx, qsm):
+    """Several Poisson solves of different sizes (different coarse grids) run
+    at once on the worker streams; each equals its stand-alone solve."""
+    cases = [_poisson(s, 700 + k) for k, s in enumerate([(40, 36, 34), (58, 50, 44), (33, 61, 29), (70, 40, 52)])]
+    with qsm.Session(poisson_workers=3) as s:
+        ids = [s.submit_mgpcg(None, f, m, [1, 1, 1], *MG_ARGS, mixed=mixed)
+               for (f, m), mixed in zip(cases, (True, False, True, True))]
+        while s.running():
+            s.step(30)
+        outs = [s.fetch(i) for i in ids]
+    for (f, m), mixed, out in zip(cases, (True, False, True, True), outs):
+        ref = qsm.mgpcg_mex(None, f, m, [1, 1, 1], *MG_ARGS, mixed=mixed)
+        assert bits_equal(out, ref), first_diff(out, ref)
