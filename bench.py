@@ -238,11 +238,13 @@ def batch_arm(qsm_gb300, ctx, torch, count=32, iters=500):
     vox = sum(int(np.prod(s)) for s in sizes)
     active = sum(int(i["active_voxels"]) for i in infos)
     # the same volumes one after another (device time of each solve's loop)
-    seq_s, same = 0.0, True
+    seq_s, same, per_vol = 0.0, True, []
     for b in range(count):
         inf = {}
         chi = qsm_gb300.pd_tv_mex(d2fs[b], masks[b], [1, 1, 1], 1e-3, 0.0, iters, fused=True, info=inf, ctx=ctx)
         seq_s += inf["seconds"]
+        per_vol.append([list(sizes[b]), int(inf["active_voxels"]), round(70 * inf["active_voxels"] * iters /
+                                                                          inf["seconds"] / 1e9, 1)])
         same = same and bool(torch.equal(chi, outs[b]))
     tiles = sorted({tuple(i["tile"]) for i in infos})
     return {"workload": f"{count} TV volumes, sizes from {{96..256}}x{{96..256}}x{{64..176}} step 16, lam 1e-3, "
@@ -253,7 +255,8 @@ def batch_arm(qsm_gb300, ctx, torch, count=32, iters=500):
             "hbm_gbs": 70 * active * iters / dev_s / 1e9, "bytes_per_voxel_iter": 70,
             "one_by_one_device_s": seq_s, "speedup_vs_one_by_one": seq_s / dev_s,
             "same_as_one_by_one": same, "tiles": [list(t) for t in tiles], "input_generation_s": gen_s,
-            "gpu_launches_per_iteration": len(tiles)}
+            "gpu_launches_per_iteration": len(tiles),
+            "one_by_one_gbs_per_volume": per_vol}
 
 
 def serve_arm(qsm_gb300, ctx, seconds=30.0, rate=4.0, per_kind=6, budget=160 * 10**9):
@@ -350,6 +353,12 @@ def run_ours(args):
 
     ctx = qsm_gb300.context(local)
     stream = torch.cuda.ExternalStream(qsm_gb300.lib().qsm_ctx_get_stream(ctx.handle))
+    if args.only in ("batch", "serve"):
+        out = batch_arm(qsm_gb300, ctx, torch) if args.only == "batch" else \
+            serve_arm(qsm_gb300, ctx, seconds=args.serve_seconds)
+        if rank == 0:
+            print(json.dumps({"profile_run": True, args.only: out}))
+        return
     ITERS = args.iters
     d2f, mask = _case(tuple(int(v) for v in args.shape.split(",")) if args.shape else None)
     N = d2f.size
@@ -493,7 +502,8 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=30.0, help="arrival window of the served arm")
     ap.add_argument("--shape", default="", help="nx,ny,nz of a reduced volume (profiler captures)")
     ap.add_argument("--iters", type=int, default=ITERS, help="iterations per inversion (profiler captures)")
-    ap.add_argument("--only", default="all", choices=["all", "fused"], help="run only the fused arm")
+    ap.add_argument("--only", default="all", choices=["all", "fused", "batch", "serve"],
+                    help="run only one arm (profiling aid)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -6,30 +6,34 @@
 // Here a session keeps every admitted solve's state resident in HBM and
 // advances all primal-dual solves together:
 //
-//   * one persistent kernel per (tile variant, TV|TGV) group and iteration
-//     walks a work list of (volume, active tile) items that spans every
-//     resident volume of that group; CTAs take items from a device counter
-//     (dynamic load balance over uneven volumes) and run the same tile /
-//     column body as the one-volume fused kernels (pd_tile.cuh), so each
-//     volume's chi is bit-identical to its one-volume fused solve;
-//   * per-volume descriptors (state pointers for each of the 6 buffer
-//     rotations, constants, iteration window, monitor scratch) live in a
-//     device table; a CTA copies its item's descriptor into shared memory;
 //   * 30 iterations (the period of the 3-buffer primal / 2-buffer dual
 //     rotation and of the every-10th-iteration monitor) are captured once
-//     into a CUDA graph with one launch chain per group on its own stream
-//     (groups touch disjoint volumes, so their chains overlap), then
-//     replayed; the graph is re-captured only when the resident set changes;
+//     into a CUDA graph and replayed; the graph is re-captured only when the
+//     resident set changes.  Kernels read the iteration count from a device
+//     counter that the graph advances, so replays need no host work;
+//   * a volume large enough to keep part of the GPU busy runs its one-volume
+//     fused kernel (pd_fused.cu / pd_stream.cu, tile shape from the
+//     autotuner) in its own graph branch; the branches of different volumes
+//     overlap on the device;
+//   * tiny volumes are packed: one persistent kernel per (tile variant,
+//     TV|TGV) chunk and iteration walks a work list of (volume, active tile)
+//     items spanning up to 56 volumes, whose descriptors (state pointers of
+//     each of the 6 buffer rotations, constants, iteration window, monitor
+//     scratch) are one kernel parameter; it runs the same tile / column body
+//     (pd_tile.cuh);
+//   * either way each volume's chi is bit-identical to its one-volume fused
+//     solve;
 //   * a volume admitted between replays starts at the session's iteration
 //     base (a multiple of 30), so its buffer phase and monitor iterations
 //     are the graph's; a volume whose monitors met tol, or that reached its
-//     maxiter, is skipped by every later item of its own;
+//     maxiter, does nothing in later launches;
 //   * Poisson solves (mgpcg) run whole on worker threads, each with its own
 //     stream and context, concurrently with the primal-dual replays.
 //
 // Admission is by device footprint against the session's byte budget.
 #include <math.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -50,9 +54,18 @@
 namespace qsm {
 
 constexpr uint32_t kGraphIters = 30;  // lcm(3, 2, 10)
+// A volume with at least (SM count) / kSoloDiv active tiles runs its
+// one-volume kernel (state pointers as constant operands) in its own graph
+// branch; branches overlap, so even a volume of a fraction of a wave keeps
+// the GPU busy.  Only tinier volumes are packed into persistent
+// multi-volume launches, whose per-item descriptor reads cost more than a
+// launch saves above that size (measured on 32 volumes of 0.5-3.8 M
+// voxels: branches 0.74 s, persistent packing 1.03 s, one volume after
+// another 0.88 s).
+constexpr int kSoloDiv = 4;
 constexpr int kPhases = 6;            // lcm(3, 2)
 
-// One volume, one buffer rotation.
+// One volume, one buffer rotation (512 bytes).
 struct BatchVol {
     FusedArgs a;        // tiles unused; part/count/ctl are the volume's own
     DualC<float> dc;
@@ -61,78 +74,71 @@ struct BatchVol {
     double tol;
     uint32_t maxiter;   // iterations of this solve
     uint32_t start;     // session iteration at which it started (multiple of kGraphIters)
-    uint32_t item0;     // first work item of this volume in its group's list
+    uint32_t item0;     // first work item of this volume in its chunk's list
     uint32_t nitems;    // its active tiles
 };
 
-// Persistent loop over the work items of one group.  items[w] = (volume,
-// tile); sched[0] hands out items, sched[1] counts exited CTAs (the last
-// one re-arms both for the next launch).
+// The descriptors of up to kChunkVols volumes travel as one kernel
+// parameter (constant bank, read-only: the kernels read state pointers as
+// cheaply as the one-volume kernels do); a larger group is split into
+// several chunks, each its own persistent launch.
+constexpr int kChunkVols = 56;
+struct BatchChunk {
+    BatchVol v[kChunkVols];
+};
+static_assert(sizeof(BatchChunk) + 64 <= 32764, "kernel parameter limit");
+
+// Persistent loop over the work items of one chunk: CTA b takes items b,
+// b + gridDim.x, ... (items are tiles of equal size, so a static stride
+// balances).  items[w] = (volume in the chunk, tile).  Whether a volume is
+// past its maxiter or converged is read once when a CTA first meets one of
+// its items: `done` cannot change while items of that volume are still
+// unprocessed in this launch (the fold that sets it is its last item's).
 template <int THREADS, typename Work>
-__device__ __forceinline__ void batch_loop(const BatchVol *__restrict__ vols, const uint2 *__restrict__ items,
-                                           uint32_t nitems, uint32_t g, unsigned *sched, bool check, double *red,
-                                           BatchVol &sv, Work work)
+__device__ __forceinline__ void batch_loop(const BatchChunk &P, const uint2 *__restrict__ items, uint32_t nitems,
+                                           uint32_t g, bool check, double *red, Work work)
 {
-    __shared__ unsigned sw;
     __shared__ int sskip;
     uint32_t loaded = 0xffffffffu;
-    for (;;) {
+    for (uint32_t w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const uint2 it = __ldg(items + w);
+        const BatchVol &v = P.v[it.x];
         __syncthreads();  // the previous item is done with shared memory
-        if (threadIdx.x == 0) sw = atomicAdd(sched, 1u);
-        __syncthreads();
-        const unsigned w = sw;
-        if (w >= nitems) break;
-        const uint2 it = items[w];
         if (it.x != loaded) {
-            const uint32_t *src = (const uint32_t *)(vols + it.x);
-            uint32_t *dst = (uint32_t *)&sv;
-            for (int k = threadIdx.x; k < (int)(sizeof(BatchVol) / 4); k += THREADS) dst[k] = src[k];
+            if (threadIdx.x == 0) sskip = (g - v.start >= v.maxiter) || *(volatile uint32_t *)&v.a.ctl->done;
             loaded = it.x;
             __syncthreads();
         }
-        if (threadIdx.x == 0)
-            sskip = (g - sv.start >= sv.maxiter) || *(volatile uint32_t *)&sv.a.ctl->done;
-        __syncthreads();
         if (sskip) continue;
         double acc[4] = {0.0, 0.0, 0.0, 0.0};
-        work(sv, it.y, acc);
+        work(v, it.y, acc);
         if (check)
-            monitor_fold<THREADS>(sv.a.part, sv.a.count, sv.a.ctl, sv.nitems, w - sv.item0, red, acc, sv.tol,
-                                  g - sv.start + 1);
-    }
-    if (threadIdx.x == 0) {
-        __threadfence();
-        if (atomicAdd(sched + 1, 1u) == gridDim.x - 1) {
-            sched[0] = 0;
-            sched[1] = 0;
-        }
+            monitor_fold<THREADS>(v.a.part, v.a.count, v.a.ctl, v.nitems, w - v.item0, red, acc, v.tol,
+                                  g - v.start + 1);
     }
 }
 
 template <int TX, int TY, int TZ, int MINB, bool TGV, bool CHECK>
 __global__ void __launch_bounds__(TX * TY, MINB)
-batch_tile_k(const BatchVol *vols, const uint2 *items, uint32_t nitems, const uint32_t *gbase, uint32_t i,
-             unsigned *sched)
+batch_tile_k(const __grid_constant__ BatchChunk P, const uint2 *items, uint32_t nitems, const uint32_t *gbase,
+             uint32_t i)
 {
     extern __shared__ double smem_raw[];
-    __shared__ BatchVol sv;
     const uint32_t g = *gbase + i;
-    batch_loop<TX * TY>(vols, items, nitems, g, sched, CHECK, smem_raw, sv,
-                        [&](const BatchVol &v, unsigned tile, double *acc) {
-                            if (TGV) tile_tgv<TX, TY, TZ>(v.a, v.dc, v.pc, v.d, tile, CHECK, (float *)smem_raw, acc);
-                            else tile_tv<TX, TY, TZ>(v.a, v.dc, v.pc, v.d, tile, CHECK, (float *)smem_raw, acc);
-                        });
+    batch_loop<TX * TY>(P, items, nitems, g, CHECK, smem_raw, [&](const BatchVol &v, unsigned tile, double *acc) {
+        if (TGV) tile_tgv<TX, TY, TZ>(v.a, v.dc, v.pc, v.d, tile, CHECK, (float *)smem_raw, acc);
+        else tile_tv<TX, TY, TZ>(v.a, v.dc, v.pc, v.d, tile, CHECK, (float *)smem_raw, acc);
+    });
 }
 
 template <int TX, int TY, bool TGV, bool CHECK>
 __global__ void __launch_bounds__((TX + 4) * (TY + 4), 1)
-batch_column_k(const BatchVol *vols, const uint2 *items, uint32_t nitems, const uint32_t *gbase, uint32_t i,
-               unsigned *sched, int cz)
+batch_column_k(const __grid_constant__ BatchChunk P, const uint2 *items, uint32_t nitems, const uint32_t *gbase,
+               uint32_t i, int cz)
 {
     extern __shared__ double smem_raw[];
-    __shared__ BatchVol sv;
     const uint32_t g = *gbase + i;
-    batch_loop<(TX + 4) * (TY + 4)>(vols, items, nitems, g, sched, CHECK, smem_raw, sv,
+    batch_loop<(TX + 4) * (TY + 4)>(P, items, nitems, g, CHECK, smem_raw,
                                     [&](const BatchVol &v, unsigned tile, double *acc) {
                                         column_pd<TX, TY, TGV>(v.a, v.dc, v.pc, v.d, cz, tile, CHECK,
                                                                (float *)smem_raw, acc);
@@ -144,9 +150,6 @@ __global__ void advance_k(uint32_t *gbase, uint32_t n) { *gbase += n; }
 // ---------------------------------------------------------------------------
 // kernel table
 // ---------------------------------------------------------------------------
-
-using BatchFn = void (*)(const BatchVol *, const uint2 *, uint32_t, const uint32_t *, uint32_t, unsigned *);
-using ColumnFn = void (*)(const BatchVol *, const uint2 *, uint32_t, const uint32_t *, uint32_t, unsigned *, int);
 
 struct BatchKernel {
     const void *fn[2];  // [check]
@@ -219,12 +222,15 @@ struct MgJob {
     size_t bytes = 0;
 };
 
-struct Group {
+// Up to kChunkVols volumes of one (tile variant, kind) group: one persistent
+// launch per iteration.
+struct Chunk {
     int var = 0;
     bool tgv = false;
+    std::vector<PdJob *> vols;
     std::vector<uint2> items;
-    uint2 *d_items = nullptr;     // inside the session's item buffer
-    unsigned *d_sched = nullptr;  // 2 counters
+    std::unique_ptr<BatchChunk[]> phase;  // descriptors of each of the kPhases rotations
+    uint2 *d_items = nullptr;             // inside the session's item buffer
     unsigned grid = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
@@ -241,18 +247,19 @@ struct qsm_session {
 
     // iteration base: host mirror and device copy
     uint32_t gbase = 0;
-    void *dev_blk = nullptr;  // gbase + sched counters
+    void *dev_blk = nullptr;  // the device iteration base
     uint32_t *d_gbase = nullptr;
-    unsigned *d_sched = nullptr;
 
     // batched work of the resident running primal-dual solves
     bool dirty = true;
+    bool serial = false;            // chunks one after another on the session stream
+    bool one_cta_per_item = false;  // grid = items instead of a persistent grid
+    uint32_t solo_tiles = 0;        // volumes with at least this many active tiles run solo
     std::vector<PdJob *> running;
-    BatchVol *d_vols = nullptr;
-    size_t vols_cap = 0;
+    std::vector<PdJob *> solo;      // one-volume kernels, one graph branch each
     uint2 *d_items = nullptr;
     size_t items_cap = 0;
-    std::vector<Group> groups;
+    std::vector<Chunk> chunks;
     cudaStream_t gstream[2 * kNumVariants] = {};
     cudaEvent_t gdone[2 * kNumVariants] = {};
     cudaEvent_t fork = nullptr, ev0 = nullptr, ev1 = nullptr;
@@ -335,55 +342,53 @@ qsm_status rebuild(qsm_session *s)
         cudaGraphExecDestroy(s->exec);
         s->exec = nullptr;
     }
-    s->groups.clear();
-    const size_t nv = s->running.size();
+    s->chunks.clear();
+    s->solo.clear();
     s->dirty = false;
-    if (nv == 0) return QSM_OK;
+    if (s->running.empty()) return QSM_OK;
 
-    // groups by (variant, kind); items in volume order, tiles ascending
-    std::map<std::pair<int, int>, size_t> gi;
-    std::vector<BatchVol> hv(kPhases * nv);
-    std::vector<uint32_t> item0(nv), gidx(nv);
-    for (size_t k = 0; k < nv; ++k) {
-        PdJob *j = s->running[k];
+    // chunks of one (variant, kind) group, volumes in admission order
+    std::map<std::pair<int, int>, size_t> open;  // group -> chunk being filled
+    for (PdJob *j : s->running) {
+        if (j->tiles.size() >= s->solo_tiles) {
+            s->solo.push_back(j);
+            continue;
+        }
         const auto key = std::make_pair(j->v.var, (int)j->v.tgv);
-        auto it = gi.find(key);
-        if (it == gi.end()) {
-            it = gi.emplace(key, s->groups.size()).first;
-            Group g;
-            g.var = j->v.var;
-            g.tgv = j->v.tgv;
-            s->groups.push_back(g);
+        auto it = open.find(key);
+        if (it == open.end() || s->chunks[it->second].vols.size() == (size_t)kChunkVols) {
+            Chunk c;
+            c.var = j->v.var;
+            c.tgv = j->v.tgv;
+            s->chunks.push_back(std::move(c));
+            open[key] = s->chunks.size() - 1;
+            it = open.find(key);
         }
-        Group &g = s->groups[it->second];
-        gidx[k] = (uint32_t)it->second;
-        item0[k] = (uint32_t)g.items.size();
-        for (unsigned t : j->tiles) g.items.push_back(make_uint2((unsigned)k, t));
-    }
-    for (size_t k = 0; k < nv; ++k) {
-        PdJob *j = s->running[k];
-        for (int p = 0; p < kPhases; ++p) {
-            BatchVol &b = hv[p * nv + k];
-            memset(&b, 0, sizeof b);
-            b.a = pd_volume_args(j->v, j->v.var, (uint32_t)p);
-            b.a.tiles = nullptr;
-            b.dc = j->v.dc;
-            b.pc = j->v.pc;
-            b.d = j->v.d;
-            b.tol = j->tol;
-            b.maxiter = j->maxiter;
-            b.start = j->start;
-            b.item0 = item0[k];
-            b.nitems = (uint32_t)j->tiles.size();
-        }
+        s->chunks[it->second].vols.push_back(j);
     }
     size_t nitems = 0;
-    for (auto &g : s->groups) nitems += g.items.size();
-    if (hv.size() > s->vols_cap) {
-        if (s->d_vols) QSM_TRY(dfree(ctx, s->d_vols));
-        s->d_vols = nullptr;
-        s->vols_cap = std::max(hv.size(), 2 * s->vols_cap);
-        QSM_TRY(dalloc(ctx, (void **)&s->d_vols, s->vols_cap * sizeof(BatchVol)));
+    for (auto &c : s->chunks) {
+        c.phase.reset(new BatchChunk[kPhases]);
+        memset(c.phase.get(), 0, kPhases * sizeof(BatchChunk));
+        for (size_t k = 0; k < c.vols.size(); ++k) {
+            PdJob *j = c.vols[k];
+            const uint32_t item0 = (uint32_t)c.items.size();
+            for (unsigned t : j->tiles) c.items.push_back(make_uint2((unsigned)k, t));
+            for (int p = 0; p < kPhases; ++p) {
+                BatchVol &b = c.phase[p].v[k];
+                b.a = pd_volume_args(j->v, j->v.var, (uint32_t)p);
+                b.a.tiles = nullptr;
+                b.dc = j->v.dc;
+                b.pc = j->v.pc;
+                b.d = j->v.d;
+                b.tol = j->tol;
+                b.maxiter = j->maxiter;
+                b.start = j->start;
+                b.item0 = item0;
+                b.nitems = (uint32_t)j->tiles.size();
+            }
+        }
+        nitems += c.items.size();
     }
     if (nitems > s->items_cap) {
         if (s->d_items) QSM_TRY(dfree(ctx, s->d_items));
@@ -391,57 +396,72 @@ qsm_status rebuild(qsm_session *s)
         s->items_cap = std::max(nitems, 2 * s->items_cap);
         QSM_TRY(dalloc(ctx, (void **)&s->d_items, s->items_cap * sizeof(uint2)));
     }
-    QSM_CUDA(cudaMemcpyAsync(s->d_vols, hv.data(), hv.size() * sizeof(BatchVol), cudaMemcpyHostToDevice, ctx->stream));
     size_t off = 0;
     int sm = 0;
     QSM_CUDA(cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, ctx->device));
-    for (size_t q = 0; q < s->groups.size(); ++q) {
-        Group &g = s->groups[q];
-        g.d_items = s->d_items + off;
-        g.d_sched = s->d_sched + 2 * q;
-        QSM_CUDA(cudaMemcpyAsync(g.d_items, g.items.data(), g.items.size() * sizeof(uint2), cudaMemcpyHostToDevice,
+    for (size_t q = 0; q < s->chunks.size(); ++q) {
+        Chunk &c = s->chunks[q];
+        c.d_items = s->d_items + off;
+        QSM_CUDA(cudaMemcpyAsync(c.d_items, c.items.data(), c.items.size() * sizeof(uint2), cudaMemcpyHostToDevice,
                                  ctx->stream));
-        off += g.items.size();
-        const BatchKernel bk = batch_kernel(g.var, g.tgv);
-        const int threads = variant_threads(g.var);
-        const size_t smem = variant_smem(g.var, g.tgv);
+        off += c.items.size();
+        const BatchKernel bk = batch_kernel(c.var, c.tgv);
         int occ = 0;
-        QSM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bk.fn[0], threads, smem));
+        QSM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bk.fn[0], variant_threads(c.var),
+                                                               variant_smem(c.var, c.tgv)));
         occ = std::max(occ, 1);
-        g.grid = (unsigned)std::min<size_t>(g.items.size(), (size_t)sm * occ);
-        g.stream = s->gstream[q];
-        g.done = s->gdone[q];
+        c.grid = (unsigned)std::min<size_t>(c.items.size(), (size_t)sm * occ);
+        if (s->one_cta_per_item) c.grid = (unsigned)c.items.size();
+        c.stream = s->serial ? ctx->stream : s->gstream[q % (2 * kNumVariants)];
+        c.done = s->gdone[q % (2 * kNumVariants)];
     }
     QSM_CUDA(cudaStreamSynchronize(ctx->stream));
 
-    // capture kGraphIters iterations: one launch chain per group, forked from
+    // capture kGraphIters iterations: one launch chain per chunk, forked from
     // and joined back into the session stream, then the base advance
     cudaGraph_t graph = nullptr;
     QSM_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     cudaError_t ce = cudaEventRecord(s->fork, ctx->stream);
-    for (size_t q = 0; q < s->groups.size() && ce == cudaSuccess; ++q) {
-        Group &g = s->groups[q];
-        ce = cudaStreamWaitEvent(g.stream, s->fork, 0);
-        const BatchKernel bk = batch_kernel(g.var, g.tgv);
-        const int threads = variant_threads(g.var);
-        const size_t smem = variant_smem(g.var, g.tgv);
-        uint32_t n = (uint32_t)g.items.size();
+    for (size_t q = 0; q < s->chunks.size() && ce == cudaSuccess; ++q) {
+        Chunk &c = s->chunks[q];
+        if (!s->serial && q < (size_t)(2 * kNumVariants)) ce = cudaStreamWaitEvent(c.stream, s->fork, 0);
+        const BatchKernel bk = batch_kernel(c.var, c.tgv);
+        const int threads = variant_threads(c.var);
+        const size_t smem = variant_smem(c.var, c.tgv);
+        uint32_t n = (uint32_t)c.items.size();
         for (uint32_t i = 0; i < kGraphIters && ce == cudaSuccess; ++i) {
             const bool chk = ((i + 1) % 10) == 0;
-            const BatchVol *vp = s->d_vols + (size_t)(i % kPhases) * nv;
+            BatchChunk *P = &c.phase[i % kPhases];
             if (bk.column) {
-                int cz = variant(g.var).tz;
-                void *args[] = {(void *)&vp, (void *)&g.d_items, (void *)&n, (void *)&s->d_gbase, (void *)&i,
-                                (void *)&g.d_sched, (void *)&cz};
-                ce = cudaLaunchKernel(bk.fn[chk], dim3(g.grid), dim3(threads), args, smem, g.stream);
+                int cz = variant(c.var).tz;
+                void *args[] = {(void *)P, (void *)&c.d_items, (void *)&n, (void *)&s->d_gbase, (void *)&i,
+                                (void *)&cz};
+                ce = cudaLaunchKernel(bk.fn[chk], dim3(c.grid), dim3(threads), args, smem, c.stream);
             } else {
-                void *args[] = {(void *)&vp, (void *)&g.d_items, (void *)&n, (void *)&s->d_gbase, (void *)&i,
-                                (void *)&g.d_sched};
-                ce = cudaLaunchKernel(bk.fn[chk], dim3(g.grid), dim3(threads), args, smem, g.stream);
+                void *args[] = {(void *)P, (void *)&c.d_items, (void *)&n, (void *)&s->d_gbase, (void *)&i};
+                ce = cudaLaunchKernel(bk.fn[chk], dim3(c.grid), dim3(threads), args, smem, c.stream);
             }
         }
-        if (ce == cudaSuccess) ce = cudaEventRecord(g.done, g.stream);
-        if (ce == cudaSuccess) ce = cudaStreamWaitEvent(ctx->stream, g.done, 0);
+    }
+    // solo volumes: their one-volume kernels, each volume on the next stream
+    const size_t nbranch = s->chunks.size() + s->solo.size();
+    for (size_t q = 0; q < s->solo.size() && ce == cudaSuccess; ++q) {
+        PdJob *j = s->solo[q];
+        const size_t slot = s->chunks.size() + q;
+        cudaStream_t st = s->serial ? ctx->stream : s->gstream[slot % (2 * kNumVariants)];
+        if (!s->serial && slot < (size_t)(2 * kNumVariants)) ce = cudaStreamWaitEvent(st, s->fork, 0);
+        for (uint32_t i = 0; i < kGraphIters && ce == cudaSuccess; ++i) {
+            FusedArgs a = pd_volume_args(j->v, j->v.var, i % kPhases);
+            a.gbase = s->d_gbase;
+            a.start = j->start;
+            a.maxiter = j->maxiter;
+            if (pd_volume_launch(ctx, st, j->v, ((i + 1) % 10) == 0, a, j->tol, i) != QSM_OK) ce = cudaErrorLaunchFailure;
+        }
+    }
+    // join every stream used (branches sharing a stream are already ordered)
+    for (size_t q = 0; q < std::min(nbranch, (size_t)(2 * kNumVariants)) && ce == cudaSuccess && !s->serial; ++q) {
+        ce = cudaEventRecord(s->gdone[q], s->gstream[q]);
+        if (ce == cudaSuccess) ce = cudaStreamWaitEvent(ctx->stream, s->gdone[q], 0);
     }
     if (ce == cudaSuccess) {
         advance_k<<<1, 1, 0, ctx->stream>>>(s->d_gbase, kGraphIters);
@@ -506,13 +526,21 @@ qsm_status qsm_session_create(qsm_ctx *ctx, size_t budget_bytes, int32_t poisson
     std::unique_ptr<qsm_session> s(new qsm_session());
     s->ctx = ctx;
     s->budget = budget_bytes;
+    {
+        const char *e = getenv("QSM_BATCH_LAUNCH");  // "serial", "items", "serial,items"
+        if (e && strstr(e, "serial")) s->serial = true;
+        if (e && strstr(e, "items")) s->one_cta_per_item = true;
+        int sm = 0;
+        cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, ctx->device);
+        s->solo_tiles = (uint32_t)std::max(sm / kSoloDiv, 1);
+        const char *t = getenv("QSM_BATCH_SOLO_TILES");
+        if (t && *t) s->solo_tiles = (uint32_t)strtoul(t, nullptr, 10);
+    }
     QSM_TRY(set_batch_smem(ctx));
-    // gbase + 2 scheduler counters per possible group
-    const size_t blk = 256 + 2 * (2 * kNumVariants) * sizeof(unsigned);
+    const size_t blk = 256;
     QSM_TRY(dalloc(ctx, &s->dev_blk, blk));
     QSM_CUDA(cudaMemsetAsync(s->dev_blk, 0, blk, ctx->stream));
     s->d_gbase = (uint32_t *)s->dev_blk;
-    s->d_sched = (unsigned *)((char *)s->dev_blk + 256);
     for (int q = 0; q < 2 * kNumVariants; ++q) {
         QSM_CUDA(cudaStreamCreateWithFlags(&s->gstream[q], cudaStreamNonBlocking));
         QSM_CUDA(cudaEventCreateWithFlags(&s->gdone[q], cudaEventDisableTiming));
@@ -521,7 +549,6 @@ qsm_status qsm_session_create(qsm_ctx *ctx, size_t budget_bytes, int32_t poisson
     QSM_CUDA(cudaEventCreate(&s->ev0));
     QSM_CUDA(cudaEventCreate(&s->ev1));
     QSM_CUDA(cudaStreamSynchronize(ctx->stream));
-    s->groups.reserve(2 * kNumVariants);
     for (int w = 0; w < poisson_workers; ++w) {
         qsm_ctx *wc = nullptr;
         qsm_status st = qsm_ctx_create(ctx->device, &wc);
@@ -554,7 +581,6 @@ qsm_status qsm_session_destroy(qsm_session *s)
     for (auto &kv : s->mg)
         if (kv.second->blk) dfree(ctx, kv.second->blk);
     if (s->exec) cudaGraphExecDestroy(s->exec);
-    if (s->d_vols) dfree(ctx, s->d_vols);
     if (s->d_items) dfree(ctx, s->d_items);
     if (s->dev_blk) dfree(ctx, s->dev_blk);
     for (int q = 0; q < 2 * kNumVariants; ++q) {

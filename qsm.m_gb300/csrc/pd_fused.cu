@@ -88,9 +88,11 @@ tgv_fused_k(FusedArgs s, DualC<float> dc, PrimalC<float> pc, Dims d, double tol,
 {
     extern __shared__ double shd_raw[];  // the dual (reused for the monitor reduction)
     if (s.ctl->done) return;
+    const uint32_t itn = launch_iter(s, it);
+    if (!itn) return;
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
     tile_tgv<TX, TY, TZ>(s, dc, pc, d, s.tiles[blockIdx.x], CHECK, (float *)shd_raw, acc);
-    if (CHECK) monitor_reduce<TX * TY>(s, shd_raw, acc, tol, it);
+    if (CHECK) monitor_reduce<TX * TY>(s, shd_raw, acc, tol, itn);
 }
 
 // ---------------------------------------------------------------------------
@@ -103,9 +105,11 @@ tv_fused_k(FusedArgs s, DualC<float> dc, PrimalC<float> pc, Dims d, double tol, 
 {
     extern __shared__ double shd_raw[];  // the dual (reused for the monitor reduction)
     if (s.ctl->done) return;
+    const uint32_t itn = launch_iter(s, it);
+    if (!itn) return;
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
     tile_tv<TX, TY, TZ>(s, dc, pc, d, s.tiles[blockIdx.x], CHECK, (float *)shd_raw, acc);
-    if (CHECK) monitor_reduce<TX * TY>(s, shd_raw, acc, tol, it);
+    if (CHECK) monitor_reduce<TX * TY>(s, shd_raw, acc, tol, itn);
 }
 
 // ---------------------------------------------------------------------------
@@ -136,15 +140,15 @@ size_t variant_smem(int v, bool tgv)
 }
 
 template <int TX, int TY, int TZ, int MINB>
-static void launch_t(qsm_ctx *ctx, bool tgv, bool chk, unsigned nact, const FusedArgs &s, const DualC<float> &dc,
+static void launch_t(cudaStream_t st, bool tgv, bool chk, unsigned nact, const FusedArgs &s, const DualC<float> &dc,
                      const PrimalC<float> &pc, const Dims &d, double tol, uint32_t it, size_t smem)
 {
     if (tgv) {
-        if (chk) tgv_fused_k<TX, TY, TZ, MINB, true><<<nact, TX * TY, smem, ctx->stream>>>(s, dc, pc, d, tol, it);
-        else tgv_fused_k<TX, TY, TZ, MINB, false><<<nact, TX * TY, smem, ctx->stream>>>(s, dc, pc, d, tol, it);
+        if (chk) tgv_fused_k<TX, TY, TZ, MINB, true><<<nact, TX * TY, smem, st>>>(s, dc, pc, d, tol, it);
+        else tgv_fused_k<TX, TY, TZ, MINB, false><<<nact, TX * TY, smem, st>>>(s, dc, pc, d, tol, it);
     } else {
-        if (chk) tv_fused_k<TX, TY, TZ, MINB, true><<<nact, TX * TY, smem, ctx->stream>>>(s, dc, pc, d, tol, it);
-        else tv_fused_k<TX, TY, TZ, MINB, false><<<nact, TX * TY, smem, ctx->stream>>>(s, dc, pc, d, tol, it);
+        if (chk) tv_fused_k<TX, TY, TZ, MINB, true><<<nact, TX * TY, smem, st>>>(s, dc, pc, d, tol, it);
+        else tv_fused_k<TX, TY, TZ, MINB, false><<<nact, TX * TY, smem, st>>>(s, dc, pc, d, tol, it);
     }
 }
 
@@ -158,21 +162,29 @@ static qsm_status set_smem_t(qsm_ctx *ctx, size_t tgv_smem, size_t tv_smem)
     return QSM_OK;
 }
 
-static qsm_status launch_variant(qsm_ctx *ctx, int v, bool tgv, bool chk, unsigned nact, const FusedArgs &s,
-                                 const DualC<float> &dc, const PrimalC<float> &pc, const Dims &d, double tol, uint32_t it)
+static qsm_status launch_variant(qsm_ctx *ctx, cudaStream_t st, int v, bool tgv, bool chk, unsigned nact,
+                                 const FusedArgs &s, const DualC<float> &dc, const PrimalC<float> &pc, const Dims &d,
+                                 double tol, uint32_t it)
 {
     const size_t sm = variant_smem(v, tgv);
     if (kVariants[v].stream)
-        return stream_launch(ctx, kVariants[v].tx, kVariants[v].ty, kVariants[v].tz, tgv, chk, nact, s, dc, pc, d, tol, it);
+        return stream_launch(ctx, st, kVariants[v].tx, kVariants[v].ty, kVariants[v].tz, tgv, chk, nact, s, dc, pc, d,
+                             tol, it);
     switch (v) {
-    case 0: launch_t<32, 8, 4, 2>(ctx, tgv, chk, nact, s, dc, pc, d, tol, it, sm); break;
-    case 1: launch_t<32, 8, 2, 3>(ctx, tgv, chk, nact, s, dc, pc, d, tol, it, sm); break;
-    case 2: launch_t<32, 4, 4, 4>(ctx, tgv, chk, nact, s, dc, pc, d, tol, it, sm); break;
-    case 3: launch_t<32, 16, 2, 1>(ctx, tgv, chk, nact, s, dc, pc, d, tol, it, sm); break;
+    case 0: launch_t<32, 8, 4, 2>(st, tgv, chk, nact, s, dc, pc, d, tol, it, sm); break;
+    case 1: launch_t<32, 8, 2, 3>(st, tgv, chk, nact, s, dc, pc, d, tol, it, sm); break;
+    case 2: launch_t<32, 4, 4, 4>(st, tgv, chk, nact, s, dc, pc, d, tol, it, sm); break;
+    case 3: launch_t<32, 16, 2, 1>(st, tgv, chk, nact, s, dc, pc, d, tol, it, sm); break;
     default: return QSM_ERR_ARG;
     }
     QSM_CUDA(cudaGetLastError());
     return QSM_OK;
+}
+
+qsm_status pd_volume_launch(qsm_ctx *ctx, cudaStream_t st, const PdVolume &v, bool chk, const FusedArgs &s,
+                            double tol, uint32_t it)
+{
+    return launch_variant(ctx, st, v.var, v.tgv, chk, v.tl[v.var].nact, s, v.dc, v.pc, v.d, tol, it);
 }
 
 static qsm_status set_all_smem(qsm_ctx *ctx)
@@ -389,12 +401,12 @@ qsm_status pd_volume_tune(qsm_ctx *ctx, PdVolume *v, uint32_t maxiter)
     float best = 1e30f;
     for (int k = 0; k < kNumVariants; ++k) {
         for (uint32_t it = 0; it < 2; ++it)
-            QSM_TRY(launch_variant(ctx, k, v->tgv, false, v->tl[k].nact, pd_volume_args(*v, k, it), v->dc, v->pc,
-                                   v->d, 0.0, it + 1));
+            QSM_TRY(launch_variant(ctx, ctx->stream, k, v->tgv, false, v->tl[k].nact, pd_volume_args(*v, k, it),
+                                   v->dc, v->pc, v->d, 0.0, it + 1));
         QSM_CUDA(cudaEventRecord(t0, ctx->stream));
         for (uint32_t it = 2; it < 8; ++it)
-            QSM_TRY(launch_variant(ctx, k, v->tgv, false, v->tl[k].nact, pd_volume_args(*v, k, it), v->dc, v->pc,
-                                   v->d, 0.0, it + 1));
+            QSM_TRY(launch_variant(ctx, ctx->stream, k, v->tgv, false, v->tl[k].nact, pd_volume_args(*v, k, it),
+                                   v->dc, v->pc, v->d, 0.0, it + 1));
         QSM_CUDA(cudaEventRecord(t1, ctx->stream));
         QSM_CUDA(cudaEventSynchronize(t1));
         float ms = 0.f;
@@ -461,7 +473,9 @@ qsm_status pd_fused(qsm_ctx *ctx, bool tgv, const Dims &d, qsm_dtype dt, const v
     uint32_t enq = 0;
     for (uint32_t it = 0; it < maxiter; ++it) {
         const bool chk = ((it + 1) % 10) == 0;
-        if (!empty) QSM_TRY(launch_variant(ctx, var, tgv, chk, nact, pd_volume_args(v, var, it), v.dc, v.pc, d, tol, it + 1));
+        if (!empty)
+            QSM_TRY(launch_variant(ctx, ctx->stream, var, tgv, chk, nact, pd_volume_args(v, var, it), v.dc, v.pc, d,
+                                   tol, it + 1));
         enq = it + 1;
         const bool print = verbose && (it == 0 || it == maxiter - 1 || ((it + 1) % pmod) == 0);
         if (print || (chk && ((it + 1) % 100) == 0)) {

@@ -20,7 +20,20 @@ struct FusedArgs {
     PdCtl *ctl;
     const unsigned *tiles;  // active tile indices (x fastest), one per block
     unsigned gx, gy;        // tiles per row / per plane
+    // replayed graphs: the iteration count comes from a device counter
+    const uint32_t *gbase;  // null: the launch's `it` is the iteration count
+    uint32_t start, maxiter;
 };
+
+// Iteration count this launch completes, 0 if it must do nothing.  Direct
+// launches pass it = the count; a graph replayed from a device iteration
+// base passes it = the node's offset in the graph and sets gbase.
+__device__ __forceinline__ uint32_t launch_iter(const FusedArgs &s, uint32_t it)
+{
+    if (!s.gbase) return it;
+    const uint32_t l = *s.gbase + it - s.start;
+    return l < s.maxiter ? l + 1 : 0;
+}
 
 // extragradient point (pd_tgv_mex.c:804-810): x_ = x^n + 1*(x^n - x^(n-1))
 __device__ __forceinline__ float xbar(const float *__restrict__ c, const float *__restrict__ p, size_t l)
@@ -90,8 +103,9 @@ __device__ __forceinline__ void monitor_reduce(const FusedArgs &s, double *red, 
 
 size_t stream_smem(int tx, int ty, bool tgv);
 qsm_status stream_set_smem(qsm_ctx *ctx);
-qsm_status stream_launch(qsm_ctx *ctx, int tx, int ty, int cz, bool tgv, bool chk, unsigned nact, const FusedArgs &s,
-                         const DualC<float> &dc, const PrimalC<float> &pc, const Dims &d, double tol, uint32_t it);
+qsm_status stream_launch(qsm_ctx *ctx, cudaStream_t st, int tx, int ty, int cz, bool tgv, bool chk, unsigned nact,
+                         const FusedArgs &s, const DualC<float> &dc, const PrimalC<float> &pc, const Dims &d,
+                         double tol, uint32_t it);
 
 // ---------------------------------------------------------------------------
 // Tile variants and the device state of one fused solve (pd_fused.cu), shared
@@ -145,6 +159,9 @@ FusedArgs pd_volume_args(const PdVolume &v, int var, uint32_t it);
 // Picks v->var: QSM_FUSED_VARIANT, the tuning table, or timing each variant
 // on this volume for a few iterations (the state is zeroed again after).
 qsm_status pd_volume_tune(qsm_ctx *ctx, PdVolume *v, uint32_t maxiter);
+// One iteration of variant v->var on stream st (the one-volume kernels).
+qsm_status pd_volume_launch(qsm_ctx *ctx, cudaStream_t st, const PdVolume &v, bool chk, const FusedArgs &s,
+                            double tol, uint32_t it);
 // chi after `iters` iterations, converted to dt.
 qsm_status pd_volume_result(qsm_ctx *ctx, const PdVolume &v, uint32_t iters, qsm_dtype dt, void *chi);
 qsm_status pd_volume_free(qsm_ctx *ctx, PdVolume *v);

@@ -11,9 +11,11 @@ stream_k(FusedArgs s, DualC<float> dc, PrimalC<float> pc, Dims d, int cz, double
 {
     extern __shared__ double smem_raw[];
     if (s.ctl->done) return;
+    const uint32_t itn = launch_iter(s, it);
+    if (!itn) return;
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
     column_pd<TX, TY, TGV>(s, dc, pc, d, cz, s.tiles[blockIdx.x], CHECK, (float *)smem_raw, acc);
-    if (CHECK) monitor_reduce<(TX + 4) * (TY + 4)>(s, smem_raw, acc, tol, it);
+    if (CHECK) monitor_reduce<(TX + 4) * (TY + 4)>(s, smem_raw, acc, tol, itn);
 }
 
 size_t stream_smem(int tx, int ty, bool tgv)
@@ -41,24 +43,25 @@ qsm_status stream_set_smem(qsm_ctx *ctx)
 }
 
 template <int TX, int TY>
-static void launch_t(qsm_ctx *ctx, bool tgv, bool chk, unsigned nact, const FusedArgs &s, const DualC<float> &dc,
+static void launch_t(cudaStream_t st, bool tgv, bool chk, unsigned nact, const FusedArgs &s, const DualC<float> &dc,
                      const PrimalC<float> &pc, const Dims &d, int cz, double tol, uint32_t it)
 {
     const size_t sm = stream_smem(TX, TY, tgv);
     const int nt = (TX + 4) * (TY + 4);
     if (tgv) {
-        if (chk) stream_k<TX, TY, true, true><<<nact, nt, sm, ctx->stream>>>(s, dc, pc, d, cz, tol, it);
-        else stream_k<TX, TY, true, false><<<nact, nt, sm, ctx->stream>>>(s, dc, pc, d, cz, tol, it);
+        if (chk) stream_k<TX, TY, true, true><<<nact, nt, sm, st>>>(s, dc, pc, d, cz, tol, it);
+        else stream_k<TX, TY, true, false><<<nact, nt, sm, st>>>(s, dc, pc, d, cz, tol, it);
     } else {
-        if (chk) stream_k<TX, TY, false, true><<<nact, nt, sm, ctx->stream>>>(s, dc, pc, d, cz, tol, it);
-        else stream_k<TX, TY, false, false><<<nact, nt, sm, ctx->stream>>>(s, dc, pc, d, cz, tol, it);
+        if (chk) stream_k<TX, TY, false, true><<<nact, nt, sm, st>>>(s, dc, pc, d, cz, tol, it);
+        else stream_k<TX, TY, false, false><<<nact, nt, sm, st>>>(s, dc, pc, d, cz, tol, it);
     }
 }
 
-qsm_status stream_launch(qsm_ctx *ctx, int tx, int ty, int cz, bool tgv, bool chk, unsigned nact, const FusedArgs &s,
-                         const DualC<float> &dc, const PrimalC<float> &pc, const Dims &d, double tol, uint32_t it)
+qsm_status stream_launch(qsm_ctx *ctx, cudaStream_t st, int tx, int ty, int cz, bool tgv, bool chk, unsigned nact,
+                         const FusedArgs &s, const DualC<float> &dc, const PrimalC<float> &pc, const Dims &d,
+                         double tol, uint32_t it)
 {
-    if (tx == 28 && ty == 12) launch_t<28, 12>(ctx, tgv, chk, nact, s, dc, pc, d, cz, tol, it);
+    if (tx == 28 && ty == 12) launch_t<28, 12>(st, tgv, chk, nact, s, dc, pc, d, cz, tol, it);
     else return QSM_ERR_ARG;
     QSM_CUDA(cudaGetLastError());
     return QSM_OK;

@@ -23,11 +23,17 @@ def _case(shape, seed, dtype=np.float32, fill=0.42):
     return d2f, np.asfortranarray((q <= 1).astype(np.uint8))
 
 
+LAUNCH = {"packed": "4294967295", "solo": "0"}  # QSM_BATCH_SOLO_TILES
+
+
+@pytest.mark.parametrize("launch", ["packed", "solo"])
 @pytest.mark.parametrize("variant", list(range(8)))
-def test_batch_matches_oracle_every_variant(gpu_ctx, qsm, port, variant, monkeypatch):
+def test_batch_matches_oracle_every_variant(gpu_ctx, qsm, port, variant, launch, monkeypatch):
     """Uneven volumes, 40 iterations (not a multiple of the 30-iteration
-    graph): each chi equals the oracle's FP32 chi."""
+    graph), packed into persistent launches or each in its own graph branch:
+    each chi equals the oracle's FP32 chi."""
     monkeypatch.setenv("QSM_FUSED_VARIANT", str(variant))
+    monkeypatch.setenv("QSM_BATCH_SOLO_TILES", LAUNCH[launch])
     cases = [_case(s, 100 + k) for k, s in enumerate(SHAPES)]
     infos = []
     out = qsm.pd_tv_batch([c[0] for c in cases], [c[1] for c in cases], [1, 1, 1], 0.003, 0.0, 40, infos=infos)
@@ -75,8 +81,10 @@ def test_batch_fp64_io_and_empty_volume(gpu_ctx, qsm):
     assert not np.any(out[1])
 
 
-def test_batch_stopping_rule(gpu_ctx, qsm):
+@pytest.mark.parametrize("launch", ["packed", "solo"])
+def test_batch_stopping_rule(gpu_ctx, qsm, launch, monkeypatch):
     """tol > 0: each volume stops at its own one-volume iteration count."""
+    monkeypatch.setenv("QSM_BATCH_SOLO_TILES", LAUNCH[launch])
     cases = [_case((30, 28, 26), 400, fill=0.3), _case((44, 40, 36), 401, fill=0.45)]
     infos = []
     out = qsm.pd_tgv_batch([c[0] for c in cases], [c[1] for c in cases], [1, 1, 1], 0.003, 2.0, 5e-3, 3000,
@@ -99,11 +107,13 @@ def _poisson(shape, seed):
 MG_ARGS = (1e-8, 200, -1.0, 2, 1, 2, 2, 2, 3)  # tolcg, maxitcg, tolmg, maxitmg, mu, npre, npost, nb, nlevels
 
 
-def test_session_result_same_alone_and_in_mix(gpu_ctx, qsm):
+@pytest.mark.parametrize("launch", ["packed", "solo", "hybrid"])
+def test_session_result_same_alone_and_in_mix(gpu_ctx, qsm, launch, monkeypatch):
     """A TGV job alone, then the same job admitted into a running mix of TV,
     TGV and Poisson jobs (admitted at different times, different sizes and
     iteration counts): chi is bit-identical.  The Poisson job equals the
     stand-alone mixed-precision mgpcg."""
+    monkeypatch.setenv("QSM_BATCH_SOLO_TILES", {"hybrid": "60", **LAUNCH}[launch])
     ja = _case((46, 42, 38), 500)
     with qsm.Session(poisson_workers=2) as s:
         ia = s.submit_pd(ja[0], ja[1], [1, 1, 1], 0.003, 2.0, 0.0, 100, tgv=True)
