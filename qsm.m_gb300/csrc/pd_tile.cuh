@@ -274,11 +274,16 @@ __device__ __forceinline__ void column_pd(const FusedArgs &s, const DualC<float>
 
     // Every global input is fetched one plane step before it is used, so the
     // memory latency of a plane overlaps the arithmetic of the previous one.
+    // The mask bytes that decide which inputs to fetch come from a register
+    // ring loaded further ahead, so no fetch waits for a mask load first.
+    auto mask_at = [&](long z) -> unsigned {
+        return (valid && z >= 0 && z < nz) ? (unsigned)__ldg(s.mm + col + nxny * (size_t)z) : 0u;
+    };
     //   raw iterates n, n-1 (+ mask bit m) of the own column, plane j+2
     float rc[NB], rp[NB];
     bool rm = false;
-    auto fetch_bars = [&](long z) {
-        rm = valid && z >= 0 && z < nz && (__ldg(s.mm + col + nxny * (size_t)z) & 1);
+    auto fetch_bars = [&](long z, unsigned mb) {
+        rm = (mb & 1u) != 0;
         const size_t l = col + nxny * (size_t)(rm ? z : 0);  // an in-bounds address even when unused
 #pragma unroll
         for (int q = 0; q < NB; ++q) {
@@ -293,8 +298,8 @@ __device__ __forceinline__ void column_pd(const FusedArgs &s, const DualC<float>
     //   dual state n and f at plane j+1 (ring threads inside mi)
     float rd[ND], rf = 0.0f;
     bool rmi = false;
-    auto fetch_dual = [&](long z) {
-        rmi = ring1 && valid && z >= 1 && z + 1 < nz && (__ldg(s.mm + col + nxny * (size_t)z) & 2);
+    auto fetch_dual = [&](long z, unsigned mb) {
+        rmi = ring1 && z >= 1 && z + 1 < nz && (mb & 2u);
         const size_t l = col + nxny * (size_t)(rmi ? z : 0);
 #pragma unroll
         for (int q = 0; q < ND; ++q) rd[q] = rmi ? __ldg(s.Dc[q] + l) : 0.0f;
@@ -303,27 +308,38 @@ __device__ __forceinline__ void column_pd(const FusedArgs &s, const DualC<float>
     //   iterate n at plane j (primal of the next step), owned threads inside m
     float rpc[NB];
     bool rpm = false;
-    auto fetch_primal = [&](long z) {
-        rpm = owned && z >= zs && z < ze && (__ldg(s.mm + col + nxny * (size_t)z) & 1);
+    auto fetch_primal = [&](long z, unsigned mb) {
+        rpm = owned && z >= zs && z < ze && (mb & 1u);
         const size_t l = col + nxny * (size_t)(rpm ? z : 0);
 #pragma unroll
         for (int q = 0; q < NB; ++q) rpc[q] = rpm ? __ldg(s.Pc[q] + l) : 0.0f;
     };
 
+    // mask ring: byte k of mr = mask of plane j+k (k = 0..3) at step j;
+    // mnext = plane j+4, loaded one step earlier
+    unsigned mr = 0;
+    for (int k = 0; k < 4; ++k) mr |= mask_at(zs - 1 + k) << (8 * k);
+    unsigned mnext = mask_at(zs + 3);
+
     // registers: extragradient point of planes j-1, j, j+1 (own column)
     float bm[NB], b0[NB], bp[NB];
-    fetch_bars(zs - 2);
+    fetch_bars(zs - 2, mask_at(zs - 2));
     make_bars(bm);
-    fetch_bars(zs - 1);
+    fetch_bars(zs - 1, mr & 0xffu);
     make_bars(b0);
     {
         float *Bw = B + ((zs - 1) & 1) * NB * NT;
 #pragma unroll
         for (int q = 0; q < NB; ++q) Bw[q * NT + tid] = b0[q];
     }
-    fetch_bars(zs);
-    fetch_dual(zs - 1);
-    // own dual of plane j-2 (read by the primal at j-1 through its z-1 neighbour)
+    fetch_bars(zs, (mr >> 8) & 0xffu);
+    fetch_dual(zs - 1, mr & 0xffu);
+    // own dual of planes j-1 (vp) and j-2 (the z-1 neighbours of the primal
+    // at j-1), kept in registers: the primal reads only x/y neighbours from
+    // shared memory
+    float vp[ND];
+#pragma unroll
+    for (int q = 0; q < ND; ++q) vp[q] = 0.0f;
     float nu_m2 = 0.f, p3_m2 = 0.f, q3_m2 = 0.f, q5_m2 = 0.f, q6_m2 = 0.f;
     __syncthreads();
 
@@ -333,22 +349,12 @@ __device__ __forceinline__ void column_pd(const FusedArgs &s, const DualC<float>
         float *Sj = S + (j & 1) * ND * NT;              // dual of plane j (written now; held plane j-2)
         const float *Sm = S + ((j + 1) & 1) * ND * NT;  // dual of plane j-1
 
-        // own dual values of plane j-2 before plane j overwrites them
-        if (owned && j - 1 >= zs) {
-            nu_m2 = Sj[tid];
-            p3_m2 = Sj[3 * NT + tid];
-            if (TGV) {
-                q3_m2 = Sj[6 * NT + tid];
-                q5_m2 = Sj[8 * NT + tid];
-                q6_m2 = Sj[9 * NT + tid];
-            }
-        }
-
         // (a) extragradient point of plane j+1 (fetched last step); fetch plane j+2
         make_bars(bp);
 #pragma unroll
         for (int q = 0; q < NB; ++q) Bn[q * NT + tid] = bp[q];
-        fetch_bars(j + 2);
+        const unsigned mfar = mask_at(j + 5);
+        fetch_bars(j + 2, (mr >> 16) & 0xffu);
 
         // (b) dual at plane j from the state fetched last step; fetch plane j+1
         float v[ND];
@@ -361,8 +367,8 @@ __device__ __forceinline__ void column_pd(const FusedArgs &s, const DualC<float>
         const bool do_primal = rpm;
 #pragma unroll
         for (int q = 0; q < NB; ++q) pcur[q] = rpc[q];
-        fetch_dual(j + 1);
-        fetch_primal(j);
+        fetch_dual(j + 1, (mr >> 8) & 0xffu);
+        fetch_primal(j, mr & 0xffu);
 #pragma unroll
         for (int q = 0; q < ND; ++q) v[q] = 0.0f;
         if (do_dual) {
@@ -424,27 +430,27 @@ __device__ __forceinline__ void column_pd(const FusedArgs &s, const DualC<float>
         // (c) primal + extragradient at plane j-1
         if (do_primal) {
             const size_t l = col + nxny * (size_t)(j - 1);
-            const float nu0 = Sm[tid];
+            const float nu0 = vp[0];
             const float xs = Sm[tid - 1] + Sm[tid + 1];
             const float ys = Sm[tid - WX] + Sm[tid + WX];
             const float zs_ = nu_m2 + v[0];
             const float cn = pcur[0], en = pcur[1];
             const float e1 = pc.tau1 * (en - pc.lhh * nu0 - pc.lhx * xs - pc.lhy * ys - pc.lhz * zs_);
             const float *P1 = Sm + NT, *P2 = Sm + 2 * NT, *P3 = Sm + 3 * NT;
-            const float c1 = cn + (pc.hx * (P1[tid] - P1[tid - 1]) + pc.hy * (P2[tid] - P2[tid - WX]) +
-                                   pc.hz * (P3[tid] - p3_m2) +
+            const float c1 = cn + (pc.hx * (vp[1] - P1[tid - 1]) + pc.hy * (vp[2] - P2[tid - WX]) +
+                                   pc.hz * (vp[3] - p3_m2) +
                                    (pc.whh * nu0 + pc.whx * xs + pc.why * ys + pc.whz * zs_));
             s.Pn[0][l] = c1;
             s.Pn[1][l] = e1;
             if (TGV) {
                 const float *Q1 = Sm + 4 * NT, *Q2 = Sm + 5 * NT, *Q3 = Sm + 6 * NT, *Q4 = Sm + 7 * NT,
                             *Q5 = Sm + 8 * NT, *Q6 = Sm + 9 * NT;
-                const float u1 = pcur[2] + (pc.tt * P1[tid] + pc.hx * (Q1[tid] - Q1[tid - 1] + Q2[tid] - Q2[tid - WX] +
-                                                                        Q3[tid] - q3_m2));
-                const float u2 = pcur[3] + (pc.tt * P2[tid] + pc.hy * (Q2[tid] - Q2[tid - 1] + Q4[tid] - Q4[tid - WX] +
-                                                                        Q5[tid] - q5_m2));
-                const float u3 = pcur[4] + (pc.tt * P3[tid] + pc.hz * (Q3[tid] - Q3[tid - 1] + Q5[tid] - Q5[tid - WX] +
-                                                                        Q6[tid] - q6_m2));
+                const float u1 = pcur[2] + (pc.tt * vp[1] + pc.hx * (vp[4] - Q1[tid - 1] + vp[5] - Q2[tid - WX] +
+                                                                      vp[6] - q3_m2));
+                const float u2 = pcur[3] + (pc.tt * vp[2] + pc.hy * (vp[5] - Q2[tid - 1] + vp[7] - Q4[tid - WX] +
+                                                                      vp[8] - q5_m2));
+                const float u3 = pcur[4] + (pc.tt * vp[3] + pc.hz * (vp[6] - Q3[tid - 1] + vp[8] - Q5[tid - WX] +
+                                                                      vp[9] - q6_m2));
                 s.Pn[2][l] = u1;
                 s.Pn[3][l] = u2;
                 s.Pn[4][l] = u3;
@@ -460,6 +466,17 @@ __device__ __forceinline__ void column_pd(const FusedArgs &s, const DualC<float>
             bm[q] = b0[q];
             b0[q] = bp[q];
         }
+        nu_m2 = vp[0];
+        p3_m2 = vp[3];
+        if (TGV) {
+            q3_m2 = vp[6];
+            q5_m2 = vp[8];
+            q6_m2 = vp[9];
+        }
+#pragma unroll
+        for (int q = 0; q < ND; ++q) vp[q] = v[q];
+        mr = (mr >> 8) | (mnext << 24);
+        mnext = mfar;
         __syncthreads();
     }
 }
