@@ -49,7 +49,6 @@
 #include "common.cuh"
 #include "pd.cuh"
 #include "pd_fused.cuh"
-#include "pd_async.cuh"
 #include "pd_tile.cuh"
 
 namespace qsm {
@@ -146,20 +145,6 @@ batch_column_k(const __grid_constant__ BatchChunk P, const uint2 *items, uint32_
                                     });
 }
 
-template <int TX, int TY, bool TGV, bool CHECK>
-__global__ void __launch_bounds__((TX + 4) * (TY + 4), 1)
-batch_async_k(const __grid_constant__ BatchChunk P, const uint2 *items, uint32_t nitems, const uint32_t *gbase,
-              uint32_t i, int cz)
-{
-    extern __shared__ double smem_raw[];
-    const uint32_t g = *gbase + i;
-    batch_loop<(TX + 4) * (TY + 4)>(P, items, nitems, g, CHECK, smem_raw,
-                                    [&](const BatchVol &v, unsigned tile, double *acc) {
-                                        column_async<TX, TY, TGV>(v.a, v.dc, v.pc, v.d, cz, tile, CHECK,
-                                                                  (float *)smem_raw, acc);
-                                    });
-}
-
 __global__ void advance_k(uint32_t *gbase, uint32_t n) { *gbase += n; }
 
 // ---------------------------------------------------------------------------
@@ -184,12 +169,6 @@ static BatchKernel column_kernel()
     return {{(const void *)batch_column_k<TX, TY, TGV, false>, (const void *)batch_column_k<TX, TY, TGV, true>}, true};
 }
 
-template <int TX, int TY, bool TGV>
-static BatchKernel async_kernel()
-{
-    return {{(const void *)batch_async_k<TX, TY, TGV, false>, (const void *)batch_async_k<TX, TY, TGV, true>}, true};
-}
-
 // Kernels of variant v (the same tile shapes as the one-volume path).
 static BatchKernel batch_kernel(int v, bool tgv)
 {
@@ -198,9 +177,6 @@ static BatchKernel batch_kernel(int v, bool tgv)
     case 1: return tgv ? tile_kernel<32, 8, 2, 4, true>() : tile_kernel<32, 8, 2, 4, false>();
     case 2: return tgv ? tile_kernel<32, 4, 4, 8, true>() : tile_kernel<32, 4, 4, 8, false>();
     case 3: return tgv ? tile_kernel<32, 16, 2, 2, true>() : tile_kernel<32, 16, 2, 2, false>();
-    case 8:
-    case 9: return tgv ? async_kernel<28, 12, true>() : async_kernel<28, 12, false>();
-    case 10: return tgv ? column_kernel<28, 14, true>() : column_kernel<28, 14, false>();
     default: return tgv ? column_kernel<28, 12, true>() : column_kernel<28, 12, false>();
     }
 }

@@ -117,10 +117,9 @@ tv_fused_k(FusedArgs s, DualC<float> dc, PrimalC<float> pc, Dims d, double tol, 
 // ---------------------------------------------------------------------------
 
 // 3-D tiles: threads = tx * ty; streaming: threads = (tx + 4) * (ty + 4)
-static const Variant kVariants[kNumVariants] = {
-    {32, 8, 4, false, false},  {32, 8, 2, false, false},  {32, 4, 4, false, false}, {32, 16, 2, false, false},
-    {28, 12, 8, true, false},  {28, 12, 16, true, false}, {28, 12, 32, true, false}, {28, 12, 64, true, false},
-    {28, 12, 16, true, true},  {28, 12, 32, true, true},  {28, 14, 16, true, false}};
+static const Variant kVariants[kNumVariants] = {{32, 8, 4, false}, {32, 8, 2, false}, {32, 4, 4, false},
+                                                {32, 16, 2, false}, {28, 12, 8, true},  {28, 12, 16, true},
+                                                {28, 12, 32, true},  {28, 12, 64, true}};
 
 const Variant &variant(int v) { return kVariants[v]; }
 
@@ -133,7 +132,7 @@ int variant_threads(int v)
 size_t variant_smem(int v, bool tgv)
 {
     const Variant &x = kVariants[v];
-    if (x.stream) return stream_smem(x.tx, x.ty, tgv, x.async);
+    if (x.stream) return stream_smem(x.tx, x.ty, tgv);
     const size_t bn = (size_t)(x.tx + 2) * (x.ty + 2) * (x.tz + 2);
     const size_t dual = (tgv ? 10 : 4) * bn * sizeof(float);
     const size_t red = 4 * (size_t)x.tx * x.ty * sizeof(double);
@@ -169,8 +168,8 @@ static qsm_status launch_variant(qsm_ctx *ctx, cudaStream_t st, int v, bool tgv,
 {
     const size_t sm = variant_smem(v, tgv);
     if (kVariants[v].stream)
-        return stream_launch(ctx, st, kVariants[v].tx, kVariants[v].ty, kVariants[v].tz, tgv, chk, kVariants[v].async,
-                             nact, s, dc, pc, d, tol, it);
+        return stream_launch(ctx, st, kVariants[v].tx, kVariants[v].ty, kVariants[v].tz, tgv, chk, nact, s, dc, pc, d,
+                             tol, it);
     switch (v) {
     case 0: launch_t<32, 8, 4, 4>(st, tgv, chk, nact, s, dc, pc, d, tol, it, sm); break;
     case 1: launch_t<32, 8, 2, 4>(st, tgv, chk, nact, s, dc, pc, d, tol, it, sm); break;

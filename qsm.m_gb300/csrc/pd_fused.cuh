@@ -101,11 +101,11 @@ __device__ __forceinline__ void monitor_reduce(const FusedArgs &s, double *red, 
     monitor_fold<THREADS>(s.part, s.count, s.ctl, gridDim.x, blockIdx.x, red, acc, tol, it);
 }
 
-size_t stream_smem(int tx, int ty, bool tgv, bool async);
+size_t stream_smem(int tx, int ty, bool tgv);
 qsm_status stream_set_smem(qsm_ctx *ctx);
-qsm_status stream_launch(qsm_ctx *ctx, cudaStream_t st, int tx, int ty, int cz, bool tgv, bool chk, bool async,
-                         unsigned nact, const FusedArgs &s, const DualC<float> &dc, const PrimalC<float> &pc,
-                         const Dims &d, double tol, uint32_t it);
+qsm_status stream_launch(qsm_ctx *ctx, cudaStream_t st, int tx, int ty, int cz, bool tgv, bool chk, unsigned nact,
+                         const FusedArgs &s, const DualC<float> &dc, const PrimalC<float> &pc, const Dims &d,
+                         double tol, uint32_t it);
 
 // ---------------------------------------------------------------------------
 // Tile variants and the device state of one fused solve (pd_fused.cu), shared
@@ -115,9 +115,8 @@ qsm_status stream_launch(qsm_ctx *ctx, cudaStream_t st, int tx, int ty, int cz, 
 struct Variant {
     int tx, ty, tz;   // tile of interior voxels (z: chunk of planes for the column kernel)
     bool stream;      // column-streaming kernel, else the 3-D tile kernel
-    bool async;       // column kernel with cp.async staging (pd_async.cuh)
 };
-constexpr int kNumVariants = 11;
+constexpr int kNumVariants = 8;
 const Variant &variant(int v);
 size_t variant_smem(int v, bool tgv);
 int variant_threads(int v);

@@ -1,7 +1,6 @@
 // Primal-dual TGV / TV, mixed-precision fused path: the one-volume
 // z-streaming kernel.  A CTA owns a TX x TY column tile of the interior and
 // a chunk of planes; the column body (column_pd) is in pd_tile.cuh.
-#include "pd_async.cuh"
 #include "pd_tile.cuh"
 
 namespace qsm {
@@ -20,68 +19,36 @@ stream_k(FusedArgs s, DualC<float> dc, PrimalC<float> pc, Dims d, int cz, double
     if (CHECK) monitor_reduce<(TX + 4) * (TY + 4)>(s, smem_raw, acc, tol, itn);
 }
 
-template <int TX, int TY, bool TGV, bool CHECK>
-__global__ void __launch_bounds__((TX + 4) * (TY + 4), 1)
-async_k(FusedArgs s, DualC<float> dc, PrimalC<float> pc, Dims d, int cz, double tol, uint32_t it)
-{
-    extern __shared__ double smem_raw[];
-    if (s.ctl->done) return;
-    const uint32_t itn = launch_iter(s, it);
-    if (!itn) return;
-    double acc[4] = {0.0, 0.0, 0.0, 0.0};
-    column_async<TX, TY, TGV>(s, dc, pc, d, cz, s.tiles[blockIdx.x], CHECK, (float *)smem_raw, acc);
-    if (CHECK) monitor_reduce<(TX + 4) * (TY + 4)>(s, smem_raw, acc, tol, itn);
-}
-
-size_t stream_smem(int tx, int ty, bool tgv, bool async)
+size_t stream_smem(int tx, int ty, bool tgv)
 {
     const size_t nt = (size_t)(tx + 4) * (ty + 4);
-    const size_t planes = async ? (tgv ? async_smem_floats<true>(tx, ty) : async_smem_floats<false>(tx, ty)) * sizeof(float)
-                                : 2 * ((tgv ? 5 : 2) + (tgv ? 10 : 4)) * nt * sizeof(float);
+    const size_t planes = 2 * ((tgv ? 5 : 2) + (tgv ? 10 : 4)) * nt * sizeof(float);
     return std::max(planes, 4 * nt * sizeof(double));
 }
 
 template <int TX, int TY>
 static qsm_status set_t(qsm_ctx *ctx)
 {
-    const int t = (int)stream_smem(TX, TY, true, false), v = (int)stream_smem(TX, TY, false, false);
+    const int t = (int)stream_smem(TX, TY, true), v = (int)stream_smem(TX, TY, false);
     QSM_CUDA(cudaFuncSetAttribute(stream_k<TX, TY, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, t));
     QSM_CUDA(cudaFuncSetAttribute(stream_k<TX, TY, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, t));
     QSM_CUDA(cudaFuncSetAttribute(stream_k<TX, TY, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v));
     QSM_CUDA(cudaFuncSetAttribute(stream_k<TX, TY, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, v));
-    if (TY == 12) {  // the staged variant exists for 28 x 12 columns only (its rings fill shared memory)
-        const int ta = (int)stream_smem(TX, TY, true, true), va = (int)stream_smem(TX, TY, false, true);
-        QSM_CUDA(cudaFuncSetAttribute(async_k<TX, TY, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, ta));
-        QSM_CUDA(cudaFuncSetAttribute(async_k<TX, TY, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, ta));
-        QSM_CUDA(cudaFuncSetAttribute(async_k<TX, TY, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, va));
-        QSM_CUDA(cudaFuncSetAttribute(async_k<TX, TY, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, va));
-    }
     return QSM_OK;
 }
 
 qsm_status stream_set_smem(qsm_ctx *ctx)
 {
     QSM_TRY((set_t<28, 12>(ctx)));
-    QSM_TRY((set_t<28, 14>(ctx)));
     return QSM_OK;
 }
 
 template <int TX, int TY>
-static void launch_t(cudaStream_t st, bool tgv, bool chk, bool async, unsigned nact, const FusedArgs &s,
-                     const DualC<float> &dc, const PrimalC<float> &pc, const Dims &d, int cz, double tol, uint32_t it)
+static void launch_t(cudaStream_t st, bool tgv, bool chk, unsigned nact, const FusedArgs &s, const DualC<float> &dc,
+                     const PrimalC<float> &pc, const Dims &d, int cz, double tol, uint32_t it)
 {
-    const size_t sm = stream_smem(TX, TY, tgv, async);
+    const size_t sm = stream_smem(TX, TY, tgv);
     const int nt = (TX + 4) * (TY + 4);
-    if (async && TY == 12) {
-        if (tgv) {
-            if (chk) async_k<TX, TY, true, true><<<nact, nt, sm, st>>>(s, dc, pc, d, cz, tol, it);
-            else async_k<TX, TY, true, false><<<nact, nt, sm, st>>>(s, dc, pc, d, cz, tol, it);
-        } else {
-            if (chk) async_k<TX, TY, false, true><<<nact, nt, sm, st>>>(s, dc, pc, d, cz, tol, it);
-            else async_k<TX, TY, false, false><<<nact, nt, sm, st>>>(s, dc, pc, d, cz, tol, it);
-        }
-        return;
-    }
     if (tgv) {
         if (chk) stream_k<TX, TY, true, true><<<nact, nt, sm, st>>>(s, dc, pc, d, cz, tol, it);
         else stream_k<TX, TY, true, false><<<nact, nt, sm, st>>>(s, dc, pc, d, cz, tol, it);
@@ -91,12 +58,11 @@ static void launch_t(cudaStream_t st, bool tgv, bool chk, bool async, unsigned n
     }
 }
 
-qsm_status stream_launch(qsm_ctx *ctx, cudaStream_t st, int tx, int ty, int cz, bool tgv, bool chk, bool async,
-                         unsigned nact, const FusedArgs &s, const DualC<float> &dc, const PrimalC<float> &pc,
-                         const Dims &d, double tol, uint32_t it)
+qsm_status stream_launch(qsm_ctx *ctx, cudaStream_t st, int tx, int ty, int cz, bool tgv, bool chk, unsigned nact,
+                         const FusedArgs &s, const DualC<float> &dc, const PrimalC<float> &pc, const Dims &d,
+                         double tol, uint32_t it)
 {
-    if (tx == 28 && ty == 12) launch_t<28, 12>(st, tgv, chk, async, nact, s, dc, pc, d, cz, tol, it);
-    else if (tx == 28 && ty == 14) launch_t<28, 14>(st, tgv, chk, async, nact, s, dc, pc, d, cz, tol, it);
+    if (tx == 28 && ty == 12) launch_t<28, 12>(st, tgv, chk, nact, s, dc, pc, d, cz, tol, it);
     else return QSM_ERR_ARG;
     QSM_CUDA(cudaGetLastError());
     return QSM_OK;

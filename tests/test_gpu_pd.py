@@ -121,11 +121,10 @@ def test_pd_errors(gpu_ctx, qsm):
 
 
 @pytest.mark.parametrize("shape", [(77, 41, 23), (70, 30, 75)])
-@pytest.mark.parametrize("variant", list(range(11)))
+@pytest.mark.parametrize("variant", list(range(8)))
 def test_fused_tile_variants_bitexact(gpu_ctx, qsm, port, variant, shape, monkeypatch):
-    """Every compiled tile shape (3-D tiles 0-3, z-streaming column tiles 4-7
-    and 10, column tiles with cp.async staging 8-9) gives the reference's FP32
-    result (partial tiles and chunks, odd extents,
+    """Every compiled tile shape (3-D tiles 0-3, z-streaming column tiles 4-7)
+    gives the reference's FP32 result (partial tiles and chunks, odd extents,
     a mask that leaves whole tiles inactive)."""
     monkeypatch.setenv("QSM_FUSED_VARIANT", str(variant))
     rng = np.random.default_rng(40 + variant)
@@ -157,4 +156,4 @@ def test_autotuned_solve_is_reset(gpu_ctx, qsm, port, monkeypatch):
     b = port.pd_tgv_mex(d2f, m, [1, 1, 1], 0.003, 2.0, 0.0, 40)
     assert bits_equal(a, b), first_diff(a, b)
     assert tuple(info["tile"]) in {(32, 8, 4), (32, 8, 2), (32, 4, 4), (32, 16, 2), (28, 12, 8), (28, 12, 16),
-                                   (28, 12, 32), (28, 12, 64), (28, 14, 16)}
+                                   (28, 12, 32), (28, 12, 64)}
