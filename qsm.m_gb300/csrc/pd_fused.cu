@@ -235,6 +235,7 @@ static void tune_store_locked(const TuneKey &k, int v)
 namespace {
 struct Layout {
     size_t stride, mstride, ntiles_total, nblk_max, bytes;
+    size_t pa, pb, da, db, dc;  // bytes of one buffer of each state family
     unsigned gx[kNumVariants], gy[kNumVariants], gz[kNumVariants];
 };
 
@@ -242,8 +243,13 @@ Layout layout(bool tgv, const Dims &d)
 {
     Layout L;
     const size_t N = d.n();
-    const int np = tgv ? 5 : 2, nd = tgv ? 10 : 4;
-    L.stride = (N * sizeof(float) + 255) & ~(size_t)255;
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    L.stride = al(N * sizeof(float));
+    L.pa = al(N * (tgv ? sizeof(float4) : sizeof(float2)));
+    L.pb = tgv ? L.stride : 0;
+    L.da = al(N * sizeof(float4));
+    L.db = tgv ? L.da : 0;
+    L.dc = tgv ? al(N * sizeof(float2)) : 0;
     L.mstride = (N + 255) & ~(size_t)255;
     const size_t ix = d.nx > 2 ? d.nx - 2 : 0, iy = d.ny > 2 ? d.ny - 2 : 0, iz = d.nz > 2 ? d.nz - 2 : 0;
     L.ntiles_total = 0;
@@ -258,7 +264,8 @@ Layout layout(bool tgv, const Dims &d)
     }
     // 3 primal buffers + 2 dual buffers + f, 3 mask arrays, tile lists, tile flags,
     // monitor partials, counter + control block
-    L.bytes = L.stride * (3 * np + 2 * nd + 1) + 3 * L.mstride + (L.ntiles_total + 64) * sizeof(unsigned) +
+    L.bytes = 3 * (L.pa + L.pb) + 2 * (L.da + L.db + L.dc) + L.stride + 3 * L.mstride +
+              (L.ntiles_total + 64) * sizeof(unsigned) +
               (L.nblk_max + 64) + 256 + 4 * (L.nblk_max + 1) * sizeof(double) + 1024;
     return L;
 }
@@ -278,10 +285,11 @@ qsm_status pd_volume_init(qsm_ctx *ctx, PdVolume *v, bool tgv, const Dims &d, qs
     QSM_TRY(dalloc(ctx, &v->blk, L.bytes));
     QSM_CUDA(cudaMemsetAsync(v->blk, 0, L.bytes, ctx->stream));
     char *c = (char *)v->blk;
-    for (int b = 0; b < 3; ++b)
-        for (int q = 0; q < v->np; ++q, c += L.stride) v->P[b][q] = (float *)c;
-    for (int b = 0; b < 2; ++b)
-        for (int q = 0; q < v->nd; ++q, c += L.stride) v->D[b][q] = (float *)c;
+    for (int b = 0; b < 3; ++b, c += L.pa) v->PA[b] = c;
+    for (int b = 0; b < 3; ++b, c += L.pb) v->PB[b] = L.pb ? (float *)c : nullptr;
+    for (int b = 0; b < 2; ++b, c += L.da) v->DA[b] = (float4 *)c;
+    for (int b = 0; b < 2; ++b, c += L.db) v->DB[b] = L.db ? (float4 *)c : nullptr;
+    for (int b = 0; b < 2; ++b, c += L.dc) v->DC[b] = L.dc ? (float2 *)c : nullptr;
     v->f = (float *)c;
     c += L.stride;
     uint8_t *m = (uint8_t *)c, *mi = m + L.mstride;
@@ -297,7 +305,7 @@ qsm_status pd_volume_init(qsm_ctx *ctx, PdVolume *v, bool tgv, const Dims &d, qs
     c = (char *)(((uintptr_t)c + 255) & ~(uintptr_t)255);
     v->count = (unsigned *)c;
     v->ctl = (PdCtl *)(c + 256);
-    v->state_bytes = L.stride * (3 * v->np + 2 * v->nd);
+    v->state_bytes = 3 * (L.pa + L.pb) + 2 * (L.da + L.db + L.dc);
 
     double tau, sigma;
     pd_steps(h, &tau, &sigma);
@@ -355,15 +363,18 @@ FusedArgs pd_volume_args(const PdVolume &v, int var, uint32_t it)
     FusedArgs s;
     memset(&s, 0, sizeof s);
     const int cur = it % 3, prv = (it + 2) % 3, nxt = (it + 1) % 3, dcur = it % 2, dnxt = (it + 1) % 2;
-    for (int q = 0; q < v.np; ++q) {
-        s.Pc[q] = v.P[cur][q];
-        s.Pp[q] = v.P[prv][q];
-        s.Pn[q] = v.P[nxt][q];
-    }
-    for (int q = 0; q < v.nd; ++q) {
-        s.Dc[q] = v.D[dcur][q];
-        s.Dn[q] = v.D[dnxt][q];
-    }
+    s.Pc = v.PA[cur];
+    s.Pp = v.PA[prv];
+    s.Pn = v.PA[nxt];
+    s.Pc1 = v.PB[cur];
+    s.Pp1 = v.PB[prv];
+    s.Pn1 = v.PB[nxt];
+    s.Dca = v.DA[dcur];
+    s.Dcb = v.DB[dcur];
+    s.Dcc = v.DC[dcur];
+    s.Dna = v.DA[dnxt];
+    s.Dnb = v.DB[dnxt];
+    s.Dnc = v.DC[dnxt];
     s.f = v.f;
     s.mm = v.mm;
     s.part = v.part;
@@ -418,20 +429,32 @@ qsm_status pd_volume_tune(qsm_ctx *ctx, PdVolume *v, uint32_t maxiter)
     }
     cudaEventDestroy(t0);
     cudaEventDestroy(t1);
-    QSM_CUDA(cudaMemsetAsync(v->P[0][0], 0, v->state_bytes, ctx->stream));
+    QSM_CUDA(cudaMemsetAsync(v->PA[0], 0, v->state_bytes, ctx->stream));
     std::lock_guard<std::mutex> lock(g_tune_mu);
     tune_store_locked(key, v->var);
     return QSM_OK;
 }
 
+// chi = the first field of primal family A (stride 4 floats for TGV, 2 for TV)
+template <typename T>
+__global__ void extract_chi_k(T *o, const float *__restrict__ a, int stride, size_t n)
+{
+    for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x)
+        o[l] = (T)a[l * stride];
+}
+
 qsm_status pd_volume_result(qsm_ctx *ctx, const PdVolume &v, uint32_t iters, qsm_dtype dt, void *chi_out)
 {
-    const float *chi = v.P[iters % 3][0];
+    const float *chi = (const float *)v.PA[iters % 3];
     const size_t N = v.d.n();
+    const int stride = v.tgv ? 4 : 2;
+    if (N == 0) return QSM_OK;
+    const unsigned g = (unsigned)std::min<size_t>((N + 255) / 256, 4096);
     if (dt == QSM_F32)
-        QSM_CUDA(cudaMemcpyAsync(chi_out, chi, N * sizeof(float), cudaMemcpyDeviceToDevice, ctx->stream));
+        extract_chi_k<float><<<g, 256, 0, ctx->stream>>>((float *)chi_out, chi, stride, N);
     else
-        QSM_TRY((launch_convert<double, float>(ctx, (double *)chi_out, chi, N)));
+        extract_chi_k<double><<<g, 256, 0, ctx->stream>>>((double *)chi_out, chi, stride, N);
+    QSM_CUDA(cudaGetLastError());
     return QSM_OK;
 }
 

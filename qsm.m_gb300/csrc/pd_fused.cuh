@@ -7,12 +7,24 @@
 
 namespace qsm {
 
+// Device state of the fused path, interleaved per voxel so that one address
+// and one 8/16-byte access serve several fields (SoA across voxels, AoS
+// within a family):
+//   primal family A: TGV (chi, eta, w1, w2) as float4, TV (chi, eta) as float2
+//   primal family B: TGV w3 as float
+//   dual families:   (nu, p1, p2, p3) float4; TGV also (q1, q2, q3, q4) float4
+//                    and (q5, q6) float2
+// Families A/B are triple-buffered (iterates n-1, n, n+1), the dual
+// families double-buffered.
 struct FusedArgs {
-    const float *Pc[5];     // chi^n, eta^n, w1^n, w2^n, w3^n (TV: chi, eta)
-    const float *Pp[5];     // iterate n-1
-    float *Pn[5];           // iterate n+1 (written)
-    const float *Dc[10];    // nu, p1..3, q1..6 at n (TV: nu, p1..3)
-    float *Dn[10];          // at n+1 (written)
+    const void *Pc, *Pp;    // family A at iterate n, n-1
+    void *Pn;               // family A at n+1 (written)
+    const float *Pc1, *Pp1; // family B at n, n-1
+    float *Pn1;             // family B at n+1
+    const float4 *Dca, *Dcb;
+    const float2 *Dcc;      // dual at n
+    float4 *Dna, *Dnb;
+    float2 *Dnc;            // dual at n+1 (written)
     const float *f;
     const uint8_t *mm;
     double *part;           // 4 x gridDim.x partial monitor sums
@@ -25,6 +37,70 @@ struct FusedArgs {
     uint32_t start, maxiter;
 };
 
+// extragradient point (pd_tgv_mex.c:804-810): x_ = x^n + 1*(x^n - x^(n-1))
+__device__ __forceinline__ float bar1(float c, float p) { return c + 1.0f * (c - p); }
+__device__ __forceinline__ float xbar(const float *__restrict__ c, const float *__restrict__ p, size_t l)
+{
+    return bar1(__ldg(c + l), __ldg(p + l));
+}
+
+// the primal family of voxel l: TGV v = (chi, eta, w1, w2, w3), TV v = (chi, eta)
+template <bool TGV>
+__device__ __forceinline__ void load_primal(const void *A, const float *B, size_t l, float *v)
+{
+    if (TGV) {
+        const float4 a = __ldg((const float4 *)A + l);
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+        v[4] = __ldg(B + l);
+    } else {
+        const float2 a = __ldg((const float2 *)A + l);
+        v[0] = a.x; v[1] = a.y;
+    }
+}
+template <bool TGV>
+__device__ __forceinline__ void store_primal(void *A, float *B, size_t l, const float *v)
+{
+    if (TGV) {
+        ((float4 *)A)[l] = make_float4(v[0], v[1], v[2], v[3]);
+        B[l] = v[4];
+    } else {
+        ((float2 *)A)[l] = make_float2(v[0], v[1]);
+    }
+}
+// the dual of voxel l: TGV v = (nu, p1..3, q1..6), TV v = (nu, p1..3)
+template <bool TGV>
+__device__ __forceinline__ void load_dual(const FusedArgs &s, size_t l, float *v)
+{
+    const float4 a = __ldg(s.Dca + l);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    if (TGV) {
+        const float4 b = __ldg(s.Dcb + l);
+        const float2 c = __ldg(s.Dcc + l);
+        v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w; v[8] = c.x; v[9] = c.y;
+    }
+}
+template <bool TGV>
+__device__ __forceinline__ void store_dual(const FusedArgs &s, size_t l, const float *v)
+{
+    s.Dna[l] = make_float4(v[0], v[1], v[2], v[3]);
+    if (TGV) {
+        s.Dnb[l] = make_float4(v[4], v[5], v[6], v[7]);
+        s.Dnc[l] = make_float2(v[8], v[9]);
+    }
+}
+// (chi_, eta_) of family A at l, and for TGV also (w1_, w2_)
+template <bool TGV>
+__device__ __forceinline__ void bar_head(const FusedArgs &s, size_t l, float *v)
+{
+    if (TGV) {
+        const float4 c = __ldg((const float4 *)s.Pc + l), p = __ldg((const float4 *)s.Pp + l);
+        v[0] = bar1(c.x, p.x); v[1] = bar1(c.y, p.y); v[2] = bar1(c.z, p.z); v[3] = bar1(c.w, p.w);
+    } else {
+        const float2 c = __ldg((const float2 *)s.Pc + l), p = __ldg((const float2 *)s.Pp + l);
+        v[0] = bar1(c.x, p.x); v[1] = bar1(c.y, p.y);
+    }
+}
+
 // Iteration count this launch completes, 0 if it must do nothing.  Direct
 // launches pass it = the count; a graph replayed from a device iteration
 // base passes it = the node's offset in the graph and sets gbase.
@@ -33,13 +109,6 @@ __device__ __forceinline__ uint32_t launch_iter(const FusedArgs &s, uint32_t it)
     if (!s.gbase) return it;
     const uint32_t l = *s.gbase + it - s.start;
     return l < s.maxiter ? l + 1 : 0;
-}
-
-// extragradient point (pd_tgv_mex.c:804-810): x_ = x^n + 1*(x^n - x^(n-1))
-__device__ __forceinline__ float xbar(const float *__restrict__ c, const float *__restrict__ p, size_t l)
-{
-    const float cn = __ldg(c + l);
-    return cn + 1.0f * (cn - __ldg(p + l));
 }
 
 // Monitor sums of one tile (block), then the last of the nblk tiles folds
@@ -135,15 +204,17 @@ struct PdVolume {
     Dims d{};
     int np = 0, nd = 0;
     void *blk = nullptr;
-    float *P[3][5] = {};
-    float *D[2][10] = {};
+    void *PA[3] = {};           // primal family A of iterates (rotating)
+    float *PB[3] = {};          // primal family B (TGV w3)
+    float4 *DA[2] = {}, *DB[2] = {};
+    float2 *DC[2] = {};         // dual families
     float *f = nullptr;
     uint8_t *mm = nullptr;       // bit 0 m, bit 1 mi
     TileList tl[kNumVariants];
     double *part = nullptr;      // 4 x (max tiles) monitor partials
     unsigned *count = nullptr;   // arrival counter of the monitor fold
     PdCtl *ctl = nullptr;
-    size_t state_bytes = 0;      // primal + dual buffers (from P[0][0])
+    size_t state_bytes = 0;      // primal + dual buffers (from PA[0])
     DualC<float> dc{};
     PrimalC<float> pc{};
     int var = 0;                 // chosen tile variant

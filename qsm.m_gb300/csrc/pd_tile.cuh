@@ -72,20 +72,28 @@ __device__ __forceinline__ void tile_tgv(const FusedArgs &s, const DualC<float> 
             // mi: all six neighbours in the mask (never true on a face); the dual is 0 outside it
             const bool inside = (__ldg(s.mm + l) & 2) != 0;
             if (inside) {
-                const float c0 = xbar(s.Pc[0], s.Pp[0], l);
-                const float cxm = xbar(s.Pc[0], s.Pp[0], l - 1), cxp = xbar(s.Pc[0], s.Pp[0], l + 1);
-                const float cym = xbar(s.Pc[0], s.Pp[0], l - nx), cyp = xbar(s.Pc[0], s.Pp[0], l + nx);
-                const float czm = xbar(s.Pc[0], s.Pp[0], l - nxny), czp = xbar(s.Pc[0], s.Pp[0], l + nxny);
-                const float lap = dc.lhh * xbar(s.Pc[1], s.Pp[1], l) +
-                                  dc.lhx * (xbar(s.Pc[1], s.Pp[1], l - 1) + xbar(s.Pc[1], s.Pp[1], l + 1)) +
-                                  dc.lhy * (xbar(s.Pc[1], s.Pp[1], l - nx) + xbar(s.Pc[1], s.Pp[1], l + nx)) +
-                                  dc.lhz * (xbar(s.Pc[1], s.Pp[1], l - nxny) + xbar(s.Pc[1], s.Pp[1], l + nxny));
+                // (chi_, eta_, w1_, w2_) at the voxel and its six neighbours
+                float C[4], Xm[4], Xp[4], Ym[4], Yp[4], Zm[4], Zp[4];
+                bar_head<true>(s, l, C);
+                bar_head<true>(s, l - 1, Xm);
+                bar_head<true>(s, l + 1, Xp);
+                bar_head<true>(s, l - nx, Ym);
+                bar_head<true>(s, l + nx, Yp);
+                bar_head<true>(s, l - nxny, Zm);
+                bar_head<true>(s, l + nxny, Zp);
+                const float c0 = C[0];
+                const float cxm = Xm[0], cxp = Xp[0], cym = Ym[0], cyp = Yp[0], czm = Zm[0], czp = Zp[0];
+                const float lap = dc.lhh * C[1] + dc.lhx * (Xm[1] + Xp[1]) + dc.lhy * (Ym[1] + Yp[1]) +
+                                  dc.lhz * (Zm[1] + Zp[1]);
                 const float wav = dc.whh * c0 + dc.whx * (cxm + cxp) + dc.why * (cym + cyp) + dc.whz * (czm + czp);
-                v[0] = __ldg(s.Dc[0] + l) + ((lap - wav) + __ldg(s.f + l));
+                const float4 da = __ldg(s.Dca + l);
+                v[0] = da.x + ((lap - wav) + __ldg(s.f + l));
                 if (nhigh == 0) {
-#pragma unroll
-                    for (int q = 1; q < 10; ++q) v[q] = __ldg(s.Dc[q] + l);
-                    const float w1 = xbar(s.Pc[2], s.Pp[2], l), w2 = xbar(s.Pc[3], s.Pp[3], l), w3 = xbar(s.Pc[4], s.Pp[4], l);
+                    const float4 db = __ldg(s.Dcb + l);
+                    const float2 dd = __ldg(s.Dcc + l);
+                    v[1] = da.y; v[2] = da.z; v[3] = da.w;
+                    v[4] = db.x; v[5] = db.y; v[6] = db.z; v[7] = db.w; v[8] = dd.x; v[9] = dd.y;
+                    const float w1 = C[2], w2 = C[3], w3 = xbar(s.Pc1, s.Pp1, l);
                     float a1 = v[1] + dc.hx * (cxp - c0) - dc.sg * w1;
                     float a2 = v[2] + dc.hy * (cyp - c0) - dc.sg * w2;
                     float a3 = v[3] + dc.hz * (czp - c0) - dc.sg * w3;
@@ -95,9 +103,10 @@ __device__ __forceinline__ void tile_tgv(const FusedArgs &s, const DualC<float> 
                         a1 = a1 * t; a2 = a2 * t; a3 = a3 * t;
                     }
                     v[1] = a1; v[2] = a2; v[3] = a3;
-                    const float w1x = xbar(s.Pc[2], s.Pp[2], l + 1), w1y = xbar(s.Pc[2], s.Pp[2], l + nx), w1z = xbar(s.Pc[2], s.Pp[2], l + nxny);
-                    const float w2x = xbar(s.Pc[3], s.Pp[3], l + 1), w2y = xbar(s.Pc[3], s.Pp[3], l + nx), w2z = xbar(s.Pc[3], s.Pp[3], l + nxny);
-                    const float w3x = xbar(s.Pc[4], s.Pp[4], l + 1), w3y = xbar(s.Pc[4], s.Pp[4], l + nx), w3z = xbar(s.Pc[4], s.Pp[4], l + nxny);
+                    const float w1x = Xp[2], w1y = Yp[2], w1z = Zp[2];
+                    const float w2x = Xp[3], w2y = Yp[3], w2z = Zp[3];
+                    const float w3x = xbar(s.Pc1, s.Pp1, l + 1), w3y = xbar(s.Pc1, s.Pp1, l + nx),
+                                w3z = xbar(s.Pc1, s.Pp1, l + nxny);
                     float b1 = v[4] + dc.hx * (w1x - w1);
                     float b2 = v[5] + dc.hx2 * (w2x - w2) + dc.hy2 * (w1y - w1);
                     float b3 = v[6] + dc.hx2 * (w3x - w3) + dc.hz2 * (w1z - w1);
@@ -111,10 +120,7 @@ __device__ __forceinline__ void tile_tgv(const FusedArgs &s, const DualC<float> 
                     }
                     v[4] = b1; v[5] = b2; v[6] = b3; v[7] = b4; v[8] = b5; v[9] = b6;
                     // the owning tile stores the new dual
-                    if (bx >= 1 && by >= 1 && bz >= 1) {
-#pragma unroll
-                        for (int q = 0; q < 10; ++q) s.Dn[q][l] = v[q];
-                    }
+                    if (bx >= 1 && by >= 1 && bz >= 1) store_dual<true>(s, l, v);
                 }
             }
         }
@@ -140,8 +146,9 @@ __device__ __forceinline__ void tile_tgv(const FusedArgs &s, const DualC<float> 
             const float xs = SH(0, -sx) + SH(0, sx);
             const float ys = SH(0, -sy) + SH(0, sy);
             const float zs = SH(0, -sz) + SH(0, sz);
-            const float en = __ldg(s.Pc[1] + l), cn = __ldg(s.Pc[0] + l);
-            const float w1n = __ldg(s.Pc[2] + l), w2n = __ldg(s.Pc[3] + l), w3n = __ldg(s.Pc[4] + l);
+            float pn[5];
+            load_primal<true>(s.Pc, s.Pc1, l, pn);
+            const float cn = pn[0], en = pn[1], w1n = pn[2], w2n = pn[3], w3n = pn[4];
             const float e1 = pc.tau1 * (en - pc.lhh * nu0 - pc.lhx * xs - pc.lhy * ys - pc.lhz * zs);
             const float c1 = cn + (pc.hx * (SH(1, 0) - SH(1, -sx)) + pc.hy * (SH(2, 0) - SH(2, -sy)) +
                                    pc.hz * (SH(3, 0) - SH(3, -sz)) + (pc.whh * nu0 + pc.whx * xs + pc.why * ys + pc.whz * zs));
@@ -149,11 +156,8 @@ __device__ __forceinline__ void tile_tgv(const FusedArgs &s, const DualC<float> 
             const float u2 = w2n + (pc.tt * SH(2, 0) + pc.hy * (SH(5, 0) - SH(5, -sx) + SH(7, 0) - SH(7, -sy) + SH(8, 0) - SH(8, -sz)));
             const float u3 = w3n + (pc.tt * SH(3, 0) + pc.hz * (SH(6, 0) - SH(6, -sx) + SH(8, 0) - SH(8, -sy) + SH(9, 0) - SH(9, -sz)));
 #undef SH
-            s.Pn[0][l] = c1;
-            s.Pn[1][l] = e1;
-            s.Pn[2][l] = u1;
-            s.Pn[3][l] = u2;
-            s.Pn[4][l] = u3;
+            const float pv[5] = {c1, e1, u1, u2, u3};
+            store_primal<true>(s.Pn, s.Pn1, l, pv);
             if (check) {
                 double a, bb, c, e;
                 mon_terms(c1, cn, e1, en, a, bb, c, e);
@@ -183,30 +187,32 @@ __device__ __forceinline__ void tile_tv(const FusedArgs &s, const DualC<float> &
             const size_t l = x + nx * y + nxny * z;
             const bool inside = (__ldg(s.mm + l) & 2) != 0;  // the dual is 0 outside mi
             if (inside) {
-                const float c0 = xbar(s.Pc[0], s.Pp[0], l);
-                const float cxm = xbar(s.Pc[0], s.Pp[0], l - 1), cxp = xbar(s.Pc[0], s.Pp[0], l + 1);
-                const float cym = xbar(s.Pc[0], s.Pp[0], l - nx), cyp = xbar(s.Pc[0], s.Pp[0], l + nx);
-                const float czm = xbar(s.Pc[0], s.Pp[0], l - nxny), czp = xbar(s.Pc[0], s.Pp[0], l + nxny);
-                const float lap = dc.lhh * xbar(s.Pc[1], s.Pp[1], l) +
-                                  dc.lhx * (xbar(s.Pc[1], s.Pp[1], l - 1) + xbar(s.Pc[1], s.Pp[1], l + 1)) +
-                                  dc.lhy * (xbar(s.Pc[1], s.Pp[1], l - nx) + xbar(s.Pc[1], s.Pp[1], l + nx)) +
-                                  dc.lhz * (xbar(s.Pc[1], s.Pp[1], l - nxny) + xbar(s.Pc[1], s.Pp[1], l + nxny));
+                float C[2], Xm[2], Xp[2], Ym[2], Yp[2], Zm[2], Zp[2];
+                bar_head<false>(s, l, C);
+                bar_head<false>(s, l - 1, Xm);
+                bar_head<false>(s, l + 1, Xp);
+                bar_head<false>(s, l - nx, Ym);
+                bar_head<false>(s, l + nx, Yp);
+                bar_head<false>(s, l - nxny, Zm);
+                bar_head<false>(s, l + nxny, Zp);
+                const float c0 = C[0];
+                const float cxm = Xm[0], cxp = Xp[0], cym = Ym[0], cyp = Yp[0], czm = Zm[0], czp = Zp[0];
+                const float lap = dc.lhh * C[1] + dc.lhx * (Xm[1] + Xp[1]) + dc.lhy * (Ym[1] + Yp[1]) +
+                                  dc.lhz * (Zm[1] + Zp[1]);
                 const float wav = dc.whh * c0 + dc.whx * (cxm + cxp) + dc.why * (cym + cyp) + dc.whz * (czm + czp);
-                v[0] = __ldg(s.Dc[0] + l) + ((lap - wav) + __ldg(s.f + l));
+                const float4 da = __ldg(s.Dca + l);
+                v[0] = da.x + ((lap - wav) + __ldg(s.f + l));
                 if (nhigh == 0) {
-                    float a1 = __ldg(s.Dc[1] + l) + dc.hx * (cxp - c0);
-                    float a2 = __ldg(s.Dc[2] + l) + dc.hy * (cyp - c0);
-                    float a3 = __ldg(s.Dc[3] + l) + dc.hz * (czp - c0);
+                    float a1 = da.y + dc.hx * (cxp - c0);
+                    float a2 = da.z + dc.hy * (cyp - c0);
+                    float a3 = da.w + dc.hz * (czp - c0);
                     float t = a1 * a1 + a2 * a2 + a3 * a3;
                     if (t > dc.alp12) {
                         t = dc.alp1 / sqrtf(t);
                         a1 = a1 * t; a2 = a2 * t; a3 = a3 * t;
                     }
                     v[1] = a1; v[2] = a2; v[3] = a3;
-                    if (bx >= 1 && by >= 1 && bz >= 1) {
-#pragma unroll
-                        for (int q = 0; q < 4; ++q) s.Dn[q][l] = v[q];
-                    }
+                    if (bx >= 1 && by >= 1 && bz >= 1) store_dual<false>(s, l, v);
                 }
             }
         }
@@ -230,13 +236,15 @@ __device__ __forceinline__ void tile_tv(const FusedArgs &s, const DualC<float> &
             const float xs = shd[b - sx] + shd[b + sx];
             const float ys = shd[b - sy] + shd[b + sy];
             const float zs = shd[b - sz] + shd[b + sz];
-            const float en = __ldg(s.Pc[1] + l), cn = __ldg(s.Pc[0] + l);
+            float pn[2];
+            load_primal<false>(s.Pc, s.Pc1, l, pn);
+            const float cn = pn[0], en = pn[1];
             const float e1 = pc.tau1 * (en - pc.lhh * nu0 - pc.lhx * xs - pc.lhy * ys - pc.lhz * zs);
             const float c1 = cn + (pc.hx * (shd[BN + b] - shd[BN + b - sx]) + pc.hy * (shd[2 * BN + b] - shd[2 * BN + b - sy]) +
                                    pc.hz * (shd[3 * BN + b] - shd[3 * BN + b - sz]) +
                                    (pc.whh * nu0 + pc.whx * xs + pc.why * ys + pc.whz * zs));
-            s.Pn[0][l] = c1;
-            s.Pn[1][l] = e1;
+            const float pv[2] = {c1, e1};
+            store_primal<false>(s.Pn, s.Pn1, l, pv);
             if (check) {
                 double a, bb, c, e;
                 mon_terms(c1, cn, e1, en, a, bb, c, e);
@@ -285,10 +293,12 @@ __device__ __forceinline__ void column_pd(const FusedArgs &s, const DualC<float>
     auto fetch_bars = [&](long z, unsigned mb) {
         rm = (mb & 1u) != 0;
         const size_t l = col + nxny * (size_t)(rm ? z : 0);  // an in-bounds address even when unused
+        if (rm) {
+            load_primal<TGV>(s.Pc, s.Pc1, l, rc);
+            load_primal<TGV>(s.Pp, s.Pp1, l, rp);
+        } else {
 #pragma unroll
-        for (int q = 0; q < NB; ++q) {
-            rc[q] = rm ? __ldg(s.Pc[q] + l) : 0.0f;
-            rp[q] = rm ? __ldg(s.Pp[q] + l) : 0.0f;
+            for (int q = 0; q < NB; ++q) rc[q] = rp[q] = 0.0f;
         }
     };
     auto make_bars = [&](float *v) {
@@ -301,9 +311,14 @@ __device__ __forceinline__ void column_pd(const FusedArgs &s, const DualC<float>
     auto fetch_dual = [&](long z, unsigned mb) {
         rmi = ring1 && z >= 1 && z + 1 < nz && (mb & 2u);
         const size_t l = col + nxny * (size_t)(rmi ? z : 0);
+        if (rmi) {
+            load_dual<TGV>(s, l, rd);
+            rf = __ldg(s.f + l);
+        } else {
 #pragma unroll
-        for (int q = 0; q < ND; ++q) rd[q] = rmi ? __ldg(s.Dc[q] + l) : 0.0f;
-        rf = rmi ? __ldg(s.f + l) : 0.0f;
+            for (int q = 0; q < ND; ++q) rd[q] = 0.0f;
+            rf = 0.0f;
+        }
     };
     //   iterate n at plane j (primal of the next step), owned threads inside m
     float rpc[NB];
@@ -311,8 +326,12 @@ __device__ __forceinline__ void column_pd(const FusedArgs &s, const DualC<float>
     auto fetch_primal = [&](long z, unsigned mb) {
         rpm = owned && z >= zs && z < ze && (mb & 1u);
         const size_t l = col + nxny * (size_t)(rpm ? z : 0);
+        if (rpm) {
+            load_primal<TGV>(s.Pc, s.Pc1, l, rpc);
+        } else {
 #pragma unroll
-        for (int q = 0; q < NB; ++q) rpc[q] = rpm ? __ldg(s.Pc[q] + l) : 0.0f;
+            for (int q = 0; q < NB; ++q) rpc[q] = 0.0f;
+        }
     };
 
     // mask ring: byte k of mr = mask of plane j+k (k = 0..3) at step j;
@@ -419,10 +438,7 @@ __device__ __forceinline__ void column_pd(const FusedArgs &s, const DualC<float>
                 }
                 v[1] = a1; v[2] = a2; v[3] = a3;
             }
-            if (owned && j >= zs && j < ze) {
-#pragma unroll
-                for (int q = 0; q < ND; ++q) s.Dn[q][l] = v[q];
-            }
+            if (owned && j >= zs && j < ze) store_dual<TGV>(s, l, v);
         }
 #pragma unroll
         for (int q = 0; q < ND; ++q) Sj[q * NT + tid] = v[q];
@@ -440,8 +456,9 @@ __device__ __forceinline__ void column_pd(const FusedArgs &s, const DualC<float>
             const float c1 = cn + (pc.hx * (vp[1] - P1[tid - 1]) + pc.hy * (vp[2] - P2[tid - WX]) +
                                    pc.hz * (vp[3] - p3_m2) +
                                    (pc.whh * nu0 + pc.whx * xs + pc.why * ys + pc.whz * zs_));
-            s.Pn[0][l] = c1;
-            s.Pn[1][l] = e1;
+            float pv[NB];
+            pv[0] = c1;
+            pv[1] = e1;
             if (TGV) {
                 const float *Q1 = Sm + 4 * NT, *Q2 = Sm + 5 * NT, *Q3 = Sm + 6 * NT, *Q4 = Sm + 7 * NT,
                             *Q5 = Sm + 8 * NT, *Q6 = Sm + 9 * NT;
@@ -451,10 +468,11 @@ __device__ __forceinline__ void column_pd(const FusedArgs &s, const DualC<float>
                                                                       vp[8] - q5_m2));
                 const float u3 = pcur[4] + (pc.tt * vp[3] + pc.hz * (vp[6] - Q3[tid - 1] + vp[8] - Q5[tid - WX] +
                                                                       vp[9] - q6_m2));
-                s.Pn[2][l] = u1;
-                s.Pn[3][l] = u2;
-                s.Pn[4][l] = u3;
+                pv[2] = u1;
+                pv[3] = u2;
+                pv[4] = u3;
             }
+            store_primal<TGV>(s.Pn, s.Pn1, l, pv);
             if (check) {
                 double a, b, c, e;
                 mon_terms(c1, cn, e1, en, a, b, c, e);
