@@ -375,6 +375,42 @@ qsm_status qsm_session_fetch(qsm_session *session, uint64_t id, void *out);
 /* Jobs admitted and not yet finished. */
 uint32_t qsm_session_running(const qsm_session *session);
 
+/* ---------------- MATLAB-level pipelines (crop, echo loop, solve) ----------------
+ *
+ * The wrappers' own steps on the device: crop to the mask's bounding box
+ * (src/utils/cropIndices.m) grown by a margin and clamped, the per-echo
+ * Laplacian and solve, and the scatter back into a zero array of the input's
+ * size.  dims[4] = {nx, ny, nz, echoes}; echo t starts at t*nx*ny*nz.  An
+ * empty mask is QSM_ERR_ARG (the MATLAB code indexes an empty array). */
+
+/* x = sstgv(phas, mask, vsz, lambda, alpha, tol, maxit, verbose):
+ * src/inversion/sstgv.m:1-87 (crop margin 2, d2u = lapw(u), pd_tgv_mex(-d2u, ...),
+ * or pd_tv_mex when alpha <= eps).  fused = 0: the plain path (bit-exact with the
+ * reference); fused != 0: the mixed-precision fused path, all echoes advanced
+ * together.  info: NULL or one entry per echo. */
+qsm_status qsm_sstgv(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[4], const void *phas,
+                     const uint8_t *mask, const double vsz[3], double lambda, double alpha,
+                     double tol, uint32_t maxit, uint32_t verbose, int32_t fused, void *x,
+                     qsm_pd_info *info);
+
+/* fl = lbv(f, mask, vsz, tol, maxit, mgopts, verbose): src/bgremove/lbv.m:1-113
+ * (crop margin 1, d2u = lap(u, m), mgpcg(-d2u, m, ...) with mgopts.maxit/npre/npost/
+ * nboundary, mu 1, tolmg -1, nlevels = max(1, floor(log2(min(size))) - 3) of the
+ * cropped grid).  maxit <= 0: ceil(sqrt(numel(mask))).  mixed != 0 (FP64 only): the
+ * FP32 V-cycle preconditioner.  info: NULL or one entry per echo (resnorm_hist is
+ * not filled). */
+qsm_status qsm_lbv(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[4], const void *f,
+                   const uint8_t *mask, const double vsz[3], double tol, int32_t maxit,
+                   int32_t mg_maxit, int32_t npre, int32_t npost, int32_t nboundary,
+                   int32_t verbose, int32_t mixed, void *fl, qsm_mg_info *info);
+
+/* [uphas, d2phas] = unwrapLaplacian(phas, mask, vsz): src/unwrap/unwrapLaplacian.m:1-87
+ * (crop margin 1, d2u = lapw(u), mgpcg(-m.*d2u, m, h, 1e-8, ceil(sqrt(numel(m))),
+ * mg maxit 2, npre = npost = 2, nboundary 2)).  d2phas may be NULL. */
+qsm_status qsm_unwrap_laplacian(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[4],
+                                const void *phas, const uint8_t *mask, const double vsz[3],
+                                int32_t mixed, void *uphas, void *d2phas);
+
 /* ---------------- lane-order inner product (BLAS-1 replacement) ---------------- */
 
 /* *out = x . y in the library's documented lane order (mx_dot,

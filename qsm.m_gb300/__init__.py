@@ -33,7 +33,7 @@ __all__ = [
     "gradf_adj_mex", "gradb_adj_mex", "gradfm_adj_mex", "gradbm_adj_mex", "gradfp_mex", "gradfp_adj_mex",
     "lap1_mex", "lapw_mex", "gauss_seidel_mex", "residual_mex", "lapmg_mex", "restrict_mex", "prolong_mex",
     "correct_mex", "coarsen_grid_mex", "boundary_mask_mex", "boundary_mask_l1_mex", "norm2_mex", "mgpcg_mex",
-    "mg_mex", "fmg_mex", "lane_dot", "tv", "pd_tv_batch", "pd_tgv_batch", "Session", "footprint", "QsmError",
+    "mg_mex", "fmg_mex", "lane_dot", "tv", "sstgv", "lbv", "unwrap_laplacian", "pd_tv_batch", "pd_tgv_batch", "Session", "footprint", "QsmError",
     "QsmLibraryError", "context", "lib",
 ]
 
@@ -424,6 +424,66 @@ def tv(f, mask, vsz, bdir=(0.0, 0.0, 1.0), opts=None, *, info=None, ctx=None):
         info.update(iters=ti.iters, rho=ti.rho, nr=ti.nr, eps_pri=ti.eps_pri, ns=ti.ns, eps_dual=ti.eps_dual,
                     seconds=ti.seconds)
     return out
+
+
+# ---------------------------------------------------------------------------
+# MATLAB-level pipelines: crop to the mask, echo loop, solve (sstgv.m, lbv.m,
+# unwrapLaplacian.m)
+# ---------------------------------------------------------------------------
+
+def _dims4(a: _Arr):
+    n3 = a.dims[0] * a.dims[1] * a.dims[2]
+    ne = a.numel // n3 if n3 else 0
+    return (ctypes.c_size_t * 4)(a.dims[0], a.dims[1], a.dims[2], ne), ne
+
+
+def sstgv(phas, mask, vsz, lambda_=1e-4, alpha=3.0, tol=3e-4, maxit=5000, verbose=0, *, fused=True, infos=None,
+          ctx=None):
+    """x = sstgv(phas, mask, vsz, lambda, alpha, tol, maxit, verbose) (sstgv.m defaults).
+    phas is 3-D or 4-D (echoes last).  fused=False runs the plain path (bit-exact with the
+    reference MEX), fused=True the mixed-precision path with the echoes batched."""
+    a, m = _Arr(phas), _Arr(mask, mask=True)
+    out = _zeros_like(a)
+    o = _Arr(out, writable=True)
+    d4, ne = _dims4(a)
+    pis = (PdInfo * max(ne, 1))()
+    _sync_torch(a, m, o)
+    _ctx(ctx).call("qsm_sstgv", a.dt, d4, a.ptr, m.ptr, _h(vsz), float(lambda_), float(alpha), float(tol), int(maxit),
+                   int(verbose), 1 if fused else 0, o.ptr, pis)
+    if infos is not None:
+        infos[:] = [_pd_info_dict(pis[t]) for t in range(ne)]
+    return out
+
+
+def lbv(f, mask, vsz, tol=1e-8, maxit=None, mgopts=None, verbose=0, *, mixed=False, infos=None, ctx=None):
+    """fl = lbv(f, mask, vsz, tol, maxit, mgopts, verbose) (lbv.m defaults: maxit
+    ceil(sqrt(numel(mask))), mgopts maxit 2, npre 2, npost 2, nboundary 2)."""
+    o_ = dict(maxit=2, npre=2, npost=2, nboundary=2)
+    if mgopts:
+        o_.update({k: v for k, v in dict(mgopts).items() if v is not None})
+    a, m = _Arr(f), _Arr(mask, mask=True)
+    out = _zeros_like(a)
+    o = _Arr(out, writable=True)
+    d4, ne = _dims4(a)
+    mis = (MgInfo * max(ne, 1))()
+    _sync_torch(a, m, o)
+    _ctx(ctx).call("qsm_lbv", a.dt, d4, a.ptr, m.ptr, _h(vsz), float(tol), int(maxit or 0), int(o_["maxit"]),
+                   int(o_["npre"]), int(o_["npost"]), int(o_["nboundary"]), int(verbose), 1 if mixed else 0, o.ptr,
+                   mis)
+    if infos is not None:
+        infos[:] = [dict(iters=mis[t].iters, resnorm=mis[t].resnorm, seconds=mis[t].seconds) for t in range(ne)]
+    return out
+
+
+def unwrap_laplacian(phas, mask, vsz, *, mixed=False, ctx=None):
+    """[uphas, d2phas] = unwrapLaplacian(phas, mask, vsz)."""
+    a, m = _Arr(phas), _Arr(mask, mask=True)
+    up, d2 = _zeros_like(a), _zeros_like(a)
+    o1, o2 = _Arr(up, writable=True), _Arr(d2, writable=True)
+    d4, _ = _dims4(a)
+    _sync_torch(a, m, o1, o2)
+    _ctx(ctx).call("qsm_unwrap_laplacian", a.dt, d4, a.ptr, m.ptr, _h(vsz), 1 if mixed else 0, o1.ptr, o2.ptr)
+    return up, d2
 
 
 # ---------------------------------------------------------------------------

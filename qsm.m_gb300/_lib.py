@@ -90,6 +90,9 @@ SIGNATURES = {
     "qsm_fmg": [I32, SZ3, P, U8, D3, DBL, I32, I32, I32, I32, I32, I32, P, ctypes.POINTER(MgInfo)],
     "qsm_tv_admm": [I32, SZ3, P, U8, D3, D3, DBL, I32, DBL, DBL, I32, DBL, DBL, DBL, DBL, DBL, I32, P,
                     ctypes.POINTER(TvInfo)],
+    "qsm_sstgv": [I32, SZ3, P, U8, D3, DBL, DBL, DBL, U32, U32, I32, P, P],
+    "qsm_lbv": [I32, SZ3, P, U8, D3, DBL, I32, I32, I32, I32, I32, I32, I32, P, P],
+    "qsm_unwrap_laplacian": [I32, SZ3, P, U8, D3, I32, P, P],
     # count volumes: dims (size_t[3*count]), arrays of d2f / mask / chi pointers
     "qsm_pd_tv_batch": [I32, U32, P, P, P, D3, DBL, DBL, U32, P, P],
     "qsm_pd_tgv_batch": [I32, U32, P, P, P, D3, DBL, DBL, DBL, U32, P, P],

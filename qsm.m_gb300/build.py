@@ -3,7 +3,9 @@
 Every translation unit is compiled for sm_103a only, without fused
 multiply-add (``-fmad=false``): the kernels evaluate QSM.m's per-voxel
 expressions in the reference's association order, and contraction into FMA
-would change the rounding.  Division and square root stay IEEE (no
+would change the rounding.  The host compiler gets ``-ffp-contract=off`` for
+the same reason: the solvers' constants (step sizes, 1/h^2 terms) are computed
+on the host, and GCC contracts by default on aarch64.  Division and square root stay IEEE (no
 ``--use_fast_math``).  Objects are compiled in parallel, then linked.
 
 Usage:  python qsm.m_gb300/build.py [--force]
@@ -23,9 +25,9 @@ LIB = os.path.join(HERE, "libqsm_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "--prec-div=true", "--prec-sqrt=true",
-    "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "-Xptxas", "-O3",
+    "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-O3",
 ]
-SOURCES = ["common.cu", "fd.cu", "pd.cu", "pd_fused.cu", "pd_stream.cu", "pd_batch.cu", "tv_admm.cu", "mg.cu", "noalloc.cu"]
+SOURCES = ["common.cu", "fd.cu", "pd.cu", "pd_fused.cu", "pd_stream.cu", "pd_batch.cu", "tv_admm.cu", "pipelines.cu", "mg.cu", "noalloc.cu"]
 
 
 def nvcc() -> str:

@@ -71,4 +71,5 @@ def test_build_flags_pin_arch_and_no_fma():
     flags = " ".join(b.NVCC_FLAGS)
     assert "arch=compute_103a,code=sm_103a" in flags
     assert "-fmad=false" in flags
+    assert "-ffp-contract=off" in flags  # host-side constants, contracted by default on aarch64
     assert "use_fast_math" not in flags
