@@ -411,6 +411,34 @@ qsm_status qsm_unwrap_laplacian(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims
                                 const void *phas, const uint8_t *mask, const double vsz[3],
                                 int32_t mixed, void *uphas, void *d2phas);
 
+/* ---------------- FFT background-field removal ----------------
+ *
+ * f and mask are cropped to cropIndices(mask), zero-padded to a 7-smooth size
+ * (padfastfft.m, third_party/nextfastfft.m) and convolved with spherical-mean-
+ * value kernels (smvKernel.m) by cuFFT; fl is zero outside the crop.  Eroded
+ * masks are real(ifft3(H .* fft3(single(mask)))) > 0.999 in FP32, as the MATLAB
+ * code computes them; the field arithmetic is in dtype.  dims[4] = {nx, ny, nz,
+ * echoes}.  mask_out (NULL allowed) receives the eroded mask the function
+ * returns as its second output.  An empty mask is QSM_ERR_ARG. */
+
+/* [fl, mask] = sharp(f, mask, vsz, r, thr): src/bgremove/sharp.m:1-84 (r 9, thr 0.05) */
+qsm_status qsm_sharp(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[4], const void *f,
+                     const uint8_t *mask, const double vsz[3], double r, double thr, void *fl,
+                     uint8_t *mask_out);
+
+/* [fl, mask] = vsharp(f, mask, vsz, rs, thr): src/bgremove/vsharp.m:1-153.
+ * nradii <= 0: rs = 9 : -2*max(vsz) : 2*max(vsz).  At least two radii. */
+qsm_status qsm_vsharp(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[4], const void *f,
+                      const uint8_t *mask, const double vsz[3], const double *radii,
+                      int32_t nradii, double thr, void *fl, uint8_t *mask_out);
+
+/* [fl, mask] = ismv(f, mask, vsz, r, tol, maxit, verbose): src/bgremove/ismv.m:1-112
+ * (r 3, tol < 0: sqrt(eps(class)), maxit 500).  iters (NULL allowed) receives the
+ * iterations of each echo. */
+qsm_status qsm_ismv(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[4], const void *f,
+                    const uint8_t *mask, const double vsz[3], double r, double tol, int32_t maxit,
+                    int32_t verbose, void *fl, uint8_t *mask_out, int32_t *iters);
+
 /* ---------------- lane-order inner product (BLAS-1 replacement) ---------------- */
 
 /* *out = x . y in the library's documented lane order (mx_dot,

@@ -33,7 +33,8 @@ __all__ = [
     "gradf_adj_mex", "gradb_adj_mex", "gradfm_adj_mex", "gradbm_adj_mex", "gradfp_mex", "gradfp_adj_mex",
     "lap1_mex", "lapw_mex", "gauss_seidel_mex", "residual_mex", "lapmg_mex", "restrict_mex", "prolong_mex",
     "correct_mex", "coarsen_grid_mex", "boundary_mask_mex", "boundary_mask_l1_mex", "norm2_mex", "mgpcg_mex",
-    "mg_mex", "fmg_mex", "lane_dot", "tv", "sstgv", "lbv", "unwrap_laplacian", "pd_tv_batch", "pd_tgv_batch", "Session", "footprint", "QsmError",
+    "mg_mex", "fmg_mex", "lane_dot", "tv", "sstgv", "lbv", "unwrap_laplacian", "sharp", "vsharp", "ismv",
+    "pd_tv_batch", "pd_tgv_batch", "Session", "footprint", "QsmError",
     "QsmLibraryError", "context", "lib",
 ]
 
@@ -484,6 +485,55 @@ def unwrap_laplacian(phas, mask, vsz, *, mixed=False, ctx=None):
     _sync_torch(a, m, o1, o2)
     _ctx(ctx).call("qsm_unwrap_laplacian", a.dt, d4, a.ptr, m.ptr, _h(vsz), 1 if mixed else 0, o1.ptr, o2.ptr)
     return up, d2
+
+
+# ---------------------------------------------------------------------------
+# FFT background-field removal (sharp.m, vsharp.m, ismv.m)
+# ---------------------------------------------------------------------------
+
+def _mask_like(m: _Arr):
+    if _is_torch(m.obj):
+        return _torch.zeros_like(m.obj, dtype=_torch.uint8)
+    return np.zeros(m.obj.shape, dtype=np.uint8, order="F")
+
+
+def sharp(f, mask, vsz, r=9.0, thr=0.05, *, ctx=None):
+    """[fl, mask] = sharp(f, mask, vsz, r, thr)."""
+    a, m = _Arr(f), _Arr(mask, mask=True)
+    fl, mo = _zeros_like(a), _mask_like(m)
+    o, om = _Arr(fl, writable=True), _Arr(mo, writable=True, mask=True)
+    d4, _ = _dims4(a)
+    _sync_torch(a, m, o, om)
+    _ctx(ctx).call("qsm_sharp", a.dt, d4, a.ptr, m.ptr, _h(vsz), float(r), float(thr), o.ptr, om.ptr)
+    return fl, mo
+
+
+def vsharp(f, mask, vsz, rs=None, thr=0.05, *, ctx=None):
+    """[fl, mask] = vsharp(f, mask, vsz, rs, thr); rs None: 9 : -2*max(vsz) : 2*max(vsz)."""
+    a, m = _Arr(f), _Arr(mask, mask=True)
+    fl, mo = _zeros_like(a), _mask_like(m)
+    o, om = _Arr(fl, writable=True), _Arr(mo, writable=True, mask=True)
+    d4, _ = _dims4(a)
+    r = np.ascontiguousarray(np.asarray(rs if rs is not None else [], dtype=np.float64).reshape(-1))
+    _sync_torch(a, m, o, om)
+    _ctx(ctx).call("qsm_vsharp", a.dt, d4, a.ptr, m.ptr, _h(vsz), r.ctypes.data if r.size else None, int(r.size),
+                   float(thr), o.ptr, om.ptr)
+    return fl, mo
+
+
+def ismv(f, mask, vsz, r=3.0, tol=None, maxit=500, verbose=0, *, info=None, ctx=None):
+    """[fl, mask] = ismv(f, mask, vsz, r, tol, maxit, verbose); tol None: sqrt(eps(class(f)))."""
+    a, m = _Arr(f), _Arr(mask, mask=True)
+    fl, mo = _zeros_like(a), _mask_like(m)
+    o, om = _Arr(fl, writable=True), _Arr(mo, writable=True, mask=True)
+    d4, ne = _dims4(a)
+    its = (ctypes.c_int32 * max(ne, 1))()
+    _sync_torch(a, m, o, om)
+    _ctx(ctx).call("qsm_ismv", a.dt, d4, a.ptr, m.ptr, _h(vsz), float(r), -1.0 if tol is None else float(tol),
+                   int(maxit), int(verbose), o.ptr, om.ptr, its)
+    if info is not None:
+        info.update(iters=[int(its[t]) for t in range(ne)])
+    return fl, mo
 
 
 # ---------------------------------------------------------------------------

@@ -93,6 +93,9 @@ SIGNATURES = {
     "qsm_sstgv": [I32, SZ3, P, U8, D3, DBL, DBL, DBL, U32, U32, I32, P, P],
     "qsm_lbv": [I32, SZ3, P, U8, D3, DBL, I32, I32, I32, I32, I32, I32, I32, P, P],
     "qsm_unwrap_laplacian": [I32, SZ3, P, U8, D3, I32, P, P],
+    "qsm_sharp": [I32, SZ3, P, U8, D3, DBL, DBL, P, P],
+    "qsm_vsharp": [I32, SZ3, P, U8, D3, P, I32, DBL, P, P],
+    "qsm_ismv": [I32, SZ3, P, U8, D3, DBL, DBL, I32, I32, P, P, P],
     # count volumes: dims (size_t[3*count]), arrays of d2f / mask / chi pointers
     "qsm_pd_tv_batch": [I32, U32, P, P, P, D3, DBL, DBL, U32, P, P],
     "qsm_pd_tgv_batch": [I32, U32, P, P, P, D3, DBL, DBL, DBL, U32, P, P],

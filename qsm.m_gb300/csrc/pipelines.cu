@@ -97,8 +97,9 @@ __global__ void neg_k(T *o, const T *__restrict__ a, const uint8_t *__restrict__
 
 static unsigned grid_for(size_t n) { return (unsigned)std::max<size_t>(1, std::min<size_t>((n + 255) / 256, 8 * 152)); }
 
-// cropIndices(mask) grown by `pad` and clamped (sstgv.m:57-63, lbv.m:86-92)
-static qsm_status crop_box(qsm_ctx *ctx, const uint8_t *mask_dev, const Dims &d, int pad, Box *b)
+// cropIndices(mask): the first and last index of each axis that holds a mask
+// voxel (src/utils/cropIndices.m); QSM_ERR_ARG for an empty mask
+qsm_status mask_bbox(qsm_ctx *ctx, const uint8_t *mask_dev, const Dims &d, size_t lo[3], size_t hi[3])
 {
     unsigned *bb = nullptr;
     QSM_TRY(dalloc(ctx, (void **)&bb, 6 * sizeof(unsigned)));
@@ -114,11 +115,23 @@ static qsm_status crop_box(qsm_ctx *ctx, const uint8_t *mask_dev, const Dims &d,
         set_error(ctx, "the mask is empty (cropIndices finds no voxel)");
         return QSM_ERR_ARG;
     }
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = h[a];
+        hi[a] = h[3 + a];
+    }
+    return QSM_OK;
+}
+
+// cropIndices(mask) grown by `pad` and clamped (sstgv.m:57-63, lbv.m:86-92)
+static qsm_status crop_box(qsm_ctx *ctx, const uint8_t *mask_dev, const Dims &d, int pad, Box *b)
+{
+    size_t h[3], g[3];
+    QSM_TRY(mask_bbox(ctx, mask_dev, d, h, g));
     const size_t n[3] = {d.nx, d.ny, d.nz};
     size_t lo[3], hi[3];
     for (int a = 0; a < 3; ++a) {
-        lo[a] = h[a] >= (unsigned)pad ? h[a] - pad : 0;
-        hi[a] = std::min<size_t>(n[a] - 1, (size_t)h[3 + a] + pad);
+        lo[a] = h[a] >= (size_t)pad ? h[a] - pad : 0;
+        hi[a] = std::min<size_t>(n[a] - 1, g[a] + pad);
     }
     b->x0 = lo[0];
     b->y0 = lo[1];
