@@ -432,6 +432,25 @@ qsm_status qsm_vsharp(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[4], const
                       const uint8_t *mask, const double vsz[3], const double *radii,
                       int32_t nradii, double thr, void *fl, uint8_t *mask_out);
 
+/* [fl, mask] = resharp(f, mask, vsz, r, lambda, tol, maxit): src/bgremove/resharp.m:1-88
+ * (r 3, lambda 1e-2, tol < 0: sqrt(eps(class)), maxit <= 0: ceil(sqrt(numel(mask)))).
+ * MATLAB's cgs is replaced by the published CGS iteration (x0 = 0, no preconditioner,
+ * stop when the updated residual is <= tol*||b||); iters (NULL allowed) per echo. */
+qsm_status qsm_resharp(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[4], const void *f,
+                       const uint8_t *mask, const double vsz[3], double r, double lambda, double tol,
+                       int32_t maxit, int32_t verbose, void *fl, uint8_t *mask_out, int32_t *iters);
+
+/* fl = pdf(f, mask, vsz, w, bdir, lambda, tol, maxit, verbose): src/bgremove/pdf.m:1-86
+ * (w NULL: the mask; bdir [0 0 1]; lambda 0; tol < 0: 1e-5; maxit <= 0:
+ * ceil(sqrt(numel(mask)))).  The least-squares problem is solved by LSMR (Fong &
+ * Saunders 2011; atol = btol = tol, conlim 1e8, no reorthogonalisation) on the full
+ * grid; the dipole kernel is psf2otf of the image-space kernel (dipoleKernel.m 'i').
+ * w has the dtype of f.  iters (NULL allowed) per echo. */
+qsm_status qsm_pdf(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[4], const void *f,
+                   const uint8_t *mask, const void *w, const double vsz[3], const double bdir[3],
+                   double lambda, double tol, int32_t maxit, int32_t verbose, void *fl,
+                   int32_t *iters);
+
 /* [fl, mask] = ismv(f, mask, vsz, r, tol, maxit, verbose): src/bgremove/ismv.m:1-112
  * (r 3, tol < 0: sqrt(eps(class)), maxit 500).  iters (NULL allowed) receives the
  * iterations of each echo. */

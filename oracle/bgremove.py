@@ -3,7 +3,11 @@
 TEST INFRASTRUCTURE ONLY: imported by tests/ as the checker of the GPU
 path; the product never imports it.
 
-Follows src/bgremove/sharp.m:1-84, vsharp.m:1-153 and ismv.m:1-112 with
+Follows src/bgremove/sharp.m:1-84, vsharp.m:1-153, ismv.m:1-112,
+resharp.m:1-88 (MATLAB's cgs restated as the published CGS iteration) and
+pdf.m:1-86 (third_party/lsmr/lsmr.m restated from Fong & Saunders 2011;
+src/utils/kernels/dipoleKernel.m 'i'; psf2otf as ifftshift + fftn, real part
+kept when the imaginary part is roundoff) with
 src/utils/cropIndices.m, padfastfft.m, unpadfastfft.m,
 src/utils/kernels/smvKernel.m:25-37 and third_party/nextfastfft.m (the smallest
 7-smooth integer >= n).  fft3 / ifft3 are numpy's pocketfft: complex128 for
@@ -100,7 +104,8 @@ def sharp(f, mask, vsz, r=9.0, thr=0.05):
     for t, ft in enumerate(echoes):
         u = padfast(ft[b], pad)
         u = mk * np.real(np.fft.ifftn(h * np.fft.fftn(u)))
-        U = np.fft.fftn(u) / h
+        with np.errstate(divide="ignore", invalid="ignore"):
+            U = np.fft.fftn(u) / h
         U[np.abs(h) < thr] = 0
         u = mk * np.real(np.fft.ifftn(U))
         out = unpadfast(u, sz, pad)
@@ -206,3 +211,224 @@ def ismv(f, mask, vsz, r=3.0, tol=None, maxit=500, info=None):
     mo = np.zeros(np.shape(mask), np.uint8, order="F")
     mo[b] = unpadfast(m, sz, pad).astype(np.uint8)
     return fl, mo
+
+
+def cgs(A, b, tol, maxit):
+    """Conjugate gradients squared (Sonneveld 1989; the unpreconditioned form of
+    Barrett et al., Templates, 1994), x0 = 0, stopping when the recursively
+    updated residual is <= tol * ||b||.  Returns (x, iterations)."""
+    x = np.zeros_like(b)
+    r = b.copy()
+    rt = b.copy()
+    nb = np.linalg.norm(b)
+    it = 0
+    if nb == 0:
+        return x, 0
+    rho1 = 1.0
+    u = p = q = None
+    for ii in range(1, maxit + 1):
+        rho = float(np.dot(rt, r))
+        if rho == 0.0:
+            break
+        if ii == 1:
+            u = r.copy()
+            p = r.copy()
+        else:
+            beta = rho / rho1
+            u = r + beta * q
+            p = u + beta * (q + beta * p)
+        vh = A(p)
+        sv = float(np.dot(rt, vh))
+        if sv == 0.0:
+            break
+        alpha = rho / sv
+        q = u - alpha * vh
+        uh = u + q
+        x = x + alpha * uh
+        r = r - alpha * A(uh)
+        rho1 = rho
+        it = ii
+        if np.linalg.norm(r) <= tol * nb:
+            break
+    return x, it
+
+
+def resharp(f, mask, vsz, r=3.0, lam=1e-2, tol=None, maxit=None, info=None):
+    """resharp.m:1-88 with MATLAB's cgs replaced by `cgs` above."""
+    f, echoes = _echoes(f)
+    tol = math.sqrt(np.finfo(np.float64).eps) if tol is None else tol
+    maxit = maxit or int(math.ceil(math.sqrt(np.asarray(mask).size)))
+    b = crop_slices(mask)
+    sz = tuple(s.stop - s.start for s in b)
+    pad = int(math.ceil(r / min(vsz)))
+    m1 = padfast(np.asarray(mask)[b] != 0, pad)
+    H = smv_spectrum(m1.shape, r, vsz)
+    mk = erode(H, m1).astype(np.float64)
+    h = 1.0 - H
+    shape = m1.shape
+
+    def A(v):
+        v = v.reshape(shape)
+        return (mk * np.real(np.fft.ifftn(h * np.fft.fftn(v))) + lam * v).ravel()
+
+    fl = np.zeros(f.shape, order="F")
+    iters = []
+    for t, ft in enumerate(echoes):
+        rhs = (mk * np.real(np.fft.ifftn(h * np.fft.fftn(padfast(ft[b], pad))))).ravel()
+        x, it = cgs(A, rhs, tol, maxit)
+        iters.append(it)
+        out = unpadfast(mk * x.reshape(shape), sz, pad)
+        if f.ndim == 3:
+            fl[b] = out
+        else:
+            fl[b + (t,)] = out
+    if info is not None:
+        info["iters"] = iters
+    mo = np.zeros(np.shape(mask), np.uint8, order="F")
+    mo[b] = unpadfast(mk, sz, pad).astype(np.uint8)
+    return fl, mo
+
+
+def psf2otf(k):
+    """fft3 of a centred kernel moved to index 0 (ifftshift); the real part when
+    the imaginary part is roundoff: max|Im| / max|K| <= N log2(N) eps."""
+    K = np.fft.fftn(np.fft.ifftshift(k))
+    n = k.size
+    eps = np.finfo(np.float32 if k.dtype == np.float32 else np.float64).eps
+    if np.abs(K.imag).max() / np.abs(K).max() <= n * math.log2(n) * eps:
+        K = K.real.astype(K.dtype)
+    return K
+
+
+def dipole_kernel_i(sz, vsz, bdir=(0.0, 0.0, 1.0)):
+    """dipoleKernel(sz, vsz, bdir, 'i') (src/utils/kernels/dipoleKernel.m:44-51):
+    (3 (b.r)^2 - |r|^2) / (4 pi |r|^5) on the centred grid, 0 at the centre."""
+    b = np.asarray(bdir, np.float64)
+    nb = math.sqrt(float(b @ b))
+    if nb != 1.0:
+        b = b / nb
+    g = []
+    for n, h in zip(sz, vsz):
+        low = n // 2
+        high = low - (1 - n % 2)
+        g.append(np.arange(-low, high + 1) * float(h))
+    X, Y, Z = np.meshgrid(*g, indexing="ij")
+    rz = b[0] * X + b[1] * Y + b[2] * Z
+    r2 = X * X + Y * Y + Z * Z
+    den = 4 * math.pi * np.sqrt(r2 * r2 * r2 * r2 * r2)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        D = (3 * (rz * rz) - r2) / den
+    D[den == 0] = 0
+    return D
+
+
+def lsmr(A, AT, b, lam=0.0, atol=1e-6, btol=1e-6, conlim=1e8, itnlim=None):
+    """LSMR (Fong & Saunders, SIAM J. Sci. Comput. 33(5), 2011) without local
+    reorthogonalisation, with the stopping rules of the published algorithm
+    (third_party/lsmr/lsmr.m).  Returns (x, itn)."""
+    u = b.copy()
+    beta = float(np.linalg.norm(u))
+    if beta > 0:
+        u = u / beta
+    v = AT(u)
+    alpha = float(np.linalg.norm(v))
+    if alpha > 0:
+        v = v / alpha
+    x = np.zeros_like(v)
+    itnlim = itnlim if itnlim is not None else min(b.size, v.size)
+    if alpha * beta == 0:
+        return x, 0
+    zetabar, alphabar, rho, rhobar, cbar, sbar = alpha * beta, alpha, 1.0, 1.0, 1.0, 0.0
+    h, hbar = v.copy(), np.zeros_like(v)
+    betadd, betad, rhodold, tautildeold, thetatilde, zeta, d = beta, 0.0, 1.0, 0.0, 0.0, 0.0, 0.0
+    normA2, maxrbar, minrbar, normb = alpha * alpha, 0.0, 1e100, beta
+    ctol = 1.0 / conlim if conlim > 0 else 0.0
+    itn = 0
+    while itn < itnlim:
+        itn += 1
+        u = A(v) - alpha * u
+        beta = float(np.linalg.norm(u))
+        if beta > 0:
+            u = u / beta
+            v = AT(u) - beta * v
+            alpha = float(np.linalg.norm(v))
+            if alpha > 0:
+                v = v / alpha
+        alphahat = math.hypot(alphabar, lam)
+        chat, shat = alphabar / alphahat, lam / alphahat
+        rhoold = rho
+        rho = math.hypot(alphahat, beta)
+        c, s = alphahat / rho, beta / rho
+        thetanew = s * alpha
+        alphabar = c * alpha
+        rhobarold, zetaold, thetabar, rhotemp = rhobar, zeta, sbar * rho, cbar * rho
+        rhobar = math.hypot(cbar * rho, thetanew)
+        cbar = cbar * rho / rhobar
+        sbar = thetanew / rhobar
+        zeta = cbar * zetabar
+        zetabar = -sbar * zetabar
+        hbar = h - (thetabar * rho / (rhoold * rhobarold)) * hbar
+        x = x + (zeta / (rho * rhobar)) * hbar
+        h = v - (thetanew / rho) * h
+        betaacute, betacheck = chat * betadd, -shat * betadd
+        betahat = c * betaacute
+        betadd = -s * betaacute
+        thetatildeold = thetatilde
+        rhotildeold = math.hypot(rhodold, thetabar)
+        ctildeold, stildeold = rhodold / rhotildeold, thetabar / rhotildeold
+        thetatilde = stildeold * rhobar
+        rhodold = ctildeold * rhobar
+        betad = -stildeold * betad + ctildeold * betahat
+        tautildeold = (zetaold - thetatildeold * tautildeold) / rhotildeold
+        taud = (zeta - thetatilde * tautildeold) / rhodold
+        d = d + betacheck * betacheck
+        normr = math.sqrt(d + (betad - taud) ** 2 + betadd * betadd)
+        normA2 = normA2 + beta * beta
+        normA = math.sqrt(normA2)
+        normA2 = normA2 + alpha * alpha
+        maxrbar = max(maxrbar, rhobarold)
+        if itn > 1:
+            minrbar = min(minrbar, rhobarold)
+        condA = max(maxrbar, rhotemp) / min(minrbar, rhotemp)
+        normAr = abs(zetabar)
+        normx = float(np.linalg.norm(x))
+        test1, test2, test3 = normr / normb, normAr / (normA * normr), 1.0 / condA
+        t1 = test1 / (1 + normA * normx / normb)
+        rtol = btol + atol * normA * normx / normb
+        if (itn >= itnlim or 1 + test3 <= 1 or 1 + test2 <= 1 or 1 + t1 <= 1 or test3 <= ctol
+                or test2 <= atol or test1 <= rtol):
+            break
+    return x, itn
+
+
+def pdf(f, mask, vsz, w=None, bdir=(0.0, 0.0, 1.0), lam=0.0, tol=1e-5, maxit=None, info=None):
+    """pdf.m:1-86 on the full grid with `lsmr` above."""
+    f, echoes = _echoes(f)
+    mask = np.asarray(mask) != 0
+    maxit = maxit or int(math.ceil(math.sqrt(mask.size)))
+    if w is None or not np.any(w):
+        w = mask
+    D = psf2otf(dipole_kernel_i(mask.shape, vsz, bdir))
+    m = mask * np.asarray(w, np.float64)
+    nm = (m == 0).astype(np.float64)
+    shape = mask.shape
+
+    def A(v):
+        return (m * np.real(np.fft.ifftn(D * np.fft.fftn(nm * v.reshape(shape))))).ravel()
+
+    def AT(v):
+        return (nm * np.real(np.fft.ifftn(np.conj(D) * np.fft.fftn(m * v.reshape(shape))))).ravel()
+
+    fl = np.zeros(f.shape, order="F")
+    iters = []
+    for t, ft in enumerate(echoes):
+        xb, it = lsmr(A, AT, (m * ft).ravel(), lam, tol, tol, 1e8, maxit)
+        iters.append(it)
+        out = (m != 0) * (ft - np.real(np.fft.ifftn(D * np.fft.fftn(nm * xb.reshape(shape)))))
+        if f.ndim == 3:
+            fl[...] = out
+        else:
+            fl[..., t] = out
+    if info is not None:
+        info["iters"] = iters
+    return fl

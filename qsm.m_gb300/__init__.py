@@ -33,7 +33,7 @@ __all__ = [
     "gradf_adj_mex", "gradb_adj_mex", "gradfm_adj_mex", "gradbm_adj_mex", "gradfp_mex", "gradfp_adj_mex",
     "lap1_mex", "lapw_mex", "gauss_seidel_mex", "residual_mex", "lapmg_mex", "restrict_mex", "prolong_mex",
     "correct_mex", "coarsen_grid_mex", "boundary_mask_mex", "boundary_mask_l1_mex", "norm2_mex", "mgpcg_mex",
-    "mg_mex", "fmg_mex", "lane_dot", "tv", "sstgv", "lbv", "unwrap_laplacian", "sharp", "vsharp", "ismv",
+    "mg_mex", "fmg_mex", "lane_dot", "tv", "sstgv", "lbv", "unwrap_laplacian", "sharp", "vsharp", "ismv", "resharp", "pdf",
     "pd_tv_batch", "pd_tgv_batch", "Session", "footprint", "QsmError",
     "QsmLibraryError", "context", "lib",
 ]
@@ -519,6 +519,49 @@ def vsharp(f, mask, vsz, rs=None, thr=0.05, *, ctx=None):
     _ctx(ctx).call("qsm_vsharp", a.dt, d4, a.ptr, m.ptr, _h(vsz), r.ctypes.data if r.size else None, int(r.size),
                    float(thr), o.ptr, om.ptr)
     return fl, mo
+
+
+def resharp(f, mask, vsz, r=3.0, lambda_=1e-2, tol=None, maxit=None, verbose=0, *, info=None, ctx=None):
+    """[fl, mask] = resharp(f, mask, vsz, r, lambda, tol, maxit); the Tikhonov system is
+    solved by CGS (x0 = 0); tol None: sqrt(eps(class(f))); maxit None: ceil(sqrt(numel(mask)))."""
+    a, m = _Arr(f), _Arr(mask, mask=True)
+    fl, mo = _zeros_like(a), _mask_like(m)
+    o, om = _Arr(fl, writable=True), _Arr(mo, writable=True, mask=True)
+    d4, ne = _dims4(a)
+    its = (ctypes.c_int32 * max(ne, 1))()
+    _sync_torch(a, m, o, om)
+    _ctx(ctx).call("qsm_resharp", a.dt, d4, a.ptr, m.ptr, _h(vsz), float(r), float(lambda_),
+                   -1.0 if tol is None else float(tol), int(maxit or 0), int(verbose), o.ptr, om.ptr, its)
+    if info is not None:
+        info.update(iters=[int(its[t]) for t in range(ne)])
+    return fl, mo
+
+
+def pdf(f, mask, vsz, w=None, bdir=(0.0, 0.0, 1.0), lambda_=0.0, tol=1e-5, maxit=None, verbose=0, *,
+        info=None, ctx=None):
+    """fl = pdf(f, mask, vsz, w, bdir, lambda, tol, maxit, verbose): projection onto dipole
+    fields solved by LSMR on the full grid; w None (or all zero): the mask; maxit None:
+    ceil(sqrt(numel(mask)))."""
+    a, m = _Arr(f), _Arr(mask, mask=True)
+    wa = None
+    if w is not None:
+        single = a.dt == _lib.QSM_F32
+        if _is_torch(w):
+            wa = _Arr(w.to(_torch.float32 if single else _torch.float64))
+        else:
+            wa = _Arr(np.asarray(w, dtype=np.float32 if single else np.float64))
+        if wa.dims != m.dims:
+            raise ValueError("w must have the mask's size")
+    fl = _zeros_like(a)
+    o = _Arr(fl, writable=True)
+    d4, ne = _dims4(a)
+    its = (ctypes.c_int32 * max(ne, 1))()
+    _sync_torch(*(x for x in (a, m, wa, o) if x is not None))
+    _ctx(ctx).call("qsm_pdf", a.dt, d4, a.ptr, m.ptr, None if wa is None else wa.ptr, _h(vsz), _h(bdir),
+                   float(lambda_), -1.0 if tol is None else float(tol), int(maxit or 0), int(verbose), o.ptr, its)
+    if info is not None:
+        info.update(iters=[int(its[t]) for t in range(ne)])
+    return fl
 
 
 def ismv(f, mask, vsz, r=3.0, tol=None, maxit=500, verbose=0, *, info=None, ctx=None):

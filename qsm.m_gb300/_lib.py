@@ -96,6 +96,8 @@ SIGNATURES = {
     "qsm_sharp": [I32, SZ3, P, U8, D3, DBL, DBL, P, P],
     "qsm_vsharp": [I32, SZ3, P, U8, D3, P, I32, DBL, P, P],
     "qsm_ismv": [I32, SZ3, P, U8, D3, DBL, DBL, I32, I32, P, P, P],
+    "qsm_resharp": [I32, SZ3, P, U8, D3, DBL, DBL, DBL, I32, I32, P, P, P],
+    "qsm_pdf": [I32, SZ3, P, U8, P, D3, D3, DBL, DBL, I32, I32, P, P],
     # count volumes: dims (size_t[3*count]), arrays of d2f / mask / chi pointers
     "qsm_pd_tv_batch": [I32, U32, P, P, P, D3, DBL, DBL, U32, P, P],
     "qsm_pd_tgv_batch": [I32, U32, P, P, P, D3, DBL, DBL, DBL, U32, P, P],

@@ -2,6 +2,12 @@
 //   sharp.m:1-84    [fl, mask] = sharp(f, mask, vsz, r, thr)
 //   vsharp.m:1-153  [fl, mask] = vsharp(f, mask, vsz, rs, thr)
 //   ismv.m:1-112    [fl, mask] = ismv(f, mask, vsz, r, tol, maxit, verbose)
+//   pdf.m:1-86      fl = pdf(f, mask, vsz, w, bdir, lambda, tol, maxit, verbose): LSMR
+//                   (Fong & Saunders 2011) on the dipole projection, full grid
+//   resharp.m:1-88  [fl, mask] = resharp(f, mask, vsz, r, lambda, tol, maxit), its
+//                   Tikhonov system solved by conjugate gradients squared (CGS,
+//                   Sonneveld 1989, without preconditioner, x0 = 0, stopping when
+//                   the recursively updated residual is <= tol * ||b||)
 // Each crops f and the mask to cropIndices(mask), zero-pads them to a
 // 7-smooth size (padfastfft.m with nextfastfft, third_party/nextfastfft.m),
 // and works with spherical-mean-value (SMV) kernels (smvKernel.m): the kernel
@@ -13,6 +19,7 @@
 // in the class of f.  Reductions (iSMV residuals) accumulate in FP64 in a
 // fixed order.
 #include <cufft.h>
+#include <float.h>
 #include <math.h>
 #include <stdio.h>
 
@@ -309,6 +316,68 @@ __global__ void ismv_out_k(T *o, const T *__restrict__ ft, const T *__restrict__
         o[l] = (T)(m[l] ? 1 : 0) * (ft[l] - fb[l]);
 }
 
+// out = mask1 .* (ifft value) + lambda .* v  (resharp.m:64-68, the operator A)
+template <typename T>
+__global__ void resharp_op_k(T *out, const T *__restrict__ v, const uint8_t *__restrict__ m, T invn, T lam, size_t n)
+{
+    for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x)
+        out[l] = (T)(m[l] ? 1 : 0) * (out[l] * invn) + lam * v[l];
+}
+
+// sum x .* y in FP64, fixed order (block partials, then fold_k)
+template <typename T>
+__global__ void __launch_bounds__(BG_BLOCK)
+dot_k(const T *__restrict__ x, const T *__restrict__ y, size_t n, double *part)
+{
+    double acc[1] = {0.0};
+    for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x)
+        acc[0] += (double)x[l] * (double)y[l];
+    block_sums<1>(part, acc);
+}
+
+// CGS direction updates: u = r + beta q; p = u + beta (q + beta p)
+template <typename T>
+__global__ void cgs_dir_k(T *u, T *p, const T *__restrict__ r, const T *__restrict__ q, T beta, size_t n, bool first)
+{
+    for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
+        if (first) {
+            u[l] = r[l];
+            p[l] = r[l];
+        } else {
+            const T un = r[l] + beta * q[l];
+            u[l] = un;
+            p[l] = un + beta * (q[l] + beta * p[l]);
+        }
+    }
+}
+
+// q = u - alpha vh; uh = u + q; x = x + alpha uh
+template <typename T>
+__global__ void cgs_q_k(T *q, T *uh, T *x, const T *__restrict__ u, const T *__restrict__ vh, T alpha, size_t n)
+{
+    for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
+        const T qn = u[l] - alpha * vh[l];
+        const T un = u[l] + qn;
+        q[l] = qn;
+        uh[l] = un;
+        x[l] = x[l] + alpha * un;
+    }
+}
+
+// r = r - alpha w; sum r^2
+template <typename T>
+__global__ void __launch_bounds__(BG_BLOCK)
+cgs_r_k(T *r, const T *__restrict__ w, T alpha, size_t n, double *part)
+{
+    double acc[1] = {0.0};
+    for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
+        const T rn = r[l] - alpha * w[l];
+        r[l] = rn;
+        acc[0] += (double)rn * (double)rn;
+    }
+    block_sums<1>(part, acc);
+}
+
 const char *fft_str(cufftResult r)
 {
     switch (r) {
@@ -497,7 +566,7 @@ qsm_status make_grid(qsm_ctx *ctx, const uint8_t *mask, const Dims &d, size_t pa
     return QSM_OK;
 }
 
-enum Method { SHARP, VSHARP, ISMV };
+enum Method { SHARP, VSHARP, ISMV, RESHARP };
 
 template <typename T>
 qsm_status run(qsm_ctx *ctx, Method meth, const Dims &d, size_t ne, const T *f, const uint8_t *mask, const double *h,
@@ -520,11 +589,17 @@ qsm_status run(qsm_ctx *ctx, Method meth, const Dims &d, size_t ne, const T *f, 
         return st;
     }
     const unsigned gn = grid_for(N), gh = grid_for(nh);
+    T *kv = nullptr;  // RESHARP's eight Krylov vectors
+    if (meth == RESHARP && (st = dalloc(ctx, (void **)&kv, 8 * N * sizeof(T))) != QSM_OK) {
+        pl.destroy();
+        w.release(ctx);
+        return st;
+    }
     auto body = [&]() -> qsm_status {
         pad<uint8_t, uint8_t>(ctx, w.m1, mask, g);
         pad<uint8_t, float>(ctx, w.mf, mask, g);
         QSM_TRY(launched(ctx));
-        if (meth != VSHARP) {
+        if (meth != VSHARP) {  // one radius
             QSM_TRY(smv_spectrum<T>(ctx, pl, w, g, h, radii[0]));
             QSM_TRY(erode<T>(ctx, pl, w, g, w.mk));  // mask1 (sharp.m:58) / m (ismv.m:65)
         }
@@ -578,6 +653,72 @@ qsm_status run(qsm_ctx *ctx, Method meth, const Dims &d, size_t ne, const T *f, 
                 QSM_TRY(launched(ctx));
                 unpad<T>(ctx, out, w.b, g);
                 mask_ret = w.mr;
+            } else if (meth == RESHARP) {
+                // RESHARP (resharp.m:62-80): b = mask1 .* real(ifft3((1 - H) .* fft3(f))),
+                // x = cgs(A, b, tol, maxit), fl = mask1 .* x
+                const T lam = (T)thr;
+                T *x = kv, *r = kv + N, *rt = kv + 2 * N, *u = kv + 3 * N, *pp = kv + 4 * N, *q = kv + 5 * N,
+                  *vh = kv + 6 * N, *uh = kv + 7 * N;
+                auto apply = [&](const T *in, T *outv) -> qsm_status {
+                    QSM_CUDA(cudaMemcpyAsync(w.e, in, N * sizeof(T), cudaMemcpyDeviceToDevice, ctx->stream));
+                    QSM_TRY(pl.fwd(ctx, w.e, w.F));
+                    mul_h_k<T><<<gh, 256, 0, ctx->stream>>>(w.F, w.H, nh, true);
+                    QSM_TRY(pl.inv(ctx, w.F, outv));
+                    resharp_op_k<T><<<gn, 256, 0, ctx->stream>>>(outv, in, w.mk, invn, lam, N);
+                    return launched(ctx);
+                };
+                auto dot = [&](const T *a_, const T *b_, double *out_) -> qsm_status {
+                    dot_k<T><<<BG_GRID, BG_BLOCK, 0, ctx->stream>>>(a_, b_, N, w.part);
+                    fold_k<<<1, 32, 0, ctx->stream>>>(w.sum, w.part, BG_GRID);
+                    QSM_TRY(launched(ctx));
+                    QSM_CUDA(cudaMemcpyAsync(out_, w.sum, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+                    QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+                    return QSM_OK;
+                };
+                pad<T, T>(ctx, w.c, ft, g);
+                QSM_TRY(launched(ctx));
+                QSM_TRY(pl.fwd(ctx, w.c, w.F));
+                mul_h_k<T><<<gh, 256, 0, ctx->stream>>>(w.F, w.H, nh, true);
+                QSM_TRY(pl.inv(ctx, w.F, w.b));
+                mask_scale_k<T><<<gn, 256, 0, ctx->stream>>>(w.b, w.mk, invn, N);  // b
+                QSM_TRY(launched(ctx));
+                QSM_CUDA(cudaMemsetAsync(x, 0, N * sizeof(T), ctx->stream));
+                QSM_CUDA(cudaMemcpyAsync(r, w.b, N * sizeof(T), cudaMemcpyDeviceToDevice, ctx->stream));
+                QSM_CUDA(cudaMemcpyAsync(rt, w.b, N * sizeof(T), cudaMemcpyDeviceToDevice, ctx->stream));
+                double nb2 = 0.0, rho = 0.0, rho1 = 1.0, sv = 0.0, rr = 0.0;
+                QSM_TRY(dot(w.b, w.b, &nb2));
+                const double nb = std::sqrt(nb2);
+                int32_t it = 0;
+                if (nb > 0.0) {
+                    for (int32_t ii = 1; ii <= maxit; ++ii) {
+                        QSM_TRY(dot(rt, r, &rho));
+                        if (rho == 0.0) break;  // breakdown
+                        const T beta = (T)(rho / rho1);
+                        cgs_dir_k<T><<<gn, 256, 0, ctx->stream>>>(u, pp, r, q, beta, N, ii == 1);
+                        QSM_TRY(launched(ctx));
+                        QSM_TRY(apply(pp, vh));
+                        QSM_TRY(dot(rt, vh, &sv));
+                        if (sv == 0.0) break;
+                        const T alpha = (T)(rho / sv);
+                        cgs_q_k<T><<<gn, 256, 0, ctx->stream>>>(q, uh, x, u, vh, alpha, N);
+                        QSM_TRY(launched(ctx));
+                        QSM_TRY(apply(uh, vh));  // vh reused for A uh
+                        cgs_r_k<T><<<BG_GRID, BG_BLOCK, 0, ctx->stream>>>(r, vh, alpha, N, w.part);
+                        fold_k<<<1, 32, 0, ctx->stream>>>(w.sum, w.part, BG_GRID);
+                        QSM_TRY(launched(ctx));
+                        QSM_CUDA(cudaMemcpyAsync(&rr, w.sum, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+                        QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+                        rho1 = rho;
+                        it = ii;
+                        if (verbose) printf("%5d/%d\t%1.3e\n", ii, maxit, std::sqrt(rr) / nb);
+                        if (std::sqrt(rr) <= tol * nb) break;
+                    }
+                }
+                if (iters) iters[t] = it;
+                QSM_CUDA(cudaMemcpyAsync(w.b, x, N * sizeof(T), cudaMemcpyDeviceToDevice, ctx->stream));
+                mask_scale_k<T><<<gn, 256, 0, ctx->stream>>>(w.b, w.mk, (T)1, N);
+                QSM_TRY(launched(ctx));
+                unpad<T>(ctx, out, w.b, g);
             } else {
                 // iSMV (ismv.m:67-107): fb from f by f = bc + m .* real(ifft3(H .* fft3(f)))
                 // until ||f0 - f|| <= tol ||m .* f||; fl = m .* (f - fb)
@@ -624,8 +765,303 @@ qsm_status run(qsm_ctx *ctx, Method meth, const Dims &d, size_t ne, const T *f, 
     };
     st = body();
     cudaStreamSynchronize(ctx->stream);
+    if (kv) dfree(ctx, kv);
     pl.destroy();
     w.release(ctx);
+    return st;
+}
+
+// ---------------------------------------------------------------------------
+// PDF (pdf.m:1-86): projection onto dipole fields by LSMR
+// ---------------------------------------------------------------------------
+
+// image-space unit dipole (dipoleKernel.m:44-51, 'i') in psf2otf's order
+// (centre at index 0): D = (3 (b.r)^2 - |r|^2) / (4 pi |r|^5), D(0) = 0
+template <typename T>
+__global__ void dipole_i_k(T *D, Dims pd, double hx, double hy, double hz, double bx, double by, double bz)
+{
+    const size_t N = pd.n();
+    for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < N; l += (size_t)gridDim.x * blockDim.x) {
+        const double x = shift_coord(l % pd.nx, pd.nx, hx), y = shift_coord((l / pd.nx) % pd.ny, pd.ny, hy),
+                     z = shift_coord(l / pd.nxny(), pd.nz, hz);
+        const double rz = bx * x + by * y + bz * z;
+        const double r2 = x * x + y * y + z * z;
+        const double den = 4.0 * 3.14159265358979323846 * sqrt(r2 * r2 * r2 * r2 * r2);
+        D[l] = den == 0.0 ? (T)0 : (T)((3.0 * (rz * rz) - r2) / den);
+    }
+}
+
+// max |Im D| and max |D| over the half spectrum (the same maxima as over the full
+// spectrum of a real kernel); non-negative doubles order like their bit patterns
+template <typename T>
+__global__ void otf_max_k(unsigned long long *mx, const typename Cx<T>::type *__restrict__ D, size_t nh)
+{
+    double mi = 0.0, ma = 0.0;
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < nh; q += (size_t)gridDim.x * blockDim.x) {
+        mi = fmax(mi, fabs((double)D[q].y));
+        ma = fmax(ma, (double)hypot(D[q].x, D[q].y));
+    }
+    atomicMax(mx, (unsigned long long)__double_as_longlong(mi));
+    atomicMax(mx + 1, (unsigned long long)__double_as_longlong(ma));
+}
+
+template <typename T>
+__global__ void drop_imag_k(typename Cx<T>::type *D, size_t nh)
+{
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < nh; q += (size_t)gridDim.x * blockDim.x)
+        D[q].y = (T)0;
+}
+
+// F .*= D (or conj(D))
+template <typename T>
+__global__ void mul_c_k(typename Cx<T>::type *F, const typename Cx<T>::type *__restrict__ D, size_t nh, bool conj)
+{
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < nh; q += (size_t)gridDim.x * blockDim.x) {
+        const T dr = D[q].x, di = conj ? -D[q].y : D[q].y;
+        const T fr = F[q].x, fi = F[q].y;
+        F[q].x = dr * fr - di * fi;
+        F[q].y = dr * fi + di * fr;
+    }
+}
+
+// t = w .* v with w = m (weights) or ~m
+template <typename T>
+__global__ void weight_k(T *t, const T *__restrict__ v, const T *__restrict__ m, bool notm, size_t n)
+{
+    for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x)
+        t[l] = (notm ? (T)(m[l] == (T)0 ? 1 : 0) : m[l]) * v[l];
+}
+
+// y = w .* (C2R value / N) - a .* y, sum y^2  (the Golub-Kahan step u = A v - alpha u)
+template <typename T>
+__global__ void __launch_bounds__(BG_BLOCK)
+gk_step_k(T *y, const T *__restrict__ g, const T *__restrict__ m, bool notm, T invn, T a, size_t n, double *part)
+{
+    double acc[1] = {0.0};
+    for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
+        const T w = notm ? (T)(m[l] == (T)0 ? 1 : 0) : m[l];
+        const T v = w * (g[l] * invn) - a * y[l];
+        y[l] = v;
+        acc[0] += (double)v * (double)v;
+    }
+    block_sums<1>(part, acc);
+}
+
+template <typename T>
+__global__ void scale_k(T *y, T s, size_t n)
+{
+    for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x)
+        y[l] = s * y[l];
+}
+
+// LSMR updates: hbar = h - c1 hbar; x = x + c2 hbar; h = v - c3 h; sum x^2
+template <typename T>
+__global__ void __launch_bounds__(BG_BLOCK)
+lsmr_upd_k(T *hbar, T *x, T *h, const T *__restrict__ v, T c1, T c2, T c3, size_t n, double *part)
+{
+    double acc[1] = {0.0};
+    for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
+        const T hb = h[l] - c1 * hbar[l];
+        const T xn = x[l] + c2 * hb;
+        hbar[l] = hb;
+        x[l] = xn;
+        h[l] = v[l] - c3 * h[l];
+        acc[0] += (double)xn * (double)xn;
+    }
+    block_sums<1>(part, acc);
+}
+
+// fl = logical(m) .* (f - real(ifft3(D .* fft3(~m .* xb))))  (pdf.m:79-80)
+template <typename T>
+__global__ void pdf_out_k(T *o, const T *__restrict__ f, const T *__restrict__ g, const T *__restrict__ m, T invn,
+                          size_t n)
+{
+    for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x)
+        o[l] = (T)(m[l] != (T)0 ? 1 : 0) * (f[l] - g[l] * invn);
+}
+
+template <typename T>
+qsm_status run_pdf(qsm_ctx *ctx, const Dims &d, size_t ne, const T *f, const uint8_t *mask, const T *wgt,
+                   const double *vsz, const double *bdir, double lambda, double tol, int32_t maxit, int32_t verbose,
+                   T *fl, int32_t *iters)
+{
+    using C = typename Cx<T>::type;
+    const size_t N = d.n(), nh = (d.nx / 2 + 1) * d.ny * d.nz;
+    const T invn = (T)(1.0 / (double)N);
+    const unsigned gn = grid_for(N), gh = grid_for(nh);
+    Plans<T> pl;
+    QSM_TRY(pl.make(ctx, d));
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t rb = al(N * sizeof(T)), cb = al(nh * sizeof(C));
+    void *blk = nullptr;
+    qsm_status st = dalloc(ctx, &blk, 8 * rb + 2 * cb + (BG_GRID + 64) * sizeof(double));
+    if (st != QSM_OK) {
+        pl.destroy();
+        return st;
+    }
+    char *p = (char *)blk;
+    T *m = (T *)p, *u = (T *)(p + rb), *v = (T *)(p + 2 * rb), *h = (T *)(p + 3 * rb), *hb = (T *)(p + 4 * rb),
+      *x = (T *)(p + 5 * rb), *t1 = (T *)(p + 6 * rb), *t2 = (T *)(p + 7 * rb);
+    C *Dh = (C *)(p + 8 * rb), *F = (C *)(p + 8 * rb + cb);
+    double *part = (double *)(p + 8 * rb + 2 * cb), *sum = part + BG_GRID;
+    auto red = [&](double *out_) -> qsm_status {
+        fold_k<<<1, 32, 0, ctx->stream>>>(sum, part, BG_GRID);
+        QSM_TRY(launched(ctx));
+        QSM_CUDA(cudaMemcpyAsync(out_, sum, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+        return QSM_OK;
+    };
+    // y = op(in) - a y and ||y||^2: op = m .* ifft(D .* fft(~m .* in)) (forward) or
+    // ~m .* ifft(conj(D) .* fft(m .* in)) (transpose), pdf.m:63-72
+    auto gk = [&](T *y, const T *in, bool transpose, T a, double *n2) -> qsm_status {
+        weight_k<T><<<gn, 256, 0, ctx->stream>>>(t1, in, m, !transpose, N);
+        QSM_TRY(launched(ctx));
+        QSM_TRY(pl.fwd(ctx, t1, F));
+        mul_c_k<T><<<gh, 256, 0, ctx->stream>>>(F, Dh, nh, transpose);
+        QSM_TRY(pl.inv(ctx, F, t2));
+        gk_step_k<T><<<BG_GRID, BG_BLOCK, 0, ctx->stream>>>(y, t2, m, transpose, invn, a, N, part);
+        return red(n2);
+    };
+    auto body = [&]() -> qsm_status {
+        // D = psf2otf(dipoleKernel(size(mask), vsz, bdir, 'i', class(f))): the kernel in
+        // double, rounded to T, transformed in T; psf2otf returns the real part when the
+        // imaginary part is roundoff, max|Im D| / max|D| <= N log2(N) eps(T)
+        const double bn = std::sqrt(bdir[0] * bdir[0] + bdir[1] * bdir[1] + bdir[2] * bdir[2]);
+        const double b0 = bn == 1.0 ? bdir[0] : bdir[0] / bn, b1 = bn == 1.0 ? bdir[1] : bdir[1] / bn,
+                     b2 = bn == 1.0 ? bdir[2] : bdir[2] / bn;
+        dipole_i_k<T><<<gn, 256, 0, ctx->stream>>>(t1, d, vsz[0], vsz[1], vsz[2], b0, b1, b2);
+        QSM_TRY(launched(ctx));
+        QSM_TRY(pl.fwd(ctx, t1, Dh));
+        unsigned long long *mx = (unsigned long long *)sum;
+        QSM_CUDA(cudaMemsetAsync(mx, 0, 2 * sizeof(unsigned long long), ctx->stream));
+        otf_max_k<T><<<gh, 256, 0, ctx->stream>>>(mx, Dh, nh);
+        QSM_TRY(launched(ctx));
+        double mxh[2];
+        QSM_CUDA(cudaMemcpyAsync(mxh, mx, sizeof(mxh), cudaMemcpyDeviceToHost, ctx->stream));
+        QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+        const double eps_t = sizeof(T) == 4 ? (double)FLT_EPSILON : DBL_EPSILON;
+        if (mxh[0] / mxh[1] <= (double)N * std::log2((double)N) * eps_t) {
+            drop_imag_k<T><<<gh, 256, 0, ctx->stream>>>(Dh, nh);
+            QSM_TRY(launched(ctx));
+        }
+        // m = mask .* w, with w = mask when w is empty or all zero (pdf.m:50-52, 61)
+        pad_k<uint8_t, T><<<gn, 256, 0, ctx->stream>>>(m, mask, d, d, 0, 0, 0, d.nx, d.ny, d.nz, 0, 0, 0);
+        QSM_TRY(launched(ctx));
+        if (wgt) {
+            double ww;
+            dot_k<T><<<BG_GRID, BG_BLOCK, 0, ctx->stream>>>(wgt, wgt, N, part);
+            QSM_TRY(red(&ww));
+            if (!(ww == 0.0)) {
+                weight_k<T><<<gn, 256, 0, ctx->stream>>>(t1, wgt, m, false, N);
+                QSM_TRY(launched(ctx));
+                QSM_CUDA(cudaMemcpyAsync(m, t1, N * sizeof(T), cudaMemcpyDeviceToDevice, ctx->stream));
+            }
+        }
+        const double conlim = 1e8, ctol = 1.0 / conlim;
+        for (size_t e = 0; e < ne; ++e) {
+            const T *fe = f + e * N;
+            // LSMR (Fong & Saunders 2011) on min ||A x - b||^2 + lambda^2 ||x||^2, b = m .* f,
+            // atol = btol = tol, conlim 1e8, no local reorthogonalisation
+            weight_k<T><<<gn, 256, 0, ctx->stream>>>(u, fe, m, false, N);
+            dot_k<T><<<BG_GRID, BG_BLOCK, 0, ctx->stream>>>(u, u, N, part);
+            double bb, aa, xx;
+            QSM_TRY(red(&bb));
+            double beta = std::sqrt(bb);
+            if (beta > 0.0) scale_k<T><<<gn, 256, 0, ctx->stream>>>(u, (T)(1.0 / beta), N);
+            QSM_CUDA(cudaMemsetAsync(v, 0, N * sizeof(T), ctx->stream));
+            QSM_CUDA(cudaMemsetAsync(x, 0, N * sizeof(T), ctx->stream));
+            QSM_TRY(gk(v, u, true, (T)0, &aa));  // v = A' u
+            double alpha = std::sqrt(aa);
+            if (alpha > 0.0) scale_k<T><<<gn, 256, 0, ctx->stream>>>(v, (T)(1.0 / alpha), N);
+            int32_t itn = 0;
+            if (alpha * beta != 0.0) {  // else x = 0 is the exact solution
+                QSM_CUDA(cudaMemcpyAsync(h, v, N * sizeof(T), cudaMemcpyDeviceToDevice, ctx->stream));
+                QSM_CUDA(cudaMemsetAsync(hb, 0, N * sizeof(T), ctx->stream));
+                double zetabar = alpha * beta, alphabar = alpha, rho = 1, rhobar = 1, cbar = 1, sbar = 0;
+                double betadd = beta, betad = 0, rhodold = 1, tautildeold = 0, thetatilde = 0, zeta = 0, dd = 0;
+                double normA2 = alpha * alpha, maxrbar = 0, minrbar = 1e100;
+                const double normb = beta;
+                if (verbose) printf("   itn       norm r    norm A'r\n");
+                while (itn < maxit) {
+                    ++itn;
+                    // bidiagonalization: beta u = A v - alpha u; alpha v = A' u - beta v
+                    double b2, a2;
+                    QSM_TRY(gk(u, v, false, (T)alpha, &b2));
+                    beta = std::sqrt(b2);
+                    if (beta > 0.0) {
+                        scale_k<T><<<gn, 256, 0, ctx->stream>>>(u, (T)(1.0 / beta), N);
+                        QSM_TRY(gk(v, u, true, (T)beta, &a2));
+                        alpha = std::sqrt(a2);
+                        if (alpha > 0.0) scale_k<T><<<gn, 256, 0, ctx->stream>>>(v, (T)(1.0 / alpha), N);
+                    }
+                    // rotation eliminating the damping term
+                    const double alphahat = std::hypot(alphabar, lambda);
+                    const double chat = alphabar / alphahat, shat = lambda / alphahat;
+                    // plane rotations Q_i and Qbar_i
+                    const double rhoold = rho;
+                    rho = std::hypot(alphahat, beta);
+                    const double c = alphahat / rho, s_ = beta / rho;
+                    const double thetanew = s_ * alpha;
+                    alphabar = c * alpha;
+                    const double rhobarold = rhobar, zetaold = zeta, thetabar = sbar * rho, rhotemp = cbar * rho;
+                    rhobar = std::hypot(cbar * rho, thetanew);
+                    cbar = cbar * rho / rhobar;
+                    sbar = thetanew / rhobar;
+                    zeta = cbar * zetabar;
+                    zetabar = -sbar * zetabar;
+                    // hbar, x, h
+                    lsmr_upd_k<T><<<BG_GRID, BG_BLOCK, 0, ctx->stream>>>(
+                        hb, x, h, v, (T)(thetabar * rho / (rhoold * rhobarold)), (T)(zeta / (rho * rhobar)),
+                        (T)(thetanew / rho), N, part);
+                    QSM_TRY(red(&xx));
+                    // ||r||
+                    const double betaacute = chat * betadd, betacheck = -shat * betadd;
+                    const double betahat = c * betaacute;
+                    betadd = -s_ * betaacute;
+                    const double thetatildeold = thetatilde;
+                    const double rhotildeold = std::hypot(rhodold, thetabar);
+                    const double ctildeold = rhodold / rhotildeold, stildeold = thetabar / rhotildeold;
+                    thetatilde = stildeold * rhobar;
+                    rhodold = ctildeold * rhobar;
+                    betad = -stildeold * betad + ctildeold * betahat;
+                    tautildeold = (zetaold - thetatildeold * tautildeold) / rhotildeold;
+                    const double taud = (zeta - thetatilde * tautildeold) / rhodold;
+                    dd = dd + betacheck * betacheck;
+                    const double normr = std::sqrt(dd + (betad - taud) * (betad - taud) + betadd * betadd);
+                    // ||A||, cond(A)
+                    normA2 = normA2 + beta * beta;
+                    const double normA = std::sqrt(normA2);
+                    normA2 = normA2 + alpha * alpha;
+                    maxrbar = std::max(maxrbar, rhobarold);
+                    if (itn > 1) minrbar = std::min(minrbar, rhobarold);
+                    const double condA = std::max(maxrbar, rhotemp) / std::min(minrbar, rhotemp);
+                    // stopping rules
+                    const double normAr = std::fabs(zetabar), normx = std::sqrt(xx);
+                    const double test1 = normr / normb, test2 = normAr / (normA * normr), test3 = 1.0 / condA;
+                    const double t1_ = test1 / (1.0 + normA * normx / normb);
+                    const double rtol = tol + tol * normA * normx / normb;
+                    if (verbose) printf("%6d %10.3e %10.3e\n", itn, normr, normAr);
+                    if (itn >= maxit || 1.0 + test3 <= 1.0 || 1.0 + test2 <= 1.0 || 1.0 + t1_ <= 1.0 ||
+                        test3 <= ctol || test2 <= tol || test1 <= rtol)
+                        break;
+                }
+            }
+            if (iters) iters[e] = itn;
+            // fl = logical(m) .* (f - real(ifft3(D .* fft3(~m .* xb))))
+            weight_k<T><<<gn, 256, 0, ctx->stream>>>(t1, x, m, true, N);
+            QSM_TRY(launched(ctx));
+            QSM_TRY(pl.fwd(ctx, t1, F));
+            mul_c_k<T><<<gh, 256, 0, ctx->stream>>>(F, Dh, nh, false);
+            QSM_TRY(pl.inv(ctx, F, t2));
+            pdf_out_k<T><<<gn, 256, 0, ctx->stream>>>(fl + e * N, fe, t2, m, invn, N);
+            QSM_TRY(launched(ctx));
+        }
+        return QSM_OK;
+    };
+    st = body();
+    cudaStreamSynchronize(ctx->stream);
+    pl.destroy();
+    dfree(ctx, blk);
     return st;
 }
 
@@ -705,6 +1141,16 @@ qsm_status qsm_vsharp(qsm_ctx *ctx, qsm_dtype dt, const size_t dims[4], const vo
     return entry(ctx, VSHARP, dt, dims, f, mask, vsz, rs, thr, 0.0, 0, 0, fl, mask_out, nullptr);
 }
 
+qsm_status qsm_resharp(qsm_ctx *ctx, qsm_dtype dt, const size_t dims[4], const void *f, const uint8_t *mask,
+                       const double vsz[3], double r, double lambda, double tol, int32_t maxit, int32_t verbose,
+                       void *fl, uint8_t *mask_out, int32_t *iters)
+{
+    if (tol < 0.0) tol = dt == QSM_F32 ? 3.4526698300124393e-04 : 1.4901161193847656e-08;  // sqrt(eps(class))
+    if (dims && maxit <= 0)  // resharp.m:42: ceil(sqrt(numel(mask)))
+        maxit = (int32_t)std::ceil(std::sqrt((double)dims[0] * (double)dims[1] * (double)dims[2]));
+    return entry(ctx, RESHARP, dt, dims, f, mask, vsz, {r}, lambda, tol, maxit, verbose, fl, mask_out, iters);
+}
+
 qsm_status qsm_ismv(qsm_ctx *ctx, qsm_dtype dt, const size_t dims[4], const void *f, const uint8_t *mask,
                     const double vsz[3], double r, double tol, int32_t maxit, int32_t verbose, void *fl,
                     uint8_t *mask_out, int32_t *iters)
@@ -712,6 +1158,46 @@ qsm_status qsm_ismv(qsm_ctx *ctx, qsm_dtype dt, const size_t dims[4], const void
     if (tol < 0.0) tol = dt == QSM_F32 ? 3.4526698300124393e-04 : 1.4901161193847656e-08;  // sqrt(eps(class))
     if (maxit < 0) return QSM_ERR_ARG;
     return entry(ctx, ISMV, dt, dims, f, mask, vsz, {r}, 0.0, tol, maxit, verbose, fl, mask_out, iters);
+}
+
+qsm_status qsm_pdf(qsm_ctx *ctx, qsm_dtype dt, const size_t dims[4], const void *f, const uint8_t *mask,
+                   const void *w, const double vsz[3], const double bdir[3], double lambda, double tol,
+                   int32_t maxit, int32_t verbose, void *fl, int32_t *iters)
+{
+    if (!ctx || !dims || !f || !mask || !vsz || !bdir || !fl) return QSM_ERR_ARG;
+    if (dt != QSM_F32 && dt != QSM_F64) return QSM_ERR_DTYPE;
+    if (!dims[0] || !dims[1] || !dims[2] || !dims[3]) return QSM_ERR_DIMS;
+    if (dims[0] > 0x7fffffff || dims[1] > 0x7fffffff || dims[2] > 0x7fffffff) return QSM_ERR_DIMS;
+    if (bdir[0] == 0.0 && bdir[1] == 0.0 && bdir[2] == 0.0) return QSM_ERR_ARG;
+    if (!(vsz[0] > 0.0 && vsz[1] > 0.0 && vsz[2] > 0.0)) return QSM_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    const Dims d{dims[0], dims[1], dims[2]};
+    if (maxit <= 0) maxit = (int32_t)std::ceil(std::sqrt((double)d.n()));  // pdf.m:47
+    if (tol < 0.0) tol = 1e-5;                                              // pdf.m:48
+    const size_t ne = dims[3], es = dt == QSM_F32 ? 4 : 8;
+    Staged sf, sm, sw, so;
+    QSM_TRY(stage_in(ctx, sf, f, ne * d.n() * es, true));
+    QSM_TRY(stage_in(ctx, sm, mask, d.n(), true));
+    if (w) QSM_TRY(stage_in(ctx, sw, w, d.n() * es, true));
+    QSM_TRY(stage_in(ctx, so, fl, ne * d.n() * es, false));
+    qsm_status st =
+        dt == QSM_F32
+            ? run_pdf<float>(ctx, d, ne, (const float *)sf.dev, (const uint8_t *)sm.dev,
+                             w ? (const float *)sw.dev : nullptr, vsz, bdir, lambda, tol, maxit, verbose,
+                             (float *)so.dev, iters)
+            : run_pdf<double>(ctx, d, ne, (const double *)sf.dev, (const uint8_t *)sm.dev,
+                              w ? (const double *)sw.dev : nullptr, vsz, bdir, lambda, tol, maxit, verbose,
+                              (double *)so.dev, iters);
+    stage_out(ctx, sf, false);
+    stage_out(ctx, sm, false);
+    if (w) stage_out(ctx, sw, false);
+    if (st != QSM_OK) {
+        stage_out(ctx, so, false);
+        return st;
+    }
+    QSM_TRY(stage_out(ctx, so, true));
+    QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+    return QSM_OK;
 }
 
 }  // extern "C"

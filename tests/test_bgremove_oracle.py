@@ -42,3 +42,33 @@ def test_sharp_removes_a_harmonic_background(bg):
     fl, mo = bg.ismv(f, m, [1, 1, 1], r=3, maxit=300)
     inside = mo != 0
     assert np.linalg.norm(fl[inside]) < 0.05 * np.linalg.norm(f[inside])
+
+
+def test_lsmr_solves_damped_least_squares(bg):
+    """The LSMR restatement reaches the damped least-squares solution of a small
+    dense system (normal equations solved directly)."""
+    rng = np.random.default_rng(3)
+    A = rng.normal(size=(60, 40))
+    b = rng.normal(size=60)
+    for lam in (0.0, 0.5):
+        x, it = bg.lsmr(lambda v: A @ v, lambda v: A.T @ v, b, lam, 1e-12, 1e-12, 1e8, 200)
+        ref = np.linalg.solve(A.T @ A + lam * lam * np.eye(40), A.T @ b)
+        assert np.linalg.norm(x - ref) <= 1e-8 * np.linalg.norm(ref) and 0 < it <= 200
+
+
+def test_lsmr_zero_rhs(bg):
+    x, it = bg.lsmr(lambda v: v, lambda v: v, np.zeros(5))
+    assert it == 0 and not x.any()
+
+
+def test_dipole_kernel_image_space(bg):
+    """dipoleKernel 'i': zero at the centre, even in r, and its transform is real
+    (within roundoff, so psf2otf drops the imaginary part) when B is along an axis."""
+    D = bg.dipole_kernel_i((9, 8, 7), (1.0, 1.0, 1.0))
+    assert D[4, 4, 3] == 0.0
+    assert D[4, 4, 4] == pytest.approx(2.0 / (4 * np.pi))
+    assert D[5, 4, 3] == pytest.approx(-1.0 / (4 * np.pi))
+    K = bg.psf2otf(D)
+    assert not K.imag.any()
+    Ko = bg.psf2otf(bg.dipole_kernel_i((9, 8, 7), (1.0, 1.0, 1.0), (0.0, 0.3, 1.0)))
+    assert np.abs(Ko.imag).max() > 1e-6

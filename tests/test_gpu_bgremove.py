@@ -1,8 +1,9 @@
-"""GPU FFT background removal (sharp.m, vsharp.m, ismv.m on cuFFT) against
-the CPU restatement (oracle/bgremove.py, numpy FFTs).  FP64 fields: relative
-L2 difference <= 1e-9 (the FFT libraries round differently); eroded masks
-identical; iSMV stops at the same iteration.  FP32 fields: <= 1e-4 against
-the FP64 restatement."""
+"""GPU FFT background removal (sharp.m, vsharp.m, ismv.m, resharp.m, pdf.m on
+cuFFT) against the CPU restatement (oracle/bgremove.py, numpy FFTs).  FP64
+fields: relative L2 difference <= 1e-9 (the FFT libraries round differently;
+iterative methods a looser bar where stated); eroded masks identical;
+iterative methods stop at the same iteration.  FP32 fields: <= 1e-4 against
+the FP64 restatement (PDF: 1e-3)."""
 import numpy as np
 import pytest
 
@@ -81,3 +82,59 @@ def test_errors(gpu_ctx, qsm):
         qsm.sharp(z, np.zeros((10, 10, 10), np.uint8), [1, 1, 1])
     with pytest.raises(qsm.QsmError, match="ARG"):
         qsm.vsharp(z, np.ones((10, 10, 10), np.uint8), [1, 1, 1], [4.0])
+
+
+def test_resharp(gpu_ctx, qsm, bg):
+    f, m = _case((40, 36, 32), 5, echoes=2)
+    info, rinfo = {}, {}
+    fl, mo = qsm.resharp(f, m, [1, 1, 1], 3.0, 1e-2, 1e-6, 100, info=info)
+    rfl, rmo = bg.resharp(f, m, [1, 1, 1], 3.0, 1e-2, 1e-6, 100, info=rinfo)
+    assert np.array_equal(mo, rmo)
+    assert info["iters"] == rinfo["iters"] and 0 < info["iters"][0] < 100
+    assert _rel(fl, rfl) <= 1e-8
+
+
+@pytest.mark.parametrize("vsz,bdir,lam,weighted", [
+    ((1.0, 1.0, 1.0), (0.0, 0.0, 1.0), 0.0, False),
+    ((1.0, 0.9, 1.1), (0.1, 0.2, 0.95), 0.0, True),
+    ((1.0, 1.0, 1.2), (0.0, 0.0, 2.0), 1e-3, False),
+])
+def test_pdf(gpu_ctx, qsm, bg, vsz, bdir, lam, weighted):
+    """30 LSMR iterations.  The GPU's reductions and cuFFT round differently from
+    numpy, and LSMR without reorthogonalisation amplifies such differences as the
+    iteration goes on: with a real-to-complex FFT in place of fftn, the oracle
+    moves by 1e-14 after 30 iterations but by 5e-9 after 60 on the weighted
+    oblique case.  So 30 iterations and 1e-9."""
+    f, m = _case((40, 36, 32), 6, echoes=2)
+    w = None
+    if weighted:
+        w = np.asfortranarray(m * (0.5 + np.random.default_rng(1).random(m.shape)))
+    info, rinfo = {}, {}
+    fl = qsm.pdf(f, m, vsz, w, bdir, lam, 1e-5, 30, info=info)
+    rfl = bg.pdf(f, m, vsz, w, bdir, lam, 1e-5, 30, info=rinfo)
+    assert info["iters"] == rinfo["iters"]
+    assert _rel(fl, rfl) <= 1e-9
+
+
+def test_pdf_defaults(gpu_ctx, qsm, bg):
+    """Default tol and maxit (ceil(sqrt(numel(mask))) = 215 here, where LSMR stops):
+    past ~120 iterations the reference's own iteration amplifies rounding
+    differences to ~1e-4 of the local field (the oracle against itself with a
+    real-to-complex FFT: 2e-4), so the bar here is the iteration count and 1e-2."""
+    f, m = _case((40, 36, 32), 6)
+    info, rinfo = {}, {}
+    fl = qsm.pdf(f, m, [1, 1, 1], info=info)
+    rfl = bg.pdf(f, m, [1, 1, 1], info=rinfo)
+    assert info["iters"] == rinfo["iters"] == [215]
+    assert _rel(fl, rfl) <= 1e-2
+    # w all zero is the mask (pdf.m:50-52)
+    fz = qsm.pdf(f, m, [1, 1, 1], np.zeros(m.shape), maxit=40)
+    fm = qsm.pdf(f, m, [1, 1, 1], None, maxit=40)
+    assert np.array_equal(fz, fm)
+
+
+def test_pdf_fp32(gpu_ctx, qsm, bg):
+    f, m = _case((40, 36, 32), 7)
+    rfl = bg.pdf(f, m, [1, 1, 1], maxit=40)
+    fl = qsm.pdf(f.astype(np.float32), m, [1, 1, 1], maxit=40)
+    assert fl.dtype == np.float32 and _rel(fl, rfl) <= 1e-3
