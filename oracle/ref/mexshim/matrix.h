@@ -42,6 +42,7 @@ typedef struct mxArray_tag mxArray;
 mxArray *mxCreateNumericArray(mwSize ndim, const mwSize *dims,
                               mxClassID classid, mxComplexity flag);
 mxArray *mxCreateDoubleMatrix(mwSize m, mwSize n, mxComplexity flag);
+mxArray *mxCreateLogicalArray(mwSize ndim, const mwSize *dims);
 mxArray *mxCreateDoubleScalar(double value);
 mxArray *mxDuplicateArray(const mxArray *in);
 void mxDestroyArray(mxArray *pa);

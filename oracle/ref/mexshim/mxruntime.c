@@ -53,6 +53,11 @@ mxArray *mxCreateNumericArray(mwSize ndim, const mwSize *dims,
     return a;
 }
 
+mxArray *mxCreateLogicalArray(mwSize ndim, const mwSize *dims)
+{
+    return mxCreateNumericArray(ndim, dims, mxLOGICAL_CLASS, mxREAL);
+}
+
 mxArray *mxCreateDoubleMatrix(mwSize m, mwSize n, mxComplexity flag)
 {
     mwSize d[2] = {m, n};
@@ -129,6 +134,21 @@ int mexPrintf(const char *fmt, ...)
     va_end(ap);
     fflush(stdout);
     return r;
+}
+
+/* mexAtExit: the function runs at shim_clear(), as MATLAB runs it at `clear mex` */
+static void (*g_atexit)(void) = NULL;
+
+int mexAtExit(void (*fn)(void))
+{
+    g_atexit = fn;
+    return 0;
+}
+
+void shim_clear(void)
+{
+    if (g_atexit) g_atexit();
+    g_atexit = NULL;
 }
 
 /* Run the gateway; returns 0 on success, 1 if it raised mexErrMsgTxt

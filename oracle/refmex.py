@@ -12,7 +12,8 @@ double arrays, as MATLAB passes them.  Every argument is copied into a fresh
 mxArray; after the call, arguments that the gateway wrote in place (the
 operator MEX files write into ``prhs[0]``) are copied back into the caller's
 numpy arrays, so ``call('gradf_mex', dx, dy, dz, u, h)`` updates ``dx, dy, dz``
-exactly as MATLAB's in-place MEX convention does.
+exactly as MATLAB's in-place MEX convention does.  Logical outputs come back
+as uint8.
 """
 from __future__ import annotations
 
@@ -40,9 +41,10 @@ def available() -> bool:
     return os.path.exists(os.path.join(REF_DIR, "pd_tgv_mex.so"))
 
 
-def _lib(name: str) -> ctypes.CDLL:
-    if name not in _libs:
-        path = os.path.join(REF_DIR, name + ".so")
+def _lib(name: str, path: str | None = None) -> ctypes.CDLL:
+    key = path or name
+    if key not in _libs:
+        path = path or os.path.join(REF_DIR, name + ".so")
         if not os.path.exists(path):
             raise FileNotFoundError(f"{path} missing: run `make -C oracle/ref`")
         lib = ctypes.CDLL(path, mode=os.RTLD_LOCAL | os.RTLD_NOW)
@@ -62,8 +64,8 @@ def _lib(name: str) -> ctypes.CDLL:
         lib.shim_call.restype = ctypes.c_int
         lib.shim_call.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
         lib.shim_last_error.restype = ctypes.c_char_p
-        _libs[name] = lib
-    return _libs[name]
+        _libs[key] = lib
+    return _libs[key]
 
 
 def _to_mx(lib, a):
@@ -92,13 +94,15 @@ def _from_mx(lib, mx):
     return out.copy(order="F")
 
 
-def call(name: str, *args, nlhs: int = 1, verbose: bool = False):
+def call(name: str, *args, nlhs: int = 1, verbose: bool = False, path: str | None = None):
     """Call gateway ``name`` (e.g. ``'pd_tgv_mex'``) with MATLAB-style args.
 
     Returns the first output (or a tuple when ``nlhs > 1``, or None when
     ``nlhs == 0``).  Raises RuntimeError with the gateway's mexErrMsgTxt text.
+    ``path`` names another gateway library linked with the same runtime (the
+    tests run the library's own MEX shims this way).
     """
-    lib = _lib(name)
+    lib = _lib(name, path)
     mxs = [_to_mx(lib, a) for a in args]
     prhs = (ctypes.c_void_p * max(1, len(mxs)))(*mxs)
     plhs = (ctypes.c_void_p * max(1, nlhs))()
