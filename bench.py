@@ -21,6 +21,10 @@ Arms (JSON line on rank 0):
                 MEASURED_PEAKS.json.
   cpu_baseline  the CPU oracle (a C restatement of the reference MEX, FP64,
                 OpenMP on all host cores) on a bounded number of iterations.
+  poisson, batch, served, next_rows
+                the MG-PCG solve, batched TV, served requests, and the widened
+                rows (TV ADMM, PDF, V-SHARP, whole sstgv/lbv wrappers), each
+                with its own workload description.
 
 --impl reference times that CPU implementation alone (the reference's MEX
 path cannot run on the GPU host: it needs MATLAB, and its sources are not
@@ -262,6 +266,109 @@ def batch_arm(qsm_gb300, ctx, torch, count=32, iters=500):
             "one_by_one_gbs_per_volume": per_vol}
 
 
+# algorithmic bytes per voxel-iteration (FP64) of the iterative next-row solvers, counting
+# every array each kernel must read or write once and each FFT as one read + one write:
+# TV ADMM: adj_rhs 7 arrays, D2Z 16 B, kmul 24 B, Z2D 16 B, grad_shrink 13 arrays,
+# adj_norms 9 arrays; PDF/LSMR: two operator applications of 112 B (weight 3 arrays,
+# R2C 16 B, spectrum multiply 24 B, C2R 16 B, Golub-Kahan update 4 arrays), two scalings
+# of 2 arrays, the LSMR update 7 arrays
+TV_BYTES_F64, PDF_BYTES_F64 = 288, 312
+
+
+def _cpu_sample(fn, iters_per_call, voxels):
+    t = time.perf_counter()
+    fn()
+    dt = time.perf_counter() - t
+    return {"value": voxels * iters_per_call / dt, "seconds": dt}
+
+
+def next_rows_arm(qsm_gb300, ctx, torch, peak, cpu=True, parts="tv64,tv32,pdf,vsharp,sstgv,lbv"):
+    """The widened rows on the 224x224x128 volume: TV ADMM (tv.m), PDF and V-SHARP
+    background removal, and the whole sstgv/lbv wrappers on 4 echoes.  Device
+    solves run on resident tensors (the wrappers from pinned host arrays, end to
+    end); each CPU figure is the oracle on a bounded sample of the same input."""
+    import qsm_gb300.synthetic as S
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    shape = (224, 224, 128)
+    n = int(np.prod(shape))
+    f4, local, mask = S.field_case(shape, 7, echoes=4)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(np.asarray(a).T)).cuda()  # noqa: E731
+    m_dev = dev(mask)
+    out = {"volume": list(shape), "echoes": 4}
+
+    def timed(fn, reps=3):
+        fn()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(reps):
+            r = fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t) / reps, r
+
+    parts = set(parts.split(","))
+    # TV ADMM, all iterations run (rtol = atol = 0).  FP64 is bound by the FP64 pipe
+    # (cuFFT double and the FP64 stencil arithmetic), FP32 by HBM.
+    it = 100
+    opts = dict(maxit=it, rtol=0.0, atol=0.0)
+    row = {"workload": f"tv.m ADMM, k-space data term, {it} iterations, mu 7.5e3, B0 along z"}
+    for name, dt in (("f64", torch.float64), ("f32", torch.float32)):
+        if "tv" + name[1:] not in parts:
+            continue
+        l_dev = dev(local).to(dt)
+        info = {}
+        sec, _ = timed(lambda: qsm_gb300.tv(l_dev, m_dev, [1, 1, 1], opts=opts, info=info, ctx=ctx))
+        b = TV_BYTES_F64 * (1 if name == "f64" else 0.5)
+        row[name] = {"value": n * it / sec, "unit": "voxel-iter/s", "seconds": sec,
+                     "hbm_gbs": b * n * it / sec / 1e9, "frac": b * n * it / sec / 1e9 / peak,
+                     "bytes_per_voxel_iter": b}
+    if cpu and "tv64" in parts:
+        import tv_admm
+        row["cpu_oracle"] = dict(_cpu_sample(lambda: tv_admm.tv(local, mask, [1, 1, 1], opts=dict(maxit=2, rtol=0.0,
+                                                                                                    atol=0.0)), 2, n),
+                                 unit="voxel-iter/s", cores=1, kind="port", sample="2 ADMM iterations, numpy FP64")
+    out["tv_admm"] = row
+
+    if "pdf" not in parts:
+        return out
+    # PDF: LSMR iterations on the full grid (tol 0: every iteration runs); FP64 cuFFT bound
+    it = 30
+    f1 = dev(f4[..., 0])
+    info = {}
+    sec, _ = timed(lambda: qsm_gb300.pdf(f1, m_dev, [1, 1, 1], None, [0, 0, 1], 0.0, 0.0, it, info=info, ctx=ctx))
+    row = {"workload": f"pdf.m, {it} LSMR iterations, FP64", "value": n * it / sec, "unit": "voxel-iter/s",
+           "seconds": sec, "hbm_gbs": PDF_BYTES_F64 * n * it / sec / 1e9,
+           "frac": PDF_BYTES_F64 * n * it / sec / 1e9 / peak, "bytes_per_voxel_iter": PDF_BYTES_F64}
+    if cpu:
+        import bgremove
+        row["cpu_oracle"] = dict(_cpu_sample(lambda: bgremove.pdf(f4[..., 0], mask, [1, 1, 1], None, (0, 0, 1), 0.0,
+                                                                  0.0, 2), 2, n),
+                                 unit="voxel-iter/s", cores=1, kind="port", sample="2 LSMR iterations, numpy FP64")
+    out["pdf"] = row
+
+    # V-SHARP, default radii (9:-2:2), 4 echoes in one call
+    f4_dev = torch.from_numpy(np.ascontiguousarray(np.transpose(f4, (3, 2, 1, 0)))).cuda()
+    sec, _ = timed(lambda: qsm_gb300.vsharp(f4_dev, m_dev, [1, 1, 1], ctx=ctx))
+    row = {"workload": "vsharp.m, radii 9:-2:2, 4 echoes, FP64", "value": 4 * n / sec, "unit": "voxels/s",
+           "seconds": sec}
+    if cpu:
+        row["cpu_oracle"] = dict(_cpu_sample(lambda: bgremove.vsharp(f4[..., 0], mask, [1, 1, 1]), 1, n),
+                                 unit="voxels/s", cores=1, kind="port", sample="1 echo, numpy FP64")
+    out["vsharp"] = row
+
+    # whole wrappers from host arrays (crop, Laplacian, solve, scatter; echoes batched)
+    it = 300
+    f4s = np.asfortranarray(f4.astype(np.float32))
+    sec, _ = timed(lambda: qsm_gb300.sstgv(f4s, mask, [1, 1, 1], 1e-4, 3.0, 0.0, it, fused=True, ctx=ctx), reps=2)
+    out["sstgv"] = {"workload": f"sstgv.m, 4 echoes FP32 fused, {it} iterations, tol 0, host arrays",
+                    "value": 4 * n * it / sec, "unit": "voxel-iter/s (dense grid)", "seconds": sec}
+    infos = []
+    sec, _ = timed(lambda: qsm_gb300.lbv(f4, mask, [1, 1, 1], infos=infos, ctx=ctx), reps=1)
+    out["lbv"] = {"workload": "lbv.m defaults, 4 echoes FP64, host arrays", "seconds": sec,
+                  "pcg_iters": [i["iters"] for i in infos]}
+    return out
+
+
 def serve_arm(qsm_gb300, ctx, seconds=30.0, rate=4.0, per_kind=6, budget=160 * 10**9):
     """Served reconstructions: Poisson arrivals at `rate`/s for `seconds`, 40%
     Poisson (LBV options), 30% TV (lam 1e-3, 500 iterations), 30% TGV (lam
@@ -356,9 +463,13 @@ def run_ours(args):
 
     ctx = qsm_gb300.context(local)
     stream = torch.cuda.ExternalStream(qsm_gb300.lib().qsm_ctx_get_stream(ctx.handle))
-    if args.only in ("batch", "serve"):
-        out = batch_arm(qsm_gb300, ctx, torch) if args.only == "batch" else \
-            serve_arm(qsm_gb300, ctx, seconds=args.serve_seconds)
+    if args.only in ("batch", "serve", "next"):
+        if args.only == "batch":
+            out = batch_arm(qsm_gb300, ctx, torch)
+        elif args.only == "serve":
+            out = serve_arm(qsm_gb300, ctx, seconds=args.serve_seconds)
+        else:
+            out = next_rows_arm(qsm_gb300, ctx, torch, _peaks()[0], cpu=not args.no_cpu, parts=args.next_parts)
         if rank == 0:
             print(json.dumps({"profile_run": True, args.only: out}))
         return
@@ -456,6 +567,7 @@ def run_ours(args):
     poisson = None if args.no_poisson else poisson_arm(qsm_gb300, ctx, torch)
     batch = None if args.no_batch else batch_arm(qsm_gb300, ctx, torch)
     served = None if args.no_serve else serve_arm(qsm_gb300, ctx, seconds=args.serve_seconds)
+    nxt = None if args.no_next else next_rows_arm(qsm_gb300, ctx, torch, peak, cpu=not args.no_cpu and rank == 0)
 
     if rank != 0:
         if dist is not None:
@@ -484,6 +596,7 @@ def run_ours(args):
         "poisson": poisson,
         "batch": batch,
         "served": served,
+        "next_rows": nxt,
         "gpu_launches": int(args.steps * (ITERS + 5)),
         "clocks": clk.summary(),
     }
@@ -503,10 +616,13 @@ def main():
     ap.add_argument("--no-poisson", action="store_true", help="skip the MG-PCG arm")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched TV arm")
     ap.add_argument("--no-serve", action="store_true", help="skip the served-requests arm")
+    ap.add_argument("--no-next", action="store_true", help="skip the TV ADMM / background removal / wrapper arm")
+    ap.add_argument("--next-parts", default="tv64,tv32,pdf,vsharp,sstgv,lbv",
+                    help="parts of the next-rows arm with --only next (profiling aid)")
     ap.add_argument("--serve-seconds", type=float, default=30.0, help="arrival window of the served arm")
     ap.add_argument("--shape", default="", help="nx,ny,nz of a reduced volume (profiler captures)")
     ap.add_argument("--iters", type=int, default=ITERS, help="iterations per inversion (profiler captures)")
-    ap.add_argument("--only", default="all", choices=["all", "fused", "batch", "serve"],
+    ap.add_argument("--only", default="all", choices=["all", "fused", "batch", "serve", "next"],
                     help="run only one arm (profiling aid)")
     args = ap.parse_args()
     if args.impl == "reference":

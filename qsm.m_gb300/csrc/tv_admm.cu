@@ -5,17 +5,21 @@
 // stencil kernels.  Only the five convergence scalars per iteration go to
 // the host, which applies tv.m's stopping test and rho update (:226-268).
 //
-// k-space terms are evaluated where they are used, from the grid indices:
+// k-space terms come from per-axis tables and one stored half-spectrum array:
 //   D(k) = 1/3 - (k.b)^2/|k|^2, D(0) = 0, k_a = fftfreq(n_a, h_a)
-//        (dipoleKernel.m:56-65, ifftshifted so DC is first);
+//        (dipoleKernel.m:56-65, ifftshifted so DC is first), stored once per
+//        solve in the working precision;
 //   L(k) = sum_a (2/h_a^2)(1 - cos(2 pi i_a/n_a)), the symbol of the negated
-//        7-point Laplacian (laplaceKernel.m, tv.m:140-142);
-//   iA   = 1/(mu D^2 + rho L), 0 where not finite (tv.m:144-145);
-// so no N-sized iA, K or L array is stored or re-read, and a rho update
-// costs nothing.  u = real(ifft3(X)) equals the C2R of the Hermitian part
-// of X; the stored half spectrum therefore carries, on planes where index
-// negation is not frequency negation (even-size Nyquist planes) and B0 is
-// oblique, the average of the multipliers at k and at the negated index.
+//        7-point Laplacian (laplaceKernel.m, tv.m:140-142): separable, so three
+//        1-D tables of FP64 terms;
+//   iA   = 1/(mu D^2 + rho L), 0 where not finite (tv.m:144-145), formed in
+//        the k-space kernel, so a rho update costs nothing.
+// No trigonometry and one division per point per iteration: FP64 arithmetic
+// runs at a small fraction of the FP32 rate on this GPU.  u = real(ifft3(X))
+// equals the C2R of the Hermitian part of X; the stored half spectrum
+// therefore carries, on planes where index negation is not frequency
+// negation (even-size Nyquist planes) and B0 is oblique, the average of the
+// multipliers at k and at the negated index.
 //
 // FP64 (the MATLAB default class) or FP32 arithmetic by dtype; every
 // reduction accumulates in FP64 with a fixed order (block partials folded
@@ -48,49 +52,73 @@ struct TvK {
 
 __device__ __forceinline__ double fftfreq(int i, int n, double h) { return (double)(i <= (n - 1) / 2 ? i : i - n) / (n * h); }
 
-// D and L at half-spectrum index (i, j, k) with signs s of the frequencies
-__device__ __forceinline__ void dl_at(const TvK &K, double fx, double fy, double fz, int i, int j, int k, double &D,
-                                      double &L)
+// per-axis tables: frequencies fx[nxh] fy[ny] fz[nz], then the Laplacian terms
+// Lx[nxh] Ly[ny] Lz[nz] (FP64)
+__global__ void ktab_k(double *tab, TvK K)
+{
+    const int na[3] = {K.nxh, K.ny, K.nz}, nn[3] = {K.nx, K.ny, K.nz};
+    const double hh[3] = {K.hx, K.hy, K.hz};
+    const int tot = K.nxh + K.ny + K.nz;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += gridDim.x * blockDim.x) {
+        int a = 0, i = t;
+        while (i >= na[a]) i -= na[a++];
+        tab[t] = fftfreq(i, nn[a], hh[a]);
+        tab[tot + t] = (2.0 / (hh[a] * hh[a])) * (1.0 - cospi(2.0 * i / nn[a]));
+    }
+}
+
+__device__ __forceinline__ double dipole_at(const TvK &K, double fx, double fy, double fz)
 {
     const double kb = K.bx * fx + K.by * fy + K.bz * fz;
     const double k2 = fx * fx + fy * fy + fz * fz;
-    D = (i == 0 && j == 0 && k == 0) ? 0.0 : 1.0 / 3.0 - (kb * kb) / k2;
-    L = (2.0 / (K.hx * K.hx)) * (1.0 - cospi(2.0 * i / K.nx)) + (2.0 / (K.hy * K.hy)) * (1.0 - cospi(2.0 * j / K.ny)) +
-        (2.0 / (K.hz * K.hz)) * (1.0 - cospi(2.0 * k / K.nz));
+    return 1.0 / 3.0 - (kb * kb) / k2;
 }
 
-__device__ __forceinline__ double inv_a(double K, double L, double rho)
-{
-    const double a = 1.0 / (K + rho * L);
-    return isfinite(a) ? a : 0.0;
-}
-
-// X = iA .* (mu D .* fhat + R) / N in place of R (tv.m:172-175)
+// D on the half spectrum, rounded to the working precision
 template <typename T>
-__global__ void kmul_k(typename CxT<T>::type *R, const typename CxT<T>::type *__restrict__ fhat, TvK K, double rho,
-                       double invn)
+__global__ void dq_k(T *Dq, const double *__restrict__ tab, TvK K)
 {
     const size_t nh = (size_t)K.nxh * K.ny * K.nz;
     for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < nh; q += (size_t)gridDim.x * blockDim.x) {
         const int i = (int)(q % K.nxh), j = (int)((q / K.nxh) % K.ny), k = (int)(q / ((size_t)K.nxh * K.ny));
-        const double fx = fftfreq(i, K.nx, K.hx), fy = fftfreq(j, K.ny, K.hy), fz = fftfreq(k, K.nz, K.hz);
-        double D, L;
-        dl_at(K, fx, fy, fz, i, j, k, D, L);
-        double a = inv_a(K.mu * D * D, L, rho), ad = a * (K.mu * D);
-        const bool nyq = (2 * i == K.nx) || (2 * j == K.ny) || (2 * k == K.nz);
-        if (K.oblique && nyq) {
+        Dq[q] = q == 0 ? (T)0 : (T)dipole_at(K, tab[i], tab[K.nxh + j], tab[K.nxh + K.ny + k]);
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ T inv_a(T K, T L, T rho)
+{
+    const T a = (T)1 / (K + rho * L);
+    return isfinite(a) ? a : (T)0;
+}
+
+// X = iA .* (mu D .* fhat + R) / N in place of R (tv.m:172-175), in the working
+// precision T
+template <typename T>
+__global__ void kmul_k(typename CxT<T>::type *R, const typename CxT<T>::type *__restrict__ fhat,
+                       const T *__restrict__ Dq, const double *__restrict__ tab, TvK K, double rho_, double invn_)
+{
+    const size_t nh = (size_t)K.nxh * K.ny * K.nz;
+    const int tot = K.nxh + K.ny + K.nz;
+    const T mu = (T)K.mu, rho = (T)rho_, invn = (T)invn_;
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < nh; q += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(q % K.nxh), j = (int)((q / K.nxh) % K.ny), k = (int)(q / ((size_t)K.nxh * K.ny));
+        const T D = Dq[q];
+        const T L = (T)((tab[tot + i] + tab[tot + K.nxh + j]) + tab[tot + K.nxh + K.ny + k]);
+        T a = inv_a<T>(mu * D * D, L, rho), ad = a * (mu * D);
+        if (K.oblique && ((2 * i == K.nx) || (2 * j == K.ny) || (2 * k == K.nz))) {
             // the negated index keeps Nyquist frequencies and flips the others
+            const double fx = tab[i], fy = tab[K.nxh + j], fz = tab[K.nxh + K.ny + k];
             const double gx = 2 * i == K.nx ? fx : -fx, gy = 2 * j == K.ny ? fy : -fy, gz = 2 * k == K.nz ? fz : -fz;
-            double D2, L2;
-            dl_at(K, gx, gy, gz, i, j, k, D2, L2);
-            const double a2 = inv_a(K.mu * D2 * D2, L2, rho);
-            ad = 0.5 * (ad + a2 * (K.mu * D2));
-            a = 0.5 * (a + a2);
+            const T D2 = (T)dipole_at(K, gx, gy, gz);
+            const T a2 = inv_a<T>(mu * D2 * D2, L, rho);
+            ad = (T)0.5 * (ad + a2 * (mu * D2));
+            a = (T)0.5 * (a + a2);
         }
         const typename CxT<T>::type fh = fhat[q], r = R[q];
         typename CxT<T>::type o;
-        o.x = (T)((ad * (double)fh.x + a * (double)r.x) * invn);
-        o.y = (T)((ad * (double)fh.y + a * (double)r.y) * invn);
+        o.x = (ad * fh.x + a * r.x) * invn;
+        o.y = (ad * fh.y + a * r.y) * invn;
         R[q] = o;
     }
 }
@@ -192,19 +220,21 @@ grad_shrink_k(T *vn, const T *__restrict__ vo, T *lm, const T *__restrict__ u, D
                 w[c] = (m > (T)0 ? m : (T)0) * sg;
             }
         }
-        double e2 = 0.0, a2 = 0.0, b2 = 0.0;
+        // per-voxel norms in the working precision (as MATLAB computes them in
+        // the class of f), summed in FP64
+        T e2 = 0, a2 = 0, b2 = 0;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             vn[c * N + l] = w[c];
             lm[c * N + l] = lm[c * N + l] + rho * (d1[c] - w[c]);
             const T e = dd[c] - w[c];
-            e2 += (double)(e * e);
-            a2 += (double)(dd[c] * dd[c]);
-            b2 += (double)(w[c] * w[c]);
+            e2 += e * e;
+            a2 += dd[c] * dd[c];
+            b2 += w[c] * w[c];
         }
-        acc[0] += sqrt(e2);
-        acc[1] += sqrt(a2);
-        acc[2] += sqrt(b2);
+        acc[0] += (double)sqrt(e2);
+        acc[1] += (double)sqrt(a2);
+        acc[2] += (double)sqrt(b2);
     }
     block_sums<3>(part, acc);
 }
@@ -325,7 +355,8 @@ static qsm_status tv_run(qsm_ctx *ctx, const Dims &d, const S *f, const uint8_t 
     // u, r, v[2] (3 components each, N apart), l (3); fhat, R; partials + sums
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     const size_t rb = al(N * sizeof(T)), vb = al(3 * N * sizeof(T)), cb = al(nh * sizeof(C));
-    const size_t bytes = 2 * rb + 3 * vb + 2 * cb + (TV_NSUM * TV_GRID + 64) * sizeof(double);
+    const size_t tb = al(2 * (size_t)(nxh + d.ny + d.nz) * sizeof(double)), db = al(nh * sizeof(T));
+    const size_t bytes = 2 * rb + 3 * vb + 2 * cb + tb + db + (TV_NSUM * TV_GRID + 64) * sizeof(double);
     void *blk = nullptr;
     QSM_TRY(dalloc(ctx, &blk, bytes));
     char *c = (char *)blk;
@@ -337,6 +368,8 @@ static qsm_status tv_run(qsm_ctx *ctx, const Dims &d, const S *f, const uint8_t 
     T *lm = (T *)c; c += vb;
     C *fhat = (C *)c; c += cb;
     C *R = (C *)c; c += cb;
+    double *tab = (double *)c; c += tb;
+    T *Dq = (T *)c; c += db;
     double *part = (double *)c;
     double *sums = part + TV_NSUM * TV_GRID;
 
@@ -374,6 +407,9 @@ static qsm_status tv_run(qsm_ctx *ctx, const Dims &d, const S *f, const uint8_t 
     QSM_STEP(cuda_st(ctx, cudaEventCreate(&e1), "event"));
     QSM_STEP(cuda_st(ctx, cudaEventRecord(e0, ctx->stream), "event"));
 
+    // k-space tables and D (once per solve)
+    ktab_k<<<1, 256, 0, ctx->stream>>>(tab, K);
+    dq_k<T><<<gk, TV_BLOCK, 0, ctx->stream>>>(Dq, tab, K);
     // u = f; fhat = fft3(f) (F = mu conj(D) fhat is formed in kmul_k)
     cvt_in_k<T, S><<<g, b, 0, ctx->stream>>>(u, f, N);
     if (sizeof(T) == 8) QSM_FFT(cufftExecD2Z(pf, (cufftDoubleReal *)u, (cufftDoubleComplex *)fhat));
@@ -392,7 +428,7 @@ static qsm_status tv_run(qsm_ctx *ctx, const Dims &d, const S *f, const uint8_t 
         adj_rhs_k<T><<<g, b, 0, ctx->stream>>>(r, v[cur], lm, d, -ihx, -ihy, -ihz, (T)rho);
         if (sizeof(T) == 8) QSM_FFT(cufftExecD2Z(pf, (cufftDoubleReal *)r, (cufftDoubleComplex *)R));
         else QSM_FFT(cufftExecR2C(pf, (cufftReal *)r, (cufftComplex *)R));
-        kmul_k<T><<<gk, TV_BLOCK, 0, ctx->stream>>>(R, fhat, K, rho, 1.0 / (double)N);
+        kmul_k<T><<<gk, TV_BLOCK, 0, ctx->stream>>>(R, fhat, Dq, tab, K, rho, 1.0 / (double)N);
         if (sizeof(T) == 8) QSM_FFT(cufftExecZ2D(pi, (cufftDoubleComplex *)R, (cufftDoubleReal *)u));
         else QSM_FFT(cufftExecC2R(pi, (cufftComplex *)R, (cufftReal *)u));
         // v-subproblem, multipliers, residuals

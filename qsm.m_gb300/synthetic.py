@@ -172,3 +172,32 @@ def poisson_case(shape, seed, *, n_gauss=40, sigma=(5.0, 30.0), semi=(80.0, 120.
 def config1(seed=1):
     """256^3 Poisson problem of the LBV / Laplacian-unwrapping form."""
     return poisson_case((256, 256, 256), seed)
+
+
+def field_case(shape, seed, *, echoes=1, n_ell=60, chi=(-0.15, 0.15), noise=0.01, mask=None,
+               vsz=(1.0, 1.0, 1.0)):
+    """Returns (f, local, mask): a total field f = (local + background) inside the
+    mask for background-field removal and the MATLAB wrappers.  local is the
+    dipole field of an ellipsoid phantom (as in tgv_case); the background is the
+    harmonic field of four point sources outside the grid (1/r, scaled to ~10x
+    the local field), growing by echo (echo t multiplies everything by t + 1).
+    f is (nx, ny, nz) for one echo, else (nx, ny, nz, echoes); Fortran order."""
+    rng = np.random.default_rng(seed)
+    if mask is None:
+        mask = ellipsoid_mask(shape, [0.42 * n for n in shape])
+    chi_true = ellipsoid_phantom(shape, n_ell, rng, mask, chi=chi)
+    local = np.real(np.fft.ifftn(dipole_kernel(shape, vsz) * np.fft.fftn(chi_true)))
+    g = np.meshgrid(*[np.arange(n, dtype=np.float64) * h for n, h in zip(shape, vsz)], indexing="ij")
+    ext = [n * h for n, h in zip(shape, vsz)]
+    bg = np.zeros(shape)
+    for _ in range(4):
+        ax = int(rng.integers(0, 3))
+        c = [float(rng.uniform(0.2, 0.8)) * e for e in ext]
+        c[ax] = -0.25 * ext[ax] if rng.random() < 0.5 else 1.25 * ext[ax]
+        r = np.sqrt((g[0] - c[0]) ** 2 + (g[1] - c[1]) ** 2 + (g[2] - c[2]) ** 2)
+        bg += float(rng.uniform(0.5, 1.5)) / r
+    bg *= 10.0 * np.abs(local).max() / np.abs(bg).max()
+    m = mask != 0
+    out = [np.where(m, (t + 1) * (local + bg) + rng.normal(0.0, noise, shape), 0.0) for t in range(echoes)]
+    f = out[0] if echoes == 1 else np.stack(out, axis=3)
+    return np.asfortranarray(f), np.asfortranarray(np.where(m, local, 0.0)), mask
