@@ -329,43 +329,47 @@ def next_rows_arm(qsm_gb300, ctx, torch, peak, cpu=True, parts="tv64,tv32,pdf,vs
                                  unit="voxel-iter/s", cores=1, kind="port", sample="2 ADMM iterations, numpy FP64")
     out["tv_admm"] = row
 
-    if "pdf" not in parts:
-        return out
-    # PDF: LSMR iterations on the full grid (tol 0: every iteration runs); FP64 cuFFT bound
-    it = 30
-    f1 = dev(f4[..., 0])
-    info = {}
-    sec, _ = timed(lambda: qsm_gb300.pdf(f1, m_dev, [1, 1, 1], None, [0, 0, 1], 0.0, 0.0, it, info=info, ctx=ctx))
-    row = {"workload": f"pdf.m, {it} LSMR iterations, FP64", "value": n * it / sec, "unit": "voxel-iter/s",
-           "seconds": sec, "hbm_gbs": PDF_BYTES_F64 * n * it / sec / 1e9,
-           "frac": PDF_BYTES_F64 * n * it / sec / 1e9 / peak, "bytes_per_voxel_iter": PDF_BYTES_F64}
-    if cpu:
-        import bgremove
-        row["cpu_oracle"] = dict(_cpu_sample(lambda: bgremove.pdf(f4[..., 0], mask, [1, 1, 1], None, (0, 0, 1), 0.0,
-                                                                  0.0, 2), 2, n),
-                                 unit="voxel-iter/s", cores=1, kind="port", sample="2 LSMR iterations, numpy FP64")
-    out["pdf"] = row
+    import bgremove
+    if "pdf" in parts:
+        # PDF: LSMR iterations on the full grid (tol 0: every iteration runs); FP64 cuFFT bound
+        it = 30
+        f1 = dev(f4[..., 0])
+        info = {}
+        sec, _ = timed(lambda: qsm_gb300.pdf(f1, m_dev, [1, 1, 1], None, [0, 0, 1], 0.0, 0.0, it, info=info,
+                                             ctx=ctx))
+        row = {"workload": f"pdf.m, {it} LSMR iterations, FP64", "value": n * it / sec, "unit": "voxel-iter/s",
+               "seconds": sec, "hbm_gbs": PDF_BYTES_F64 * n * it / sec / 1e9,
+               "frac": PDF_BYTES_F64 * n * it / sec / 1e9 / peak, "bytes_per_voxel_iter": PDF_BYTES_F64}
+        if cpu:
+            row["cpu_oracle"] = dict(_cpu_sample(lambda: bgremove.pdf(f4[..., 0], mask, [1, 1, 1], None, (0, 0, 1),
+                                                                      0.0, 0.0, 2), 2, n),
+                                     unit="voxel-iter/s", cores=1, kind="port", sample="2 LSMR iterations, numpy FP64")
+        out["pdf"] = row
 
-    # V-SHARP, default radii (9:-2:2), 4 echoes in one call
-    f4_dev = torch.from_numpy(np.ascontiguousarray(np.transpose(f4, (3, 2, 1, 0)))).cuda()
-    sec, _ = timed(lambda: qsm_gb300.vsharp(f4_dev, m_dev, [1, 1, 1], ctx=ctx))
-    row = {"workload": "vsharp.m, radii 9:-2:2, 4 echoes, FP64", "value": 4 * n / sec, "unit": "voxels/s",
-           "seconds": sec}
-    if cpu:
-        row["cpu_oracle"] = dict(_cpu_sample(lambda: bgremove.vsharp(f4[..., 0], mask, [1, 1, 1]), 1, n),
-                                 unit="voxels/s", cores=1, kind="port", sample="1 echo, numpy FP64")
-    out["vsharp"] = row
+    if "vsharp" in parts:
+        # V-SHARP, default radii (9:-2:2), 4 echoes in one call
+        f4_dev = torch.from_numpy(np.ascontiguousarray(np.transpose(f4, (3, 2, 1, 0)))).cuda()
+        sec, _ = timed(lambda: qsm_gb300.vsharp(f4_dev, m_dev, [1, 1, 1], ctx=ctx))
+        row = {"workload": "vsharp.m, radii 9:-2:2, 4 echoes, FP64", "value": 4 * n / sec, "unit": "voxels/s",
+               "seconds": sec}
+        if cpu:
+            row["cpu_oracle"] = dict(_cpu_sample(lambda: bgremove.vsharp(f4[..., 0], mask, [1, 1, 1]), 1, n),
+                                     unit="voxels/s", cores=1, kind="port", sample="1 echo, numpy FP64")
+        out["vsharp"] = row
 
     # whole wrappers from host arrays (crop, Laplacian, solve, scatter; echoes batched)
-    it = 300
-    f4s = np.asfortranarray(f4.astype(np.float32))
-    sec, _ = timed(lambda: qsm_gb300.sstgv(f4s, mask, [1, 1, 1], 1e-4, 3.0, 0.0, it, fused=True, ctx=ctx), reps=2)
-    out["sstgv"] = {"workload": f"sstgv.m, 4 echoes FP32 fused, {it} iterations, tol 0, host arrays",
-                    "value": 4 * n * it / sec, "unit": "voxel-iter/s (dense grid)", "seconds": sec}
-    infos = []
-    sec, _ = timed(lambda: qsm_gb300.lbv(f4, mask, [1, 1, 1], infos=infos, ctx=ctx), reps=1)
-    out["lbv"] = {"workload": "lbv.m defaults, 4 echoes FP64, host arrays", "seconds": sec,
-                  "pcg_iters": [i["iters"] for i in infos]}
+    if "sstgv" in parts:
+        it = 300
+        f4s = np.asfortranarray(f4.astype(np.float32))
+        sec, _ = timed(lambda: qsm_gb300.sstgv(f4s, mask, [1, 1, 1], 1e-4, 3.0, 0.0, it, fused=True, ctx=ctx),
+                       reps=2)
+        out["sstgv"] = {"workload": f"sstgv.m, 4 echoes FP32 fused, {it} iterations, tol 0, host arrays",
+                        "value": 4 * n * it / sec, "unit": "voxel-iter/s (dense grid)", "seconds": sec}
+    if "lbv" in parts:
+        infos = []
+        sec, _ = timed(lambda: qsm_gb300.lbv(f4, mask, [1, 1, 1], infos=infos, ctx=ctx), reps=1)
+        out["lbv"] = {"workload": "lbv.m defaults, 4 echoes FP64, host arrays", "seconds": sec,
+                      "pcg_iters": [i["iters"] for i in infos]}
     return out
 
 

@@ -267,12 +267,21 @@ __device__ __forceinline__ void block_sums(double *part, double (&acc)[NS])
         for (int q = 0; q < NS; ++q) part[q * gridDim.x + blockIdx.x] = red[q][0];
 }
 
-__global__ void fold_k(double *out, const double *__restrict__ part, int nblk)
+// the block partials summed in a fixed order: thread t adds partials t, t + 256,
+// ... in turn, then a shared-memory tree (one block of BG_BLOCK threads)
+__global__ void __launch_bounds__(BG_BLOCK) fold_k(double *out, const double *__restrict__ part, int nblk)
 {
-    if (threadIdx.x != 0) return;
+    __shared__ double red[BG_BLOCK];
+    const int t = threadIdx.x;
     double s = 0.0;
-    for (int b = 0; b < nblk; ++b) s += part[b];
-    *out = s;
+    for (int b = t; b < nblk; b += BG_BLOCK) s += part[b];
+    red[t] = s;
+    __syncthreads();
+    for (int h = BG_BLOCK / 2; h > 0; h >>= 1) {
+        if (t < h) red[t] += red[t + h];
+        __syncthreads();
+    }
+    if (t == 0) *out = red[0];
 }
 
 // iSMV set-up (ismv.m:68-73): bc = (mask1 - m) .* f; sum (m .* f)^2
@@ -281,13 +290,14 @@ __global__ void __launch_bounds__(BG_BLOCK)
 ismv_init_k(T *bc, const T *__restrict__ f, const uint8_t *__restrict__ m1, const uint8_t *__restrict__ m, size_t n,
             double *part)
 {
-    double acc[1] = {0.0};
+    PartialSum<T> ps;
     for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
         const T v = f[l];
         bc[l] = ((T)(m1[l] ? 1 : 0) - (T)(m[l] ? 1 : 0)) * v;
         const T w = (T)(m[l] ? 1 : 0) * v;
-        acc[0] += (double)w * (double)w;
+        ps.add(w * w);
     }
+    double acc[1] = {ps.get()};
     block_sums<1>(part, acc);
 }
 
@@ -297,13 +307,14 @@ __global__ void __launch_bounds__(BG_BLOCK)
 ismv_step_k(T *f, const T *__restrict__ g, const T *__restrict__ bc, const uint8_t *__restrict__ m, T invn, size_t n,
             double *part)
 {
-    double acc[1] = {0.0};
+    PartialSum<T> ps;
     for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
         const T fn = bc[l] + (T)(m[l] ? 1 : 0) * (g[l] * invn);
         const T dlt = f[l] - fn;
-        acc[0] += (double)dlt * (double)dlt;
+        ps.add(dlt * dlt);
         f[l] = fn;
     }
+    double acc[1] = {ps.get()};
     block_sums<1>(part, acc);
 }
 
@@ -329,9 +340,10 @@ template <typename T>
 __global__ void __launch_bounds__(BG_BLOCK)
 dot_k(const T *__restrict__ x, const T *__restrict__ y, size_t n, double *part)
 {
-    double acc[1] = {0.0};
+    PartialSum<T> ps;
     for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x)
-        acc[0] += (double)x[l] * (double)y[l];
+        ps.add(x[l] * y[l]);
+    double acc[1] = {ps.get()};
     block_sums<1>(part, acc);
 }
 
@@ -369,12 +381,13 @@ template <typename T>
 __global__ void __launch_bounds__(BG_BLOCK)
 cgs_r_k(T *r, const T *__restrict__ w, T alpha, size_t n, double *part)
 {
-    double acc[1] = {0.0};
+    PartialSum<T> ps;
     for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
         const T rn = r[l] - alpha * w[l];
         r[l] = rn;
-        acc[0] += (double)rn * (double)rn;
+        ps.add(rn * rn);
     }
+    double acc[1] = {ps.get()};
     block_sums<1>(part, acc);
 }
 
@@ -669,7 +682,7 @@ qsm_status run(qsm_ctx *ctx, Method meth, const Dims &d, size_t ne, const T *f, 
                 };
                 auto dot = [&](const T *a_, const T *b_, double *out_) -> qsm_status {
                     dot_k<T><<<BG_GRID, BG_BLOCK, 0, ctx->stream>>>(a_, b_, N, w.part);
-                    fold_k<<<1, 32, 0, ctx->stream>>>(w.sum, w.part, BG_GRID);
+                    fold_k<<<1, BG_BLOCK, 0, ctx->stream>>>(w.sum, w.part, BG_GRID);
                     QSM_TRY(launched(ctx));
                     QSM_CUDA(cudaMemcpyAsync(out_, w.sum, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
                     QSM_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -704,7 +717,7 @@ qsm_status run(qsm_ctx *ctx, Method meth, const Dims &d, size_t ne, const T *f, 
                         QSM_TRY(launched(ctx));
                         QSM_TRY(apply(uh, vh));  // vh reused for A uh
                         cgs_r_k<T><<<BG_GRID, BG_BLOCK, 0, ctx->stream>>>(r, vh, alpha, N, w.part);
-                        fold_k<<<1, 32, 0, ctx->stream>>>(w.sum, w.part, BG_GRID);
+                        fold_k<<<1, BG_BLOCK, 0, ctx->stream>>>(w.sum, w.part, BG_GRID);
                         QSM_TRY(launched(ctx));
                         QSM_CUDA(cudaMemcpyAsync(&rr, w.sum, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
                         QSM_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -725,7 +738,7 @@ qsm_status run(qsm_ctx *ctx, Method meth, const Dims &d, size_t ne, const T *f, 
                 pad<T, T>(ctx, w.c, ft, g);
                 QSM_TRY(launched(ctx));
                 ismv_init_k<T><<<BG_GRID, BG_BLOCK, 0, ctx->stream>>>(w.b, w.c, w.m1, w.mk, N, w.part);
-                fold_k<<<1, 32, 0, ctx->stream>>>(w.sum, w.part, BG_GRID);
+                fold_k<<<1, BG_BLOCK, 0, ctx->stream>>>(w.sum, w.part, BG_GRID);
                 QSM_TRY(launched(ctx));
                 double r2 = 0.0;
                 QSM_CUDA(cudaMemcpyAsync(&r2, w.sum, sizeof r2, cudaMemcpyDeviceToHost, ctx->stream));
@@ -741,7 +754,7 @@ qsm_status run(qsm_ctx *ctx, Method meth, const Dims &d, size_t ne, const T *f, 
                     mul_h_k<T><<<gh, 256, 0, ctx->stream>>>(w.F, w.H, nh, false);
                     QSM_TRY(pl.inv(ctx, w.F, w.e));
                     ismv_step_k<T><<<BG_GRID, BG_BLOCK, 0, ctx->stream>>>(w.a, w.e, w.b, w.mk, invn, N, w.part);
-                    fold_k<<<1, 32, 0, ctx->stream>>>(w.sum, w.part, BG_GRID);
+                    fold_k<<<1, BG_BLOCK, 0, ctx->stream>>>(w.sum, w.part, BG_GRID);
                     QSM_TRY(launched(ctx));
                     QSM_CUDA(cudaMemcpyAsync(&r2, w.sum, sizeof r2, cudaMemcpyDeviceToHost, ctx->stream));
                     QSM_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -837,13 +850,14 @@ template <typename T>
 __global__ void __launch_bounds__(BG_BLOCK)
 gk_step_k(T *y, const T *__restrict__ g, const T *__restrict__ m, bool notm, T invn, T a, size_t n, double *part)
 {
-    double acc[1] = {0.0};
+    PartialSum<T> ps;
     for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
         const T w = notm ? (T)(m[l] == (T)0 ? 1 : 0) : m[l];
         const T v = w * (g[l] * invn) - a * y[l];
         y[l] = v;
-        acc[0] += (double)v * (double)v;
+        ps.add(v * v);
     }
+    double acc[1] = {ps.get()};
     block_sums<1>(part, acc);
 }
 
@@ -859,15 +873,16 @@ template <typename T>
 __global__ void __launch_bounds__(BG_BLOCK)
 lsmr_upd_k(T *hbar, T *x, T *h, const T *__restrict__ v, T c1, T c2, T c3, size_t n, double *part)
 {
-    double acc[1] = {0.0};
+    PartialSum<T> ps;
     for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
         const T hb = h[l] - c1 * hbar[l];
         const T xn = x[l] + c2 * hb;
         hbar[l] = hb;
         x[l] = xn;
         h[l] = v[l] - c3 * h[l];
-        acc[0] += (double)xn * (double)xn;
+        ps.add(xn * xn);
     }
+    double acc[1] = {ps.get()};
     block_sums<1>(part, acc);
 }
 
@@ -905,7 +920,7 @@ qsm_status run_pdf(qsm_ctx *ctx, const Dims &d, size_t ne, const T *f, const uin
     C *Dh = (C *)(p + 8 * rb), *F = (C *)(p + 8 * rb + cb);
     double *part = (double *)(p + 8 * rb + 2 * cb), *sum = part + BG_GRID;
     auto red = [&](double *out_) -> qsm_status {
-        fold_k<<<1, 32, 0, ctx->stream>>>(sum, part, BG_GRID);
+        fold_k<<<1, BG_BLOCK, 0, ctx->stream>>>(sum, part, BG_GRID);
         QSM_TRY(launched(ctx));
         QSM_CUDA(cudaMemcpyAsync(out_, sum, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
         QSM_CUDA(cudaStreamSynchronize(ctx->stream));

@@ -48,6 +48,29 @@ struct Dims {
 
 static inline Dims make_dims(const size_t *d) { return Dims{d[0], d[1], d[2]}; }
 
+// A thread's partial sum for the FP64 block reductions.  FP64 arithmetic runs at
+// 1/64 of the FP32 rate on this GPU, so an FP32 kernel that converted and added
+// every voxel's term in FP64 would be bound by the FP64 pipe: FP32 terms are
+// summed per thread with compensation (Kahan; exact under -fmad=false), and
+// only the thread's total goes to FP64.  FP64 terms are summed in FP64.
+template <typename T> struct PartialSum;
+template <> struct PartialSum<double> {
+    double s = 0.0;
+    __device__ __forceinline__ void add(double x) { s += x; }
+    __device__ __forceinline__ double get() const { return s; }
+};
+template <> struct PartialSum<float> {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float x)
+    {
+        const float y = x - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double get() const { return (double)s - (double)c; }
+};
+
 // One thread per voxel: block 32 x 4 x 2 over (x, y, z).
 static inline dim3 vox_block() { return dim3(32, 4, 2); }
 static inline dim3 vox_grid(const Dims &d)

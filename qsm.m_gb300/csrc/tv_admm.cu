@@ -50,6 +50,51 @@ struct TvK {
     bool oblique;          // B0 has two or more non-zero components
 };
 
+struct Vox {
+    size_t l, NX, NY, NZ;
+    int i, j, k;
+};
+
+// The voxels of a grid-stride loop in order, with their (i, j, k) advanced by
+// carries instead of a 64-bit division per voxel: the stride is split into
+// (si, sj, sk) once per thread.
+struct VoxWalk {
+    Vox v;
+    size_t S;
+    int si, sj, sk, nx, ny;
+    __device__ __forceinline__ VoxWalk(size_t l0, size_t stride, const Dims &d)
+    {
+        nx = (int)d.nx;
+        ny = (int)d.ny;
+        v.l = l0;
+        v.i = (int)(l0 % d.nx);
+        v.j = (int)((l0 / d.nx) % d.ny);
+        v.k = (int)(l0 / d.nxny());
+        v.NX = d.nx - 1;
+        v.NY = d.nx * (d.ny - 1);
+        v.NZ = d.nxny() * (d.nz - 1);
+        S = stride;
+        si = (int)(stride % d.nx);
+        sj = (int)((stride / d.nx) % d.ny);
+        sk = (int)(stride / d.nxny());
+    }
+    __device__ __forceinline__ void next()
+    {
+        v.l += S;
+        v.i += si;
+        int c = v.i >= nx;
+        v.i -= c ? nx : 0;
+        v.j += sj + c;
+        c = v.j >= ny;
+        v.j -= c ? ny : 0;
+        v.k += sk + c;
+    }
+};
+
+#define VOX_LOOP(W, D)                                                                                  \
+    for (VoxWalk W((size_t)blockIdx.x * blockDim.x + threadIdx.x, (size_t)gridDim.x * blockDim.x, D); \
+         W.v.l < (D).n(); W.next())
+
 __device__ __forceinline__ double fftfreq(int i, int n, double h) { return (double)(i <= (n - 1) / 2 ? i : i - n) / (n * h); }
 
 // per-axis tables: frequencies fx[nxh] fy[ny] fz[nz], then the Laplacian terms
@@ -101,8 +146,10 @@ __global__ void kmul_k(typename CxT<T>::type *R, const typename CxT<T>::type *__
     const size_t nh = (size_t)K.nxh * K.ny * K.nz;
     const int tot = K.nxh + K.ny + K.nz;
     const T mu = (T)K.mu, rho = (T)rho_, invn = (T)invn_;
-    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < nh; q += (size_t)gridDim.x * blockDim.x) {
-        const int i = (int)(q % K.nxh), j = (int)((q / K.nxh) % K.ny), k = (int)(q / ((size_t)K.nxh * K.ny));
+    const Dims hd{(size_t)K.nxh, (size_t)K.ny, (size_t)K.nz};
+    VOX_LOOP(wk, hd) {
+        const size_t q = wk.v.l;
+        const int i = wk.v.i, j = wk.v.j, k = wk.v.k;
         const T D = Dq[q];
         const T L = (T)((tab[tot + i] + tab[tot + K.nxh + j]) + tab[tot + K.nxh + K.ny + k]);
         T a = inv_a<T>(mu * D * D, L, rho), ad = a * (mu * D);
@@ -123,23 +170,6 @@ __global__ void kmul_k(typename CxT<T>::type *R, const typename CxT<T>::type *__
     }
 }
 
-struct Vox {
-    size_t l, NX, NY, NZ;
-    int i, j, k;
-};
-
-__device__ __forceinline__ Vox vox_at(size_t l, const Dims &d)
-{
-    Vox v;
-    v.l = l;
-    v.i = (int)(l % d.nx);
-    v.j = (int)((l / d.nx) % d.ny);
-    v.k = (int)(l / d.nxny());
-    v.NX = d.nx - 1;
-    v.NY = d.nx * (d.ny - 1);
-    v.NZ = d.nxny() * (d.nz - 1);
-    return v;
-}
 
 // gradfp_adj_mex.c:156-257 of the field g_c(l) (h holds -1/h), with the
 // reference's association order of the three axis terms.
@@ -159,9 +189,8 @@ __global__ void adj_rhs_k(T *r, const T *__restrict__ v, const T *__restrict__ l
 {
     const size_t N = d.n();
     const T ih[3] = {nx_, ny_, nz_};
-    for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < N; l += (size_t)gridDim.x * blockDim.x) {
-        const Vox vx = vox_at(l, d);
-        r[l] = adj_at<T>(vx, d, ih, [&](int c, size_t m) { return rho * v[c * N + m] - lm[c * N + m]; });
+    VOX_LOOP(wk, d) {
+        r[wk.v.l] = adj_at<T>(wk.v, d, ih, [&](int c, size_t m) { return rho * v[c * N + m] - lm[c * N + m]; });
     }
 }
 
@@ -192,9 +221,10 @@ grad_shrink_k(T *vn, const T *__restrict__ vo, T *lm, const T *__restrict__ u, D
               T rho, T irho, double *part)
 {
     const size_t N = d.n();
-    double acc[3] = {0.0, 0.0, 0.0};  // nr, na, nb
-    for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < N; l += (size_t)gridDim.x * blockDim.x) {
-        const Vox v = vox_at(l, d);
+    PartialSum<T> ps[3];  // nr, na, nb
+    VOX_LOOP(wk, d) {
+        const Vox &v = wk.v;
+        const size_t l = v.l;
         const T u0 = u[l];
         T dd[3];
         dd[0] = hx * ((v.i + 1 < (int)d.nx ? u[l + 1] : u[l - v.NX]) - u0);
@@ -232,10 +262,11 @@ grad_shrink_k(T *vn, const T *__restrict__ vo, T *lm, const T *__restrict__ u, D
             a2 += dd[c] * dd[c];
             b2 += w[c] * w[c];
         }
-        acc[0] += (double)sqrt(e2);
-        acc[1] += (double)sqrt(a2);
-        acc[2] += (double)sqrt(b2);
+        ps[0].add(sqrt(e2));
+        ps[1].add(sqrt(a2));
+        ps[2].add(sqrt(b2));
     }
+    double acc[3] = {ps[0].get(), ps[1].get(), ps[2].get()};
     block_sums<3>(part, acc);
 }
 
@@ -247,14 +278,14 @@ adj_norms_k(const T *__restrict__ vn, const T *__restrict__ vo, const T *__restr
 {
     const size_t N = d.n();
     const T ih[3] = {nx_, ny_, nz_};
-    double acc[2] = {0.0, 0.0};
-    for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < N; l += (size_t)gridDim.x * blockDim.x) {
-        const Vox v = vox_at(l, d);
-        const T s = rho * adj_at<T>(v, d, ih, [&](int c, size_t m) { return vn[c * N + m] - vo[c * N + m]; });
-        const T t = rho * adj_at<T>(v, d, ih, [&](int c, size_t m) { return lm[c * N + m]; });
-        acc[0] += (double)(s * s);
-        acc[1] += (double)(t * t);
+    PartialSum<T> ps[2];
+    VOX_LOOP(wk, d) {
+        const T s = rho * adj_at<T>(wk.v, d, ih, [&](int c, size_t m) { return vn[c * N + m] - vo[c * N + m]; });
+        const T t = rho * adj_at<T>(wk.v, d, ih, [&](int c, size_t m) { return lm[c * N + m]; });
+        ps[0].add(s * s);
+        ps[1].add(t * t);
     }
+    double acc[2] = {ps[0].get(), ps[1].get()};
     block_sums<2>(part, acc);
 }
 
@@ -264,9 +295,10 @@ __global__ void __launch_bounds__(TV_BLOCK)
 grad_init_k(T *v, const T *__restrict__ u, Dims d, T hx, T hy, T hz, double *part)
 {
     const size_t N = d.n();
-    double acc[1] = {0.0};
-    for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < N; l += (size_t)gridDim.x * blockDim.x) {
-        const Vox x = vox_at(l, d);
+    PartialSum<T> ps;
+    VOX_LOOP(wk, d) {
+        const Vox &x = wk.v;
+        const size_t l = x.l;
         const T u0 = u[l];
         const T a = hx * ((x.i + 1 < (int)d.nx ? u[l + 1] : u[l - x.NX]) - u0);
         const T b = hy * ((x.j + 1 < (int)d.ny ? u[l + d.nx] : u[l - x.NY]) - u0);
@@ -274,19 +306,30 @@ grad_init_k(T *v, const T *__restrict__ u, Dims d, T hx, T hy, T hz, double *par
         v[l] = a;
         v[N + l] = b;
         v[2 * N + l] = c;
-        acc[0] += sqrt((double)(a * a + b * b + c * c));
+        ps.add(sqrt(a * a + b * b + c * c));
     }
+    double acc[1] = {ps.get()};
     block_sums<1>(part, acc);
 }
 
-// fold the block partials of `ns` sums in block order
-__global__ void fold_k(double *out, const double *__restrict__ part, int ns, int nblk)
+// fold the block partials of `ns` sums in a fixed order: thread t adds partials
+// t, t + 256, ... in turn, then a shared-memory tree (one block of 256 threads)
+__global__ void __launch_bounds__(TV_BLOCK) fold_k(double *out, const double *__restrict__ part, int ns, int nblk)
 {
-    const int q = threadIdx.x;
-    if (q >= ns) return;
-    double s = 0.0;
-    for (int b = 0; b < nblk; ++b) s += part[q * nblk + b];
-    out[q] = s;
+    __shared__ double red[TV_BLOCK];
+    const int t = threadIdx.x;
+    for (int q = 0; q < ns; ++q) {
+        double s = 0.0;
+        for (int b = t; b < nblk; b += TV_BLOCK) s += part[q * nblk + b];
+        red[t] = s;
+        __syncthreads();
+        for (int h = TV_BLOCK / 2; h > 0; h >>= 1) {
+            if (t < h) red[t] += red[t + h];
+            __syncthreads();
+        }
+        if (t == 0) out[q] = red[0];
+        __syncthreads();
+    }
 }
 
 template <typename T, typename S>
@@ -415,7 +458,7 @@ static qsm_status tv_run(qsm_ctx *ctx, const Dims &d, const S *f, const uint8_t 
     if (sizeof(T) == 8) QSM_FFT(cufftExecD2Z(pf, (cufftDoubleReal *)u, (cufftDoubleComplex *)fhat));
     else QSM_FFT(cufftExecR2C(pf, (cufftReal *)u, (cufftComplex *)fhat));
     grad_init_k<T><<<g, b, 0, ctx->stream>>>(v[0], u, d, ihx, ihy, ihz, part);
-    fold_k<<<1, 32, 0, ctx->stream>>>(sums, part, 1, TV_GRID);
+    fold_k<<<1, TV_BLOCK, 0, ctx->stream>>>(sums, part, 1, TV_GRID);
     QSM_STEP(cuda_st(ctx, cudaMemcpyAsync(hs, sums, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "copy"));
     QSM_STEP(cuda_st(ctx, cudaStreamSynchronize(ctx->stream), "sync"));
     nr = hs[0];
@@ -439,7 +482,7 @@ static qsm_status tv_run(qsm_ctx *ctx, const Dims &d, const S *f, const uint8_t 
             grad_shrink_k<T, true><<<g, b, 0, ctx->stream>>>(v[nxt], v[cur], lm, u, d, ihx, ihy, ihz, (T)o.alpha,
                                                              (T)rho, (T)irho, part);
         adj_norms_k<T><<<g, b, 0, ctx->stream>>>(v[nxt], v[cur], lm, d, -ihx, -ihy, -ihz, (T)rho, part + 3 * TV_GRID);
-        fold_k<<<1, 32, 0, ctx->stream>>>(sums, part, TV_NSUM, TV_GRID);
+        fold_k<<<1, TV_BLOCK, 0, ctx->stream>>>(sums, part, TV_NSUM, TV_GRID);
         QSM_STEP(cuda_st(ctx, cudaGetLastError(), "launch"));
         QSM_STEP(cuda_st(ctx, cudaMemcpyAsync(hs, sums, TV_NSUM * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "copy"));
         QSM_STEP(cuda_st(ctx, cudaStreamSynchronize(ctx->stream), "sync"));
