@@ -39,7 +39,12 @@ template <> struct CxT<double> { using type = cufftDoubleComplex; };
 template <> struct CxT<float> { using type = cufftComplex; };
 
 constexpr int TV_BLOCK = 256;
-constexpr int TV_GRID = 4 * 152;   // grid-stride reductions: fixed block count
+// Grid-stride kernels run a fixed, fully resident grid (the block partials of the
+// reductions then have a fixed count and order): 5 blocks of 256 threads per SM
+// in FP32 (<= 51 registers), 3 in FP64 (<= 85 registers).
+template <typename T> struct TvOcc { static constexpr int minb = sizeof(T) == 4 ? 5 : 3; };
+template <typename T> constexpr int tv_grid() { return 152 * TvOcc<T>::minb; }
+constexpr int TV_GRID_MAX = 152 * 5;
 constexpr int TV_NSUM = 5;         // nr, na, nb, ||s||^2, ||rho grad' l||^2
 
 struct TvK {
@@ -140,7 +145,7 @@ __device__ __forceinline__ T inv_a(T K, T L, T rho)
 // X = iA .* (mu D .* fhat + R) / N in place of R (tv.m:172-175), in the working
 // precision T
 template <typename T>
-__global__ void kmul_k(typename CxT<T>::type *R, const typename CxT<T>::type *__restrict__ fhat,
+__global__ void __launch_bounds__(TV_BLOCK, TvOcc<T>::minb) kmul_k(typename CxT<T>::type *R, const typename CxT<T>::type *__restrict__ fhat,
                        const T *__restrict__ Dq, const double *__restrict__ tab, TvK K, double rho_, double invn_)
 {
     const size_t nh = (size_t)K.nxh * K.ny * K.nz;
@@ -185,7 +190,7 @@ __device__ __forceinline__ T adj_at(const Vox &v, const Dims &d, const T *ih, G 
 
 // r = gradfp_adj(rho v - l) (tv.m:166-170)
 template <typename T>
-__global__ void adj_rhs_k(T *r, const T *__restrict__ v, const T *__restrict__ lm, Dims d, T nx_, T ny_, T nz_, T rho)
+__global__ void __launch_bounds__(TV_BLOCK, TvOcc<T>::minb) adj_rhs_k(T *r, const T *__restrict__ v, const T *__restrict__ lm, Dims d, T nx_, T ny_, T nz_, T rho)
 {
     const size_t N = d.n();
     const T ih[3] = {nx_, ny_, nz_};
@@ -216,7 +221,7 @@ __device__ __forceinline__ void block_sums(double *part, double (&acc)[NS])
 // grad, over-relaxation, shrinkage, multiplier update and the primal
 // residual sums of one ADMM iteration (tv.m:185-221, :227-234)
 template <typename T, bool ISO>
-__global__ void __launch_bounds__(TV_BLOCK)
+__global__ void __launch_bounds__(TV_BLOCK, TvOcc<T>::minb)
 grad_shrink_k(T *vn, const T *__restrict__ vo, T *lm, const T *__restrict__ u, Dims d, T hx, T hy, T hz, T alpha,
               T rho, T irho, double *part)
 {
@@ -272,7 +277,7 @@ grad_shrink_k(T *vn, const T *__restrict__ vo, T *lm, const T *__restrict__ u, D
 
 // ||rho gradfp_adj(v - v_)||^2 and ||rho gradfp_adj(l)||^2 (tv.m:230, :239)
 template <typename T>
-__global__ void __launch_bounds__(TV_BLOCK)
+__global__ void __launch_bounds__(TV_BLOCK, TvOcc<T>::minb)
 adj_norms_k(const T *__restrict__ vn, const T *__restrict__ vo, const T *__restrict__ lm, Dims d, T nx_, T ny_, T nz_,
             T rho, double *part)
 {
@@ -291,7 +296,7 @@ adj_norms_k(const T *__restrict__ vn, const T *__restrict__ vo, const T *__restr
 
 // initial v = grad(u), nr = sum |v| (tv.m:150-152)
 template <typename T>
-__global__ void __launch_bounds__(TV_BLOCK)
+__global__ void __launch_bounds__(TV_BLOCK, TvOcc<T>::minb)
 grad_init_k(T *v, const T *__restrict__ u, Dims d, T hx, T hy, T hz, double *part)
 {
     const size_t N = d.n();
@@ -399,7 +404,7 @@ static qsm_status tv_run(qsm_ctx *ctx, const Dims &d, const S *f, const uint8_t 
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     const size_t rb = al(N * sizeof(T)), vb = al(3 * N * sizeof(T)), cb = al(nh * sizeof(C));
     const size_t tb = al(2 * (size_t)(nxh + d.ny + d.nz) * sizeof(double)), db = al(nh * sizeof(T));
-    const size_t bytes = 2 * rb + 3 * vb + 2 * cb + tb + db + (TV_NSUM * TV_GRID + 64) * sizeof(double);
+    const size_t bytes = 2 * rb + 3 * vb + 2 * cb + tb + db + (TV_NSUM * TV_GRID_MAX + 64) * sizeof(double);
     void *blk = nullptr;
     QSM_TRY(dalloc(ctx, &blk, bytes));
     char *c = (char *)blk;
@@ -414,7 +419,7 @@ static qsm_status tv_run(qsm_ctx *ctx, const Dims &d, const S *f, const uint8_t 
     double *tab = (double *)c; c += tb;
     T *Dq = (T *)c; c += db;
     double *part = (double *)c;
-    double *sums = part + TV_NSUM * TV_GRID;
+    double *sums = part + TV_NSUM * TV_GRID_MAX;
 
     qsm_status st = QSM_OK;
     cufftHandle pf = 0, pi = 0;
@@ -436,8 +441,9 @@ static qsm_status tv_run(qsm_ctx *ctx, const Dims &d, const S *f, const uint8_t 
     }
     K.mu = o.mu;
     const T ihx = (T)(1.0 / h[0]), ihy = (T)(1.0 / h[1]), ihz = (T)(1.0 / h[2]);
+    const int TV_GRID = tv_grid<T>();
     const dim3 g(TV_GRID), b(TV_BLOCK);
-    const unsigned gk = (unsigned)std::min<size_t>((nh + TV_BLOCK - 1) / TV_BLOCK, 8 * 152);
+    const unsigned gk = (unsigned)std::min<size_t>((nh + TV_BLOCK - 1) / TV_BLOCK, (size_t)TV_GRID);
 
     QSM_STEP(cuda_st(ctx, cudaMemsetAsync(lm, 0, 3 * N * sizeof(T), ctx->stream), "memset"));
     QSM_FFT(cufftPlan3d(&pf, (int)d.nz, (int)d.ny, (int)d.nx, tf));
