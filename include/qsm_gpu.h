@@ -458,6 +458,69 @@ qsm_status qsm_ismv(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[4], const v
                     const uint8_t *mask, const double vsz[3], double r, double tol, int32_t maxit,
                     int32_t verbose, void *fl, uint8_t *mask_out, int32_t *iters);
 
+/* ---------------- NIfTI-1 (src/io/loadNii.m, saveNii.m) ----------------
+ *
+ * loadNii(filename) = third_party/NIfTI/load_nii.m: the header (either byte
+ * order), the image as stored, then xform_nii.m: scl_slope / scl_inter applied
+ * to real images (the result single, or double for a double image), and the
+ * sform (else qform) affine, which must be a generalized permutation matrix
+ * once entries below tolerance x the smallest of its three largest are
+ * cleared, turned into axis flips and a permutation to x, y, z order; voxel
+ * sizes from the affine, in millimetres.  saveNii(filename, img, vsz) =
+ * make_nii(img, vsz) + save_nii: a 352-byte 'n+1' header (sform_code 1 from
+ * vsz) and the image in its own class.  File access and gzip are the
+ * caller's. */
+typedef struct {
+    /* as stored */
+    int32_t filetype;            /* 2: 'n+1' single file, 1: 'ni1' .hdr/.img pair, 0: Analyze 7.5 */
+    int32_t big_endian;
+    int32_t stored_datatype;
+    int32_t bitpix;              /* of the stored datatype */
+    int64_t stored_dim[8];       /* dim, entries < 1 read as 1 */
+    int64_t vox_offset;          /* first voxel byte in an 'n+1' file; 0 for a separate .img */
+    double vox_offset_stored;
+    double scl_slope, scl_inter;
+    double quatern[3], qoffset[3], srow[12];
+    /* the loaded image */
+    int32_t datatype;            /* 16 or 64 after scaling, else as stored */
+    int32_t scaled;              /* load_nii applied scl_slope / scl_inter */
+    int64_t dim[8];              /* spatial sizes in loaded axis order */
+    double pixdim[8];            /* abs, millimetres, loaded axis order (as stored for Analyze) */
+    double originator[5];
+    int32_t perm[3];             /* loaded axis j is stored axis perm[j] (0-based) */
+    int32_t flip[3];             /* loaded axis j runs backwards through that stored axis */
+    int32_t reoriented;          /* perm / flip is not the identity */
+    int32_t qform_code, sform_code;  /* 0 once the affine was applied */
+    int32_t xyzt_units;          /* spatial unit set to mm when it was m or um */
+    char data_type[11], db_name[19], descrip[81], aux_file[25], intent_name[17], magic[5];
+    char error[160];             /* message of a failed parse */
+} qsm_nifti_hdr;
+
+/* Parse the first nbytes (>= 348) of a .nii file or a .hdr file: load_nii_hdr.m
+ * and the header side of load_nii_img.m / xform_nii.m.  tolerance <= 0 means eps
+ * (load_nii's default is 0.1); preferred_form 's', 'q', 'S' or 'Q' as in
+ * load_nii.m ('s': sform, else qform).  Host only; no context.  A bad header
+ * returns QSM_ERR_ARG or QSM_ERR_DTYPE with hdr->error set. */
+qsm_status qsm_nifti_parse(const void *header, size_t nbytes, double tolerance, char preferred_form,
+                           qsm_nifti_hdr *hdr);
+/* Bytes of the stored image: prod(stored_dim[1..7]) * bitpix / 8. */
+size_t qsm_nifti_payload_bytes(const qsm_nifti_hdr *hdr);
+/* img (host or device, prod(dim[1..7]) elements, MATLAB order of hdr->dim) = the
+ * loaded image of the stored bytes `payload` (host or device, starting at the first
+ * voxel): byte order, scaling, flips and permutation in one device pass.
+ * out_datatype 0 gives the loaded class (hdr->datatype); 16 / 64 convert to
+ * single / double.  Bit, complex and RGB datatypes are QSM_ERR_DTYPE. */
+qsm_status qsm_nifti_decode(qsm_ctx *ctx, const qsm_nifti_hdr *hdr, const void *payload,
+                            int32_t out_datatype, void *img);
+/* The header saveNii writes for img (host or device) of NIfTI `datatype` (the
+ * class of img: 2, 4, 8, 16, 64, 256, 512, 768) with MATLAB size
+ * size[0..ndims-1] and voxel size vsz: filetype 2, 352 bytes of a single .nii
+ * (the image bytes follow unchanged); filetype 1, the 348 bytes of a .hdr whose
+ * image goes to the .img (save_nii.m).  glmax / glmin are rounded from img. */
+qsm_status qsm_nifti_make_header(qsm_ctx *ctx, int32_t datatype, int32_t ndims, const int64_t *size,
+                                 const double vsz[3], int32_t filetype, const void *img,
+                                 uint8_t *hdr_out);
+
 /* ---------------- lane-order inner product (BLAS-1 replacement) ---------------- */
 
 /* *out = x . y in the library's documented lane order (mx_dot,

@@ -27,13 +27,14 @@ import numpy as np
 
 from . import _lib
 from ._lib import MgInfo, PdInfo, QsmError, QsmLibraryError, TvInfo, context, lib
+from . import nifti  # noqa: E402  (loadNii / saveNii)
 
 __all__ = [
     "pd_tgv_mex", "pd_tv_mex", "gradf_mex", "gradb_mex", "gradc_mex", "gradfm_mex", "gradbm_mex", "gradcm_mex",
     "gradf_adj_mex", "gradb_adj_mex", "gradfm_adj_mex", "gradbm_adj_mex", "gradfp_mex", "gradfp_adj_mex",
     "lap1_mex", "lapw_mex", "gauss_seidel_mex", "residual_mex", "lapmg_mex", "restrict_mex", "prolong_mex",
     "correct_mex", "coarsen_grid_mex", "boundary_mask_mex", "boundary_mask_l1_mex", "norm2_mex", "mgpcg_mex",
-    "mg_mex", "fmg_mex", "lane_dot", "tv", "sstgv", "lbv", "unwrap_laplacian", "sharp", "vsharp", "ismv", "resharp", "pdf",
+    "mg_mex", "fmg_mex", "lane_dot", "tv", "sstgv", "lbv", "unwrap_laplacian", "sharp", "vsharp", "ismv", "resharp", "pdf", "nifti",
     "pd_tv_batch", "pd_tgv_batch", "Session", "footprint", "QsmError",
     "QsmLibraryError", "context", "lib",
 ]

@@ -57,6 +57,22 @@ class MgInfo(ctypes.Structure):
                 ("resnorm_hist", ctypes.POINTER(ctypes.c_double))]
 
 
+class NiftiHdr(ctypes.Structure):
+    """qsm_nifti_hdr (include/qsm_gpu.h)."""
+    _fields_ = [("filetype", ctypes.c_int32), ("big_endian", ctypes.c_int32),
+                ("stored_datatype", ctypes.c_int32), ("bitpix", ctypes.c_int32),
+                ("stored_dim", ctypes.c_int64 * 8), ("vox_offset", ctypes.c_int64),
+                ("vox_offset_stored", ctypes.c_double), ("scl_slope", ctypes.c_double), ("scl_inter", ctypes.c_double),
+                ("quatern", ctypes.c_double * 3), ("qoffset", ctypes.c_double * 3), ("srow", ctypes.c_double * 12),
+                ("datatype", ctypes.c_int32), ("scaled", ctypes.c_int32), ("dim", ctypes.c_int64 * 8),
+                ("pixdim", ctypes.c_double * 8), ("originator", ctypes.c_double * 5),
+                ("perm", ctypes.c_int32 * 3), ("flip", ctypes.c_int32 * 3), ("reoriented", ctypes.c_int32),
+                ("qform_code", ctypes.c_int32), ("sform_code", ctypes.c_int32), ("xyzt_units", ctypes.c_int32),
+                ("data_type", ctypes.c_char * 11), ("db_name", ctypes.c_char * 19), ("descrip", ctypes.c_char * 81),
+                ("aux_file", ctypes.c_char * 25), ("intent_name", ctypes.c_char * 17), ("magic", ctypes.c_char * 5),
+                ("error", ctypes.c_char * 160)]
+
+
 # name -> argtypes (after ctx); every function returns qsm_status
 _GRAD = [I32, SZ3, P, P, P, P, D3]
 _GRADM = [I32, SZ3, P, P, P, P, U8, D3]
@@ -98,6 +114,8 @@ SIGNATURES = {
     "qsm_ismv": [I32, SZ3, P, U8, D3, DBL, DBL, I32, I32, P, P, P],
     "qsm_resharp": [I32, SZ3, P, U8, D3, DBL, DBL, DBL, I32, I32, P, P, P],
     "qsm_pdf": [I32, SZ3, P, U8, P, D3, D3, DBL, DBL, I32, I32, P, P],
+    "qsm_nifti_decode": [ctypes.POINTER(NiftiHdr), P, I32, P],
+    "qsm_nifti_make_header": [I32, I32, ctypes.POINTER(ctypes.c_int64), D3, I32, P, P],
     # count volumes: dims (size_t[3*count]), arrays of d2f / mask / chi pointers
     "qsm_pd_tv_batch": [I32, U32, P, P, P, D3, DBL, DBL, U32, P, P],
     "qsm_pd_tgv_batch": [I32, U32, P, P, P, D3, DBL, DBL, DBL, U32, P, P],
@@ -119,6 +137,12 @@ SESSION_SIGNATURES = {
                          STATUS),
     "qsm_session_fetch": ([SES, ctypes.c_uint64, P], STATUS),
     "qsm_session_running": ([SES], U32),
+}
+
+# host-only functions without a context: name -> (argtypes, restype)
+HOST_SIGNATURES = {
+    "qsm_nifti_parse": ([P, ctypes.c_size_t, DBL, ctypes.c_char, ctypes.POINTER(NiftiHdr)], STATUS),
+    "qsm_nifti_payload_bytes": ([ctypes.POINTER(NiftiHdr)], ctypes.c_size_t),
 }
 
 QSM_JOB_TV, QSM_JOB_TGV, QSM_JOB_MGPCG, QSM_JOB_MGPCG_F64 = 0, 1, 2, 3
@@ -158,7 +182,7 @@ def lib() -> ctypes.CDLL:
         fn = getattr(L, name)
         fn.argtypes = [CTX] + args
         fn.restype = STATUS
-    for name, (args, res) in SESSION_SIGNATURES.items():
+    for name, (args, res) in list(SESSION_SIGNATURES.items()) + list(HOST_SIGNATURES.items()):
         fn = getattr(L, name)
         fn.argtypes = args
         fn.restype = res
@@ -168,7 +192,7 @@ def lib() -> ctypes.CDLL:
 
 def exported_symbols() -> list[str]:
     """Names of every function include/qsm_gpu.h declares."""
-    return sorted(list(SIGNATURES) + list(SESSION_SIGNATURES) + ["qsm_ctx_create", "qsm_ctx_destroy", "qsm_ctx_set_stream",
+    return sorted(list(SIGNATURES) + list(SESSION_SIGNATURES) + list(HOST_SIGNATURES) + ["qsm_ctx_create", "qsm_ctx_destroy", "qsm_ctx_set_stream",
                                       "qsm_ctx_get_stream", "qsm_ctx_set_verbose", "qsm_last_error",
                                       "qsm_status_string", "qsm_abi_version", "qsm_norm2_noalloc"])
 

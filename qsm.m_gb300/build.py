@@ -27,7 +27,7 @@ NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "--prec-div=true", "--prec-sqrt=true",
     "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-O3",
 ]
-SOURCES = ["common.cu", "fd.cu", "pd.cu", "pd_fused.cu", "pd_stream.cu", "pd_batch.cu", "tv_admm.cu", "pipelines.cu", "bgremove.cu", "mg.cu", "noalloc.cu"]
+SOURCES = ["common.cu", "fd.cu", "pd.cu", "pd_fused.cu", "pd_stream.cu", "pd_batch.cu", "tv_admm.cu", "pipelines.cu", "bgremove.cu", "mg.cu", "noalloc.cu", "nifti.cu"]
 
 
 def nvcc() -> str:
