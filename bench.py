@@ -282,9 +282,68 @@ def _cpu_sample(fn, iters_per_call, voxels):
     return {"value": voxels * iters_per_call / dt, "seconds": dt}
 
 
-def next_rows_arm(qsm_gb300, ctx, torch, peak, cpu=True, parts="tv64,tv32,pdf,vsharp,sstgv,lbv"):
+def nifti_part(qsm_gb300, ctx, torch, f4, mask, peak, cpu):
+    """loadNii of a 4-echo int16 phase series (224x224x128x4, scl_slope/scl_inter,
+    LPS sform: x and y flipped) into HBM as single, and saveNii of a double volume.
+    The decode pass reads 2 B and writes 4 B per voxel."""
+    import tempfile
+
+    import qsm_gb300.nifti as qn
+    import nifti as nio  # the oracle, for the CPU figure
+
+    shape = f4.shape
+    n = int(np.prod(shape))
+    raw = np.clip(np.round(f4 / np.abs(f4).max() * 32000), -32768, 32767).astype(np.int16)
+    b = bytearray(qn.header_bytes(raw.astype(np.float32), (1, 1, 1), ctx=ctx))
+    import struct
+    struct.pack_into("<hh", b, 70, 4, 16)                    # int16
+    struct.pack_into("<ff", b, 112, float(np.abs(f4).max() / 32000), 0.0)  # scl_slope, scl_inter
+    struct.pack_into("<12f", b, 280, -1, 0, 0, 224, 0, -1, 0, 224, 0, 0, 1, 0)  # LPS sform
+    hdr = bytes(b)
+    payload = np.asfortranarray(raw).tobytes(order="F")
+    res = {"workload": "loadNii int16 224x224x128x4, scaled, LPS sform -> single in HBM; saveNii double 224x224x128"}
+    dp = torch.from_numpy(np.frombuffer(payload, np.uint8).copy()).cuda()
+    qn.decode(hdr, dp, device=True, ctx=ctx)
+    torch.cuda.synchronize()
+    reps = 20
+    t = time.perf_counter()
+    for _ in range(reps):
+        img, _ = qn.decode(hdr, dp, device=True, ctx=ctx)
+    torch.cuda.synchronize()
+    sec = (time.perf_counter() - t) / reps
+    res["decode_device"] = {"seconds": sec, "voxels_per_s": n / sec, "hbm_gbs": 6 * n / sec / 1e9,
+                            "frac": 6 * n / sec / 1e9 / peak, "bytes_per_voxel": 6}
+    with tempfile.TemporaryDirectory() as d:
+        fn = os.path.join(d, "phase.nii")
+        with open(fn, "wb") as fh:
+            fh.write(hdr + payload)
+        qn.loadNii(fn, device=True, ctx=ctx)
+        t = time.perf_counter()
+        for _ in range(3):
+            img = qn.loadNii(fn, device=True, ctx=ctx).img
+        torch.cuda.synchronize()
+        sec = (time.perf_counter() - t) / 3
+        res["loadNii_e2e"] = {"seconds": sec, "voxels_per_s": n / sec, "file_bytes": len(hdr) + len(payload)}
+        x = torch.from_numpy(np.ascontiguousarray(f4[..., 0].T)).cuda()
+        out = os.path.join(d, "chi.nii")
+        t = time.perf_counter()
+        for _ in range(3):
+            qn.saveNii(out, x, (1, 1, 1), ctx=ctx)
+        sec = (time.perf_counter() - t) / 3
+        res["saveNii_e2e"] = {"seconds": sec, "voxels_per_s": x.numel() / sec}
+        if cpu:
+            def cpu_load():
+                data = open(fn, "rb").read()
+                nio.load_nii(data[:348], data[352:])
+            res["cpu_oracle"] = dict(_cpu_sample(cpu_load, 1, n), unit="voxels/s", cores=1, kind="port",
+                                     sample="one loadNii of the same file, numpy")
+    return res
+
+
+def next_rows_arm(qsm_gb300, ctx, torch, peak, cpu=True, parts="tv64,tv32,pdf,vsharp,sstgv,lbv,nifti"):
     """The widened rows on the 224x224x128 volume: TV ADMM (tv.m), PDF and V-SHARP
-    background removal, and the whole sstgv/lbv wrappers on 4 echoes.  Device
+    background removal, the whole sstgv/lbv wrappers on 4 echoes, and NIfTI
+    loading / saving.  Device
     solves run on resident tensors (the wrappers from pinned host arrays, end to
     end); each CPU figure is the oracle on a bounded sample of the same input."""
     import qsm_gb300.synthetic as S
@@ -365,6 +424,8 @@ def next_rows_arm(qsm_gb300, ctx, torch, peak, cpu=True, parts="tv64,tv32,pdf,vs
                        reps=2)
         out["sstgv"] = {"workload": f"sstgv.m, 4 echoes FP32 fused, {it} iterations, tol 0, host arrays",
                         "value": 4 * n * it / sec, "unit": "voxel-iter/s (dense grid)", "seconds": sec}
+    if "nifti" in parts:
+        out["nifti"] = nifti_part(qsm_gb300, ctx, torch, f4, mask, peak, cpu)
     if "lbv" in parts:
         infos = []
         sec, _ = timed(lambda: qsm_gb300.lbv(f4, mask, [1, 1, 1], infos=infos, ctx=ctx), reps=1)
@@ -621,7 +682,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched TV arm")
     ap.add_argument("--no-serve", action="store_true", help="skip the served-requests arm")
     ap.add_argument("--no-next", action="store_true", help="skip the TV ADMM / background removal / wrapper arm")
-    ap.add_argument("--next-parts", default="tv64,tv32,pdf,vsharp,sstgv,lbv",
+    ap.add_argument("--next-parts", default="tv64,tv32,pdf,vsharp,sstgv,lbv,nifti",
                     help="parts of the next-rows arm with --only next (profiling aid)")
     ap.add_argument("--serve-seconds", type=float, default=30.0, help="arrival window of the served arm")
     ap.add_argument("--shape", default="", help="nx,ny,nz of a reduced volume (profiler captures)")

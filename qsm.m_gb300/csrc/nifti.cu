@@ -128,93 +128,197 @@ struct Orient {
     int perm[3];     // loaded axis j = stored axis perm[j]
     int flip[3];     // loaded axis j runs backwards
     int64_t total;   // elements
+    int64_t rows;    // loaded rows: n[1] * n[2] * (extra dimensions)
     int swap;
 };
 
-__device__ __forceinline__ int64_t stored_index(const Orient &o, int64_t q)
+// Rows of the loaded image, (64 x 4)-thread blocks: threadIdx.y picks a row,
+// threadIdx.x strides along it.  The stored index of loaded (o0, o1, o2, t)
+// is base(o1, o2, t) + step * o0 (step < 0 when loaded x runs backwards).
+struct RowMap {
+    int64_t base, step;
+};
+
+__device__ __forceinline__ RowMap row_map(const Orient &o, int64_t r)
 {
-    int64_t oj[3];
-    oj[0] = q % o.n[0];
-    q /= o.n[0];
-    oj[1] = q % o.n[1];
-    q /= o.n[1];
-    oj[2] = q % o.n[2];
-    const int64_t t = q / o.n[2];
-    int64_t s[3];
+    const int64_t o1 = r % o.n[1], r2 = r / o.n[1];
+    const int64_t o2 = r2 % o.n[2], t = r2 / o.n[2];
+    const int64_t st[3] = {1, o.m[0], o.m[0] * o.m[1]};
+    const int64_t oj[3] = {0, o1, o2};
+    int64_t base = t * o.m[0] * o.m[1] * o.m[2];
 #pragma unroll
-    for (int j = 0; j < 3; ++j) {
+    for (int j = 1; j < 3; ++j) {
         const int a = o.perm[j];
-        s[a] = o.flip[j] ? o.m[a] - 1 - oj[j] : oj[j];
+        base += st[a] * (o.flip[j] ? o.m[a] - 1 - oj[j] : oj[j]);
     }
-    return s[0] + o.m[0] * (s[1] + o.m[1] * (s[2] + o.m[2] * t));
+    const int a0 = o.perm[0];
+    RowMap rm;
+    rm.base = base + (o.flip[0] ? st[a0] * (o.m[a0] - 1) : 0);
+    rm.step = o.flip[0] ? -st[a0] : st[a0];
+    return rm;
 }
 
+template <int B> struct Word;
+template <> struct Word<1> { using T = uint8_t; __device__ static T bswap(T x) { return x; } };
+template <> struct Word<2> {
+    using T = uint16_t;
+    __device__ static T bswap(T x) { return (T)((x >> 8) | (x << 8)); }
+};
+template <> struct Word<4> {
+    using T = uint32_t;
+    __device__ static T bswap(T x) { return __byte_perm(x, 0u, 0x0123); }
+};
+template <> struct Word<8> {
+    using T = unsigned long long;
+    __device__ static T bswap(T x)
+    {
+        const uint32_t lo = (uint32_t)x, hi = (uint32_t)(x >> 32);
+        return ((T)__byte_perm(lo, 0u, 0x0123) << 32) | (T)__byte_perm(hi, 0u, 0x0123);
+    }
+};
+
 template <typename S>
-__device__ __forceinline__ S load_elem(const uint8_t *__restrict__ p, int64_t i, int swap)
+__device__ __forceinline__ S load_elem(const S *__restrict__ p, int64_t i, int swap)
 {
-    uint8_t t[sizeof(S)];
-    const uint8_t *q = p + i * (int64_t)sizeof(S);
-#pragma unroll
-    for (int k = 0; k < (int)sizeof(S); ++k) t[k] = q[swap ? sizeof(S) - 1 - k : k];
+    using W = Word<sizeof(S)>;
+    typename W::T w = __ldg((const typename W::T *)p + i);
+    if (swap) w = W::bswap(w);
     S v;
-    memcpy(&v, t, sizeof(S));
+    memcpy(&v, &w, sizeof(S));
     return v;
 }
 
 // the loaded class unchanged: a reoriented, byte-order-corrected copy
 template <int B>
-__global__ void copy_k(uint8_t *__restrict__ out, const uint8_t *__restrict__ in, Orient o)
+__global__ void __launch_bounds__(256) copy_k(typename Word<B>::T *__restrict__ out,
+                                              const typename Word<B>::T *__restrict__ in, Orient o)
 {
-    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < o.total;
-         q += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t s = stored_index(o, q);
-#pragma unroll
-        for (int k = 0; k < B; ++k) out[q * B + k] = in[s * B + (o.swap ? B - 1 - k : k)];
+    using W = Word<B>;
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.y + threadIdx.y; r < o.rows; r += (int64_t)gridDim.x * blockDim.y) {
+        const RowMap rm = row_map(o, r);
+        typename W::T *dst = out + r * o.n[0];
+        for (int64_t x = threadIdx.x; x < o.n[0]; x += blockDim.x) {
+            typename W::T w = __ldg(in + rm.base + rm.step * x);
+            dst[x] = o.swap ? W::bswap(w) : w;
+        }
     }
 }
 
 // converted (and, when load_nii scales, scl_slope * double(x) + scl_inter,
 // rounded to single unless the stored class is double)
 template <typename S, typename O>
-__global__ void convert_k(O *__restrict__ out, const uint8_t *__restrict__ in, Orient o, int scaled, double slope,
-                          double inter, int to_single)
+__global__ void __launch_bounds__(256) convert_k(O *__restrict__ out, const S *__restrict__ in, Orient o, int scaled,
+                                                 double slope, double inter, int to_single)
 {
-    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < o.total;
-         q += (int64_t)gridDim.x * blockDim.x) {
-        const S v = load_elem<S>(in, stored_index(o, q), o.swap);
-        if (scaled) {
-            const double w = slope * (double)v + inter;
-            out[q] = to_single ? (O)(float)w : (O)w;
-        } else {
-            out[q] = (O)v;
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.y + threadIdx.y; r < o.rows; r += (int64_t)gridDim.x * blockDim.y) {
+        const RowMap rm = row_map(o, r);
+        O *dst = out + r * o.n[0];
+        for (int64_t x = threadIdx.x; x < o.n[0]; x += blockDim.x) {
+            const S v = load_elem<S>(in, rm.base + rm.step * x, o.swap);
+            if (scaled) {
+                const double w = slope * (double)v + inter;
+                dst[x] = to_single ? (O)(float)w : (O)w;
+            } else {
+                dst[x] = (O)v;
+            }
+        }
+    }
+}
+
+// scaled 8- and 16-bit images: every stored value's result, computed once as
+// load_nii computes it (FP64 scl_slope * x + scl_inter, then single), indexed
+// by the stored bits; FP64 per voxel would bind the pass to the FP64 pipe
+template <typename S, typename O>
+__global__ void scale_table_k(O *__restrict__ tab, double slope, double inter, int to_single)
+{
+    using W = typename Word<sizeof(S)>::T;
+    const unsigned n = 1u << (8 * sizeof(S));
+    for (unsigned u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
+        const W w = (W)u;
+        S v;
+        memcpy(&v, &w, sizeof(S));
+        const double r = slope * (double)v + inter;
+        tab[u] = to_single ? (O)(float)r : (O)r;
+    }
+}
+
+template <typename S, typename O>
+__global__ void __launch_bounds__(256) lookup_k(O *__restrict__ out, const S *__restrict__ in,
+                                                const O *__restrict__ tab, Orient o)
+{
+    using W = Word<sizeof(S)>;
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.y + threadIdx.y; r < o.rows; r += (int64_t)gridDim.x * blockDim.y) {
+        const RowMap rm = row_map(o, r);
+        O *dst = out + r * o.n[0];
+        for (int64_t x = threadIdx.x; x < o.n[0]; x += blockDim.x) {
+            typename W::T w = __ldg((const typename W::T *)in + rm.base + rm.step * x);
+            if (o.swap) w = W::bswap(w);
+            dst[x] = __ldg(tab + w);
         }
     }
 }
 
 // max and min over the non-NaN elements of an image (for glmax / glmin)
+// order-preserving 64-bit key of a double
+__device__ __forceinline__ unsigned long long order_key(double d)
+{
+    const unsigned long long u = (unsigned long long)__double_as_longlong(d);
+    return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+
+template <typename T> struct Cmp {  // integers and float compare in their own type
+    __device__ static bool nan(T v) { return v != v; }
+    __device__ static bool less(T a, T b) { return a < b; }
+};
+template <> struct Cmp<double> {     // doubles by their bits (no FP64 instruction per element)
+    __device__ static bool nan(double v)
+    {
+        const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+        return (u & 0x7fffffffffffffffull) > 0x7ff0000000000000ull;
+    }
+    __device__ static bool less(double a, double b) { return order_key(a) < order_key(b); }
+};
+
 template <typename T>
 __global__ void minmax_k(const T *__restrict__ a, int64_t n, unsigned long long *mx, unsigned long long *mn,
                          int *any)
 {
-    // order-preserving 64-bit keys of doubles
-    auto key = [](double d) {
-        unsigned long long u = (unsigned long long)__double_as_longlong(d);
-        return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
-    };
-    unsigned long long hi = 0ull, lo = ~0ull;
+    T hi = 0, lo = 0;
     int seen = 0;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double d = (double)a[i];
-        if (d != d) continue;
-        const unsigned long long k = key(d);
-        hi = k > hi ? k : hi;
-        lo = k < lo ? k : lo;
+        const T v = a[i];
+        if (Cmp<T>::nan(v)) continue;
+        if (!seen || Cmp<T>::less(hi, v)) hi = v;
+        if (!seen || Cmp<T>::less(v, lo)) lo = v;
         seen = 1;
     }
-    if (seen) {
-        atomicMax(mx, hi);
-        atomicMin(mn, lo);
-        atomicOr(any, 1);
+    // block reduction of the keys (warp shuffles, then warp 0), one atomic per block
+    unsigned long long kh = seen ? order_key((double)hi) : 0ull, kl = seen ? order_key((double)lo) : ~0ull;
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) {
+        kh = max(kh, __shfl_xor_sync(0xffffffffu, kh, s));
+        kl = min(kl, __shfl_xor_sync(0xffffffffu, kl, s));
+    }
+    __shared__ unsigned long long sh[2][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    if (lane == 0) {
+        sh[0][wid] = kh;
+        sh[1][wid] = kl;
+    }
+    __syncthreads();
+    if (wid == 0) {
+        kh = lane < nw ? sh[0][lane] : 0ull;
+        kl = lane < nw ? sh[1][lane] : ~0ull;
+#pragma unroll
+        for (int s = 16; s > 0; s >>= 1) {
+            kh = max(kh, __shfl_xor_sync(0xffffffffu, kh, s));
+            kl = min(kl, __shfl_xor_sync(0xffffffffu, kl, s));
+        }
+        if (lane == 0 && kl != ~0ull) {  // a non-NaN element was seen in this block
+            atomicMax(mx, kh);
+            atomicMin(mn, kl);
+            atomicOr(any, 1);
+        }
     }
 }
 
@@ -426,24 +530,60 @@ qsm_status qsm_nifti_decode(qsm_ctx *ctx, const qsm_nifti_hdr *h, const void *pa
         stage_out(ctx, si, false);
         return st;
     }
-    const unsigned g = (unsigned)std::min<int64_t>((o.total + 255) / 256, 152 * 8);
-    const uint8_t *in = (const uint8_t *)si.dev;
+    // element loads and stores are whole words: device buffers given by the caller
+    // must be aligned to their element size (staged host buffers always are)
+    if (((uintptr_t)si.dev % eb) || ((uintptr_t)so.dev % ob)) {
+        stage_out(ctx, si, false);
+        stage_out(ctx, so, false);
+        set_error(ctx, "payload and image must be aligned to their element sizes (%d, %d bytes)", eb, ob);
+        return QSM_ERR_ARG;
+    }
+    o.rows = o.total / o.n[0];
+    const dim3 blk(64, 4);
+    const unsigned g = (unsigned)std::min<int64_t>((o.rows + 3) / 4, 152 * 16);
+    const void *in = si.dev;
     const bool to_single = h->datatype == 16;
     if (!h->scaled && out_datatype == h->datatype) {
         switch (eb) {
-        case 1: copy_k<1><<<g, 256, 0, ctx->stream>>>((uint8_t *)so.dev, in, o); break;
-        case 2: copy_k<2><<<g, 256, 0, ctx->stream>>>((uint8_t *)so.dev, in, o); break;
-        case 4: copy_k<4><<<g, 256, 0, ctx->stream>>>((uint8_t *)so.dev, in, o); break;
-        default: copy_k<8><<<g, 256, 0, ctx->stream>>>((uint8_t *)so.dev, in, o); break;
+        case 1: copy_k<1><<<g, blk, 0, ctx->stream>>>((uint8_t *)so.dev, (const uint8_t *)in, o); break;
+        case 2: copy_k<2><<<g, blk, 0, ctx->stream>>>((uint16_t *)so.dev, (const uint16_t *)in, o); break;
+        case 4: copy_k<4><<<g, blk, 0, ctx->stream>>>((uint32_t *)so.dev, (const uint32_t *)in, o); break;
+        default:
+            copy_k<8><<<g, blk, 0, ctx->stream>>>((unsigned long long *)so.dev, (const unsigned long long *)in, o);
+            break;
         }
+    } else if (h->scaled && eb <= 2) {
+        const size_t nt = (size_t)1 << (8 * eb);
+        void *tab = nullptr;
+        st = dalloc(ctx, &tab, nt * ob);
+        if (st != QSM_OK) {
+            stage_out(ctx, si, false);
+            stage_out(ctx, so, false);
+            return st;
+        }
+#define QSM_LOOKUP(S, O)                                                                                         \
+    scale_table_k<S, O><<<(unsigned)((nt + 255) / 256), 256, 0, ctx->stream>>>((O *)tab, h->scl_slope,          \
+                                                                             h->scl_inter, to_single);        \
+    lookup_k<S, O><<<g, blk, 0, ctx->stream>>>((O *)so.dev, (const S *)in, (const O *)tab, o);
+#define QSM_LOOKUP2(S)                                                                                           \
+    if (out_datatype == 64) { QSM_LOOKUP(S, double) } else { QSM_LOOKUP(S, float) }
+        switch (sdt) {
+        case 2: QSM_LOOKUP2(uint8_t) break;
+        case 256: QSM_LOOKUP2(int8_t) break;
+        case 4: QSM_LOOKUP2(int16_t) break;
+        default: QSM_LOOKUP2(uint16_t) break;
+        }
+#undef QSM_LOOKUP2
+#undef QSM_LOOKUP
+        dfree(ctx, tab);
     } else {
 #define QSM_CONVERT(S)                                                                                           \
     if (out_datatype == 64)                                                                                      \
-        convert_k<S, double><<<g, 256, 0, ctx->stream>>>((double *)so.dev, in, o, h->scaled, h->scl_slope,       \
-                                                         h->scl_inter, to_single);                               \
+        convert_k<S, double><<<g, blk, 0, ctx->stream>>>((double *)so.dev, (const S *)in, o, h->scaled,          \
+                                                         h->scl_slope, h->scl_inter, to_single);                 \
     else                                                                                                         \
-        convert_k<S, float><<<g, 256, 0, ctx->stream>>>((float *)so.dev, in, o, h->scaled, h->scl_slope,         \
-                                                        h->scl_inter, to_single);
+        convert_k<S, float><<<g, blk, 0, ctx->stream>>>((float *)so.dev, (const S *)in, o, h->scaled,            \
+                                                        h->scl_slope, h->scl_inter, to_single);
         switch (sdt) {
         case 2: QSM_CONVERT(uint8_t) break;
         case 256: QSM_CONVERT(int8_t) break;

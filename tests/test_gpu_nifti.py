@@ -103,3 +103,19 @@ def test_file_round_trips(qn, nio, tmp_path):
     assert torch.equal(back.img, dev)
     with pytest.raises(ValueError, match="extension"):
         qn.loadNii(str(tmp_path / "pair" / "chi.hdr"))
+
+
+def test_misaligned_device_payload_is_rejected(qn, nio):
+    """Whole-word loads need an aligned payload: a device buffer at an odd byte
+    offset is refused before any launch."""
+    torch = pytest.importorskip("torch")
+    from qsm_gb300 import _lib
+    hb = build_header("<", datatype=4)
+    pl = _payload(nio, 4, 6 * 5 * 4, "<", 1)
+    buf = torch.zeros(len(pl) + 1, dtype=torch.uint8, device="cuda")
+    buf[1:] = torch.from_numpy(np.frombuffer(pl, np.uint8).copy()).cuda()
+    with pytest.raises(_lib.QsmError, match="aligned"):
+        qn.decode(hb, buf[1:])
+    img, _ = qn.decode(hb, buf[1:].clone())
+    ref, _ = nio.load_nii(hb, pl)
+    assert np.array_equal(img, ref)
