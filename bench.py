@@ -64,6 +64,23 @@ def _dist():
     return ws, rank, local
 
 
+def max_over_ranks(x: float, dist=None, device="cpu") -> float:
+    """The largest x over all ranks, returned on every rank (x itself without a
+    process group): the step time a multi-replica run reports."""
+    if dist is None:
+        return float(x)
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, world_size: int, seconds: float) -> float:
+    """Units all replicas processed per second of the slowest replica (weak scaling)."""
+    return world_size * units_per_rank / seconds
+
+
 def _peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -561,12 +578,7 @@ def run_ours(args):
             out = fn()
         e1.record(stream)
         barrier()
-        ms = e0.elapsed_time(e1)
-        if dist is not None:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms, out
+        return max_over_ranks(e0.elapsed_time(e1), dist, "cuda"), out
 
     info = {}
 
@@ -578,7 +590,7 @@ def run_ours(args):
     with ClockSampler(local) as clk:
         ms, chi_mixed = timed(mixed_step, args.steps)
     loop_s = info["seconds"]
-    value = ws * N * ITERS * args.steps / (ms * 1e-3)
+    value = whole_job_rate(N * ITERS * args.steps, ws, ms * 1e-3)
     if args.only == "fused":
         if rank == 0:
             print(json.dumps({"profile_run": True, "value": value, "unit": "voxel-iter/s", "shape": list(d2f.shape),
@@ -601,7 +613,7 @@ def run_ours(args):
 
     plain_step()
     ms64, chi64 = timed(plain_step, max(1, min(2, args.steps)))
-    value64 = ws * N * ITERS * max(1, min(2, args.steps)) / (ms64 * 1e-3)
+    value64 = whole_job_rate(N * ITERS * max(1, min(2, args.steps)), ws, ms64 * 1e-3)
     rel = float(torch.linalg.vector_norm(chi_mixed - chi64) / torch.linalg.vector_norm(chi64))
 
     # end to end through the C ABI with pinned host buffers
@@ -622,12 +634,8 @@ def run_ours(args):
     for _ in range(args.steps):
         e2e_step()
     barrier()
-    e2e_s = time.perf_counter() - t0
-    if dist is not None:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = ws * N * ITERS * args.steps / e2e_s
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist, "cuda")
+    e2e_value = whole_job_rate(N * ITERS * args.steps, ws, e2e_s)
 
     poisson = None if args.no_poisson else poisson_arm(qsm_gb300, ctx, torch)
     batch = None if args.no_batch else batch_arm(qsm_gb300, ctx, torch)
