@@ -500,14 +500,17 @@ typedef struct {
  * and the header side of load_nii_img.m / xform_nii.m.  tolerance <= 0 means eps
  * (load_nii's default is 0.1); preferred_form 's', 'q', 'S' or 'Q' as in
  * load_nii.m ('s': sform, else qform).  Host only; no context.  A bad header
- * returns QSM_ERR_ARG or QSM_ERR_DTYPE with hdr->error set. */
+ * returns QSM_ERR_ARG or QSM_ERR_DTYPE with hdr->error set; images over 2^40
+ * elements are QSM_ERR_DIMS. */
 qsm_status qsm_nifti_parse(const void *header, size_t nbytes, double tolerance, char preferred_form,
                            qsm_nifti_hdr *hdr);
 /* Bytes of the stored image: prod(stored_dim[1..7]) * bitpix / 8. */
 size_t qsm_nifti_payload_bytes(const qsm_nifti_hdr *hdr);
 /* img (host or device, prod(dim[1..7]) elements, MATLAB order of hdr->dim) = the
  * loaded image of the stored bytes `payload` (host or device, starting at the first
- * voxel): byte order, scaling, flips and permutation in one device pass.
+ * voxel, at least qsm_nifti_payload_bytes(hdr) bytes; device buffers aligned to
+ * their element sizes): byte order, scaling, flips and permutation in one device
+ * pass.
  * out_datatype 0 gives the loaded class (hdr->datatype); 16 / 64 convert to
  * single / double.  Bit, complex and RGB datatypes are QSM_ERR_DTYPE. */
 qsm_status qsm_nifti_decode(qsm_ctx *ctx, const qsm_nifti_hdr *hdr, const void *payload,

@@ -371,6 +371,12 @@ qsm_status qsm_nifti_parse(const void *bytes, size_t nbytes, double tolerance, c
     h->bitpix = bitpix_of(h->stored_datatype);
     if (!h->bitpix) return fail(h, QSM_ERR_DTYPE, "datatype %d is not supported", h->stored_datatype);
     for (int i = 0; i < 8; ++i) h->stored_dim[i] = dim[i] < 1 ? 1 : dim[i];
+    {
+        // seven int16 sizes can multiply past any buffer: refuse images over 2^40 elements
+        double n = 1.0;
+        for (int i = 1; i < 8; ++i) n *= (double)h->stored_dim[i];
+        if (n > 1099511627776.0) return fail(h, QSM_ERR_DIMS, "image of %.3g elements is too large", n);
+    }
     h->vox_offset = h->filetype == 2 ? (int64_t)h->vox_offset_stored : 0;
     h->datatype = h->stored_datatype;
 

@@ -148,3 +148,10 @@ def test_restatement_round_trip_and_layout(nio):
     assert struct.unpack_from("<8h", raw, 40) == (3, 4, 3, 2, 1, 1, 1, 1)
     with pytest.raises(ValueError):
         nio.make_header(np.zeros((2, 2, 2), bool))
+
+
+def test_oversized_dims_are_refused(qn):
+    from qsm_gb300 import _lib
+    hb = build_header("<", dim=(7, 32767, 32767, 32767, 32767, 2, 2, 2))
+    with pytest.raises(_lib.QsmError, match="too large"):
+        qn.parse_header(hb)
