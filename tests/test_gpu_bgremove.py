@@ -138,3 +138,41 @@ def test_pdf_fp32(gpu_ctx, qsm, bg):
     rfl = bg.pdf(f, m, [1, 1, 1], maxit=40)
     fl = qsm.pdf(f.astype(np.float32), m, [1, 1, 1], maxit=40)
     assert fl.dtype == np.float32 and _rel(fl, rfl) <= 1e-3
+
+
+def test_krylov_fp32(gpu_ctx, qsm, bg):
+    """FP32 iSMV and RESHARP (per-thread compensated FP32 sums, FP64 across threads)
+    against the FP64 restatement."""
+    f, m = _case((40, 36, 32), 8)
+    f32 = f.astype(np.float32)
+    rfl, rmo = bg.ismv(f, m, [1, 1, 1], 3.0, 1e-4, 100)
+    fl, mo = qsm.ismv(f32, m, [1, 1, 1], 3.0, 1e-4, 100)
+    assert fl.dtype == np.float32 and np.array_equal(mo, rmo) and _rel(fl, rfl) <= 1e-3
+    rfl, rmo = bg.resharp(f, m, [1, 1, 1], 3.0, 1e-2, 1e-4, 50)
+    fl, mo = qsm.resharp(f32, m, [1, 1, 1], 3.0, 1e-2, 1e-4, 50)
+    assert np.array_equal(mo, rmo) and _rel(fl, rfl) <= 1e-3
+
+
+def test_device_tensors_4d(gpu_ctx, qsm, bg):
+    """Echoes as a CUDA tensor (torch shape = MATLAB size reversed) give the host result."""
+    torch = pytest.importorskip("torch")
+    f, m = _case((36, 32, 28), 9, echoes=2)
+    fd = torch.from_numpy(np.ascontiguousarray(np.transpose(f, (3, 2, 1, 0)))).cuda()
+    md = torch.from_numpy(np.ascontiguousarray(m.T)).cuda()
+    fl, mo = qsm.vsharp(fd, md, [1, 1, 1], [5.0, 3.0], 0.05)
+    hfl, hmo = qsm.vsharp(f, m, [1, 1, 1], [5.0, 3.0], 0.05)
+    assert np.array_equal(fl.cpu().numpy().transpose(3, 2, 1, 0), hfl)
+    assert np.array_equal(mo.cpu().numpy().T, hmo)
+    pl = qsm.pdf(fd, md, [1, 1, 1], maxit=10)
+    assert np.array_equal(pl.cpu().numpy().transpose(3, 2, 1, 0), qsm.pdf(f, m, [1, 1, 1], maxit=10))
+
+
+def test_pdf_errors(gpu_ctx, qsm):
+    f = np.zeros((10, 10, 10), order="F")
+    m = np.ones((10, 10, 10), np.uint8)
+    with pytest.raises(qsm.QsmError, match="ARG"):
+        qsm.pdf(f, m, [1, 1, 1], bdir=[0, 0, 0])
+    with pytest.raises(qsm.QsmError, match="ARG"):
+        qsm.pdf(f, m, [1, 0, 1])
+    with pytest.raises(ValueError):
+        qsm.pdf(f, m, [1, 1, 1], w=np.ones((5, 5, 5)))
