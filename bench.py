@@ -6,7 +6,8 @@ lam = 0.003, alpha = 2, 1000 iterations, tol = 0 (every step runs all 1000
 iterations).  Synthetic, seeded (qsm_gb300.synthetic.config2).
 
 Arms (JSON line on rank 0):
-  value         mixed-precision fused path (FP32 stencils, FP64 monitors),
+  value         mixed-precision fused path (FP32 stencils, monitors summed in
+                compensated FP32 per thread and FP64 across threads),
                 inputs resident in HBM, voxel-iterations per second over all
                 ranks; every step allocates/initialises its solver state and
                 runs the 1000 iterations; the ~1 GB working set exceeds L2.
@@ -237,7 +238,7 @@ def _batch_case(b, shape):
 def batch_arm(qsm_gb300, ctx, torch, count=32, iters=500):
     """Batched TV: 32 volumes of uneven size (each axis from {96..256} x
     {96..256} x {64..176} in steps of 16), lam 1e-3, 500 iterations each,
-    FP32 stencils with FP64 monitors, all volumes in one persistent launch
+    FP32 stencils, FP64-folded monitors, all volumes in one persistent launch
     per tile shape and iteration replayed from a captured CUDA graph.  The
     tile shape per grid size comes from the autotuner (a short batch of the
     same sizes runs first and fills its table).  Against: the same volumes
@@ -650,7 +651,7 @@ def run_ours(args):
     line = {
         "metric": METRIC, "value": value, "unit": "voxel-iter/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 (FP64 monitors)", "data": "synthetic",
+        "vs_baseline": None, "dtype": "f32 (FP64-folded monitors)", "data": "synthetic",
         "config": {"workload": WORKLOAD, "volume": [224, 224, 128], "iterations": ITERS, "lam": LAM, "alpha": ALPHA,
                    "l2": "inputs larger than L2 (solver state ~0.93 GB per volume)", "parallelism": f"replicas x{ws}"},
         "fp64_plain": {"value": value64, "unit": "voxel-iter/s", "ms_per_step": ms64 / max(1, min(2, args.steps))},

@@ -104,8 +104,9 @@ qsm_status qsm_pd_tv(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3],
 
 /* Mixed-precision fused variants of the two gateways above (same arguments
  * and meaning).  The stencil arithmetic runs in FP32 inside one fused
- * dual+primal(+extragradient) kernel per iteration; convergence monitors
- * accumulate in FP64.  Per voxel it evaluates the reference's FP32
+ * dual+primal(+extragradient) kernel per iteration; the convergence
+ * monitors' per-voxel terms are summed per thread in compensated FP32 and
+ * across threads in FP64.  Per voxel it evaluates the reference's FP32
  * expressions (pd_tgv_mex.c:332-485, :659-812) without fused multiply-add,
  * so chi equals the reference's own single-precision result (mx_pdf).
  * dtype gives the type of d2f/chi in memory (F64 inputs are rounded to

@@ -152,7 +152,7 @@ def pd_tgv_mex(d2f, mask, vsz, lam, alpha, tol, maxiter, verbose=0, *, fused=Fal
     """chi = pd_tgv_mex(d2f, mask, vsz, lam, alpha, tol, maxiter, verbose).
 
     fused=False: plain path, bit-identical to the reference in d2f's dtype.
-    fused=True: mixed-precision fused FP32 kernel with FP64 monitors (chi
+    fused=True: mixed-precision fused FP32 kernel, monitors folded in FP64 (chi
     equals the reference's FP32 result; FP64 input is rounded, output widened).
     out: optional preallocated result (same kind, shape and dtype as d2f).
     """

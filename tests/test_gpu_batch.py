@@ -51,7 +51,7 @@ def test_batch_matches_oracle_every_variant(gpu_ctx, qsm, port, variant, launch,
 
 def test_batch_equals_alone_autotuned(gpu_ctx, qsm, monkeypatch):
     """Tile shapes from the autotuner (tuned per grid size at admission): each
-    volume's chi and FP64 monitors equal its one-volume fused solve."""
+    volume's chi and monitors equal its one-volume fused solve."""
     monkeypatch.delenv("QSM_FUSED_VARIANT", raising=False)
     shapes = [(61, 39, 33), (45, 58, 27), (50, 50, 50), (33, 29, 64)]
     cases = [_case(s, 200 + k) for k, s in enumerate(shapes)]
