@@ -44,6 +44,8 @@ constexpr int TV_BLOCK = 256;
 // in FP32 (<= 51 registers), 3 in FP64 (<= 85 registers).
 template <typename T> struct TvOcc { static constexpr int minb = sizeof(T) == 4 ? 5 : 3; };
 template <typename T> constexpr int tv_grid() { return 152 * TvOcc<T>::minb; }
+// grad_shrink_k needs more registers in FP32 (it spills at 48): 4 blocks per SM
+template <typename T> struct TvOccGS { static constexpr int minb = sizeof(T) == 4 ? 4 : 3; };
 constexpr int TV_GRID_MAX = 152 * 5;
 constexpr int TV_NSUM = 5;         // nr, na, nb, ||s||^2, ||rho grad' l||^2
 
@@ -221,7 +223,7 @@ __device__ __forceinline__ void block_sums(double *part, double (&acc)[NS])
 // grad, over-relaxation, shrinkage, multiplier update and the primal
 // residual sums of one ADMM iteration (tv.m:185-221, :227-234)
 template <typename T, bool ISO>
-__global__ void __launch_bounds__(TV_BLOCK, TvOcc<T>::minb)
+__global__ void __launch_bounds__(TV_BLOCK, TvOccGS<T>::minb)
 grad_shrink_k(T *vn, const T *__restrict__ vo, T *lm, const T *__restrict__ u, Dims d, T hx, T hy, T hz, T alpha,
               T rho, T irho, double *part)
 {
@@ -317,24 +319,32 @@ grad_init_k(T *v, const T *__restrict__ u, Dims d, T hx, T hy, T hz, double *par
     block_sums<1>(part, acc);
 }
 
-// fold the block partials of `ns` sums in a fixed order: thread t adds partials
-// t, t + 256, ... in turn, then a shared-memory tree (one block of 256 threads)
-__global__ void __launch_bounds__(TV_BLOCK) fold_k(double *out, const double *__restrict__ part, int ns, int nblk)
+// fold block partials in a fixed order: sums 0..ns1-1 have nblk1 partials
+// each (at part), sums ns1..ns1+ns2-1 have nblk2 each (after them); thread t
+// adds partials t, t + 256, ... of every sum in turn, then one shared-memory
+// tree over all sums together (one block of 256 threads)
+__global__ void __launch_bounds__(TV_BLOCK) fold_k(double *out, const double *__restrict__ part, int ns1, int nblk1,
+                                                   int ns2, int nblk2)
 {
-    __shared__ double red[TV_BLOCK];
-    const int t = threadIdx.x;
-    for (int q = 0; q < ns; ++q) {
+    __shared__ double red[TV_NSUM][TV_BLOCK];
+    const int t = threadIdx.x, ns = ns1 + ns2;
+    for (int q = 0; q < TV_NSUM; ++q) {
         double s = 0.0;
-        for (int b = t; b < nblk; b += TV_BLOCK) s += part[q * nblk + b];
-        red[t] = s;
-        __syncthreads();
-        for (int h = TV_BLOCK / 2; h > 0; h >>= 1) {
-            if (t < h) red[t] += red[t + h];
-            __syncthreads();
+        if (q < ns) {
+            const double *p = q < ns1 ? part + q * nblk1 : part + ns1 * nblk1 + (q - ns1) * nblk2;
+            const int nb = q < ns1 ? nblk1 : nblk2;
+            for (int b = t; b < nb; b += TV_BLOCK) s += p[b];
         }
-        if (t == 0) out[q] = red[0];
+        red[q][t] = s;
+    }
+    __syncthreads();
+    for (int h = TV_BLOCK / 2; h > 0; h >>= 1) {
+        if (t < h)
+#pragma unroll
+            for (int q = 0; q < TV_NSUM; ++q) red[q][t] += red[q][t + h];
         __syncthreads();
     }
+    if (t < ns) out[t] = red[t][0];
 }
 
 template <typename T, typename S>
@@ -441,8 +451,8 @@ static qsm_status tv_run(qsm_ctx *ctx, const Dims &d, const S *f, const uint8_t 
     }
     K.mu = o.mu;
     const T ihx = (T)(1.0 / h[0]), ihy = (T)(1.0 / h[1]), ihz = (T)(1.0 / h[2]);
-    const int TV_GRID = tv_grid<T>();
-    const dim3 g(TV_GRID), b(TV_BLOCK);
+    const int TV_GRID = tv_grid<T>(), GS_GRID = 152 * TvOccGS<T>::minb;
+    const dim3 g(TV_GRID), gs(GS_GRID), b(TV_BLOCK);
     const unsigned gk = (unsigned)std::min<size_t>((nh + TV_BLOCK - 1) / TV_BLOCK, (size_t)TV_GRID);
 
     QSM_STEP(cuda_st(ctx, cudaMemsetAsync(lm, 0, 3 * N * sizeof(T), ctx->stream), "memset"));
@@ -464,7 +474,7 @@ static qsm_status tv_run(qsm_ctx *ctx, const Dims &d, const S *f, const uint8_t 
     if (sizeof(T) == 8) QSM_FFT(cufftExecD2Z(pf, (cufftDoubleReal *)u, (cufftDoubleComplex *)fhat));
     else QSM_FFT(cufftExecR2C(pf, (cufftReal *)u, (cufftComplex *)fhat));
     grad_init_k<T><<<g, b, 0, ctx->stream>>>(v[0], u, d, ihx, ihy, ihz, part);
-    fold_k<<<1, TV_BLOCK, 0, ctx->stream>>>(sums, part, 1, TV_GRID);
+    fold_k<<<1, TV_BLOCK, 0, ctx->stream>>>(sums, part, 1, TV_GRID, 0, 0);
     QSM_STEP(cuda_st(ctx, cudaMemcpyAsync(hs, sums, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "copy"));
     QSM_STEP(cuda_st(ctx, cudaStreamSynchronize(ctx->stream), "sync"));
     nr = hs[0];
@@ -482,13 +492,13 @@ static qsm_status tv_run(qsm_ctx *ctx, const Dims &d, const S *f, const uint8_t 
         else QSM_FFT(cufftExecC2R(pi, (cufftComplex *)R, (cufftReal *)u));
         // v-subproblem, multipliers, residuals
         if (o.tv == 1)
-            grad_shrink_k<T, false><<<g, b, 0, ctx->stream>>>(v[nxt], v[cur], lm, u, d, ihx, ihy, ihz, (T)o.alpha,
+            grad_shrink_k<T, false><<<gs, b, 0, ctx->stream>>>(v[nxt], v[cur], lm, u, d, ihx, ihy, ihz, (T)o.alpha,
                                                               (T)rho, (T)irho, part);
         else
-            grad_shrink_k<T, true><<<g, b, 0, ctx->stream>>>(v[nxt], v[cur], lm, u, d, ihx, ihy, ihz, (T)o.alpha,
+            grad_shrink_k<T, true><<<gs, b, 0, ctx->stream>>>(v[nxt], v[cur], lm, u, d, ihx, ihy, ihz, (T)o.alpha,
                                                              (T)rho, (T)irho, part);
-        adj_norms_k<T><<<g, b, 0, ctx->stream>>>(v[nxt], v[cur], lm, d, -ihx, -ihy, -ihz, (T)rho, part + 3 * TV_GRID);
-        fold_k<<<1, TV_BLOCK, 0, ctx->stream>>>(sums, part, TV_NSUM, TV_GRID);
+        adj_norms_k<T><<<g, b, 0, ctx->stream>>>(v[nxt], v[cur], lm, d, -ihx, -ihy, -ihz, (T)rho, part + 3 * GS_GRID);
+        fold_k<<<1, TV_BLOCK, 0, ctx->stream>>>(sums, part, 3, GS_GRID, 2, TV_GRID);
         QSM_STEP(cuda_st(ctx, cudaGetLastError(), "launch"));
         QSM_STEP(cuda_st(ctx, cudaMemcpyAsync(hs, sums, TV_NSUM * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "copy"));
         QSM_STEP(cuda_st(ctx, cudaStreamSynchronize(ctx->stream), "sync"));
