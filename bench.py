@@ -503,6 +503,10 @@ def serve_arm(qsm_gb300, ctx, seconds=30.0, rate=4.0, per_kind=6, budget=160 * 1
         "max_resident": loop.max_resident, "max_queue": loop.max_queue, "steps": loop.steps,
         "same_alone_vs_mix": not mism, "mismatches": mism[:10],
         "rel_l2_vs_fp64_max": {k: (max(v) if v else None) for k, v in err.items()},
+        "slowest": [{"kind": r.kind, "shape": list(r.shape), "arrive_s": round(r.t_arrive, 3),
+                     "queue_ms": round(1e3 * (r.t_admit - r.t_arrive), 1),
+                     "service_ms": round(1e3 * (r.t_done - r.t_admit), 1)}
+                    for r in sorted(recs, key=lambda r: -r.latency)[:6]],
         "input_generation_s": gen_s})
     return summ
 
