@@ -142,15 +142,33 @@ def loadNii(filename, **kw) -> Nii:  # noqa: N802 (the MATLAB name)
     return load_nii(fn, **kw)
 
 
+def _torch_layout(img):
+    """MATLAB size of a CUDA tensor that is C-contiguous (torch shape = MATLAB size
+    reversed) or F-contiguous (torch shape = MATLAB size), as the rest of the
+    package reads tensors; either way its memory is in MATLAB order."""
+    shp = tuple(img.shape)
+    if img.is_contiguous():
+        return list(reversed(shp))
+    exp, acc = [], 1
+    for n in shp:
+        exp.append(acc)
+        acc *= n
+    if list(img.stride()) != exp:
+        raise ValueError("tensor must be contiguous in C or Fortran order")
+    return list(shp)
+
+
 def header_bytes(img, vsz=(1.0, 1.0, 1.0), filetype=2, *, ctx=None) -> bytes:
     """The header save_nii writes for make_nii(img, vsz) (img: numpy or CUDA tensor)."""
     if hasattr(img, "data_ptr"):
         import torch
 
-        npdt = {torch.float32: np.float32, torch.float64: np.float64, torch.uint8: np.uint8, torch.int8: np.int8,
-                torch.int16: np.int16, torch.int32: np.int32}[img.dtype]
-        dt = _CLASS[np.dtype(npdt)]
-        size = list(reversed(img.shape)) if img.is_contiguous() else list(img.shape)
+        tdt = {torch.float32: np.float32, torch.float64: np.float64, torch.uint8: np.uint8, torch.int8: np.int8,
+               torch.int16: np.int16, torch.int32: np.int32}
+        if img.dtype not in tdt:
+            raise TypeError("Datatype is not supported by make_nii.")
+        dt = _CLASS[np.dtype(tdt[img.dtype])]
+        size = _torch_layout(img)
         ptr = ctypes.c_void_p(img.data_ptr())
         torch.cuda.current_stream().synchronize()
     else:
@@ -189,7 +207,8 @@ def save_nii(img, filename, vsz=(1.0, 1.0, 1.0), *, ctx=None):
     pair = not base.endswith(".nii")
     hdr = header_bytes(body_src, vsz, 1 if pair else 2, ctx=ctx)
     if arr is None:
-        body = img.detach().cpu().numpy().tobytes()  # C order of the reversed shape = MATLAB order
+        _torch_layout(img)  # C- or F-contiguous: either way its memory order is MATLAB order
+        body = img.detach().cpu().numpy().tobytes(order="A")
     else:
         body = arr.tobytes(order="F")
     w = (lambda p, b: open(p, "wb").write(gzip.compress(b))) if gz else (lambda p, b: open(p, "wb").write(b))

@@ -119,3 +119,15 @@ def test_misaligned_device_payload_is_rejected(qn, nio):
     img, _ = qn.decode(hb, buf[1:].clone())
     ref, _ = nio.load_nii(hb, pl)
     assert np.array_equal(img, ref)
+
+
+def test_fortran_ordered_tensor_saves_in_matlab_order(qn, nio, tmp_path):
+    torch = pytest.importorskip("torch")
+    chi = np.asfortranarray(np.random.default_rng(8).standard_normal((12, 10, 8)).astype(np.float32))
+    f_tensor = torch.from_numpy(np.ascontiguousarray(chi.T)).cuda().T   # F-contiguous, shape = MATLAB size
+    c_tensor = torch.from_numpy(np.ascontiguousarray(chi.T)).cuda()     # C-contiguous, shape reversed
+    for t, name in ((f_tensor, "f.nii"), (c_tensor, "c.nii")):
+        qn.saveNii(str(tmp_path / name), t, [1, 1, 1])
+        assert open(tmp_path / name, "rb").read() == nio.save_bytes(chi, [1, 1, 1])
+    with pytest.raises(ValueError, match="contiguous"):
+        qn.header_bytes(torch.zeros((6, 6, 6), device="cuda")[:, ::2, :])
