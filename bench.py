@@ -38,6 +38,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import struct
 import subprocess
 import sys
 import threading
@@ -313,7 +314,6 @@ def nifti_part(qsm_gb300, ctx, torch, f4, mask, peak, cpu):
     n = int(np.prod(shape))
     raw = np.clip(np.round(f4 / np.abs(f4).max() * 32000), -32768, 32767).astype(np.int16)
     b = bytearray(qn.header_bytes(raw.astype(np.float32), (1, 1, 1), ctx=ctx))
-    import struct
     struct.pack_into("<hh", b, 70, 4, 16)                    # int16
     struct.pack_into("<ff", b, 112, float(np.abs(f4).max() / 32000), 0.0)  # scl_slope, scl_inter
     struct.pack_into("<12f", b, 280, -1, 0, 0, 224, 0, -1, 0, 224, 0, 0, 1, 0)  # LPS sform
