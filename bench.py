@@ -53,9 +53,10 @@ METRIC = "TGV voxel-iter/s & HBM GB/s, mixed vs FP64 GPU at ≤1e-4 rel err; ser
 ITERS = 1000
 LAM, ALPHA = 0.003, 2.0
 ALG_BYTES_FP32 = 166  # algorithmic bytes per voxel-iteration of fused FP32 TGV
-# DRAM bytes (read + write) per launch of the fused kernel on the headline workload, from
-# one ncu capture (profiles/tgv_224x224x128_launch_list.md); None for other shapes
-NCU_TRAFFIC_224x224x128 = 272.5e6
+# DRAM bytes (read + write) per launch of the fused kernel on the headline workload, by
+# tile (tx, ty, z-chunk), from one ncu capture each (profiles/tgv_224x224x128_launch_list.md);
+# None for other shapes and tiles
+NCU_TRAFFIC_224x224x128 = {(28, 12, 16): 272.5e6, (28, 16, 16): 276.5e6}
 WORKLOAD = "TGV-QSM 224x224x128, 1 mm isotropic, B0 along z, 1000 iterations, tol 0"
 
 
@@ -661,9 +662,11 @@ def run_ours(args):
         "fp64_plain": {"value": value64, "unit": "voxel-iter/s", "ms_per_step": ms64 / max(1, min(2, args.steps))},
         "speedup_vs_fp64": value / value64, "rel_l2_vs_fp64": rel,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": (NCU_TRAFFIC_224x224x128 / 1e9 if not args.shape else None),
+                     "traffic": (NCU_TRAFFIC_224x224x128[tuple(info["tile"])] / 1e9
+                                 if not args.shape and tuple(info["tile"]) in NCU_TRAFFIC_224x224x128 else None),
                      "traffic_unit": "GB per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
-                     "kernel": "stream_k<28,12,TGV>" if info["tile"][0] == 28 else "tgv_fused_k<%d,%d,%d>" % tuple(info["tile"]),
+                     "kernel": ("stream_k<%d,%d,TGV> z-chunk %d" if info["tile"][0] == 28 else "tgv_fused_k<%d,%d,%d>")
+                               % tuple(info["tile"]),
                      "bytes_per_voxel_iter": ALG_BYTES_FP32,
                      "avg_launch_us": t_launch * 1e6, "peak_source": peak_kind, "active_voxels": active,
                      "tile": list(info["tile"]),

@@ -177,6 +177,8 @@ static BatchKernel batch_kernel(int v, bool tgv)
     case 1: return tgv ? tile_kernel<32, 8, 2, 4, true>() : tile_kernel<32, 8, 2, 4, false>();
     case 2: return tgv ? tile_kernel<32, 4, 4, 8, true>() : tile_kernel<32, 4, 4, 8, false>();
     case 3: return tgv ? tile_kernel<32, 16, 2, 2, true>() : tile_kernel<32, 16, 2, 2, false>();
+    case 8:
+    case 9: return tgv ? column_kernel<28, 16, true>() : column_kernel<28, 16, false>();
     default: return tgv ? column_kernel<28, 12, true>() : column_kernel<28, 12, false>();
     }
 }

@@ -40,6 +40,7 @@ static qsm_status set_t(qsm_ctx *ctx)
 qsm_status stream_set_smem(qsm_ctx *ctx)
 {
     QSM_TRY((set_t<28, 12>(ctx)));
+    QSM_TRY((set_t<28, 16>(ctx)));
     return QSM_OK;
 }
 
@@ -63,6 +64,7 @@ qsm_status stream_launch(qsm_ctx *ctx, cudaStream_t st, int tx, int ty, int cz, 
                          double tol, uint32_t it)
 {
     if (tx == 28 && ty == 12) launch_t<28, 12>(st, tgv, chk, nact, s, dc, pc, d, cz, tol, it);
+    else if (tx == 28 && ty == 16) launch_t<28, 16>(st, tgv, chk, nact, s, dc, pc, d, cz, tol, it);
     else return QSM_ERR_ARG;
     QSM_CUDA(cudaGetLastError());
     return QSM_OK;

@@ -121,9 +121,9 @@ def test_pd_errors(gpu_ctx, qsm):
 
 
 @pytest.mark.parametrize("shape", [(77, 41, 23), (70, 30, 75)])
-@pytest.mark.parametrize("variant", list(range(8)))
+@pytest.mark.parametrize("variant", list(range(10)))
 def test_fused_tile_variants_bitexact(gpu_ctx, qsm, port, variant, shape, monkeypatch):
-    """Every compiled tile shape (3-D tiles 0-3, z-streaming column tiles 4-7)
+    """Every compiled tile shape (3-D tiles 0-3, z-streaming column tiles 4-9)
     gives the reference's FP32 result (partial tiles and chunks, odd extents,
     a mask that leaves whole tiles inactive)."""
     monkeypatch.setenv("QSM_FUSED_VARIANT", str(variant))
@@ -137,7 +137,9 @@ def test_fused_tile_variants_bitexact(gpu_ctx, qsm, port, variant, shape, monkey
     a = qsm.pd_tgv_mex(d2f, m, [1, 1, 1], 0.003, 2.0, 0.0, 30, fused=True, info=info)
     b = port.pd_tgv_mex(d2f, m, [1, 1, 1], 0.003, 2.0, 0.0, 30)
     assert bits_equal(a, b), first_diff(a, b)
-    assert info["active_voxels"] < (shape[0] - 2) * (shape[1] - 2) * (shape[2] - 2)  # inactive tiles skipped
+    interior = (shape[0] - 2) * (shape[1] - 2) * (shape[2] - 2)
+    if 8 * int(np.prod(info["tile"])) <= interior:  # small tiles: some miss the mask and are skipped
+        assert info["active_voxels"] < interior
     a = qsm.pd_tv_mex(d2f, m, [1, 1, 1], 0.003, 0.0, 30, fused=True)
     b = port.pd_tv_mex(d2f, m, [1, 1, 1], 0.003, 0.0, 30)
     assert bits_equal(a, b), first_diff(a, b)
