@@ -124,7 +124,7 @@ def test_misaligned_device_payload_is_rejected(qn, nio):
 def test_fortran_ordered_tensor_saves_in_matlab_order(qn, nio, tmp_path):
     torch = pytest.importorskip("torch")
     chi = np.asfortranarray(np.random.default_rng(8).standard_normal((12, 10, 8)).astype(np.float32))
-    f_tensor = torch.from_numpy(np.ascontiguousarray(chi.T)).cuda().T   # F-contiguous, shape = MATLAB size
+    f_tensor = torch.from_numpy(np.ascontiguousarray(chi.T)).cuda().permute(2, 1, 0)  # F-contiguous, MATLAB size
     c_tensor = torch.from_numpy(np.ascontiguousarray(chi.T)).cuda()     # C-contiguous, shape reversed
     for t, name in ((f_tensor, "f.nii"), (c_tensor, "c.nii")):
         qn.saveNii(str(tmp_path / name), t, [1, 1, 1])
