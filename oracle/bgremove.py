@@ -1,6 +1,6 @@
 """CPU restatement of QSM.m's FFT background-field removal.
 
-TEST INFRASTRUCTURE ONLY: imported by tests/ as the checker of the GPU
+TEST INFRASTRUCTURE ONLY: imported by tests/ as the oracle of the GPU
 path; the product never imports it.
 
 Follows src/bgremove/sharp.m:1-84, vsharp.m:1-153, ismv.m:1-112,

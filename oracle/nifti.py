@@ -1,6 +1,6 @@
 """CPU restatement of QSM.m's NIfTI reading and writing.
 
-TEST INFRASTRUCTURE ONLY: imported by tests/ as the checker of the library's
+TEST INFRASTRUCTURE ONLY: imported by tests/ as the oracle of the library's
 NIfTI path; the product never imports it.
 
 Follows src/io/loadNii.m and saveNii.m over the NIfTI toolbox in

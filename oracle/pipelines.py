@@ -1,6 +1,6 @@
 """CPU restatement of QSM.m's MATLAB-level wrappers around the MEX gateways.
 
-TEST INFRASTRUCTURE ONLY: imported by tests/ as the checker of the GPU
+TEST INFRASTRUCTURE ONLY: imported by tests/ as the oracle of the GPU
 pipelines; the product never imports it.
 
 Follows src/utils/cropIndices.m, src/inversion/sstgv.m:1-87,

@@ -2,8 +2,8 @@
 ``oracle/qsm_oracle.c`` by ``make -C oracle``).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, ``__graft_entry__.smoke()``
-and bench.py's CPU-baseline leg as the checker.  The product never imports
-it.
+and bench.py's CPU-baseline leg as the oracle the library is compared
+against.  The product never imports it.
 
 Function names and argument order follow the QSM.m MEX gateways they
 restate (``pd_tgv_mex(d2f, mask, vsz, lam, alpha, tol, maxiter, verbose)``

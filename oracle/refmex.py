@@ -1,9 +1,9 @@
 """Run QSM.m's own C-MEX gateways (compiled by ``oracle/ref/Makefile`` into
 ``oracle/_ref/*.so``) from numpy, through the project-written mxArray runtime.
 
-TEST INFRASTRUCTURE ONLY.  This module is the checker: it is used to pin the
-C restatement in ``oracle/qsm_oracle.c`` and to generate the golden fixtures
-under ``tests/golden/``.  The product never imports it.
+TEST INFRASTRUCTURE ONLY.  It pins the C restatement in ``oracle/qsm_oracle.c``,
+generates the golden fixtures under ``tests/golden/`` and runs the library's own
+MEX shims in the tests.  The product never imports it.
 
 Arrays follow MATLAB's layout: a volume is a numpy array of shape
 ``(nx, ny, nz)`` in Fortran order (x fastest), vector fields have a trailing

@@ -1,6 +1,6 @@
 """CPU restatement of QSM.m's FFT total-variation inversion (ADMM).
 
-TEST INFRASTRUCTURE ONLY: imported by tests/ as the checker of the GPU
+TEST INFRASTRUCTURE ONLY: imported by tests/ as the oracle of the GPU
 path; the product never imports it.
 
 Follows src/inversion/tv.m (tv :1-98 defaults and echo loop, tv_ :101-277),
