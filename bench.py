@@ -309,7 +309,6 @@ def nifti_part(qsm_gb300, ctx, torch, f4, mask, peak, cpu):
     import tempfile
 
     import qsm_gb300.nifti as qn
-    import nifti as nio  # the oracle, for the CPU figure
 
     shape = f4.shape
     n = int(np.prod(shape))
@@ -351,6 +350,8 @@ def nifti_part(qsm_gb300, ctx, torch, f4, mask, peak, cpu):
         sec = (time.perf_counter() - t) / 3
         res["saveNii_e2e"] = {"seconds": sec, "voxels_per_s": x.numel() / sec}
         if cpu:
+            import nifti as nio  # the oracle, for the CPU figure only
+
             def cpu_load():
                 data = open(fn, "rb").read()
                 nio.load_nii(data[:348], data[352:])
@@ -362,12 +363,13 @@ def nifti_part(qsm_gb300, ctx, torch, f4, mask, peak, cpu):
 def next_rows_arm(qsm_gb300, ctx, torch, peak, cpu=True, parts="tv64,tv32,pdf,vsharp,sstgv,lbv,nifti"):
     """The widened rows on the 224x224x128 volume: TV ADMM (tv.m), PDF and V-SHARP
     background removal, the whole sstgv/lbv wrappers on 4 echoes, and NIfTI
-    loading / saving.  Device
-    solves run on resident tensors (the wrappers from pinned host arrays, end to
-    end); each CPU figure is the oracle on a bounded sample of the same input."""
+    loading / saving.  Device solves run on resident tensors (the wrappers from
+    host arrays, end to end); each CPU figure is the oracle on a bounded sample
+    of the same input."""
     import qsm_gb300.synthetic as S
 
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    if cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))  # the oracle, for the CPU figures
     shape = (224, 224, 128)
     n = int(np.prod(shape))
     f4, local, mask = S.field_case(shape, 7, echoes=4)
@@ -407,7 +409,8 @@ def next_rows_arm(qsm_gb300, ctx, torch, peak, cpu=True, parts="tv64,tv32,pdf,vs
                                  unit="voxel-iter/s", cores=1, kind="port", sample="2 ADMM iterations, numpy FP64")
     out["tv_admm"] = row
 
-    import bgremove
+    if cpu:
+        import bgremove  # the oracle, for the CPU figures only
     if "pdf" in parts:
         # PDF: LSMR iterations on the full grid (tol 0: every iteration runs); FP64 cuFFT bound
         it = 30
