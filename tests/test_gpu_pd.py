@@ -179,3 +179,24 @@ def test_pd_anisotropic_voxels(gpu_ctx, qsm, port, h):
             a = qsm.pd_tv_mex(d2f, m, h, 0.003, 0.0, 20, fused=fused)
             b = port.pd_tv_mex(d2f, m, h, 0.003, 0.0, 20)
             assert bits_equal(a, b), f"tv {dt} fused={fused} {first_diff(a, b)}"
+
+
+def test_fused_large_volume_matches_plain(gpu_ctx, qsm):
+    """384x384x256 (37.7 M voxels, about 9 GB of solver state): the fused FP32 solve
+    equals the plain FP32 solve (the reference's loop structure) bit for bit, so
+    offsets past 2^31 bytes and tile counts past 65535 index correctly."""
+    torch = pytest.importorskip("torch")
+    shape = (384, 384, 256)
+    g = torch.Generator(device="cuda").manual_seed(5)
+    d2f = (torch.randn(tuple(reversed(shape)), generator=g, device="cuda", dtype=torch.float32) * 0.05)
+    z, y, x = torch.meshgrid(*[torch.arange(n, device="cuda", dtype=torch.float32) for n in reversed(shape)],
+                             indexing="ij")
+    r2 = ((x - 191.5) / 170) ** 2 + ((y - 191.5) / 170) ** 2 + ((z - 127.5) / 110) ** 2
+    mask = (r2 <= 1).to(torch.uint8)
+    info = {}
+    a = qsm.pd_tgv_mex(d2f, mask, [1, 1, 1], 0.003, 2.0, 0.0, 12, fused=True, info=info)
+    b = qsm.pd_tgv_mex(d2f, mask, [1, 1, 1], 0.003, 2.0, 0.0, 12)
+    assert torch.equal(a, b)
+    a = qsm.pd_tv_mex(d2f, mask, [1, 1, 1], 0.003, 0.0, 12, fused=True)
+    b = qsm.pd_tv_mex(d2f, mask, [1, 1, 1], 0.003, 0.0, 12)
+    assert torch.equal(a, b)
