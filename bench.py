@@ -291,8 +291,10 @@ def batch_arm(qsm_gb300, ctx, torch, count=32, iters=500):
 # TV ADMM: adj_rhs 7 arrays, D2Z 16 B, kmul 24 B, Z2D 16 B, grad_shrink 13 arrays,
 # adj_norms 9 arrays; PDF/LSMR: two operator applications of 112 B (weight 3 arrays,
 # R2C 16 B, spectrum multiply 24 B, C2R 16 B, Golub-Kahan update 4 arrays), two scalings
-# of 2 arrays, the LSMR update 7 arrays
-TV_BYTES_F64, PDF_BYTES_F64 = 288, 312
+# of 2 arrays, the LSMR update 7 arrays.  FP32 anisotropic TV (the default) folds the
+# two adjoint norms into the shrinkage pass (13 arrays; no 9-array norm pass):
+# 7 x 4 + 8 + 12 + 8 + 13 x 4 = 108 B
+TV_BYTES_F64, TV_BYTES_F32, PDF_BYTES_F64 = 288, 108, 312
 
 
 def _cpu_sample(fn, iters_per_call, voxels):
@@ -398,7 +400,7 @@ def next_rows_arm(qsm_gb300, ctx, torch, peak, cpu=True, parts="tv64,tv32,pdf,vs
         l_dev = dev(local).to(dt)
         info = {}
         sec, _ = timed(lambda: qsm_gb300.tv(l_dev, m_dev, [1, 1, 1], opts=opts, info=info, ctx=ctx))
-        b = TV_BYTES_F64 * (1 if name == "f64" else 0.5)
+        b = TV_BYTES_F64 if name == "f64" else TV_BYTES_F32
         row[name] = {"value": n * it / sec, "unit": "voxel-iter/s", "seconds": sec,
                      "hbm_gbs": b * n * it / sec / 1e9, "frac": b * n * it / sec / 1e9 / peak,
                      "bytes_per_voxel_iter": b}

@@ -277,6 +277,72 @@ grad_shrink_k(T *vn, const T *__restrict__ vo, T *lm, const T *__restrict__ u, D
     block_sums<3>(part, acc);
 }
 
+// Anisotropic TV in FP32: grad_shrink_k and adj_norms_k in one pass.  Each
+// thread also evaluates, for c = x, y, z, component c of the shrinkage at its
+// backward neighbour along c -- the values the adjoint reads there -- with the
+// neighbour owner's own arithmetic (bit-identical), so the new v and l are not
+// read back; l is double-buffered (lmo in, lmn out) because neighbours read
+// the old value.
+template <typename T>
+__global__ void __launch_bounds__(TV_BLOCK, TvOccGS<T>::minb)
+grad_shrink_norms_k(T *vn, const T *__restrict__ vo, T *__restrict__ lmn, const T *__restrict__ lmo,
+                    const T *__restrict__ u, Dims d, T hx, T hy, T hz, T alpha, T rho, T irho, T nx_, T ny_, T nz_,
+                    double *part)
+{
+    const size_t N = d.n();
+    const T hh[3] = {hx, hy, hz}, ih[3] = {nx_, ny_, nz_};
+    PartialSum<T> ps[5];  // nr, na, nb, ||s||^2, ||rho grad' l||^2
+    VOX_LOOP(wk, d) {
+        const Vox &v = wk.v;
+        const size_t l = v.l;
+        const T u0 = u[l];
+        const size_t fw[3] = {v.i + 1 < (int)d.nx ? l + 1 : l - v.NX, v.j + 1 < (int)d.ny ? l + d.nx : l - v.NY,
+                              v.k + 1 < (int)d.nz ? l + d.nxny() : l - v.NZ};
+        const size_t bw[3] = {v.i > 0 ? l - 1 : l + v.NX, v.j > 0 ? l - d.nx : l + v.NY,
+                              v.k > 0 ? l - d.nxny() : l + v.NZ};
+        T e2 = 0, a2 = 0, b2 = 0, gs[3], gt[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            // own voxel (grad_shrink_k, ISO = false)
+            const T dd = hh[c] * (u[fw[c]] - u0);
+            const T vo0 = vo[c * N + l], lo0 = lmo[c * N + l];
+            const T d1 = alpha * dd + ((T)1 - alpha) * vo0;
+            const T r = d1 + irho * lo0;
+            const T mg = fabs(r) - irho;
+            const T w = (mg > (T)0 ? mg : (T)0) * (r > (T)0 ? (T)1 : r < (T)0 ? (T)-1 : (T)0);
+            const T ln = lo0 + rho * (d1 - w);
+            vn[c * N + l] = w;
+            lmn[c * N + l] = ln;
+            const T e = dd - w;
+            e2 += e * e;
+            a2 += dd * dd;
+            b2 += w * w;
+            // component c at the backward neighbour m, whose forward neighbour along c is l
+            const size_t m = bw[c];
+            const T ddm = hh[c] * (u0 - u[m]);
+            const T vom = vo[c * N + m], lom = lmo[c * N + m];
+            const T d1m = alpha * ddm + ((T)1 - alpha) * vom;
+            const T rm = d1m + irho * lom;
+            const T mgm = fabs(rm) - irho;
+            const T wm = (mgm > (T)0 ? mgm : (T)0) * (rm > (T)0 ? (T)1 : rm < (T)0 ? (T)-1 : (T)0);
+            const T lnm = lom + rho * (d1m - wm);
+            gs[c] = ih[c] * ((w - vo0) - (wm - vom));
+            gt[c] = ih[c] * (ln - lnm);
+        }
+        ps[0].add(sqrt(e2));
+        ps[1].add(sqrt(a2));
+        ps[2].add(sqrt(b2));
+        // adj_at's association order (gradfp_adj_mex.c regions)
+        const T sa = v.k == 0 ? (gs[0] + gs[1]) + gs[2] : v.j == 0 ? (gs[2] + gs[0]) + gs[1] : (gs[2] + gs[1]) + gs[0];
+        const T ta = v.k == 0 ? (gt[0] + gt[1]) + gt[2] : v.j == 0 ? (gt[2] + gt[0]) + gt[1] : (gt[2] + gt[1]) + gt[0];
+        const T sv = rho * sa, tv = rho * ta;
+        ps[3].add(sv * sv);
+        ps[4].add(tv * tv);
+    }
+    double acc[5] = {ps[0].get(), ps[1].get(), ps[2].get(), ps[3].get(), ps[4].get()};
+    block_sums<5>(part, acc);
+}
+
 // ||rho gradfp_adj(v - v_)||^2 and ||rho gradfp_adj(l)||^2 (tv.m:230, :239)
 template <typename T>
 __global__ void __launch_bounds__(TV_BLOCK, TvOcc<T>::minb)
@@ -414,7 +480,7 @@ static qsm_status tv_run(qsm_ctx *ctx, const Dims &d, const S *f, const uint8_t 
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     const size_t rb = al(N * sizeof(T)), vb = al(3 * N * sizeof(T)), cb = al(nh * sizeof(C));
     const size_t tb = al(2 * (size_t)(nxh + d.ny + d.nz) * sizeof(double)), db = al(nh * sizeof(T));
-    const size_t bytes = 2 * rb + 3 * vb + 2 * cb + tb + db + (TV_NSUM * TV_GRID_MAX + 64) * sizeof(double);
+    const size_t bytes = 2 * rb + 4 * vb + 2 * cb + tb + db + (TV_NSUM * TV_GRID_MAX + 64) * sizeof(double);
     void *blk = nullptr;
     QSM_TRY(dalloc(ctx, &blk, bytes));
     char *c = (char *)blk;
@@ -423,7 +489,10 @@ static qsm_status tv_run(qsm_ctx *ctx, const Dims &d, const S *f, const uint8_t 
     T *v[2];
     v[0] = (T *)c; c += vb;
     v[1] = (T *)c; c += vb;
-    T *lm = (T *)c; c += vb;
+    T *lmb[2];  // l, double-buffered where the fused FP32 pass reads the old value at neighbours
+    lmb[0] = (T *)c; c += vb;
+    lmb[1] = (T *)c; c += vb;
+    int lc = 0;
     C *fhat = (C *)c; c += cb;
     C *R = (C *)c; c += cb;
     double *tab = (double *)c; c += tb;
@@ -455,7 +524,7 @@ static qsm_status tv_run(qsm_ctx *ctx, const Dims &d, const S *f, const uint8_t 
     const dim3 g(TV_GRID), gs(GS_GRID), b(TV_BLOCK);
     const unsigned gk = (unsigned)std::min<size_t>((nh + TV_BLOCK - 1) / TV_BLOCK, (size_t)TV_GRID);
 
-    QSM_STEP(cuda_st(ctx, cudaMemsetAsync(lm, 0, 3 * N * sizeof(T), ctx->stream), "memset"));
+    QSM_STEP(cuda_st(ctx, cudaMemsetAsync(lmb[0], 0, 3 * N * sizeof(T), ctx->stream), "memset"));
     QSM_FFT(cufftPlan3d(&pf, (int)d.nz, (int)d.ny, (int)d.nx, tf));
     havef = true;
     QSM_FFT(cufftPlan3d(&pi, (int)d.nz, (int)d.ny, (int)d.nx, ti));
@@ -484,21 +553,30 @@ static qsm_status tv_run(qsm_ctx *ctx, const Dims &d, const S *f, const uint8_t 
         it = (uint32_t)ii;
         const int nxt = cur ^ 1;
         // u-subproblem
-        adj_rhs_k<T><<<g, b, 0, ctx->stream>>>(r, v[cur], lm, d, -ihx, -ihy, -ihz, (T)rho);
+        adj_rhs_k<T><<<g, b, 0, ctx->stream>>>(r, v[cur], lmb[lc], d, -ihx, -ihy, -ihz, (T)rho);
         if (sizeof(T) == 8) QSM_FFT(cufftExecD2Z(pf, (cufftDoubleReal *)r, (cufftDoubleComplex *)R));
         else QSM_FFT(cufftExecR2C(pf, (cufftReal *)r, (cufftComplex *)R));
         kmul_k<T><<<gk, TV_BLOCK, 0, ctx->stream>>>(R, fhat, Dq, tab, K, rho, 1.0 / (double)N);
         if (sizeof(T) == 8) QSM_FFT(cufftExecZ2D(pi, (cufftDoubleComplex *)R, (cufftDoubleReal *)u));
         else QSM_FFT(cufftExecC2R(pi, (cufftComplex *)R, (cufftReal *)u));
         // v-subproblem, multipliers, residuals
-        if (o.tv == 1)
-            grad_shrink_k<T, false><<<gs, b, 0, ctx->stream>>>(v[nxt], v[cur], lm, u, d, ihx, ihy, ihz, (T)o.alpha,
-                                                              (T)rho, (T)irho, part);
-        else
-            grad_shrink_k<T, true><<<gs, b, 0, ctx->stream>>>(v[nxt], v[cur], lm, u, d, ihx, ihy, ihz, (T)o.alpha,
-                                                             (T)rho, (T)irho, part);
-        adj_norms_k<T><<<g, b, 0, ctx->stream>>>(v[nxt], v[cur], lm, d, -ihx, -ihy, -ihz, (T)rho, part + 3 * GS_GRID);
-        fold_k<<<1, TV_BLOCK, 0, ctx->stream>>>(sums, part, 3, GS_GRID, 2, TV_GRID);
+        if (sizeof(T) == 4 && o.tv == 1) {
+            grad_shrink_norms_k<T><<<gs, b, 0, ctx->stream>>>(v[nxt], v[cur], lmb[lc ^ 1], lmb[lc], u, d, ihx, ihy,
+                                                              ihz, (T)o.alpha, (T)rho, (T)irho, -ihx, -ihy, -ihz,
+                                                              part);
+            lc ^= 1;
+            fold_k<<<1, TV_BLOCK, 0, ctx->stream>>>(sums, part, TV_NSUM, GS_GRID, 0, 0);
+        } else {
+            if (o.tv == 1)
+                grad_shrink_k<T, false><<<gs, b, 0, ctx->stream>>>(v[nxt], v[cur], lmb[lc], u, d, ihx, ihy, ihz,
+                                                                   (T)o.alpha, (T)rho, (T)irho, part);
+            else
+                grad_shrink_k<T, true><<<gs, b, 0, ctx->stream>>>(v[nxt], v[cur], lmb[lc], u, d, ihx, ihy, ihz,
+                                                                  (T)o.alpha, (T)rho, (T)irho, part);
+            adj_norms_k<T><<<g, b, 0, ctx->stream>>>(v[nxt], v[cur], lmb[lc], d, -ihx, -ihy, -ihz, (T)rho,
+                                                     part + 3 * GS_GRID);
+            fold_k<<<1, TV_BLOCK, 0, ctx->stream>>>(sums, part, 3, GS_GRID, 2, TV_GRID);
+        }
         QSM_STEP(cuda_st(ctx, cudaGetLastError(), "launch"));
         QSM_STEP(cuda_st(ctx, cudaMemcpyAsync(hs, sums, TV_NSUM * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "copy"));
         QSM_STEP(cuda_st(ctx, cudaStreamSynchronize(ctx->stream), "sync"));
