@@ -69,9 +69,12 @@ def test_tv_stops_on_tolerance(gpu_ctx, qsm, tvo):
     assert _rel(x, ref) <= 1e-9
 
 
-def test_tv_fp32(gpu_ctx, qsm, tvo):
+@pytest.mark.parametrize("mode", [1, 2])
+def test_tv_fp32(gpu_ctx, qsm, tvo, mode):
+    """FP32: anisotropic TV runs the fused shrinkage + norm pass, isotropic the
+    two-kernel path."""
     f, m = _case((40, 36, 32), 14)
-    opts = dict(maxit=12)
+    opts = dict(maxit=12, tv=mode)
     ref = tvo.tv(f, m, [1, 1, 1], opts=opts)
     x = qsm.tv(f.astype(np.float32), m, [1, 1, 1], opts=opts)
     assert x.dtype == np.float32
