@@ -160,6 +160,22 @@ def _case(shape=None):
     return d2f, mask
 
 
+def _cpu_model() -> str:
+    """Host CPU description for the baseline record (model name when the kernel gives one)."""
+    import platform
+
+    name = ""
+    try:
+        with open("/proc/cpuinfo") as fh:
+            for line in fh:
+                if line.lower().startswith(("model name", "cpu model", "hardware")):
+                    name = line.split(":", 1)[1].strip()
+                    break
+    except OSError:
+        pass
+    return f"{name or platform.processor() or 'unknown'} ({platform.machine()}, {os.cpu_count()} cores)"
+
+
 def cpu_baseline(d2f, mask, budget_s=15.0):
     """The CPU oracle (FP64, OpenMP on every host core) on a bounded sample."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -178,7 +194,7 @@ def cpu_baseline(d2f, mask, budget_s=15.0):
     port.pd_tgv_mex(d2f, mask, [1, 1, 1], LAM, ALPHA, 0.0, iters)
     dt = time.perf_counter() - t
     return {"value": n * iters / dt, "unit": "voxel-iter/s", "cores": int(os.environ.get("OMP_NUM_THREADS", cores)),
-            "kind": "port", "seconds": dt,
+            "kind": "port", "seconds": dt, "cpu": _cpu_model(),
             "sample": f"{iters} FP64 iterations of the same 224x224x128 TGV inversion (CPU oracle, OpenMP)"}
 
 
@@ -208,7 +224,13 @@ def poisson_arm(qsm_gb300, ctx, torch):
         wall = time.perf_counter() - t0
         key = "fp32_vcycle" if mixed else "fp64"
         sols[key] = v
-        out[key] = {"iters": info["iters"], "seconds": info["seconds"], "wall_s": wall, "resnorm": info["resnorm"]}
+        # algorithmic bytes per voxel and PCG iteration on the padded grid: fine V-cycle
+        # ~13.25 array passes x (1 + 1/7 coarse levels) + 16 PCG passes of 8 B + ~5 mask B
+        bpv = 194 if mixed else 254
+        npad = int(np.prod([s + 2 for s in f.shape]))
+        gbs = bpv * npad * info["iters"] / info["seconds"] / 1e9
+        out[key] = {"iters": info["iters"], "seconds": info["seconds"], "wall_s": wall, "resnorm": info["resnorm"],
+                    "hbm_gbs": gbs, "frac": gbs / _peaks()[0], "bytes_per_voxel_iter": bpv}
     out["rel_l2_fp32_vcycle_vs_fp64"] = float(torch.linalg.vector_norm(sols["fp32_vcycle"] - sols["fp64"]) /
                                               torch.linalg.vector_norm(sols["fp64"]))
     out["speedup_fp32_vcycle"] = out["fp64"]["seconds"] / out["fp32_vcycle"]["seconds"]
