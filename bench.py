@@ -230,7 +230,8 @@ def poisson_arm(qsm_gb300, ctx, torch):
         npad = int(np.prod([s + 2 for s in f.shape]))
         gbs = bpv * npad * info["iters"] / info["seconds"] / 1e9
         out[key] = {"iters": info["iters"], "seconds": info["seconds"], "wall_s": wall, "resnorm": info["resnorm"],
-                    "hbm_gbs": gbs, "frac": gbs / _peaks()[0], "bytes_per_voxel_iter": bpv}
+                    "hbm_gbs": gbs, "frac": gbs / _peaks()[0], "bytes_per_voxel_iter": bpv,
+                    "coarse_ctas": info["coarse_ctas"], "coarse_outer": info["coarse_outer"]}
     out["rel_l2_fp32_vcycle_vs_fp64"] = float(torch.linalg.vector_norm(sols["fp32_vcycle"] - sols["fp64"]) /
                                               torch.linalg.vector_norm(sols["fp64"]))
     out["speedup_fp32_vcycle"] = out["fp64"]["seconds"] / out["fp32_vcycle"]["seconds"]
@@ -578,9 +579,11 @@ def run_ours(args):
 
     ctx = qsm_gb300.context(local)
     stream = torch.cuda.ExternalStream(qsm_gb300.lib().qsm_ctx_get_stream(ctx.handle))
-    if args.only in ("batch", "serve", "next"):
+    if args.only in ("batch", "serve", "next", "poisson"):
         if args.only == "batch":
             out = batch_arm(qsm_gb300, ctx, torch)
+        elif args.only == "poisson":
+            out = poisson_arm(qsm_gb300, ctx, torch)
         elif args.only == "serve":
             out = serve_arm(qsm_gb300, ctx, seconds=args.serve_seconds)
         else:
@@ -730,7 +733,7 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=30.0, help="arrival window of the served arm")
     ap.add_argument("--shape", default="", help="nx,ny,nz of a reduced volume (profiler captures)")
     ap.add_argument("--iters", type=int, default=ITERS, help="iterations per inversion (profiler captures)")
-    ap.add_argument("--only", default="all", choices=["all", "fused", "batch", "serve", "next"],
+    ap.add_argument("--only", default="all", choices=["all", "fused", "batch", "serve", "next", "poisson"],
                     help="run only one arm (profiling aid)")
     args = ap.parse_args()
     if args.impl == "reference":

@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define QSM_GPU_ABI_VERSION 1
+#define QSM_GPU_ABI_VERSION 2
 
 /* Number of blocks of the lane-order reduction (lanes = 256 * QSM_RED_NBLK). */
 #define QSM_RED_NBLK 1024
@@ -261,6 +261,9 @@ typedef struct {
     double resnorm;         /* final ||r||_2 (padded array, as the reference) */
     double seconds;         /* device time */
     double *resnorm_hist;   /* optional, caller-owned, >= maxitcg doubles */
+    int32_t coarse_ctas;    /* coarsest-level solver: 0 host-driven loop, 1 one CTA,
+                               > 1 a thread-block cluster of that many CTAs */
+    int32_t coarse_outer;   /* outer iterations (256 sweeps each) it ran in total */
 } qsm_mg_info;
 
 /* v = mgpcg_mex(v, f, mask, vsz, tolcg, maxitcg, tolmg, maxitmg, mu, npre,
@@ -531,6 +534,15 @@ qsm_status qsm_nifti_make_header(qsm_ctx *ctx, int32_t datatype, int32_t ndims, 
  * src/utils/poisson_solver/mex/mx_blas.c:108-131 over MATLAB's ddot/sdot). */
 qsm_status qsm_dot(qsm_ctx *ctx, qsm_dtype dtype, size_t n, const void *x, const void *y,
                    double *out);
+
+/* ---------------- diagnostics ---------------- */
+
+/* *ops_per_s = the device's throughput of separate multiplies and adds in
+ * dtype (the instructions the exact kernels issue; no fused multiply-add):
+ * every SM fully occupied, eight independent x = x * m + c chains per thread,
+ * timed with events on the context's stream (best of three launches).  The
+ * FP64 figure is the roofline of the bit-exact FP64 solvers. */
+qsm_status qsm_fp_pipe_rate(qsm_ctx *ctx, qsm_dtype dtype, double *ops_per_s);
 
 #ifdef __cplusplus
 }

@@ -34,7 +34,7 @@ __all__ = [
     "gradf_adj_mex", "gradb_adj_mex", "gradfm_adj_mex", "gradbm_adj_mex", "gradfp_mex", "gradfp_adj_mex",
     "lap1_mex", "lapw_mex", "gauss_seidel_mex", "residual_mex", "lapmg_mex", "restrict_mex", "prolong_mex",
     "correct_mex", "coarsen_grid_mex", "boundary_mask_mex", "boundary_mask_l1_mex", "norm2_mex", "mgpcg_mex",
-    "mg_mex", "fmg_mex", "lane_dot", "tv", "sstgv", "lbv", "unwrap_laplacian", "sharp", "vsharp", "ismv", "resharp", "pdf", "nifti",
+    "mg_mex", "fmg_mex", "lane_dot", "fp_pipe_rate", "tv", "sstgv", "lbv", "unwrap_laplacian", "sharp", "vsharp", "ismv", "resharp", "pdf", "nifti",
     "pd_tv_batch", "pd_tgv_batch", "Session", "footprint", "QsmError",
     "QsmLibraryError", "context", "lib",
 ]
@@ -322,6 +322,15 @@ def lane_dot(x, y, *, ctx=None):
     return out.value
 
 
+def fp_pipe_rate(dtype="float64", *, ctx=None) -> float:
+    """Measured multiply/add throughput (operations per second) of the device
+    in dtype: the roofline of the bit-exact FP64 solvers."""
+    out = ctypes.c_double(0.0)
+    dt = _lib.QSM_F64 if np.dtype(dtype) == np.float64 else _lib.QSM_F32
+    _ctx(ctx).call("qsm_fp_pipe_rate", dt, ctypes.byref(out))
+    return out.value
+
+
 # ---------------------------------------------------------------------------
 # Poisson solvers
 # ---------------------------------------------------------------------------
@@ -352,7 +361,8 @@ def mgpcg_mex(v, f, mask, vsz, tolcg, maxitcg, tolmg, maxitmg, mu, npre, npost, 
                        float(tolmg), int(maxitmg), int(mu), int(npre), int(npost), int(nboundary), int(nlevels),
                        int(verbose), o.ptr, ctypes.byref(mi))
     if info is not None:
-        info.update(iters=mi.iters, resnorm=mi.resnorm, seconds=mi.seconds, resnorm_hist=hist[: mi.iters].copy())
+        info.update(iters=mi.iters, resnorm=mi.resnorm, seconds=mi.seconds, resnorm_hist=hist[: mi.iters].copy(),
+                    coarse_ctas=mi.coarse_ctas, coarse_outer=mi.coarse_outer)
     return out
 
 
@@ -368,7 +378,7 @@ def mg_mex(v, f, mask, vsz, tol, maxit, mu, npre, npost, nboundary, nlevels, *, 
                    float(tol), int(maxit), int(mu), int(npre), int(npost), int(nboundary), int(nlevels), o.ptr,
                    ctypes.byref(mi))
     if info is not None:
-        info.update(cycles=mi.iters, seconds=mi.seconds)
+        info.update(cycles=mi.iters, seconds=mi.seconds, coarse_ctas=mi.coarse_ctas, coarse_outer=mi.coarse_outer)
     return out
 
 
@@ -382,7 +392,7 @@ def fmg_mex(f, mask, vsz, tol, maxit, mu, npre, npost, nboundary, nlevels, *, in
     _ctx(ctx).call("qsm_fmg", fa.dt, fa.dims_c(), fa.ptr, m.ptr, _h(vsz), float(tol), int(maxit), int(mu),
                    int(npre), int(npost), int(nboundary), int(nlevels), o.ptr, ctypes.byref(mi))
     if info is not None:
-        info.update(cycles=mi.iters, seconds=mi.seconds)
+        info.update(cycles=mi.iters, seconds=mi.seconds, coarse_ctas=mi.coarse_ctas, coarse_outer=mi.coarse_outer)
     return out
 
 

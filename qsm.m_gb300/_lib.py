@@ -24,6 +24,9 @@ STATUS = ctypes.c_int
 
 QSM_F64, QSM_F32 = 0, 1
 
+# QSM_GPU_ABI_VERSION these bindings are written for (struct layouts included)
+ABI_VERSION = 2
+
 STATUS_NAMES = {
     0: "QSM_OK", 1: "QSM_ERR_ARG", 2: "QSM_ERR_DIMS", 3: "QSM_ERR_DTYPE", 4: "QSM_ERR_NOMEM",
     5: "QSM_ERR_CUDA", 6: "QSM_ERR_NONFINITE", 7: "QSM_ERR_DEPTH", 8: "QSM_ERR_BUSY", 9: "QSM_ERR_TIMEOUT",
@@ -54,7 +57,8 @@ class TvInfo(ctypes.Structure):
 
 class MgInfo(ctypes.Structure):
     _fields_ = [("iters", ctypes.c_int32), ("resnorm", ctypes.c_double), ("seconds", ctypes.c_double),
-                ("resnorm_hist", ctypes.POINTER(ctypes.c_double))]
+                ("resnorm_hist", ctypes.POINTER(ctypes.c_double)), ("coarse_ctas", ctypes.c_int32),
+                ("coarse_outer", ctypes.c_int32)]
 
 
 class NiftiHdr(ctypes.Structure):
@@ -176,6 +180,11 @@ def lib() -> ctypes.CDLL:
     L.qsm_status_string.restype = ctypes.c_char_p
     L.qsm_abi_version.argtypes = []
     L.qsm_abi_version.restype = ctypes.c_int
+    if L.qsm_abi_version() != ABI_VERSION:
+        raise QsmLibraryError(f"{LIB_PATH} has ABI {L.qsm_abi_version()}, these bindings need {ABI_VERSION}; "
+                              "rebuild it with `python qsm.m_gb300/build.py`")
+    L.qsm_fp_pipe_rate.argtypes = [CTX, I32, ctypes.POINTER(DBL)]
+    L.qsm_fp_pipe_rate.restype = STATUS
     L.qsm_norm2_noalloc.argtypes = [I32, ctypes.c_size_t, P, U8, P, P]
     L.qsm_norm2_noalloc.restype = STATUS
     for name, args in SIGNATURES.items():
@@ -194,7 +203,8 @@ def exported_symbols() -> list[str]:
     """Names of every function include/qsm_gpu.h declares."""
     return sorted(list(SIGNATURES) + list(SESSION_SIGNATURES) + list(HOST_SIGNATURES) + ["qsm_ctx_create", "qsm_ctx_destroy", "qsm_ctx_set_stream",
                                       "qsm_ctx_get_stream", "qsm_ctx_set_verbose", "qsm_last_error",
-                                      "qsm_status_string", "qsm_abi_version", "qsm_norm2_noalloc"])
+                                      "qsm_status_string", "qsm_abi_version", "qsm_norm2_noalloc",
+                                      "qsm_fp_pipe_rate"])
 
 
 class Context:

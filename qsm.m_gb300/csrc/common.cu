@@ -77,34 +77,21 @@ qsm_status stage_out(qsm_ctx *ctx, Staged &s, bool copy_out)
 // lane-order dot product
 // ---------------------------------------------------------------------------
 
+// Throughput probe: eight independent chains x = x * m + c per thread (a
+// multiply and an add each, -fmad=false), 16 operations per iteration.
 template <typename T>
-__device__ __forceinline__ T halve_block(T *sm, int tid, T v)
+__global__ void __launch_bounds__(256) fp_rate_k(T *out, T m, T c, int iters)
 {
-    sm[tid] = v;
-    __syncthreads();
-    for (int s = RED_BLOCK / 2; s > 0; s >>= 1) {
-        if (tid < s) sm[tid] = sm[tid] + sm[tid + s];
-        __syncthreads();
-    }
-    return sm[0];
-}
-
-// Final halving over the RED_NBLK block partials by one block of RED_BLOCK
-// threads: level s = 512 is done by each thread for t and t + 256, then the
-// remaining levels in shared memory.
-template <typename T>
-__device__ __forceinline__ T halve_partials(T *sm, int tid, const T *part)
-{
-    static_assert(RED_NBLK == 4 * RED_BLOCK, "lane order layout");
-    T a = __ldcg(part + tid), b = __ldcg(part + tid + 256), c = __ldcg(part + tid + 512), d = __ldcg(part + tid + 768);
-    // s = 512: a[t] += a[t+512] for t < 512
-    sm[tid] = a + c;
-    T hi = b + d;  // element t + 256 after the s = 512 level
-    __syncthreads();
-    // s = 256: a[t] += a[t+256]
-    T v = sm[tid] + hi;
-    __syncthreads();
-    return halve_block(sm, tid, v);
+    T a[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) a[u] = (T)(threadIdx.x + u);
+    for (int it = 0; it < iters; ++it)
+#pragma unroll
+        for (int u = 0; u < 8; ++u) a[u] = a[u] * m + c;
+    T s = (T)0;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) s = s + a[u];
+    if (s == (T)-1) out[0] = s;  // keeps the chains live; never true for these inputs
 }
 
 template <typename T>
@@ -116,7 +103,18 @@ __global__ void __launch_bounds__(RED_BLOCK) lane_dot_kernel(const T *__restrict
     const int tid = threadIdx.x;
     const size_t t = (size_t)blockIdx.x * RED_BLOCK + tid;
     T acc = (T)0;
-    for (size_t i = t; i < n; i += RED_LANES) acc = acc + x[i] * y[i];
+    size_t i = t;
+    // four elements' loads in flight per thread; the lane still adds them in
+    // increasing i
+    for (; i + 3 * RED_LANES < n; i += 4 * RED_LANES) {
+        const T x0 = x[i], x1 = x[i + RED_LANES], x2 = x[i + 2 * RED_LANES], x3 = x[i + 3 * RED_LANES];
+        const T y0 = y[i], y1 = y[i + RED_LANES], y2 = y[i + 2 * RED_LANES], y3 = y[i + 3 * RED_LANES];
+        acc = acc + x0 * y0;
+        acc = acc + x1 * y1;
+        acc = acc + x2 * y2;
+        acc = acc + x3 * y3;
+    }
+    for (; i < n; i += RED_LANES) acc = acc + x[i] * y[i];
     T b = halve_block(sm, tid, acc);
     if (tid == 0) {
         part[blockIdx.x] = b;
@@ -252,6 +250,37 @@ qsm_status qsm_ctx_set_verbose(qsm_ctx *ctx, int verbose)
 {
     if (!ctx) return QSM_ERR_ARG;
     ctx->verbose = verbose;
+    return QSM_OK;
+}
+
+qsm_status qsm_fp_pipe_rate(qsm_ctx *ctx, qsm_dtype dtype, double *ops_per_s)
+{
+    if (!ctx || !ops_per_s) return QSM_ERR_ARG;
+    if (dtype != QSM_F32 && dtype != QSM_F64) return QSM_ERR_DTYPE;
+    cudaSetDevice(ctx->device);
+    int sms = 0;
+    QSM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    const dim3 grid((unsigned)sms * 8), block(256);
+    const int iters = dtype == QSM_F64 ? 1000 : 40000;
+    cudaEvent_t e0, e1;
+    QSM_CUDA(cudaEventCreate(&e0));
+    QSM_CUDA(cudaEventCreate(&e1));
+    float best = 0.f;
+    for (int rep = 0; rep < 4; ++rep) {
+        QSM_CUDA(cudaEventRecord(e0, ctx->stream));
+        if (dtype == QSM_F64)
+            fp_rate_k<double><<<grid, block, 0, ctx->stream>>>(ctx->red_out, 0.999999, 1e-3, iters);
+        else
+            fp_rate_k<float><<<grid, block, 0, ctx->stream>>>((float *)ctx->red_out, 0.9999f, 1e-3f, iters);
+        QSM_CUDA(cudaEventRecord(e1, ctx->stream));
+        QSM_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        QSM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (rep > 0 && (best == 0.f || ms < best)) best = ms;  // launch 0 warms up
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ops_per_s = (double)grid.x * block.x * 16.0 * iters / (best * 1e-3);
     return QSM_OK;
 }
 

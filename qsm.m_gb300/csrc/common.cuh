@@ -134,6 +134,36 @@ constexpr int RED_BLOCK = 256;
 constexpr int RED_NBLK = QSM_RED_NBLK;
 constexpr size_t RED_LANES = (size_t)RED_BLOCK * RED_NBLK;
 
+template <typename T>
+__device__ __forceinline__ T halve_block(T *sm, int tid, T v)
+{
+    sm[tid] = v;
+    __syncthreads();
+    for (int s = RED_BLOCK / 2; s > 0; s >>= 1) {
+        if (tid < s) sm[tid] = sm[tid] + sm[tid + s];
+        __syncthreads();
+    }
+    return sm[0];
+}
+
+// Final halving over the RED_NBLK block partials by one block of RED_BLOCK
+// threads: level s = 512 is done by each thread for t and t + 256, then the
+// remaining levels in shared memory.
+template <typename T>
+__device__ __forceinline__ T halve_partials(T *sm, int tid, const T *part)
+{
+    static_assert(RED_NBLK == 4 * RED_BLOCK, "lane order layout");
+    T a = __ldcg(part + tid), b = __ldcg(part + tid + 256), c = __ldcg(part + tid + 512), d = __ldcg(part + tid + 768);
+    // s = 512: a[t] += a[t+512] for t < 512
+    sm[tid] = a + c;
+    T hi = b + d;  // element t + 256 after the s = 512 level
+    __syncthreads();
+    // s = 256: a[t] += a[t+256]
+    T v = sm[tid] + hi;
+    __syncthreads();
+    return halve_block(sm, tid, v);
+}
+
 // out[0] = dot(x, y) (or sum x*x when y == x) in lane order, on ctx->stream,
 // written to device memory `dout`.  T in {float, double}; FP32 inputs
 // accumulate in FP32 like sdot and the result is widened.

@@ -53,6 +53,44 @@ template <typename T> static LapC<T> lap_consts(const double *h)
 }
 
 // ---------------------------------------------------------------------------
+// thread-block cluster primitives (inline PTX)
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ uint32_t cl_rank()
+{
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ uint32_t cl_size()
+{
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+    return r;
+}
+// all threads of all CTAs in the cluster; release / acquire at cluster scope
+__device__ __forceinline__ void cl_sync()
+{
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// shared::cluster address of this shared-memory location in CTA `rank`
+__device__ __forceinline__ uint32_t cl_map(const void *p, uint32_t rank)
+{
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ void cl_st(uint32_t a, double v)
+{
+    asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(a), "d"(v) : "memory");
+}
+__device__ __forceinline__ void cl_st(uint32_t a, float v)
+{
+    asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(a), "f"(v) : "memory");
+}
+
+// ---------------------------------------------------------------------------
 // Gauss-Seidel colour pass (gauss_seidel_mex.c:138-190 / :256-308)
 // Pass over voxels with (i + j + k) = par (mod 2) in the interior, except
 // x index skip_i.
@@ -162,7 +200,7 @@ __global__ void restrict_k(T *x2, const T *__restrict__ x, const uint8_t *__rest
     }
     const size_t nx = d.nx, nxny = d.nxny();
     const size_t l = (2 * i2 - 1) + nx * (2 * j2 - 1) + nxny * (2 * k2 - 1);
-#define X(a, b, c) x[l + (a) + (b) * (ptrdiff_t)nx + (c) * (ptrdiff_t)nxny]
+#define X(a, b, c) x[(ptrdiff_t)l + (a) + (b) * (ptrdiff_t)nx + (c) * (ptrdiff_t)nxny]
     const T A = X(-1, -1, -1) + X(1, -1, -1) + X(-1, 1, -1) + X(1, 1, -1) + X(-1, -1, 1) + X(1, -1, 1) + X(-1, 1, 1) + X(1, 1, 1);
     const T B = X(0, -1, -1) + X(-1, 0, -1) + X(1, 0, -1) + X(0, 1, -1) + X(1, -1, 0) + X(-1, -1, 0) + X(-1, 1, 0) +
                 X(1, 1, 0) + X(0, -1, 1) + X(-1, 0, 1) + X(1, 0, 1) + X(0, 1, 1);
@@ -171,36 +209,42 @@ __global__ void restrict_k(T *x2, const T *__restrict__ x, const uint8_t *__rest
     x2[l2] = (T)0.015625 * A + (T)0.03125 * B + (T)0.0625 * C + (T)0.125 * x[l];
 }
 
-// One thread per fine voxel (i, j, k) in [1, 2(n2-2)]^3: coarse parent
-// i2 = (i+1)/2 and offset a = (i+1) mod 2 select the interpolation case.
+// Fine voxels (i, j, k) in [1, 2(n2-2)]^3: coarse parent i2 = (i+1)/2 and
+// offset a = (i+1) mod 2 select the interpolation case.  One thread takes
+// the two fine voxels i = 2 i2 - 1 (a = 0) and 2 i2 (a = 1) of one coarse
+// column, so the case (b, c) is uniform across a warp (one x row) and the
+// FP64 pipe never runs two cases' instructions for one warp.
 template <typename T, bool ADD>
 __global__ void prolong_k(T *x, const T *__restrict__ x2, const uint8_t *__restrict__ G, Dims d, Dims d2)
 {
-    const size_t i = 1 + (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t i2 = 1 + (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const size_t j = 1 + (size_t)blockIdx.y * blockDim.y + threadIdx.y;
     const size_t k = 1 + (size_t)blockIdx.z * blockDim.z + threadIdx.z;
-    if (i > 2 * (d2.nx - 2) || j > 2 * (d2.ny - 2) || k > 2 * (d2.nz - 2)) return;
-    const size_t lf = i + d.nx * j + d.nxny() * k;
-    T val = (T)0;
-    if (G[lf]) {
-        const size_t i2 = (i + 1) >> 1, j2 = (j + 1) >> 1, k2 = (k + 1) >> 1;
-        const int a = (int)((i + 1) & 1), b = (int)((j + 1) & 1), c = (int)((k + 1) & 1);
-        const size_t l2 = i2 + d2.nx * j2 + d2.nxny() * k2, ox = 1, oy = d2.nx, oz = d2.nxny();
-        const T c0 = x2[l2];
-        switch (a + 2 * b + 4 * c) {
-        case 0: val = c0; break;
-        case 1: val = (T)0.5 * (c0 + x2[l2 + ox]); break;
-        case 2: val = (T)0.5 * (c0 + x2[l2 + oy]); break;
-        case 4: val = (T)0.5 * (c0 + x2[l2 + oz]); break;
-        case 3: val = (T)0.25 * (c0 + x2[l2 + ox] + x2[l2 + oy] + x2[l2 + ox + oy]); break;
-        case 5: val = (T)0.25 * (c0 + x2[l2 + ox] + x2[l2 + oz] + x2[l2 + ox + oz]); break;
-        case 6: val = (T)0.25 * (c0 + x2[l2 + oy] + x2[l2 + oz] + x2[l2 + oy + oz]); break;
-        default:
-            val = (T)0.125 * (c0 + x2[l2 + ox] + x2[l2 + oy] + x2[l2 + oz] + x2[l2 + ox + oy] + x2[l2 + ox + oz] +
-                              x2[l2 + oy + oz] + x2[l2 + ox + oy + oz]);
+    if (i2 + 1 >= d2.nx || j > 2 * (d2.ny - 2) || k > 2 * (d2.nz - 2)) return;
+    const size_t j2 = (j + 1) >> 1, k2 = (k + 1) >> 1;
+    const int b = (int)((j + 1) & 1), c = (int)((k + 1) & 1);
+    const size_t l2 = i2 + d2.nx * j2 + d2.nxny() * k2, ox = 1, oy = d2.nx, oz = d2.nxny();
+#pragma unroll
+    for (int a = 0; a < 2; ++a) {
+        const size_t lf = (2 * i2 - 1 + a) + d.nx * j + d.nxny() * k;
+        T val = (T)0;
+        if (G[lf]) {
+            const T c0 = x2[l2];
+            switch (a + 2 * b + 4 * c) {
+            case 0: val = c0; break;
+            case 1: val = (T)0.5 * (c0 + x2[l2 + ox]); break;
+            case 2: val = (T)0.5 * (c0 + x2[l2 + oy]); break;
+            case 4: val = (T)0.5 * (c0 + x2[l2 + oz]); break;
+            case 3: val = (T)0.25 * (c0 + x2[l2 + ox] + x2[l2 + oy] + x2[l2 + ox + oy]); break;
+            case 5: val = (T)0.25 * (c0 + x2[l2 + ox] + x2[l2 + oz] + x2[l2 + ox + oz]); break;
+            case 6: val = (T)0.25 * (c0 + x2[l2 + oy] + x2[l2 + oz] + x2[l2 + oy + oz]); break;
+            default:
+                val = (T)0.125 * (c0 + x2[l2 + ox] + x2[l2 + oy] + x2[l2 + oz] + x2[l2 + ox + oy] + x2[l2 + ox + oz] +
+                                  x2[l2 + oy + oz] + x2[l2 + ox + oy + oz]);
+            }
         }
+        x[lf] = ADD ? x[lf] + val : val;
     }
-    x[lf] = ADD ? x[lf] + val : val;
 }
 
 template <typename T>
@@ -217,7 +261,7 @@ template <typename T>
 static qsm_status prolong(qsm_ctx *ctx, T *x, const T *x2, const uint8_t *G, const Dims &d, const Dims &d2, bool add)
 {
     if (d2.nx < 3 || d2.ny < 3 || d2.nz < 3) return QSM_OK;
-    const Dims e{2 * (d2.nx - 2), 2 * (d2.ny - 2), 2 * (d2.nz - 2)};
+    const Dims e{d2.nx - 2, 2 * (d2.ny - 2), 2 * (d2.nz - 2)};
     const dim3 g = vox_grid(e);
     if (add) prolong_k<T, true><<<g, vox_block(), 0, ctx->stream>>>(x, x2, G, d, d2);
     else prolong_k<T, false><<<g, vox_block(), 0, ctx->stream>>>(x, x2, G, d, d2);
@@ -284,6 +328,195 @@ static qsm_status boundary_mask(qsm_ctx *ctx, uint8_t *B, const uint8_t *G, cons
     bmask_b_k<<<vox_grid(d), vox_block(), 0, ctx->stream>>>(scratch, G, d);
     bmask_grow_k<<<interior_grid3(d), vox_block(), 0, ctx->stream>>>(B, scratch, G, d);
     QSM_CUDA(cudaGetLastError());
+    return QSM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// boundary-band sweeps over voxel lists.  The band B is a thin shell of G; a
+// full-grid colour pass over it would launch every voxel to update a few
+// percent of them.  Each level keeps the linear indices of its B voxels,
+// split by colour (i + j + k) mod 2, with flags for i == 1 and i == nx - 2
+// (the voxels the reference's second colour pass skips).  A pass reads only
+// the other colour, so the list order does not change the result.
+// ---------------------------------------------------------------------------
+
+constexpr uint32_t BL_I1 = 1u << 31, BL_INX2 = 1u << 30, BL_IDX = 0x3FFFFFFFu;
+
+// fill == 0: count the B voxels of each colour into cnt[0..1]; fill == 1:
+// also write them to list0 / list1 at positions taken from cnt (reset first).
+__global__ void blist_k(uint32_t *list0, uint32_t *list1, unsigned *cnt, const uint8_t *__restrict__ B, Dims d,
+                        int fill)
+{
+    const size_t i = 1 + (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t j = 1 + (size_t)blockIdx.y * blockDim.y + threadIdx.y;
+    const size_t k = 1 + (size_t)blockIdx.z * blockDim.z + threadIdx.z;
+    bool on = false;
+    int par = 0;
+    uint32_t e = 0;
+    if (i + 1 < d.nx && j + 1 < d.ny && k + 1 < d.nz) {
+        const size_t l = i + d.nx * j + d.nxny() * k;
+        if (B[l]) {
+            on = true;
+            par = (int)((i + j + k) & 1);
+            e = (uint32_t)l | (i == 1 ? BL_I1 : 0u) | (i == d.nx - 2 ? BL_INX2 : 0u);
+        }
+    }
+    const int lane = threadIdx.x & 31;  // blockDim.x == 32: a warp is one x row
+    for (int p = 0; p < 2; ++p) {
+        const unsigned m = __ballot_sync(0xffffffffu, on && par == p);
+        if (!m) continue;
+        const int leader = __ffs(m) - 1;
+        unsigned pos = 0;
+        if (lane == leader) pos = atomicAdd(cnt + p, (unsigned)__popc(m));
+        pos = __shfl_sync(0xffffffffu, pos, leader);
+        if (fill && on && par == p) (p ? list1 : list0)[pos + __popc(m & ((1u << lane) - 1u))] = e;
+    }
+}
+
+template <typename T>
+__global__ void gs_list_k(T *v, const T *__restrict__ f, const uint32_t *__restrict__ list, unsigned cnt,
+                          uint32_t skip, GsC<T> c, size_t nx, size_t nxny)
+{
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= cnt) return;
+    const uint32_t e = list[t];
+    if (e & skip) return;
+    const size_t l = e & BL_IDX;
+    v[l] = c.hh * (f[l] + (c.hx * (v[l - 1] + v[l + 1]) + c.hy * (v[l - nx] + v[l + nx]) + c.hz * (v[l - nxny] + v[l + nxny])));
+}
+
+// ---------------------------------------------------------------------------
+// All colour passes of one smoothing call on one thread-block cluster.  On a
+// coarse level a pass updates a few thousand voxels and a launch per pass
+// costs several times the pass itself; here the cluster's CTAs share each
+// pass and meet at the cluster barrier between passes.  v stays in global
+// memory (L2-resident at these sizes); its reads bypass L1 (ld.global.cg), so
+// after the barrier's release / acquire a CTA reads what the others wrote.
+// The list order within a pass is immaterial (a pass reads the other colour
+// only), so results equal the per-pass launches bit for bit.
+// ---------------------------------------------------------------------------
+
+constexpr int SW_THREADS = 256;
+
+// A thread's share of one list: at most SW_PER entries (longer lists keep one
+// launch per pass), loaded once with their f values, since neither changes
+// during the sweeps.
+constexpr int SW_PER = 4;
+
+template <typename T>
+struct SwShare {
+    uint32_t l[SW_PER];
+    T f[SW_PER];
+    uint32_t flags[SW_PER];
+    int n;
+    __device__ __forceinline__ void load(const uint32_t *list, unsigned cnt, const T *__restrict__ fg, unsigned t0,
+                                         unsigned stride)
+    {
+        n = 0;
+#pragma unroll
+        for (int u = 0; u < SW_PER; ++u) {
+            const unsigned m = t0 + u * stride;
+            if (m < cnt) {
+                const uint32_t e = list[m];
+                l[u] = e & BL_IDX;
+                flags[u] = e & ~BL_IDX;
+                f[u] = fg[l[u]];
+                n = u + 1;
+            }
+        }
+    }
+    __device__ __forceinline__ void pass(T *v, uint32_t skip, GsC<T> c, size_t nx, size_t nxny) const
+    {
+#pragma unroll
+        for (int u = 0; u < SW_PER; ++u) {
+            if (u >= n || (flags[u] & skip)) continue;
+            const size_t q = l[u];
+            v[q] = c.hh * (f[u] + (c.hx * (__ldcg(v + q - 1) + __ldcg(v + q + 1)) +
+                                   c.hy * (__ldcg(v + q - nx) + __ldcg(v + q + nx)) +
+                                   c.hz * (__ldcg(v + q - nxny) + __ldcg(v + q + nxny))));
+        }
+    }
+};
+
+// iter sweeps of (colour-a pass over la, colour-b pass over lb skipping the
+// entries flagged skipb); the grid is exactly one cluster and each list holds
+// at most SW_PER x (the grid's threads) entries.
+template <typename T>
+__global__ void __launch_bounds__(SW_THREADS) sweeps_cluster_k(T *v, const T *__restrict__ f,
+                                                               const uint32_t *__restrict__ la, unsigned ca,
+                                                               const uint32_t *__restrict__ lb, unsigned cb,
+                                                               uint32_t skipb, int32_t iter, GsC<T> c, size_t nx,
+                                                               size_t nxny)
+{
+    const unsigned stride = gridDim.x * SW_THREADS, t0 = blockIdx.x * SW_THREADS + threadIdx.x;
+    SwShare<T> a, b;
+    a.load(la, ca, f, t0, stride);
+    b.load(lb, cb, f, t0, stride);
+    for (int32_t s = 0; s < iter; ++s) {
+        a.pass(v, 0u, c, nx, nxny);
+        cl_sync();
+        b.pass(v, skipb, c, nx, nxny);
+        cl_sync();
+    }
+}
+
+// Cluster size for sweeps_cluster_k (16, else 8, else 0 = not available),
+// settled once per device.
+template <typename T>
+static int sweeps_cluster_size(qsm_ctx *ctx)
+{
+    static std::mutex mu;
+    static int size[64];
+    static bool done[64];
+    std::lock_guard<std::mutex> lock(mu);
+    const int dv = ctx->device & 63;
+    if (done[dv]) return size[dv];
+    done[dv] = true;
+    size[dv] = 0;
+    if (cudaFuncSetAttribute(sweeps_cluster_k<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    for (int cn = 16; cn >= 8; cn -= 8) {
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = (unsigned)cn;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.gridDim = dim3((unsigned)cn);
+        cfg.blockDim = dim3(SW_THREADS);
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int ncl = 0;
+        if (cudaOccupancyMaxActiveClusters(&ncl, sweeps_cluster_k<T>, &cfg) == cudaSuccess && ncl >= 1) {
+            size[dv] = cn;
+            break;
+        }
+        cudaGetLastError();
+    }
+    return size[dv];
+}
+
+template <typename T>
+static qsm_status sweeps_cluster(qsm_ctx *ctx, int cn, T *v, const T *f, uint32_t *const lists[2],
+                                 const unsigned cnt[2], const double *h, const Dims &d, int32_t iter, bool rev)
+{
+    const int par0 = rev ? (int)((d.nx + 1) & 1) : 0;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)cn;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3((unsigned)cn);
+    cfg.blockDim = dim3(SW_THREADS);
+    cfg.stream = ctx->stream;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    QSM_CUDA(cudaLaunchKernelEx(&cfg, sweeps_cluster_k<T>, v, f, (const uint32_t *)lists[par0], cnt[par0],
+                                (const uint32_t *)lists[par0 ^ 1], cnt[par0 ^ 1], rev ? BL_INX2 : BL_I1, iter,
+                                gs_consts<T>(h), d.nx, d.nxny()));
     return QSM_OK;
 }
 
@@ -387,13 +620,6 @@ __global__ void cvt_k(T *o, const S *__restrict__ a, size_t n)
 // PCG scalar slots
 enum { S_RHO = 0, S_PREV = 1, S_BETA = 2, S_A = 3, S_PQ = 4, S_RES = 5, S_TMP = 6, S_N = 8 };
 
-__global__ void pcg_beta_k(double *sc)
-{
-    // prevrho = rho (done before the V-cycle), beta = rho / prevrho
-    sc[S_BETA] = sc[S_RHO] / sc[S_PREV];
-}
-__global__ void pcg_prev_k(double *sc) { sc[S_PREV] = sc[S_RHO]; }
-__global__ void pcg_alpha_k(double *sc) { sc[S_A] = sc[S_RHO] / sc[S_PQ]; }
 __global__ void sqrt_k(double *dst, const double *src, bool f32)
 {
     *dst = f32 ? (double)sqrtf((float)*src) : sqrt(*src);
@@ -535,6 +761,186 @@ __global__ void __launch_bounds__(CS_THREADS) coarse_solve_k(T *gv, const T *__r
 }
 
 // ---------------------------------------------------------------------------
+// coarsest level on a thread-block cluster (mgpcg_mex.c:265-275)
+//
+// The one-CTA solver runs the reference's 256 sweeps per outer iteration on a
+// single SM; in FP64 (two operations per clock per SM on this GPU) that is
+// ~2.4 ms for an 18^3 grid.  Here the cn CTAs of a cluster split the interior
+// z planes into slabs: CTA c owns planes [k0, k1) and keeps in shared memory
+// v of planes k0-1 .. k1 (its slab plus one halo plane each side) and f, G of
+// its slab.  Each colour pass updates the slab's voxels of that colour from a
+// list built once (so no index arithmetic per pass), pushes the new values of
+// its first and last plane into the neighbours' halo planes
+// (st.shared::cluster), and ends at the cluster barrier, whose release /
+// acquire makes the pushes visible.  A pass reads only the other colour, so
+// the order of updates within a pass does not matter: results are those of
+// the one-CTA solver, bit for bit.  The residual goes to global r, and its
+// lane-order norm is formed as in cta_lane_sum: CTA c halves the 256-element
+// blocks b = c, c + cn, ... and pushes the block sums into CTA 0, which
+// halves the 1024 block sums and broadcasts the total.
+// ---------------------------------------------------------------------------
+
+constexpr int CC_THREADS = RED_BLOCK;
+constexpr int CC_MAX_CTAS = 16;
+constexpr uint32_t CC_IDX = 0x0FFFFFFFu;  // list entry: v index in the CTA's planes
+constexpr uint32_t CC_I1 = 1u << 28;      // i == 1
+constexpr uint32_t CC_INX2 = 1u << 29;    // i == nx - 2
+constexpr uint32_t CC_DOWN = 1u << 30;    // first slab plane: push to CTA c - 1
+constexpr uint32_t CC_UP = 1u << 31;      // last slab plane: push to CTA c + 1
+
+// Shared-memory layout of one CTA (host and device agree on it).
+struct CcLayout {
+    size_t v, f, blk, red, bc, G, list, bytes;
+    __host__ __device__ CcLayout(size_t nxny, int npmax, size_t es)
+    {
+        const size_t pl = (size_t)npmax * nxny;
+        v = 0;
+        f = v + (pl + 2 * nxny) * es;
+        blk = f + pl * es;
+        red = blk + (size_t)RED_NBLK * es;
+        bc = red + (size_t)RED_BLOCK * es;
+        G = (bc + 2 * sizeof(double) + 15) & ~(size_t)15;
+        list = (G + pl + 15) & ~(size_t)15;
+        bytes = list + 2 * pl * sizeof(uint32_t);
+    }
+};
+
+// Lane-order sum of src[e]^2 over e < n (src in global memory, written
+// before the last cluster barrier): the same pairing as cta_lane_sum.
+template <typename T>
+__device__ T cl_lane_sum(const T *src, int n, T *red, T *blk, T *bc, uint32_t c, uint32_t cn)
+{
+    const int tid = threadIdx.x;
+    const int nb = (n + RED_BLOCK - 1) / RED_BLOCK;
+    const uint32_t blk0 = cl_map(blk, 0);
+    for (int b = (int)c; b < nb; b += (int)cn) {
+        const int e = b * RED_BLOCK + tid;
+        const T x = e < n ? __ldcg(src + e) : (T)0;
+        red[tid] = x * x;
+        __syncthreads();
+        for (int s = RED_BLOCK / 2; s > 0; s >>= 1) {
+            if (tid < s) red[tid] = red[tid] + red[tid + s];
+            __syncthreads();
+        }
+        if (tid == 0) cl_st(blk0 + (uint32_t)(b * sizeof(T)), red[0]);
+        __syncthreads();
+    }
+    cl_sync();
+    if (c == 0) {
+        // block sums b >= nb stay +0: never pushed, and t >= nb only ever adds +0 + +0
+        for (int s = RED_NBLK / 2; s > 0; s >>= 1) {
+            for (int t = tid; t < s; t += CC_THREADS) blk[t] = blk[t] + blk[t + s];
+            __syncthreads();
+        }
+        if (tid < (int)cn) cl_st(cl_map(bc, (uint32_t)tid), blk[0]);
+    }
+    cl_sync();
+    return bc[0];
+}
+
+template <typename T>
+__device__ __forceinline__ void cc_pass(T *v, const T *f, const uint32_t *list, int cnt, uint32_t skip, GsC<T> c,
+                                        int nx, int nxny, uint32_t vdn, uint32_t offdn, uint32_t vup, uint32_t offup)
+{
+    for (int m = threadIdx.x; m < cnt; m += CC_THREADS) {
+        const uint32_t e = list[m];
+        if (e & skip) continue;
+        const int l = (int)(e & CC_IDX);
+        const T val = c.hh * (f[l - nxny] + (c.hx * (v[l - 1] + v[l + 1]) + c.hy * (v[l - nx] + v[l + nx]) +
+                                             c.hz * (v[l - nxny] + v[l + nxny])));
+        v[l] = val;
+        if (e & CC_DOWN) cl_st(vdn + (uint32_t)((l + offdn) * sizeof(T)), val);
+        if (e & CC_UP) cl_st(vup + (uint32_t)((l - offup) * sizeof(T)), val);
+    }
+    cl_sync();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(CC_THREADS) coarse_cluster_k(T *gv, const T *__restrict__ gf,
+                                                               const uint8_t *__restrict__ gG, T *gr, Dims d,
+                                                               GsC<T> gc, LapC<T> lc, double tol, int npmax,
+                                                               int *outer_out)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int nx = (int)d.nx, ny = (int)d.ny, nz = (int)d.nz, nxny = nx * ny, n = nxny * nz;
+    const uint32_t c = cl_rank(), cn = cl_size();
+    const int P = nz - 2;
+    const int k0 = 1 + (int)((long long)P * c / cn), k1 = 1 + (int)((long long)P * (c + 1) / cn), np = k1 - k0;
+    const int kp = 1 + (int)((long long)P * (c > 0 ? c - 1 : 0) / cn);  // first plane of CTA c - 1
+    const CcLayout lay((size_t)nxny, npmax, sizeof(T));
+    T *v = (T *)(smraw + lay.v), *f = (T *)(smraw + lay.f), *blk = (T *)(smraw + lay.blk);
+    T *red = (T *)(smraw + lay.red), *bc = (T *)(smraw + lay.bc);
+    uint8_t *G = smraw + lay.G;
+    uint32_t *list = (uint32_t *)(smraw + lay.list);
+    const int cap = npmax * nxny;
+    __shared__ int cnt[2];
+    const int tid = threadIdx.x;
+    if (tid < 2) cnt[tid] = 0;
+    for (int t = tid; t < RED_NBLK; t += CC_THREADS) blk[t] = (T)0;
+    const size_t base = (size_t)(k0 - 1) * nxny;
+    for (int t = tid; t < (np + 2) * nxny; t += CC_THREADS) v[t] = gv[base + t];
+    for (int t = tid; t < np * nxny; t += CC_THREADS) {
+        f[t] = gf[base + nxny + t];
+        G[t] = gG[base + nxny + t];
+    }
+    __syncthreads();
+    // colour lists of the slab's interior G voxels
+    for (int t = tid; t < np * nxny; t += CC_THREADS) {
+        const int kl = t / nxny, rem = t - kl * nxny, j = rem / nx, i = rem - j * nx, k = k0 + kl;
+        if (i < 1 || i > nx - 2 || j < 1 || j > ny - 2 || !G[t]) continue;
+        const int par = (i + j + k) & 1;
+        uint32_t e = (uint32_t)(t + nxny);
+        if (i == 1) e |= CC_I1;
+        if (i == nx - 2) e |= CC_INX2;
+        if (kl == 0 && c > 0) e |= CC_DOWN;
+        if (kl == np - 1 && c + 1 < cn) e |= CC_UP;
+        list[par * cap + atomicAdd(&cnt[par], 1)] = e;
+    }
+    // halo planes are loaded everywhere before any neighbour pushes into them
+    cl_sync();
+    const uint32_t vdn = c > 0 ? cl_map(v, c - 1) : 0u, vup = c + 1 < cn ? cl_map(v, c + 1) : 0u;
+    const uint32_t offdn = (uint32_t)(nxny * (k0 - kp)), offup = (uint32_t)(nxny * np);
+    const int n0 = cnt[0], n1 = cnt[1];
+    const uint32_t *list0 = list, *list1 = list + cap;
+
+    const T ff = cl_lane_sum<T>(gf, n, red, blk, bc, c, cn);
+    const double fn = sizeof(T) == 4 ? (double)sqrtf((float)ff) : sqrt((double)ff);
+    const double reltol = tol * fn;
+    const int rpar0 = (nx + 1) & 1;
+    const uint32_t *lr0 = rpar0 ? list1 : list0, *lr1 = rpar0 ? list0 : list1;
+    const int cr0 = rpar0 ? n1 : n0, cr1 = rpar0 ? n0 : n1;
+    int outer = 0;
+    for (int it = 0; it < 1024; ++it) {
+        outer = it + 1;
+        for (int s = 0; s < 128; ++s) {  // reverse sweeps
+            cc_pass<T>(v, f, lr0, cr0, 0u, gc, nx, nxny, vdn, offdn, vup, offup);
+            cc_pass<T>(v, f, lr1, cr1, CC_INX2, gc, nx, nxny, vdn, offdn, vup, offup);
+        }
+        for (int s = 0; s < 128; ++s) {  // forward sweeps
+            cc_pass<T>(v, f, list0, n0, 0u, gc, nx, nxny, vdn, offdn, vup, offup);
+            cc_pass<T>(v, f, list1, n1, CC_I1, gc, nx, nxny, vdn, offdn, vup, offup);
+        }
+        // residual of the slab's interior G voxels into global r
+        for (int q = 0; q < 2; ++q) {
+            const uint32_t *ls = q ? list1 : list0;
+            const int cq = q ? n1 : n0;
+            for (int m = tid; m < cq; m += CC_THREADS) {
+                const int l = (int)(ls[m] & CC_IDX);
+                gr[base + l] = f[l - nxny] + (lc.hh * v[l] + lc.hx * (v[l - 1] + v[l + 1]) +
+                                              lc.hy * (v[l - nx] + v[l + nx]) + lc.hz * (v[l - nxny] + v[l + nxny]));
+            }
+        }
+        cl_sync();
+        const T rr = cl_lane_sum<T>(gr, n, red, blk, bc, c, cn);
+        const double rn = sizeof(T) == 4 ? (double)sqrtf((float)rr) : sqrt((double)rr);
+        if (rn < reltol) break;
+    }
+    for (int t = tid; t < np * nxny; t += CC_THREADS) gv[base + nxny + t] = v[nxny + t];
+    if (c == 0 && tid == 0 && outer_out) *outer_out += outer;
+    cl_sync();  // no CTA leaves while a peer may still address its shared memory
+}
+
+// ---------------------------------------------------------------------------
 // hierarchy and drivers (mgpcg_mex.c:126-332, mg_mex.c:94-207, fmg_mex.c:93-212)
 // ---------------------------------------------------------------------------
 
@@ -545,6 +951,11 @@ struct Level {
     T *v, *f, *r;
     uint8_t *G, *B;
     double h[3];
+    uint32_t *bl[2];     // B voxels of each colour (null: full-grid passes over B)
+    unsigned bn[2];
+    uint32_t *gl[2];     // G voxels of each colour, kept for small levels only
+    unsigned gn[2];
+    bool bcl, gcl;       // B / G passes of a smoothing call run on one cluster launch
 };
 
 template <typename T>
@@ -556,6 +967,12 @@ struct Hier {
     int *counters;       // device: coarse outer iterations
     bool coarse_in_smem;
     size_t coarse_smem;
+    void *lists;         // the levels' colour lists (one allocation)
+    int sw_ctas;         // cluster size of the list passes (0: not available)
+    int host_outer;      // outer iterations of the host-driven coarsest solve
+    int cc_ctas;         // > 0: the coarsest level runs on a cluster of this many CTAs
+    int cc_npmax;        // planes per CTA (largest slab)
+    size_t cc_smem;
 };
 
 static inline size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -575,6 +992,78 @@ static qsm_status coarse_smem_limit(qsm_ctx *ctx, int maxsm)
     return QSM_OK;
 }
 
+// The cluster solver's dynamic shared-memory limit: the opt-in maximum less
+// its static shared memory, raised once per device together with the
+// permission for clusters of more than 8 CTAs.  0 if either is refused.
+template <typename T>
+static size_t cluster_smem_limit(qsm_ctx *ctx, int maxsm)
+{
+    static std::mutex mu;
+    static std::set<int> done;
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, coarse_cluster_k<T>) != cudaSuccess || (size_t)maxsm <= fa.sharedSizeBytes) {
+        cudaGetLastError();
+        return 0;
+    }
+    const size_t lim = (size_t)maxsm - fa.sharedSizeBytes;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!done.count(ctx->device)) {
+        if (cudaFuncSetAttribute(coarse_cluster_k<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim) !=
+                cudaSuccess ||
+            cudaFuncSetAttribute(coarse_cluster_k<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                cudaSuccess) {
+            cudaGetLastError();
+            return 0;
+        }
+        done.insert(ctx->device);
+    }
+    return lim;
+}
+
+// Whether a cluster of cn CTAs with `smem` dynamic bytes each can be resident.
+template <typename T>
+static bool cluster_fits(int cn, size_t smem)
+{
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)cn;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3((unsigned)cn);
+    cfg.blockDim = dim3(CC_THREADS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, coarse_cluster_k<T>, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return nclusters >= 1;
+}
+
+// Cluster shape of the coarsest level: up to 16 CTAs, at least one interior
+// plane each, within the shared-memory limit; cc_ctas = 0 if no cluster fits.
+template <typename T>
+static void plan_cluster(qsm_ctx *ctx, Hier<T> &H, int maxsm)
+{
+    H.cc_ctas = 0;
+    const Dims dc = H.L[H.nl - 1].d;
+    const int P = (int)dc.nz - 2;
+    if (dc.nx < 3 || dc.ny < 3 || P < 2 || dc.n() >= (1u << 27)) return;
+    const size_t lim = cluster_smem_limit<T>(ctx, maxsm);
+    for (int cn = P < CC_MAX_CTAS ? P : CC_MAX_CTAS; cn >= 2 && lim > 0; cn = cn > 8 ? 8 : cn - 1) {
+        const int npmax = (P + cn - 1) / cn;
+        const CcLayout lay(dc.nxny(), npmax, sizeof(T));
+        if (lay.bytes > lim || !cluster_fits<T>(cn, lay.bytes)) continue;
+        H.cc_ctas = cn;
+        H.cc_npmax = npmax;
+        H.cc_smem = lay.bytes;
+        return;
+    }
+}
+
 template <typename T>
 static qsm_status hier_init(qsm_ctx *ctx, Hier<T> &H, int nl, const Dims &dp, const double *h)
 {
@@ -589,7 +1078,7 @@ static qsm_status hier_init(qsm_ctx *ctx, Hier<T> &H, int nl, const Dims &dp, co
         for (int q = 0; q < 3; ++q) H.L[i].h[q] = i == 0 ? h[q] : H.L[i - 1].h[q] * 2.0;
         bytes += 3 * al256(d.n() * sizeof(T)) + 2 * al256(d.n());
     }
-    bytes += al256(dp.n()) + 256;
+    bytes += al256(dp.n()) + 512;
     QSM_TRY(dalloc(ctx, &H.blk, bytes));
     QSM_CUDA(cudaMemsetAsync(H.blk, 0, bytes, ctx->stream));
     char *c = (char *)H.blk;
@@ -609,7 +1098,112 @@ static qsm_status hier_init(qsm_ctx *ctx, Hier<T> &H, int nl, const Dims &dp, co
     cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
     H.coarse_in_smem = H.coarse_smem <= (size_t)maxsm && nc < (1u << 18);
     if (H.coarse_in_smem) QSM_TRY(coarse_smem_limit<T>(ctx, maxsm));
+    plan_cluster<T>(ctx, H, maxsm);
     return QSM_OK;
+}
+
+// Colour lists of every level's boundary band B and, on levels small enough
+// for the cluster passes, of G (counted, then filled into one allocation).
+// Grids of 2^30 voxels or more keep the full-grid passes.
+template <typename T>
+static qsm_status boundary_lists(qsm_ctx *ctx, Hier<T> &H)
+{
+    if (H.L[0].n >= ((size_t)1 << 30)) return QSM_OK;
+    const int cn = sweeps_cluster_size<T>(ctx);
+    unsigned *cnt = (unsigned *)H.counters + 8;  // B: 4i, 4i+1; G: 4i+2, 4i+3 (nl <= 16)
+    QSM_CUDA(cudaMemsetAsync(cnt, 0, 4 * H.nl * sizeof(unsigned), ctx->stream));
+    for (int i = 0; i < H.nl; ++i) {
+        const Level<T> &L = H.L[i];
+        const dim3 g = interior_grid3(L.d);
+        if (!(g.x && g.y && g.z)) continue;
+        blist_k<<<g, vox_block(), 0, ctx->stream>>>(nullptr, nullptr, cnt + 4 * i, L.B, L.d, 0);
+        if (i > 0) blist_k<<<g, vox_block(), 0, ctx->stream>>>(nullptr, nullptr, cnt + 4 * i + 2, L.G, L.d, 0);
+    }
+    QSM_CUDA(cudaGetLastError());
+    unsigned hc[64];
+    QSM_CUDA(cudaMemcpyAsync(hc, cnt, 4 * H.nl * sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+    QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+    size_t tot = 0;
+    for (int i = 0; i < H.nl; ++i) {
+        Level<T> &L = H.L[i];
+        const unsigned cap = (unsigned)cn * SW_THREADS * SW_PER;
+        const bool small_g = i > 0 && cn > 0 && hc[4 * i + 2] <= cap && hc[4 * i + 3] <= cap;
+        L.bcl = i > 0 && cn > 0 && hc[4 * i] <= cap && hc[4 * i + 1] <= cap;
+        L.gcl = small_g;
+        for (int p = 0; p < 2; ++p) {
+            tot += al256((size_t)hc[4 * i + p] * sizeof(uint32_t));
+            if (small_g) tot += al256((size_t)hc[4 * i + 2 + p] * sizeof(uint32_t));
+        }
+    }
+    QSM_TRY(dalloc(ctx, &H.lists, tot + 256));
+    H.sw_ctas = cn;
+    char *c = (char *)H.lists;
+    for (int i = 0; i < H.nl; ++i) {
+        Level<T> &L = H.L[i];
+        for (int p = 0; p < 2; ++p) {
+            L.bl[p] = (uint32_t *)c;
+            L.bn[p] = hc[4 * i + p];
+            c += al256((size_t)hc[4 * i + p] * sizeof(uint32_t));
+        }
+        for (int p = 0; p < 2; ++p) {
+            L.gl[p] = nullptr;
+            L.gn[p] = hc[4 * i + 2 + p];
+            if (L.gcl) {
+                L.gl[p] = (uint32_t *)c;
+                c += al256((size_t)hc[4 * i + 2 + p] * sizeof(uint32_t));
+            }
+        }
+    }
+    QSM_CUDA(cudaMemsetAsync(cnt, 0, 4 * H.nl * sizeof(unsigned), ctx->stream));
+    for (int i = 0; i < H.nl; ++i) {
+        const Level<T> &L = H.L[i];
+        const dim3 g = interior_grid3(L.d);
+        if (!(g.x && g.y && g.z)) continue;
+        blist_k<<<g, vox_block(), 0, ctx->stream>>>(L.bl[0], L.bl[1], cnt + 4 * i, L.B, L.d, 1);
+        if (L.gcl) blist_k<<<g, vox_block(), 0, ctx->stream>>>(L.gl[0], L.gl[1], cnt + 4 * i + 2, L.G, L.d, 1);
+    }
+    QSM_CUDA(cudaGetLastError());
+    return QSM_OK;
+}
+
+// `iter` colour-pass pairs over a level's G (gauss_seidel over G): one
+// cluster launch on small levels, else one full-grid launch per pass.
+template <typename T>
+static qsm_status smooth(qsm_ctx *ctx, const Hier<T> &H, Level<T> &L, int32_t iter, bool rev)
+{
+    if (L.gcl && iter > 0 && L.d.nx >= 3 && L.d.ny >= 3 && L.d.nz >= 3)
+        return sweeps_cluster<T>(ctx, H.sw_ctas, L.v, L.f, L.gl, L.gn, L.h, L.d, iter, rev);
+    return gauss_seidel<T>(ctx, L.v, L.f, L.G, L.h, L.d, iter, rev);
+}
+
+// `iter` colour-pass pairs over a level's boundary band (gauss_seidel over B).
+template <typename T>
+static qsm_status boundary_sweeps(qsm_ctx *ctx, const Hier<T> &H, Level<T> &L, int32_t iter, bool rev)
+{
+    if (!L.bl[0]) return gauss_seidel<T>(ctx, L.v, L.f, L.B, L.h, L.d, iter, rev);
+    if (L.d.nx < 3 || L.d.ny < 3 || L.d.nz < 3 || iter <= 0) return QSM_OK;
+    if (L.bcl) return sweeps_cluster<T>(ctx, H.sw_ctas, L.v, L.f, L.bl, L.bn, L.h, L.d, iter, rev);
+    const GsC<T> c = gs_consts<T>(L.h);
+    const int par0 = rev ? (int)((L.d.nx + 1) & 1) : 0;
+    const uint32_t skip = rev ? BL_INX2 : BL_I1;
+    for (int32_t s = 0; s < iter; ++s)
+        for (int q = 0; q < 2; ++q) {
+            const int par = par0 ^ q;
+            const unsigned cnt = L.bn[par];
+            if (!cnt) continue;
+            gs_list_k<T><<<(cnt + 255) / 256, 256, 0, ctx->stream>>>(L.v, L.f, L.bl[par], cnt, q ? skip : 0u, c, L.d.nx,
+                                                                    L.d.nxny());
+        }
+    QSM_CUDA(cudaGetLastError());
+    return QSM_OK;
+}
+
+template <typename T>
+static qsm_status hier_free(qsm_ctx *ctx, Hier<T> &H)
+{
+    if (H.lists) QSM_TRY(dfree(ctx, H.lists));
+    H.lists = nullptr;
+    return dfree(ctx, H.blk);
 }
 
 // masks of every level (mx_init): coarsen, boundary masks; FMG restricts f.
@@ -624,7 +1218,7 @@ static qsm_status hier_masks(qsm_ctx *ctx, Hier<T> &H, bool restrict_f)
         }
         QSM_TRY(boundary_mask(ctx, H.L[i].B, H.L[i].G, H.L[i].d, H.scratch));
     }
-    return QSM_OK;
+    return boundary_lists(ctx, H);
 }
 
 template <typename T>
@@ -632,6 +1226,23 @@ static qsm_status coarse_solve(qsm_ctx *ctx, Hier<T> &H, int l, double *scal_dev
 {
     Level<T> &L = H.L[l];
     const double tol = sizeof(T) == 4 ? 1e-4 : 1e-8;
+    if (H.cc_ctas > 0) {
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = (unsigned)H.cc_ctas;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.gridDim = dim3((unsigned)H.cc_ctas);
+        cfg.blockDim = dim3(CC_THREADS);
+        cfg.dynamicSmemBytes = H.cc_smem;
+        cfg.stream = ctx->stream;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        QSM_CUDA(cudaLaunchKernelEx(&cfg, coarse_cluster_k<T>, L.v, (const T *)L.f, (const uint8_t *)L.G, L.r, L.d,
+                                    gs_consts<T>(L.h), lap_consts<T>(L.h), tol, H.cc_npmax, H.counters));
+        return QSM_OK;
+    }
     if (H.coarse_in_smem) {
         coarse_solve_k<T><<<1, CS_THREADS, H.coarse_smem, ctx->stream>>>(L.v, L.f, L.G, L.r, L.d, gs_consts<T>(L.h),
                                                                         lap_consts<T>(L.h), tol, H.counters);
@@ -649,6 +1260,7 @@ static qsm_status coarse_solve(qsm_ctx *ctx, Hier<T> &H, int l, double *scal_dev
         QSM_TRY(residual<T>(ctx, L.r, L.f, L.v, L.G, L.h, L.d));
         QSM_TRY(nrm2<T>(ctx, L.r, L.n, scal_dev + S_TMP));
         QSM_TRY(read_double(ctx, scal_dev + S_TMP, &rn));
+        ++H.host_outer;
         if (rn < reltol) break;
     }
     return QSM_OK;
@@ -660,8 +1272,8 @@ static qsm_status cycle(qsm_ctx *ctx, Hier<T> &H, int l, int mu, int pre, int po
     if (l < H.nl - 1) {
         Level<T> &L = H.L[l], &C = H.L[l + 1];
         const int32_t bs = (1 << l) * nb;
-        QSM_TRY(gauss_seidel<T>(ctx, L.v, L.f, L.G, L.h, L.d, pre, true));
-        QSM_TRY(gauss_seidel<T>(ctx, L.v, L.f, L.B, L.h, L.d, bs, true));
+        QSM_TRY(smooth<T>(ctx, H, L, pre, true));
+        QSM_TRY(boundary_sweeps<T>(ctx, H, L, bs, true));
         QSM_TRY(residual<T>(ctx, L.r, L.f, L.v, L.G, L.h, L.d));
         QSM_TRY(restrict_<T>(ctx, C.f, L.r, C.G, C.d, L.d));
         QSM_CUDA(cudaMemsetAsync(C.v, 0, C.n * sizeof(T), ctx->stream));
@@ -670,8 +1282,8 @@ static qsm_status cycle(qsm_ctx *ctx, Hier<T> &H, int l, int mu, int pre, int po
             if (l + 1 == H.nl - 1) break;
         }
         QSM_TRY(prolong<T>(ctx, L.v, C.v, L.G, L.d, C.d, true));
-        QSM_TRY(gauss_seidel<T>(ctx, L.v, L.f, L.B, L.h, L.d, bs, false));
-        QSM_TRY(gauss_seidel<T>(ctx, L.v, L.f, L.G, L.h, L.d, post, false));
+        QSM_TRY(boundary_sweeps<T>(ctx, H, L, bs, false));
+        QSM_TRY(smooth<T>(ctx, H, L, post, false));
         return QSM_OK;
     }
     return coarse_solve<T>(ctx, H, l, sc);
@@ -726,6 +1338,192 @@ static qsm_status pad_mask(qsm_ctx *ctx, uint8_t *Gp, const uint8_t *G, const Di
     return QSM_OK;
 }
 
+// ---------------------------------------------------------------------------
+// fused PCG vector steps (mgpcg_mex.c:160-205).  Each kernel runs on the
+// lane_dot grid (RED_NBLK blocks of RED_BLOCK threads; thread t is lane t and
+// visits elements t, t + 2^18, ... in increasing order), so the inner product
+// it forms while it updates the vectors has lane_dot's order; the last block
+// to finish folds the block partials and updates the PCG scalars, as the
+// single-thread scalar kernels did.  Element updates keep the BLAS-1
+// expressions: scal is a * x, axpy is y + a * x; multiplying by 1.0 is exact
+// and multiplying by -1.0 is a sign flip, so those two are done without the
+// FP64 pipe.
+// ---------------------------------------------------------------------------
+
+template <typename T>
+__device__ __forceinline__ T neg_bits(T x)
+{
+    if (sizeof(T) == 8) return (T)__longlong_as_double(__double_as_longlong((double)x) ^ (long long)0x8000000000000000ull);
+    return (T)__int_as_float(__float_as_int((float)x) ^ (int)0x80000000u);
+}
+
+// true in the last block to finish (all its threads), with the lane-order total
+template <typename T>
+__device__ __forceinline__ bool lane_fold(T *sm, T acc, T *part, unsigned *count, T *tot)
+{
+    __shared__ bool last;
+    const int tid = threadIdx.x;
+    const T b = halve_block(sm, tid, acc);
+    if (tid == 0) {
+        part[blockIdx.x] = b;
+        __threadfence();
+        last = atomicAdd(count, 1u) == RED_NBLK - 1;
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    *tot = halve_partials(sm, tid, part);
+    return true;
+}
+
+// rho = r . q (q widened from the V-cycle's vm first when it runs in another
+// precision); prevrho = old rho; beta = rho / prevrho
+template <typename TP, typename TM>
+__global__ void __launch_bounds__(RED_BLOCK) pcg_rho_k(const TP *__restrict__ r, TP *__restrict__ q,
+                                                       const TM *__restrict__ vm, size_t n, TP *part,
+                                                       unsigned *count, double *sc)
+{
+    __shared__ TP sm[RED_BLOCK];
+    const size_t L = RED_LANES;
+    size_t l = (size_t)blockIdx.x * RED_BLOCK + threadIdx.x;
+    TP acc = (TP)0;
+    for (; l + 3 * L < n; l += 4 * L) {
+        TP a[4], b[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            a[u] = r[l + u * L];
+            b[u] = vm ? (TP)vm[l + u * L] : q[l + u * L];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (vm) q[l + u * L] = b[u];
+            acc = acc + a[u] * b[u];
+        }
+    }
+    for (; l < n; l += L) {
+        const TP b = vm ? (TP)vm[l] : q[l];
+        if (vm) q[l] = b;
+        acc = acc + r[l] * b;
+    }
+    TP tot;
+    if (lane_fold(sm, acc, part, count, &tot) && threadIdx.x == 0) {
+        sc[S_PREV] = sc[S_RHO];
+        sc[S_RHO] = (double)tot;
+        sc[S_BETA] = sc[S_RHO] / sc[S_PREV];
+        *count = 0;
+    }
+}
+
+// p = beta * p, then p = p + 1 * q
+template <typename T>
+__global__ void pcg_p_k(T *__restrict__ p, const T *__restrict__ q, size_t n, const double *sc)
+{
+    const T beta = (T)sc[S_BETA];
+    for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x)
+        p[l] = beta * p[l] + q[l];
+}
+
+// q = lapmg(p) on G (interior), then q = -1 * q everywhere; pq = p . q;
+// alpha = rho / pq
+template <typename T>
+__global__ void __launch_bounds__(RED_BLOCK) pcg_q_k(T *__restrict__ q, const T *__restrict__ p,
+                                                     const uint8_t *__restrict__ G, LapC<T> c, Dims d, T *part,
+                                                     unsigned *count, double *sc)
+{
+    __shared__ T sm[RED_BLOCK];
+    const size_t nx = d.nx, nxny = d.nxny(), n = d.n();
+    const bool small = n <= 0xFFFFFFFFull;  // 32-bit index arithmetic
+    T acc = (T)0;
+    for (size_t l = (size_t)blockIdx.x * RED_BLOCK + threadIdx.x; l < n; l += RED_LANES) {
+        size_t i, j, k;
+        if (small) {
+            const uint32_t l32 = (uint32_t)l, k32 = l32 / (uint32_t)nxny, rem = l32 - k32 * (uint32_t)nxny;
+            const uint32_t j32 = rem / (uint32_t)nx;
+            i = rem - j32 * (uint32_t)nx;
+            j = j32;
+            k = k32;
+        } else {
+            k = l / nxny;
+            const size_t rem = l - k * nxny;
+            j = rem / nx;
+            i = rem - j * nx;
+        }
+        const T pl = p[l];
+        T qv;
+        if (i >= 1 && j >= 1 && k >= 1 && i + 1 < nx && j + 1 < d.ny && k + 1 < d.nz && G[l])
+            qv = c.hh * pl + c.hx * (p[l - 1] + p[l + 1]) + c.hy * (p[l - nx] + p[l + nx]) + c.hz * (p[l - nxny] + p[l + nxny]);
+        else
+            qv = q[l];
+        qv = neg_bits(qv);
+        q[l] = qv;
+        acc = acc + pl * qv;
+    }
+    T tot;
+    if (lane_fold(sm, acc, part, count, &tot) && threadIdx.x == 0) {
+        sc[S_PQ] = (double)tot;
+        sc[S_A] = sc[S_RHO] / sc[S_PQ];
+        *count = 0;
+    }
+}
+
+// x = x + alpha * p; r = r + (-alpha) * q; ||r|| (and r in the V-cycle's
+// precision for the next cycle when that differs)
+template <typename TP, typename TM>
+__global__ void __launch_bounds__(RED_BLOCK) pcg_xr_k(TP *__restrict__ x, const TP *__restrict__ p,
+                                                      TP *__restrict__ r, const TP *__restrict__ q,
+                                                      TM *__restrict__ rm, size_t n, TP *part, unsigned *count,
+                                                      double *sc)
+{
+    __shared__ TP sm[RED_BLOCK];
+    const TP a = (TP)sc[S_A], na = (TP)(-sc[S_A]);
+    const size_t L = RED_LANES;
+    size_t l = (size_t)blockIdx.x * RED_BLOCK + threadIdx.x;
+    TP acc = (TP)0;
+    for (; l + 3 * L < n; l += 4 * L) {
+        TP xv[4], pv[4], rv[4], qv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            xv[u] = x[l + u * L];
+            pv[u] = p[l + u * L];
+            rv[u] = r[l + u * L];
+            qv[u] = q[l + u * L];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            x[l + u * L] = xv[u] + a * pv[u];
+            const TP rn = rv[u] + na * qv[u];
+            r[l + u * L] = rn;
+            if (rm) rm[l + u * L] = (TM)rn;
+            acc = acc + rn * rn;
+        }
+    }
+    for (; l < n; l += L) {
+        x[l] = x[l] + a * p[l];
+        const TP rn = r[l] + na * q[l];
+        r[l] = rn;
+        if (rm) rm[l] = (TM)rn;
+        acc = acc + rn * rn;
+    }
+    TP tot;
+    if (lane_fold(sm, acc, part, count, &tot) && threadIdx.x == 0) {
+        sc[S_RES] = sizeof(TP) == 4 ? (double)sqrtf((float)tot) : sqrt((double)tot);
+        *count = 0;
+    }
+}
+
+// Which coarsest-level solver ran and its outer iterations (after the stream
+// has been synchronised).
+template <typename T>
+static qsm_status coarse_report(qsm_ctx *ctx, const Hier<T> &H, qsm_mg_info *info)
+{
+    if (!info) return QSM_OK;
+    int dev_outer = 0;
+    QSM_CUDA(cudaMemcpy(&dev_outer, H.counters, sizeof(int), cudaMemcpyDeviceToHost));
+    info->coarse_ctas = H.cc_ctas > 0 ? H.cc_ctas : (H.coarse_in_smem ? 1 : 0);
+    info->coarse_outer = dev_outer + H.host_outer;
+    return QSM_OK;
+}
+
 // PCG (mx_pcg, mgpcg_mex.c:126-216).  TP = PCG precision, TM = V-cycle
 // precision.  With TP == TM the V-cycle's level-0 v/f are the PCG q/r (as in
 // the reference); with TM = float they are FP32 copies converted per call.
@@ -774,28 +1572,24 @@ static qsm_status pcg(qsm_ctx *ctx, const Dims &d, const TP *v0, const TP *f, co
     QSM_TRY(read_double(ctx, sc + S_RES, &res));
     if (verbose) printf("\niter%6s\tresidual\n", "");
     int32_t it = 0;
+    TP *part = (TP *)ctx->red_partial;
+    const LapC<TP> lc = lap_consts<TP>(h);
+    // the V-cycle's right-hand side in its own precision; pcg_xr_k refreshes it
+    if (!same) cvt_k<TM, TP><<<1216, 256, 0, ctx->stream>>>(H.L[0].f, r, n);
     for (int32_t i = 0; i < maxitcg; ++i) {
         if (res <= reltol) break;
-        pcg_prev_k<<<1, 1, 0, ctx->stream>>>(sc);
-        if (same) {
+        if (same)
             QSM_CUDA(cudaMemsetAsync(q, 0, n * sizeof(TP), ctx->stream));
-        } else {
-            cvt_k<TM, TP><<<1216, 256, 0, ctx->stream>>>(H.L[0].f, r, n);
+        else
             QSM_CUDA(cudaMemsetAsync(H.L[0].v, 0, n * sizeof(TM), ctx->stream));
-        }
         QSM_TRY(mg_run<TM>(ctx, H, tolmg, maxitmg, mu, npre, npost, nb, sc, nullptr));
-        if (!same) cvt_k<TP, TM><<<1216, 256, 0, ctx->stream>>>(q, H.L[0].v, n);
-        QSM_TRY(lane_dot<TP>(ctx, r, q, n, sc + S_RHO));
-        pcg_beta_k<<<1, 1, 0, ctx->stream>>>(sc);
-        QSM_TRY(scal<TP>(ctx, p, n, sc, S_BETA, false));
-        QSM_TRY(axpy<TP>(ctx, p, q, n, sc, -1, false, 1.0));
-        QSM_TRY(lapmg<TP>(ctx, q, p, H.L[0].G, h, dp));
-        QSM_TRY(scal<TP>(ctx, q, n, sc, -1, false, -1.0));
-        QSM_TRY(lane_dot<TP>(ctx, p, q, n, sc + S_PQ));
-        pcg_alpha_k<<<1, 1, 0, ctx->stream>>>(sc);
-        QSM_TRY(axpy<TP>(ctx, x, p, n, sc, S_A, false));
-        QSM_TRY(axpy<TP>(ctx, r, q, n, sc, S_A, true));
-        QSM_TRY(nrm2<TP>(ctx, r, n, sc + S_RES));
+        pcg_rho_k<TP, TM><<<RED_NBLK, RED_BLOCK, 0, ctx->stream>>>(r, q, same ? nullptr : H.L[0].v, n, part,
+                                                                   ctx->red_count, sc);
+        pcg_p_k<TP><<<1216, 256, 0, ctx->stream>>>(p, q, n, sc);
+        pcg_q_k<TP><<<RED_NBLK, RED_BLOCK, 0, ctx->stream>>>(q, p, H.L[0].G, lc, dp, part, ctx->red_count, sc);
+        pcg_xr_k<TP, TM><<<RED_NBLK, RED_BLOCK, 0, ctx->stream>>>(x, p, r, q, same ? nullptr : H.L[0].f, n, part,
+                                                                  ctx->red_count, sc);
+        QSM_CUDA(cudaGetLastError());
         QSM_TRY(read_double(ctx, sc + S_RES, &res));
         if (info && info->resnorm_hist) info->resnorm_hist[i] = res;
         it += 1;
@@ -814,8 +1608,9 @@ static qsm_status pcg(qsm_ctx *ctx, const Dims &d, const TP *v0, const TP *f, co
         info->resnorm = res;
         info->seconds = ms * 1e-3;
     }
+    QSM_TRY(coarse_report(ctx, H, info));
     QSM_TRY(dfree(ctx, pv));
-    return dfree(ctx, H.blk);
+    return hier_free(ctx, H);
 }
 
 template <typename T>
@@ -875,8 +1670,9 @@ static qsm_status mg_solve(qsm_ctx *ctx, const Dims &d, const T *v0, const T *f,
         info->resnorm = 0.0;
         info->seconds = ms * 1e-3;
     }
+    QSM_TRY(coarse_report(ctx, H, info));
     QSM_TRY(dfree(ctx, sv));
-    return dfree(ctx, H.blk);
+    return hier_free(ctx, H);
 }
 
 // ---------------------------------------------------------------------------

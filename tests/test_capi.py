@@ -41,7 +41,7 @@ def test_python_binding_covers_header(built):
 
     assert sorted(_lib.exported_symbols()) == declared()
     L = _lib.lib()
-    assert L.qsm_abi_version() == 1
+    assert L.qsm_abi_version() == _lib.ABI_VERSION == 2
     assert L.qsm_status_string(7) == b"nlevels too large. Increase MAX_DEPTH."
 
 

@@ -106,6 +106,47 @@ def test_mgpcg_lbv_options_vs_oracle(gpu_ctx, qsm, port):
     assert mi["iters"] <= oi["iters"] + 3
 
 
+@pytest.mark.parametrize("dt", ("float64", "float32"))
+@pytest.mark.parametrize("shape,nl", [((62, 62, 62), 2), ((62, 62, 62), 3), ((40, 36, 45), 2), ((30, 26, 12), 2),
+                                      ((28, 24, 16), 1), ((26, 22, 13), 1)])
+def test_coarse_levels_vs_oracle(gpu_ctx, qsm, port, dt, shape, nl):
+    """Coarsest grids from 5 to 31 interior planes: solved on a thread-block
+    cluster (one slab of planes per CTA, uneven slabs included), including
+    grids too large for one CTA's shared memory; the boundary-band sweeps run
+    from voxel lists.  Bit-for-bit against the oracle for the PCG, the plain
+    V-cycle iteration and FMG."""
+    import qsm_gb300.synthetic as S
+
+    f, m, _ = S.poisson_case(shape, 7 + nl, semi=(8.0, 30.0))
+    f = f.astype(dt)
+    v0 = np.zeros(shape, dtype=dt, order="F")
+    oi, gi = {}, {}
+    b = port.mgpcg_mex(v0, f, m, [1, 1, 1], 1e-8, 30, -1.0, 2, 1, 2, 2, 2, nl, info=oi)
+    a = qsm.mgpcg_mex(v0, f, m, [1, 1, 1], 1e-8, 30, -1.0, 2, 1, 2, 2, 2, nl, info=gi)
+    assert gi["iters"] == oi["iters"]
+    assert gi["coarse_ctas"] >= 2, gi  # the cluster solver ran
+    assert bits_equal(a, b), first_diff(a, b)
+    a = qsm.mg_mex(v0, f, m, [1, 1, 1], 1e-6, 3, 1, 2, 2, 2, nl)
+    assert bits_equal(a, port.mg_mex(v0, f, m, [1, 1, 1], 1e-6, 3, 1, 2, 2, 2, nl))
+    a = qsm.fmg_mex(f, m, [1, 0.9, 1.2], -1.0, 2, 1, 2, 2, 2, nl)
+    assert bits_equal(a, port.fmg_mex(f, m, [1, 0.9, 1.2], -1.0, 2, 1, 2, 2, 2, nl))
+
+
+def test_mixed_pcg_cluster_coarse(gpu_ctx, qsm, port):
+    """FP64 PCG with the FP32 V-cycle (FP32 coarsest solve on the cluster):
+    same stopping rule, error against the FP64 oracle."""
+    import qsm_gb300.synthetic as S
+
+    f, m, _ = S.poisson_case((70, 64, 58), 5, semi=(20.0, 30.0))
+    v0 = np.zeros(f.shape, order="F")
+    oi, mi = {}, {}
+    b = port.mgpcg_mex(v0, f, m, [1, 1, 1], 1e-8, 100, -1.0, 2, 1, 2, 2, 2, 3, info=oi)
+    c = qsm.mgpcg_mex(v0, f, m, [1, 1, 1], 1e-8, 100, -1.0, 2, 1, 2, 2, 2, 3, mixed=True, info=mi)
+    assert mi["coarse_ctas"] >= 2, mi
+    assert np.linalg.norm(c - b) / np.linalg.norm(b) < 1e-6
+    assert mi["iters"] <= oi["iters"] + 3
+
+
 def test_mg_errors(gpu_ctx, qsm):
     f = np.zeros((8, 8, 8), order="F")
     with pytest.raises(qsm.QsmError, match="DEPTH"):
