@@ -198,6 +198,79 @@ def cpu_baseline(d2f, mask, budget_s=15.0):
             "sample": f"{iters} FP64 iterations of the same 224x224x128 TGV inversion (CPU oracle, OpenMP)"}
 
 
+def _coarsen(G):
+    """Next-level mask (coarsen_grid_mex.c:52-125): coarse interior voxel =
+    AND of its 2x2x2 fine block, block voxels past the fine interior waived."""
+    n = G.shape
+    n2 = tuple(((m - 2 + 1) >> 1) + 2 for m in n)
+    E = np.ones(tuple(2 * (m2 - 2) + 2 for m2 in n2), bool)  # fine index 0 .. 2(n2-2)+1
+    c = tuple(slice(0, min(m - 1, 2 * (m2 - 2) + 2)) for m, m2 in zip(n, n2))
+    E[c] = G[c]
+    for ax, m in enumerate(n):  # a +1 neighbour past the fine interior (index >= m - 1) is waived
+        sl = [slice(None)] * 3
+        sl[ax] = slice(m - 1, None)
+        E[tuple(sl)] = True
+    G2 = np.zeros(n2, bool)
+    core = np.ones(tuple(m2 - 2 for m2 in n2), bool)
+    for a in (0, 1):
+        for b in (0, 1):
+            for cc in (0, 1):
+                core &= E[1 + a::2, 1 + b::2, 1 + cc::2][: n2[0] - 2, : n2[1] - 2, : n2[2] - 2]
+    anchor = G[1::2, 1::2, 1::2][: n2[0] - 2, : n2[1] - 2, : n2[2] - 2]
+    G2[1:-1, 1:-1, 1:-1] = core & anchor
+    return G2
+
+
+def _band(G):
+    """Boundary band B (boundary_mask_mex.c:46-132): G voxels on the outer
+    interior shell or in a 2x2x2 block (odd anchors) not wholly in G, grown by
+    one voxel inside G."""
+    n = G.shape
+    b = np.zeros(n, bool)
+    inner = np.zeros(n, bool)
+    inner[1:-1, 1:-1, 1:-1] = True
+    shell = inner.copy()
+    shell[2:-2, 2:-2, 2:-2] = False
+    b |= shell & G
+    full = np.ones(tuple((m - 1) // 2 for m in n), bool)  # blocks anchored at 1, 3, 5, ...
+    for a in (0, 1):
+        for c in (0, 1):
+            for d in (0, 1):
+                full &= G[1 + a::2, 1 + c::2, 1 + d::2][: full.shape[0], : full.shape[1], : full.shape[2]]
+    nf = np.repeat(np.repeat(np.repeat(~full, 2, 0), 2, 1), 2, 2)
+    blk = np.zeros(n, bool)
+    blk[1: 1 + nf.shape[0], 1: 1 + nf.shape[1], 1: 1 + nf.shape[2]] = nf[: n[0] - 1, : n[1] - 1, : n[2] - 1]
+    b |= blk & G & inner
+    grown = b.copy()
+    for ax in range(3):
+        grown |= np.roll(b, 1, ax) | np.roll(b, -1, ax)
+    return grown & G & inner
+
+
+def mgpcg_fp64_ops(mask, nlevels=5, maxitmg=2, npre=2, npost=2, nb=2, coarse_outer_per_cycle=1):
+    """Algorithmic floating-point operations of one PCG iteration (the
+    reference's expressions, counted per updated voxel): smoothing 10 per G
+    update, residual 11, restriction 30 per coarse G voxel, correction 1 add
+    per fine voxel + 3.25 (mean interpolation cost) per G voxel, the
+    coarsest solve's 256 sweeps per outer iteration, and the PCG vector steps
+    (12 per padded voxel + 10 per G voxel for lapmg)."""
+    G = np.zeros(tuple(m + 2 for m in mask.shape), bool)
+    G[1:-1, 1:-1, 1:-1] = mask != 0
+    levels = [G]
+    for _ in range(nlevels - 1):
+        levels.append(_coarsen(levels[-1]))
+    vcycle = 0.0
+    for l in range(nlevels - 1):
+        g, bnd = float(levels[l].sum()), float(_band(levels[l]).sum())
+        nint = float(np.prod([m - 2 for m in levels[l].shape]))
+        bs = (1 << l) * nb
+        vcycle += (npre + npost) * g * 10 + 2 * bs * bnd * 10 + 11 * g + 30 * levels[l + 1].sum() + nint + 3.25 * g
+    gc = float(levels[-1].sum())
+    vcycle += coarse_outer_per_cycle * (256 * gc * 10 + 11 * gc + 2 * levels[-1].size)
+    n = float(G.size)
+    return maxitmg * vcycle + 12 * n + 10 * float(G.sum())
+
+
 def poisson_arm(qsm_gb300, ctx, torch):
     """256^3 MG-PCG Poisson solve with LBV's options (src/bgremove/lbv.m:58-75):
     FP64 PCG with an FP64 V-cycle (bit-identical to the oracle) beside FP64 PCG
@@ -211,7 +284,9 @@ def poisson_arm(qsm_gb300, ctx, torch):
     m_dev = torch.from_numpy(np.ascontiguousarray(mask.transpose(2, 1, 0))).cuda()
     v0 = torch.zeros_like(f_dev)
     maxit = int(np.ceil(np.sqrt(n)))
-    out = {"workload": "MG-PCG 256^3 FP64, rtol 1e-8, mg maxit 2, npre=npost=2, nboundary 2, mu 1, 5 levels"}
+    pipe = qsm_gb300.fp_pipe_rate("float64", ctx=ctx)
+    out = {"workload": "MG-PCG 256^3 FP64, rtol 1e-8, mg maxit 2, npre=npost=2, nboundary 2, mu 1, 5 levels",
+           "fp64_pipe_ops_per_s": pipe}
     sols = {}
     for mixed in (False, True):
         info = {}
@@ -224,14 +299,15 @@ def poisson_arm(qsm_gb300, ctx, torch):
         wall = time.perf_counter() - t0
         key = "fp32_vcycle" if mixed else "fp64"
         sols[key] = v
-        # algorithmic bytes per voxel and PCG iteration on the padded grid: fine V-cycle
-        # ~13.25 array passes x (1 + 1/7 coarse levels) + 16 PCG passes of 8 B + ~5 mask B
-        bpv = 194 if mixed else 254
-        npad = int(np.prod([s + 2 for s in f.shape]))
-        gbs = bpv * npad * info["iters"] / info["seconds"] / 1e9
-        out[key] = {"iters": info["iters"], "seconds": info["seconds"], "wall_s": wall, "resnorm": info["resnorm"],
-                    "hbm_gbs": gbs, "frac": gbs / _peaks()[0], "bytes_per_voxel_iter": bpv,
-                    "coarse_ctas": info["coarse_ctas"], "coarse_outer": info["coarse_outer"]}
+        rec = {"iters": info["iters"], "seconds": info["seconds"], "wall_s": wall, "resnorm": info["resnorm"],
+               "coarse_ctas": info["coarse_ctas"], "coarse_outer": info["coarse_outer"]}
+        if not mixed:
+            # bound by the FP64 pipe: algorithmic FP64 operations of the solve over its time
+            per_cycle = info["coarse_outer"] / max(1, 2 * info["iters"])
+            ops = mgpcg_fp64_ops(mask, coarse_outer_per_cycle=per_cycle)
+            rec.update(fp64_ops_per_iter=ops, fp64_ops_per_s=ops * info["iters"] / info["seconds"],
+                       fp64_frac=ops * info["iters"] / info["seconds"] / pipe)
+        out[key] = rec
     out["rel_l2_fp32_vcycle_vs_fp64"] = float(torch.linalg.vector_norm(sols["fp32_vcycle"] - sols["fp64"]) /
                                               torch.linalg.vector_norm(sols["fp64"]))
     out["speedup_fp32_vcycle"] = out["fp64"]["seconds"] / out["fp32_vcycle"]["seconds"]
