@@ -173,6 +173,13 @@ def _cpu_model() -> str:
                     break
     except OSError:
         pass
+    if not name:  # Arm kernels list implementer / part codes only; lscpu names the core
+        try:
+            out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+            name = next((ln.split(":", 1)[1].strip() for ln in out.splitlines()
+                         if ln.lower().startswith("model name")), "")
+        except (OSError, subprocess.SubprocessError):
+            pass
     return f"{name or platform.processor() or 'unknown'} ({platform.machine()}, {os.cpu_count()} cores)"
 
 
@@ -185,10 +192,15 @@ def cpu_baseline(d2f, mask, budget_s=15.0):
     cores = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
     n = d2f.size
+    # per-iteration cost from two probes (their difference drops the set-up cost)
     t = time.perf_counter()
     port.pd_tgv_mex(d2f, mask, [1, 1, 1], LAM, ALPHA, 0.0, 5)
     t5 = time.perf_counter() - t
-    iters = int(max(10, min(1000, budget_s / max(t5 / 5, 1e-6))))
+    t = time.perf_counter()
+    port.pd_tgv_mex(d2f, mask, [1, 1, 1], LAM, ALPHA, 0.0, 15)
+    t15 = time.perf_counter() - t
+    per_iter = max((t15 - t5) / 10, t15 / 15 / 4, 1e-6)
+    iters = int(max(10, min(1000, budget_s / per_iter)))
     iters -= iters % 10
     t = time.perf_counter()
     port.pd_tgv_mex(d2f, mask, [1, 1, 1], LAM, ALPHA, 0.0, iters)
@@ -553,7 +565,8 @@ def next_rows_arm(qsm_gb300, ctx, torch, peak, cpu=True, parts="tv64,tv32,pdf,vs
         infos = []
         sec, _ = timed(lambda: qsm_gb300.lbv(f4, mask, [1, 1, 1], infos=infos, ctx=ctx), reps=1)
         out["lbv"] = {"workload": "lbv.m defaults, 4 echoes FP64, host arrays", "seconds": sec,
-                      "pcg_iters": [i["iters"] for i in infos]}
+                      "pcg_iters": [i["iters"] for i in infos], "solve_s": [i["seconds"] for i in infos],
+                      "coarse_ctas": infos[0]["coarse_ctas"], "coarse_outer": [i["coarse_outer"] for i in infos]}
     return out
 
 

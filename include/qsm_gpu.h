@@ -262,7 +262,8 @@ typedef struct {
     double seconds;         /* device time */
     double *resnorm_hist;   /* optional, caller-owned, >= maxitcg doubles */
     int32_t coarse_ctas;    /* coarsest-level solver: 0 host-driven loop, 1 one CTA,
-                               > 1 a thread-block cluster of that many CTAs */
+                               > 1 a thread-block cluster of that many CTAs, < 0 a
+                               cooperative launch of -coarse_ctas CTAs (one per SM) */
     int32_t coarse_outer;   /* outer iterations (256 sweeps each) it ran in total */
 } qsm_mg_info;
 

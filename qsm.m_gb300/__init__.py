@@ -483,7 +483,8 @@ def lbv(f, mask, vsz, tol=1e-8, maxit=None, mgopts=None, verbose=0, *, mixed=Fal
                    int(o_["npre"]), int(o_["npost"]), int(o_["nboundary"]), int(verbose), 1 if mixed else 0, o.ptr,
                    mis)
     if infos is not None:
-        infos[:] = [dict(iters=mis[t].iters, resnorm=mis[t].resnorm, seconds=mis[t].seconds) for t in range(ne)]
+        infos[:] = [dict(iters=mis[t].iters, resnorm=mis[t].resnorm, seconds=mis[t].seconds,
+                         coarse_ctas=mis[t].coarse_ctas, coarse_outer=mis[t].coarse_outer) for t in range(ne)]
     return out
 
 

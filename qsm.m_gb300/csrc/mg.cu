@@ -520,6 +520,151 @@ static qsm_status sweeps_cluster(qsm_ctx *ctx, int cn, T *v, const T *f, uint32_
     return QSM_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Coarsest level over the whole GPU (mgpcg_mex.c:265-275).  When a colour
+// pass of the coarsest grid is large (a shallow hierarchy, e.g. lbv's on a
+// cropped volume: ~16k FP64 updates per colour), one cluster's 16 SMs are
+// bound by their FP64 pipes (~5 us per pass).  Here one CTA per SM, launched
+// cooperatively so that all are resident, takes every pass over the level's
+// G colour lists and the CTAs meet at a grid barrier between passes.  The
+// residual norm keeps the lane order: CTA b halves the 256-element blocks
+// b, b + grid, ..., CTA 0 halves the 1024 block sums.  Every wait is bounded:
+// a barrier that does not complete within CG_SPIN_LIMIT polls sets the error
+// flag, and every CTA leaves at its next barrier.
+// ---------------------------------------------------------------------------
+
+constexpr int CG_THREADS = 256;
+constexpr long long CG_SPIN_LIMIT = 1ll << 22;  // polls of the generation word (seconds)
+constexpr unsigned CG_MIN_PASS = 6000;          // per-colour G count from which the grid beats a cluster
+
+struct GridBar {
+    unsigned *count;  // arrivals since the launch (zeroed by the host before it)
+    int *err;
+};
+
+// Barrier number k (1, 2, ...) of the grid: each CTA adds one arrival with
+// release semantics and polls the count with acquire loads until all
+// gridDim.x x k arrivals are in.  False once any CTA's wait has run out
+// (then every CTA leaves at its next barrier).
+__device__ __forceinline__ bool grid_bar(const GridBar &g, unsigned &k)
+{
+    __shared__ int bad;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned target = ++k * gridDim.x;
+        __threadfence();
+        asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(g.count) : "memory");
+        long long spins = 0;
+        for (;;) {
+            unsigned cur;
+            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(g.count) : "memory");
+            if ((int)(cur - target) >= 0) break;
+            if ((++spins & 1023) == 0 && *(volatile int *)g.err != 0) break;
+            if (spins > CG_SPIN_LIMIT) {
+                atomicExch(g.err, 1);
+                break;
+            }
+        }
+        bad = *(volatile int *)g.err;
+    }
+    __syncthreads();
+    return bad == 0;
+}
+
+// lane-order sum of src[e]^2, e < n (src written before the last barrier);
+// part holds RED_NBLK + 1 values, entries nb .. RED_NBLK - 1 zero
+template <typename T>
+__device__ bool grid_lane_sum(const T *src, unsigned n, T *part, T *red, const GridBar &gb, unsigned &k, T *out)
+{
+    const int tid = threadIdx.x;
+    const unsigned nb = (n + RED_BLOCK - 1) / RED_BLOCK;
+    for (unsigned b = blockIdx.x; b < nb; b += gridDim.x) {
+        const unsigned e = b * RED_BLOCK + tid;
+        const T x = e < n ? __ldcg(src + e) : (T)0;
+        red[tid] = x * x;
+        __syncthreads();
+        for (int st = RED_BLOCK / 2; st > 0; st >>= 1) {
+            if (tid < st) red[tid] = red[tid] + red[tid + st];
+            __syncthreads();
+        }
+        if (tid == 0) part[b] = red[0];
+        __syncthreads();
+    }
+    if (!grid_bar(gb, k)) return false;
+    if (blockIdx.x == 0) {
+        const T tot = halve_partials(red, tid, part);
+        if (tid == 0) part[RED_NBLK] = tot;
+    }
+    if (!grid_bar(gb, k)) return false;
+    *out = __ldcg(part + RED_NBLK);
+    return true;
+}
+
+template <typename T>
+__device__ __forceinline__ void grid_pass(T *v, const T *__restrict__ f, const uint32_t *__restrict__ ls,
+                                          unsigned cnt, uint32_t skip, GsC<T> c, size_t nx, size_t nxny)
+{
+    for (unsigned m = blockIdx.x * CG_THREADS + threadIdx.x; m < cnt; m += gridDim.x * CG_THREADS) {
+        const uint32_t e = ls[m];
+        if (e & skip) continue;
+        const size_t l = e & BL_IDX;
+        v[l] = c.hh * (f[l] + (c.hx * (__ldcg(v + l - 1) + __ldcg(v + l + 1)) +
+                               c.hy * (__ldcg(v + l - nx) + __ldcg(v + l + nx)) +
+                               c.hz * (__ldcg(v + l - nxny) + __ldcg(v + l + nxny))));
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(CG_THREADS) coarse_grid_k(T *v, const T *__restrict__ f, T *r,
+                                                            const uint32_t *__restrict__ l0, unsigned c0,
+                                                            const uint32_t *__restrict__ l1, unsigned c1, Dims d,
+                                                            GsC<T> gc, LapC<T> lc, double tol, GridBar gb, T *part,
+                                                            int *outer_out)
+{
+    __shared__ T red[RED_BLOCK];
+    const size_t nx = d.nx, nxny = d.nxny();
+    const unsigned n = (unsigned)d.n(), nb = (n + RED_BLOCK - 1) / RED_BLOCK;
+    if (blockIdx.x == 0)
+        for (unsigned b = nb + threadIdx.x; b < RED_NBLK; b += CG_THREADS) part[b] = (T)0;
+    unsigned bk = 0;  // barriers passed
+    T ff;
+    if (!grid_lane_sum(f, n, part, red, gb, bk, &ff)) return;
+    const double fn = sizeof(T) == 4 ? (double)sqrtf((float)ff) : sqrt((double)ff);
+    const double reltol = tol * fn;
+    const int rpar0 = (int)((d.nx + 1) & 1);
+    const uint32_t *lr0 = rpar0 ? l1 : l0, *lr1 = rpar0 ? l0 : l1;
+    const unsigned cr0 = rpar0 ? c1 : c0, cr1 = rpar0 ? c0 : c1;
+    int outer = 0;
+    for (int it = 0; it < 1024; ++it) {
+        outer = it + 1;
+        for (int s = 0; s < 128; ++s) {  // reverse sweeps
+            grid_pass(v, f, lr0, cr0, 0u, gc, nx, nxny);
+            if (!grid_bar(gb, bk)) return;
+            grid_pass(v, f, lr1, cr1, BL_INX2, gc, nx, nxny);
+            if (!grid_bar(gb, bk)) return;
+        }
+        for (int s = 0; s < 128; ++s) {  // forward sweeps
+            grid_pass(v, f, l0, c0, 0u, gc, nx, nxny);
+            if (!grid_bar(gb, bk)) return;
+            grid_pass(v, f, l1, c1, BL_I1, gc, nx, nxny);
+            if (!grid_bar(gb, bk)) return;
+        }
+        // residual of the interior G voxels (both colour lists), then its norm over all of r
+        for (unsigned m = blockIdx.x * CG_THREADS + threadIdx.x; m < c0 + c1; m += gridDim.x * CG_THREADS) {
+            const size_t l = (m < c0 ? l0[m] : l1[m - c0]) & BL_IDX;
+            r[l] = f[l] + (lc.hh * __ldcg(v + l) + lc.hx * (__ldcg(v + l - 1) + __ldcg(v + l + 1)) +
+                           lc.hy * (__ldcg(v + l - nx) + __ldcg(v + l + nx)) +
+                           lc.hz * (__ldcg(v + l - nxny) + __ldcg(v + l + nxny)));
+        }
+        if (!grid_bar(gb, bk)) return;
+        T rr;
+        if (!grid_lane_sum(r, n, part, red, gb, bk, &rr)) return;
+        const double rn = sizeof(T) == 4 ? (double)sqrtf((float)rr) : sqrt((double)rr);
+        if (rn < reltol) break;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0 && outer_out) *outer_out += outer;
+}
+
 __global__ void bmask_l1_init_k(uint8_t *B, uint8_t *GL, const uint8_t *__restrict__ G, Dims d)
 {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -953,7 +1098,7 @@ struct Level {
     double h[3];
     uint32_t *bl[2];     // B voxels of each colour (null: full-grid passes over B)
     unsigned bn[2];
-    uint32_t *gl[2];     // G voxels of each colour, kept for small levels only
+    uint32_t *gl[2];     // G voxels of each colour (null: full-grid passes)
     unsigned gn[2];
     bool bcl, gcl;       // B / G passes of a smoothing call run on one cluster launch
 };
@@ -970,6 +1115,9 @@ struct Hier {
     void *lists;         // the levels' colour lists (one allocation)
     int sw_ctas;         // cluster size of the list passes (0: not available)
     int host_outer;      // outer iterations of the host-driven coarsest solve
+    int cg_ctas;         // > 0: the coarsest level runs on this many CTAs, cooperatively (wins over the cluster)
+    GridBar gb;          // their barrier words (arrival count, error flag)
+    void *gpart;         // RED_NBLK + 1 lane-order block sums
     int cc_ctas;         // > 0: the coarsest level runs on a cluster of this many CTAs
     int cc_npmax;        // planes per CTA (largest slab)
     size_t cc_smem;
@@ -1078,7 +1226,7 @@ static qsm_status hier_init(qsm_ctx *ctx, Hier<T> &H, int nl, const Dims &dp, co
         for (int q = 0; q < 3; ++q) H.L[i].h[q] = i == 0 ? h[q] : H.L[i - 1].h[q] * 2.0;
         bytes += 3 * al256(d.n() * sizeof(T)) + 2 * al256(d.n());
     }
-    bytes += al256(dp.n()) + 512;
+    bytes += al256(dp.n()) + 512 + al256((RED_NBLK + 1) * sizeof(double)) + 256;
     QSM_TRY(dalloc(ctx, &H.blk, bytes));
     QSM_CUDA(cudaMemsetAsync(H.blk, 0, bytes, ctx->stream));
     char *c = (char *)H.blk;
@@ -1092,6 +1240,11 @@ static qsm_status hier_init(qsm_ctx *ctx, Hier<T> &H, int nl, const Dims &dp, co
     }
     H.scratch = (uint8_t *)c; c += al256(dp.n());
     H.counters = (int *)c;
+    c += 512;
+    H.gpart = c;
+    c += al256((RED_NBLK + 1) * sizeof(double));
+    H.gb.count = (unsigned *)c;
+    H.gb.err = (int *)c + 1;
     const size_t nc = H.L[nl - 1].n;
     H.coarse_smem = nc * (3 * sizeof(T) + 1) + RED_NBLK * sizeof(T) + 64;
     int maxsm = 0;
@@ -1102,8 +1255,35 @@ static qsm_status hier_init(qsm_ctx *ctx, Hier<T> &H, int nl, const Dims &dp, co
     return QSM_OK;
 }
 
-// Colour lists of every level's boundary band B and, on levels small enough
-// for the cluster passes, of G (counted, then filled into one allocation).
+// The whole-GPU coarsest solver: for large colour passes, or where neither a
+// cluster nor one CTA holds the grid; needs the coarsest level's G lists and
+// cooperative launch.  cg_ctas = one CTA per SM, else 0.
+template <typename T>
+static void plan_coarse_grid(qsm_ctx *ctx, Hier<T> &H)
+{
+    H.cg_ctas = 0;
+    const Level<T> &C = H.L[H.nl - 1];
+    if (!C.gl[0] || C.d.nx < 3 || C.d.ny < 3 || C.d.nz < 3 || C.n >= (1u << 30)) return;
+    const bool large = C.gn[0] > CG_MIN_PASS || C.gn[1] > CG_MIN_PASS;
+    if (!large && (H.cc_ctas > 0 || H.coarse_in_smem)) return;
+    int coop = 0, sms = 0, per_sm = 0;
+    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device) != cudaSuccess || !coop ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, coarse_grid_k<T>, CG_THREADS, 0) != cudaSuccess ||
+        per_sm < 1) {
+        cudaGetLastError();
+        return;
+    }
+    H.cg_ctas = sms;
+    // QSM_COARSE_GRID_CTAS overrides the CTA count (1 .. SMs), for tuning
+    if (const char *e = getenv("QSM_COARSE_GRID_CTAS")) {
+        const int want = atoi(e);
+        if (want >= 1 && want <= sms) H.cg_ctas = want;
+    }
+}
+
+// Colour lists of every level's G and boundary band B (counted, then filled
+// into one allocation); small levels run their passes on one cluster launch.
 // Grids of 2^30 voxels or more keep the full-grid passes.
 template <typename T>
 static qsm_status boundary_lists(qsm_ctx *ctx, Hier<T> &H)
@@ -1117,7 +1297,7 @@ static qsm_status boundary_lists(qsm_ctx *ctx, Hier<T> &H)
         const dim3 g = interior_grid3(L.d);
         if (!(g.x && g.y && g.z)) continue;
         blist_k<<<g, vox_block(), 0, ctx->stream>>>(nullptr, nullptr, cnt + 4 * i, L.B, L.d, 0);
-        if (i > 0) blist_k<<<g, vox_block(), 0, ctx->stream>>>(nullptr, nullptr, cnt + 4 * i + 2, L.G, L.d, 0);
+        blist_k<<<g, vox_block(), 0, ctx->stream>>>(nullptr, nullptr, cnt + 4 * i + 2, L.G, L.d, 0);
     }
     QSM_CUDA(cudaGetLastError());
     unsigned hc[64];
@@ -1130,10 +1310,8 @@ static qsm_status boundary_lists(qsm_ctx *ctx, Hier<T> &H)
         const bool small_g = i > 0 && cn > 0 && hc[4 * i + 2] <= cap && hc[4 * i + 3] <= cap;
         L.bcl = i > 0 && cn > 0 && hc[4 * i] <= cap && hc[4 * i + 1] <= cap;
         L.gcl = small_g;
-        for (int p = 0; p < 2; ++p) {
-            tot += al256((size_t)hc[4 * i + p] * sizeof(uint32_t));
-            if (small_g) tot += al256((size_t)hc[4 * i + 2 + p] * sizeof(uint32_t));
-        }
+        for (int p = 0; p < 2; ++p)
+            tot += al256((size_t)hc[4 * i + p] * sizeof(uint32_t)) + al256((size_t)hc[4 * i + 2 + p] * sizeof(uint32_t));
     }
     QSM_TRY(dalloc(ctx, &H.lists, tot + 256));
     H.sw_ctas = cn;
@@ -1146,12 +1324,9 @@ static qsm_status boundary_lists(qsm_ctx *ctx, Hier<T> &H)
             c += al256((size_t)hc[4 * i + p] * sizeof(uint32_t));
         }
         for (int p = 0; p < 2; ++p) {
-            L.gl[p] = nullptr;
+            L.gl[p] = (uint32_t *)c;
             L.gn[p] = hc[4 * i + 2 + p];
-            if (L.gcl) {
-                L.gl[p] = (uint32_t *)c;
-                c += al256((size_t)hc[4 * i + 2 + p] * sizeof(uint32_t));
-            }
+            c += al256((size_t)hc[4 * i + 2 + p] * sizeof(uint32_t));
         }
     }
     QSM_CUDA(cudaMemsetAsync(cnt, 0, 4 * H.nl * sizeof(unsigned), ctx->stream));
@@ -1160,20 +1335,67 @@ static qsm_status boundary_lists(qsm_ctx *ctx, Hier<T> &H)
         const dim3 g = interior_grid3(L.d);
         if (!(g.x && g.y && g.z)) continue;
         blist_k<<<g, vox_block(), 0, ctx->stream>>>(L.bl[0], L.bl[1], cnt + 4 * i, L.B, L.d, 1);
-        if (L.gcl) blist_k<<<g, vox_block(), 0, ctx->stream>>>(L.gl[0], L.gl[1], cnt + 4 * i + 2, L.G, L.d, 1);
+        blist_k<<<g, vox_block(), 0, ctx->stream>>>(L.gl[0], L.gl[1], cnt + 4 * i + 2, L.G, L.d, 1);
     }
+    QSM_CUDA(cudaGetLastError());
+    plan_coarse_grid<T>(ctx, H);
+    return QSM_OK;
+}
+
+// `iter` colour-pass pairs (gauss_seidel's order and skips) over colour lists,
+// one launch per pass.
+template <typename T>
+static qsm_status list_sweeps(qsm_ctx *ctx, T *v, const T *f, uint32_t *const lists[2], const unsigned cnt[2],
+                              const double *h, const Dims &d, int32_t iter, bool rev)
+{
+    const GsC<T> c = gs_consts<T>(h);
+    const int par0 = rev ? (int)((d.nx + 1) & 1) : 0;
+    const uint32_t skip = rev ? BL_INX2 : BL_I1;
+    for (int32_t s = 0; s < iter; ++s)
+        for (int q = 0; q < 2; ++q) {
+            const int par = par0 ^ q;
+            if (!cnt[par]) continue;
+            gs_list_k<T><<<(cnt[par] + 255) / 256, 256, 0, ctx->stream>>>(v, f, lists[par], cnt[par], q ? skip : 0u, c,
+                                                                         d.nx, d.nxny());
+        }
     QSM_CUDA(cudaGetLastError());
     return QSM_OK;
 }
 
 // `iter` colour-pass pairs over a level's G (gauss_seidel over G): one
-// cluster launch on small levels, else one full-grid launch per pass.
+// cluster launch on small levels, else one launch per pass over the colour
+// lists (full-grid passes only where there are no lists).
 template <typename T>
 static qsm_status smooth(qsm_ctx *ctx, const Hier<T> &H, Level<T> &L, int32_t iter, bool rev)
 {
-    if (L.gcl && iter > 0 && L.d.nx >= 3 && L.d.ny >= 3 && L.d.nz >= 3)
-        return sweeps_cluster<T>(ctx, H.sw_ctas, L.v, L.f, L.gl, L.gn, L.h, L.d, iter, rev);
-    return gauss_seidel<T>(ctx, L.v, L.f, L.G, L.h, L.d, iter, rev);
+    if (!L.gl[0]) return gauss_seidel<T>(ctx, L.v, L.f, L.G, L.h, L.d, iter, rev);
+    if (L.d.nx < 3 || L.d.ny < 3 || L.d.nz < 3 || iter <= 0) return QSM_OK;
+    if (L.gcl) return sweeps_cluster<T>(ctx, H.sw_ctas, L.v, L.f, L.gl, L.gn, L.h, L.d, iter, rev);
+    return list_sweeps<T>(ctx, L.v, L.f, L.gl, L.gn, L.h, L.d, iter, rev);
+}
+
+// residual on G from its colour lists (residual_k restricted to G, in any order)
+template <typename T>
+__global__ void residual_list_k(T *r, const T *__restrict__ f, const T *__restrict__ x,
+                                const uint32_t *__restrict__ l0, unsigned c0, const uint32_t *__restrict__ l1,
+                                unsigned c1, LapC<T> c, size_t nx, size_t nxny)
+{
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= c0 + c1) return;
+    const size_t l = (t < c0 ? l0[t] : l1[t - c0]) & BL_IDX;
+    r[l] = f[l] + (c.hh * x[l] + c.hx * (x[l - 1] + x[l + 1]) + c.hy * (x[l - nx] + x[l + nx]) + c.hz * (x[l - nxny] + x[l + nxny]));
+}
+
+template <typename T>
+static qsm_status level_residual(qsm_ctx *ctx, Level<T> &L)
+{
+    if (!L.gl[0]) return residual<T>(ctx, L.r, L.f, L.v, L.G, L.h, L.d);
+    const unsigned n = L.gn[0] + L.gn[1];
+    if (n == 0 || L.d.nx < 3 || L.d.ny < 3 || L.d.nz < 3) return QSM_OK;
+    residual_list_k<T><<<(n + 255) / 256, 256, 0, ctx->stream>>>(L.r, L.f, L.v, L.gl[0], L.gn[0], L.gl[1], L.gn[1],
+                                                                 lap_consts<T>(L.h), L.d.nx, L.d.nxny());
+    QSM_CUDA(cudaGetLastError());
+    return QSM_OK;
 }
 
 // `iter` colour-pass pairs over a level's boundary band (gauss_seidel over B).
@@ -1183,19 +1405,7 @@ static qsm_status boundary_sweeps(qsm_ctx *ctx, const Hier<T> &H, Level<T> &L, i
     if (!L.bl[0]) return gauss_seidel<T>(ctx, L.v, L.f, L.B, L.h, L.d, iter, rev);
     if (L.d.nx < 3 || L.d.ny < 3 || L.d.nz < 3 || iter <= 0) return QSM_OK;
     if (L.bcl) return sweeps_cluster<T>(ctx, H.sw_ctas, L.v, L.f, L.bl, L.bn, L.h, L.d, iter, rev);
-    const GsC<T> c = gs_consts<T>(L.h);
-    const int par0 = rev ? (int)((L.d.nx + 1) & 1) : 0;
-    const uint32_t skip = rev ? BL_INX2 : BL_I1;
-    for (int32_t s = 0; s < iter; ++s)
-        for (int q = 0; q < 2; ++q) {
-            const int par = par0 ^ q;
-            const unsigned cnt = L.bn[par];
-            if (!cnt) continue;
-            gs_list_k<T><<<(cnt + 255) / 256, 256, 0, ctx->stream>>>(L.v, L.f, L.bl[par], cnt, q ? skip : 0u, c, L.d.nx,
-                                                                    L.d.nxny());
-        }
-    QSM_CUDA(cudaGetLastError());
-    return QSM_OK;
+    return list_sweeps<T>(ctx, L.v, L.f, L.bl, L.bn, L.h, L.d, iter, rev);
 }
 
 template <typename T>
@@ -1226,6 +1436,23 @@ static qsm_status coarse_solve(qsm_ctx *ctx, Hier<T> &H, int l, double *scal_dev
 {
     Level<T> &L = H.L[l];
     const double tol = sizeof(T) == 4 ? 1e-4 : 1e-8;
+    if (H.cg_ctas > 0) {
+        T *vv = L.v, *rr = L.r, *part = (T *)H.gpart;
+        const T *ff = L.f;
+        const uint32_t *la = L.gl[0], *lb = L.gl[1];
+        unsigned ca = L.gn[0], cb = L.gn[1];
+        Dims dd = L.d;
+        GsC<T> gc = gs_consts<T>(L.h);
+        LapC<T> lc = lap_consts<T>(L.h);
+        double tl = tol;
+        GridBar gb = H.gb;
+        int *outer = H.counters;
+        void *args[] = {&vv, &ff, &rr, &la, &ca, &lb, &cb, &dd, &gc, &lc, &tl, &gb, &part, &outer};
+        QSM_CUDA(cudaMemsetAsync(H.gb.count, 0, sizeof(unsigned), ctx->stream));
+        QSM_CUDA(cudaLaunchCooperativeKernel((const void *)coarse_grid_k<T>, dim3((unsigned)H.cg_ctas),
+                                             dim3(CG_THREADS), args, 0, ctx->stream));
+        return QSM_OK;
+    }
     if (H.cc_ctas > 0) {
         cudaLaunchConfig_t cfg = {};
         cudaLaunchAttribute at[1];
@@ -1274,7 +1501,7 @@ static qsm_status cycle(qsm_ctx *ctx, Hier<T> &H, int l, int mu, int pre, int po
         const int32_t bs = (1 << l) * nb;
         QSM_TRY(smooth<T>(ctx, H, L, pre, true));
         QSM_TRY(boundary_sweeps<T>(ctx, H, L, bs, true));
-        QSM_TRY(residual<T>(ctx, L.r, L.f, L.v, L.G, L.h, L.d));
+        QSM_TRY(level_residual<T>(ctx, L));
         QSM_TRY(restrict_<T>(ctx, C.f, L.r, C.G, C.d, L.d));
         QSM_CUDA(cudaMemsetAsync(C.v, 0, C.n * sizeof(T), ctx->stream));
         for (int i = 0; i < mu; ++i) {
@@ -1431,23 +1658,13 @@ __global__ void __launch_bounds__(RED_BLOCK) pcg_q_k(T *__restrict__ q, const T 
                                                      unsigned *count, double *sc)
 {
     __shared__ T sm[RED_BLOCK];
-    const size_t nx = d.nx, nxny = d.nxny(), n = d.n();
-    const bool small = n <= 0xFFFFFFFFull;  // 32-bit index arithmetic
+    const size_t nx = d.nx, ny = d.ny, nxny = d.nxny(), n = d.n();
+    // (i, j, k) of l, then advanced by the lane stride in mixed radix (no division per element)
+    const size_t t = (size_t)blockIdx.x * RED_BLOCK + threadIdx.x;
+    size_t k = t / nxny, j = (t - k * nxny) / nx, i = t - k * nxny - j * nx;
+    const size_t Lk = RED_LANES / nxny, Lj = (RED_LANES - Lk * nxny) / nx, Li = RED_LANES - Lk * nxny - Lj * nx;
     T acc = (T)0;
-    for (size_t l = (size_t)blockIdx.x * RED_BLOCK + threadIdx.x; l < n; l += RED_LANES) {
-        size_t i, j, k;
-        if (small) {
-            const uint32_t l32 = (uint32_t)l, k32 = l32 / (uint32_t)nxny, rem = l32 - k32 * (uint32_t)nxny;
-            const uint32_t j32 = rem / (uint32_t)nx;
-            i = rem - j32 * (uint32_t)nx;
-            j = j32;
-            k = k32;
-        } else {
-            k = l / nxny;
-            const size_t rem = l - k * nxny;
-            j = rem / nx;
-            i = rem - j * nx;
-        }
+    for (size_t l = t; l < n; l += RED_LANES) {
         const T pl = p[l];
         T qv;
         if (i >= 1 && j >= 1 && k >= 1 && i + 1 < nx && j + 1 < d.ny && k + 1 < d.nz && G[l])
@@ -1457,6 +1674,13 @@ __global__ void __launch_bounds__(RED_BLOCK) pcg_q_k(T *__restrict__ q, const T 
         qv = neg_bits(qv);
         q[l] = qv;
         acc = acc + pl * qv;
+        i += Li;
+        const size_t cj = i >= nx;
+        i -= cj * nx;
+        j += Lj + cj;
+        const size_t ck = j >= ny;
+        j -= ck * ny;
+        k += Lk + ck;
     }
     T tot;
     if (lane_fold(sm, acc, part, count, &tot) && threadIdx.x == 0) {
@@ -1513,13 +1737,22 @@ __global__ void __launch_bounds__(RED_BLOCK) pcg_xr_k(TP *__restrict__ x, const 
 
 // Which coarsest-level solver ran and its outer iterations (after the stream
 // has been synchronised).
+// (Also fails the solve if a whole-GPU coarsest solve's barrier ran out.)
 template <typename T>
 static qsm_status coarse_report(qsm_ctx *ctx, const Hier<T> &H, qsm_mg_info *info)
 {
+    if (H.cg_ctas > 0) {
+        int err = 0;
+        QSM_CUDA(cudaMemcpy(&err, H.gb.err, sizeof(int), cudaMemcpyDeviceToHost));
+        if (err) {
+            set_error(ctx, "coarsest-level solve: a grid barrier timed out");
+            return QSM_ERR_TIMEOUT;
+        }
+    }
     if (!info) return QSM_OK;
     int dev_outer = 0;
     QSM_CUDA(cudaMemcpy(&dev_outer, H.counters, sizeof(int), cudaMemcpyDeviceToHost));
-    info->coarse_ctas = H.cc_ctas > 0 ? H.cc_ctas : (H.coarse_in_smem ? 1 : 0);
+    info->coarse_ctas = H.cg_ctas > 0 ? -H.cg_ctas : H.cc_ctas > 0 ? H.cc_ctas : (H.coarse_in_smem ? 1 : 0);
     info->coarse_outer = dev_outer + H.host_outer;
     return QSM_OK;
 }

@@ -132,6 +132,28 @@ def test_coarse_levels_vs_oracle(gpu_ctx, qsm, port, dt, shape, nl):
     assert bits_equal(a, port.fmg_mex(f, m, [1, 0.9, 1.2], -1.0, 2, 1, 2, 2, 2, nl))
 
 
+@pytest.mark.parametrize("dt", ("float64", "float32"))
+def test_coarse_grid_solver_vs_oracle(gpu_ctx, qsm, port, dt):
+    """A shallow hierarchy (2 levels) whose coarsest colour passes hold ~9.5k
+    voxels: the coarsest solve runs over the whole GPU (one CTA per SM, grid
+    barrier per pass).  Bit-for-bit against the oracle."""
+    import qsm_gb300.synthetic as S
+
+    f, m, _ = S.poisson_case((96, 88, 80), 9, semi=(30.0, 40.0))
+    f = f.astype(dt)
+    v0 = np.zeros(f.shape, dtype=dt, order="F")
+    oi, gi = {}, {}
+    b = port.mgpcg_mex(v0, f, m, [1, 1, 1], 1e-8, 30, -1.0, 1, 1, 2, 2, 2, 2, info=oi)
+    a = qsm.mgpcg_mex(v0, f, m, [1, 1, 1], 1e-8, 30, -1.0, 1, 1, 2, 2, 2, 2, info=gi)
+    assert gi["coarse_ctas"] < 0, gi  # the whole-GPU solver ran
+    assert gi["iters"] == oi["iters"] and gi["coarse_outer"] > 0
+    assert bits_equal(a, b), first_diff(a, b)
+    gm = {}
+    a = qsm.mg_mex(v0, f, m, [1, 1, 1], 1e-6, 2, 1, 2, 2, 2, 2, info=gm)
+    assert gm["coarse_ctas"] < 0
+    assert bits_equal(a, port.mg_mex(v0, f, m, [1, 1, 1], 1e-6, 2, 1, 2, 2, 2, 2))
+
+
 def test_mixed_pcg_cluster_coarse(gpu_ctx, qsm, port):
     """FP64 PCG with the FP32 V-cycle (FP32 coarsest solve on the cluster):
     same stopping rule, error against the FP64 oracle."""
