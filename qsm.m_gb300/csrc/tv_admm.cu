@@ -2,8 +2,10 @@
 // GPU: the data term's solve u = real(ifft3(iA .* (F + fft3(r)))) runs as a
 // cuFFT R2C, one fused pointwise k-space kernel, and a cuFFT C2R; the
 // gradient, shrinkage, multiplier update and residual norms are fused
-// stencil kernels.  Only the five convergence scalars per iteration go to
-// the host, which applies tv.m's stopping test and rho update (:226-268).
+// stencil kernels.  tv.m's stopping test and rho update (:226-268) run on the
+// device (tv_ctl_k, FP64, the host's arithmetic), so iterations are queued
+// without a host round trip; the host reads the control state every eighth
+// iteration.
 //
 // k-space terms come from per-axis tables and one stored half-spectrum array:
 //   D(k) = 1/3 - (k.b)^2/|k|^2, D(0) = 0, k_a = fftfreq(n_a, h_a)
@@ -48,6 +50,9 @@ template <typename T> constexpr int tv_grid() { return 152 * TvOcc<T>::minb; }
 template <typename T> struct TvOccGS { static constexpr int minb = sizeof(T) == 4 ? 4 : 3; };
 constexpr int TV_GRID_MAX = 152 * 5;
 constexpr int TV_NSUM = 5;         // nr, na, nb, ||s||^2, ||rho grad' l||^2
+// ADMM control state on the device (doubles): rho and its inverse, the last
+// iteration's residuals and tolerances, the rho-schedule flag, done, iteration
+enum { C_RHO, C_IRHO, C_NR, C_NS, C_NA, C_NB, C_EP, C_ED, C_FLAG, C_DONE, C_IT, C_N };
 
 struct TvK {
     int nx, ny, nz, nxh;   // real dims, half-spectrum x extent
@@ -148,11 +153,10 @@ __device__ __forceinline__ T inv_a(T K, T L, T rho)
 // precision T
 template <typename T>
 __global__ void __launch_bounds__(TV_BLOCK, TvOcc<T>::minb) kmul_k(typename CxT<T>::type *R, const typename CxT<T>::type *__restrict__ fhat,
-                       const T *__restrict__ Dq, const double *__restrict__ tab, TvK K, double rho_, double invn_)
+                       const T *__restrict__ Dq, const double *__restrict__ tab, TvK K, const double *ctl, double invn_)
 {
-    const size_t nh = (size_t)K.nxh * K.ny * K.nz;
     const int tot = K.nxh + K.ny + K.nz;
-    const T mu = (T)K.mu, rho = (T)rho_, invn = (T)invn_;
+    const T mu = (T)K.mu, rho = (T)ctl[C_RHO], invn = (T)invn_;
     const Dims hd{(size_t)K.nxh, (size_t)K.ny, (size_t)K.nz};
     VOX_LOOP(wk, hd) {
         const size_t q = wk.v.l;
@@ -190,13 +194,19 @@ __device__ __forceinline__ T adj_at(const Vox &v, const Dims &d, const T *ih, G 
     return v.k == 0 ? (a + b) + c : v.j == 0 ? (c + a) + b : (c + b) + a;
 }
 
-// r = gradfp_adj(rho v - l) (tv.m:166-170)
+// r = gradfp_adj(rho v - l) (tv.m:166-170).  Iteration ii also keeps u when
+// the control state says iteration ii - 1 converged: the iterations the host
+// launched past convergence overwrite u.
 template <typename T>
-__global__ void __launch_bounds__(TV_BLOCK, TvOcc<T>::minb) adj_rhs_k(T *r, const T *__restrict__ v, const T *__restrict__ lm, Dims d, T nx_, T ny_, T nz_, T rho)
+__global__ void __launch_bounds__(TV_BLOCK, TvOcc<T>::minb) adj_rhs_k(T *r, const T *__restrict__ v, const T *__restrict__ lm, Dims d, T nx_, T ny_, T nz_,
+                                       const double *ctl, int ii, T *usave, const T *__restrict__ u)
 {
     const size_t N = d.n();
     const T ih[3] = {nx_, ny_, nz_};
+    const T rho = (T)ctl[C_RHO];
+    const bool save = ctl[C_DONE] != 0.0 && ctl[C_IT] == (double)(ii - 1);
     VOX_LOOP(wk, d) {
+        if (save) usave[wk.v.l] = u[wk.v.l];
         r[wk.v.l] = adj_at<T>(wk.v, d, ih, [&](int c, size_t m) { return rho * v[c * N + m] - lm[c * N + m]; });
     }
 }
@@ -225,8 +235,9 @@ __device__ __forceinline__ void block_sums(double *part, double (&acc)[NS])
 template <typename T, bool ISO>
 __global__ void __launch_bounds__(TV_BLOCK, TvOccGS<T>::minb)
 grad_shrink_k(T *vn, const T *__restrict__ vo, T *lm, const T *__restrict__ u, Dims d, T hx, T hy, T hz, T alpha,
-              T rho, T irho, double *part)
+              const double *ctl, double *part)
 {
+    const T rho = (T)ctl[C_RHO], irho = (T)ctl[C_IRHO];
     const size_t N = d.n();
     PartialSum<T> ps[3];  // nr, na, nb
     VOX_LOOP(wk, d) {
@@ -286,9 +297,10 @@ grad_shrink_k(T *vn, const T *__restrict__ vo, T *lm, const T *__restrict__ u, D
 template <typename T>
 __global__ void __launch_bounds__(TV_BLOCK, TvOccGS<T>::minb)
 grad_shrink_norms_k(T *vn, const T *__restrict__ vo, T *__restrict__ lmn, const T *__restrict__ lmo,
-                    const T *__restrict__ u, Dims d, T hx, T hy, T hz, T alpha, T rho, T irho, T nx_, T ny_, T nz_,
+                    const T *__restrict__ u, Dims d, T hx, T hy, T hz, T alpha, const double *ctl, T nx_, T ny_, T nz_,
                     double *part)
 {
+    const T rho = (T)ctl[C_RHO], irho = (T)ctl[C_IRHO];
     const size_t N = d.n();
     const T hh[3] = {hx, hy, hz}, ih[3] = {nx_, ny_, nz_};
     PartialSum<T> ps[5];  // nr, na, nb, ||s||^2, ||rho grad' l||^2
@@ -347,8 +359,9 @@ grad_shrink_norms_k(T *vn, const T *__restrict__ vo, T *__restrict__ lmn, const 
 template <typename T>
 __global__ void __launch_bounds__(TV_BLOCK, TvOcc<T>::minb)
 adj_norms_k(const T *__restrict__ vn, const T *__restrict__ vo, const T *__restrict__ lm, Dims d, T nx_, T ny_, T nz_,
-            T rho, double *part)
+            const double *ctl, double *part)
 {
+    const T rho = (T)ctl[C_RHO];
     const size_t N = d.n();
     const T ih[3] = {nx_, ny_, nz_};
     PartialSum<T> ps[2];
@@ -440,6 +453,45 @@ static const char *cufft_str(cufftResult r)
     }
 }
 
+// tv.m's stopping test and rho schedule (tv.m:226-268) for iteration ii, in
+// FP64 with the host's operations and order (no fused multiply-add on either
+// side), from the five sums of the iteration.  Nothing changes once done.
+struct TvCtlOpts {
+    double rtol, atolp, atold, rtau, stau, gamma;
+};
+
+__global__ void tv_ctl_k(double *ctl, const double *__restrict__ sums, TvCtlOpts o, int ii)
+{
+    if (ctl[C_DONE] != 0.0) return;
+    const double nrp = ctl[C_NR];
+    const double nr = sums[0], na = sums[1], nb = sums[2], ns = sqrt(sums[3]);
+    const double ep = o.atolp + o.rtol * (na < nb ? nb : na);
+    const double ed = o.atold + o.rtol * sqrt(sums[4]);
+    ctl[C_NR] = nr;
+    ctl[C_NS] = ns;
+    ctl[C_NA] = na;
+    ctl[C_NB] = nb;
+    ctl[C_EP] = ep;
+    ctl[C_ED] = ed;
+    ctl[C_IT] = (double)ii;
+    if (nr < ep && ns < ed) {
+        ctl[C_DONE] = 1.0;
+        return;
+    }
+    double rho = ctl[C_RHO], flag = ctl[C_FLAG];
+    if (nr > o.stau * ns || (nr > o.rtau * nrp && flag < 3.0)) {
+        rho = o.gamma * rho;
+        ctl[C_IRHO] = 1.0 / rho;
+        if (flag > 5.0) flag = 0.0;
+    } else if (nr < ns / o.stau) {
+        rho = rho / (o.gamma * o.gamma);
+        ctl[C_IRHO] = 1.0 / rho;
+        flag = flag + 1.0;
+    }
+    ctl[C_RHO] = rho;
+    ctl[C_FLAG] = flag;
+}
+
 #define QSM_FFT(call)                                                                           \
     do {                                                                                        \
         cufftResult r_ = (call);                                                                \
@@ -480,12 +532,13 @@ static qsm_status tv_run(qsm_ctx *ctx, const Dims &d, const S *f, const uint8_t 
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     const size_t rb = al(N * sizeof(T)), vb = al(3 * N * sizeof(T)), cb = al(nh * sizeof(C));
     const size_t tb = al(2 * (size_t)(nxh + d.ny + d.nz) * sizeof(double)), db = al(nh * sizeof(T));
-    const size_t bytes = 2 * rb + 4 * vb + 2 * cb + tb + db + (TV_NSUM * TV_GRID_MAX + 64) * sizeof(double);
+    const size_t bytes = 3 * rb + 4 * vb + 2 * cb + tb + db + (TV_NSUM * TV_GRID_MAX + 64 + C_N) * sizeof(double);
     void *blk = nullptr;
     QSM_TRY(dalloc(ctx, &blk, bytes));
     char *c = (char *)blk;
     T *u = (T *)c; c += rb;
     T *r = (T *)c; c += rb;
+    T *usave = (T *)c; c += rb;  // u of the converged iteration
     T *v[2];
     v[0] = (T *)c; c += vb;
     v[1] = (T *)c; c += vb;
@@ -499,16 +552,17 @@ static qsm_status tv_run(qsm_ctx *ctx, const Dims &d, const S *f, const uint8_t 
     T *Dq = (T *)c; c += db;
     double *part = (double *)c;
     double *sums = part + TV_NSUM * TV_GRID_MAX;
+    double *ctl = sums + 64;
 
     qsm_status st = QSM_OK;
     cufftHandle pf = 0, pi = 0;
     bool havef = false, havei = false;
     const cufftType tf = sizeof(T) == 8 ? CUFFT_D2Z : CUFFT_R2C, ti = sizeof(T) == 8 ? CUFFT_Z2D : CUFFT_C2R;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
-    double hs[TV_NSUM];
-    double nr = 0.0, nr_, ns = 0.0, na, nb, ep = 0.0, ed = 0.0, rho = o.rho, irho = 1.0 / o.rho;
-    int flag = 0, cur = 0;
+    double hc[C_N] = {};
+    int cur = 0;
     uint32_t it = 0;
+    bool from_save = false;
     const double atolp = sqrt(3.0 * (double)N) * o.atol, atold = sqrt((double)N) * o.atol;
     TvK K;
     K.nx = (int)d.nx; K.ny = (int)d.ny; K.nz = (int)d.nz; K.nxh = nxh;
@@ -544,77 +598,81 @@ static qsm_status tv_run(qsm_ctx *ctx, const Dims &d, const S *f, const uint8_t 
     else QSM_FFT(cufftExecR2C(pf, (cufftReal *)u, (cufftComplex *)fhat));
     grad_init_k<T><<<g, b, 0, ctx->stream>>>(v[0], u, d, ihx, ihy, ihz, part);
     fold_k<<<1, TV_BLOCK, 0, ctx->stream>>>(sums, part, 1, TV_GRID, 0, 0);
-    QSM_STEP(cuda_st(ctx, cudaMemcpyAsync(hs, sums, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "copy"));
-    QSM_STEP(cuda_st(ctx, cudaStreamSynchronize(ctx->stream), "sync"));
-    nr = hs[0];
+    // control state: rho, 1/rho (as the host forms it), nr of the initial v, flag 0
+    hc[C_RHO] = o.rho;
+    hc[C_IRHO] = 1.0 / o.rho;
+    QSM_STEP(cuda_st(ctx, cudaMemcpyAsync(ctl, hc, C_N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream), "copy"));
+    QSM_STEP(cuda_st(ctx, cudaMemcpyAsync(ctl + C_NR, sums, sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream), "copy"));
     if (o.verbose) printf("\niter\t\t||r||\t\teps_pri\t\t||s||\t\teps_dual\n");
 
-    for (int ii = 1; ii <= o.maxit; ++ii) {
-        it = (uint32_t)ii;
-        const int nxt = cur ^ 1;
-        // u-subproblem
-        adj_rhs_k<T><<<g, b, 0, ctx->stream>>>(r, v[cur], lmb[lc], d, -ihx, -ihy, -ihz, (T)rho);
-        if (sizeof(T) == 8) QSM_FFT(cufftExecD2Z(pf, (cufftDoubleReal *)r, (cufftDoubleComplex *)R));
-        else QSM_FFT(cufftExecR2C(pf, (cufftReal *)r, (cufftComplex *)R));
-        kmul_k<T><<<gk, TV_BLOCK, 0, ctx->stream>>>(R, fhat, Dq, tab, K, rho, 1.0 / (double)N);
-        if (sizeof(T) == 8) QSM_FFT(cufftExecZ2D(pi, (cufftDoubleComplex *)R, (cufftDoubleReal *)u));
-        else QSM_FFT(cufftExecC2R(pi, (cufftComplex *)R, (cufftReal *)u));
-        // v-subproblem, multipliers, residuals
-        if (sizeof(T) == 4 && o.tv == 1) {
-            grad_shrink_norms_k<T><<<gs, b, 0, ctx->stream>>>(v[nxt], v[cur], lmb[lc ^ 1], lmb[lc], u, d, ihx, ihy,
-                                                              ihz, (T)o.alpha, (T)rho, (T)irho, -ihx, -ihy, -ihz,
-                                                              part);
-            lc ^= 1;
-            fold_k<<<1, TV_BLOCK, 0, ctx->stream>>>(sums, part, TV_NSUM, GS_GRID, 0, 0);
-        } else {
-            if (o.tv == 1)
-                grad_shrink_k<T, false><<<gs, b, 0, ctx->stream>>>(v[nxt], v[cur], lmb[lc], u, d, ihx, ihy, ihz,
-                                                                   (T)o.alpha, (T)rho, (T)irho, part);
-            else
-                grad_shrink_k<T, true><<<gs, b, 0, ctx->stream>>>(v[nxt], v[cur], lmb[lc], u, d, ihx, ihy, ihz,
-                                                                  (T)o.alpha, (T)rho, (T)irho, part);
-            adj_norms_k<T><<<g, b, 0, ctx->stream>>>(v[nxt], v[cur], lmb[lc], d, -ihx, -ihy, -ihz, (T)rho,
-                                                     part + 3 * GS_GRID);
-            fold_k<<<1, TV_BLOCK, 0, ctx->stream>>>(sums, part, 3, GS_GRID, 2, TV_GRID);
+    // Iterations are queued without waiting: tv_ctl_k applies the stopping
+    // test and the rho schedule on the device, and the host reads the state
+    // every `chunk` iterations (every iteration when printing).  Iterations
+    // queued past convergence compute on with frozen rho; the converged u is
+    // kept by the next adj_rhs_k, and the solve reports the converged state.
+    {
+        const TvCtlOpts co{o.rtol, atolp, atold, o.rtau, o.stau, o.gamma};
+        const int chunk = o.verbose ? 1 : 8;
+        int ii = 1, last = 0;
+        bool done = false;
+        while (ii <= o.maxit && !done) {
+            const int end = std::min(o.maxit, ii + chunk - 1);
+            for (; ii <= end; ++ii) {
+                const int nxt = cur ^ 1;
+                // u-subproblem
+                adj_rhs_k<T><<<g, b, 0, ctx->stream>>>(r, v[cur], lmb[lc], d, -ihx, -ihy, -ihz, ctl, ii, usave, u);
+                if (sizeof(T) == 8) QSM_FFT(cufftExecD2Z(pf, (cufftDoubleReal *)r, (cufftDoubleComplex *)R));
+                else QSM_FFT(cufftExecR2C(pf, (cufftReal *)r, (cufftComplex *)R));
+                kmul_k<T><<<gk, TV_BLOCK, 0, ctx->stream>>>(R, fhat, Dq, tab, K, ctl, 1.0 / (double)N);
+                if (sizeof(T) == 8) QSM_FFT(cufftExecZ2D(pi, (cufftDoubleComplex *)R, (cufftDoubleReal *)u));
+                else QSM_FFT(cufftExecC2R(pi, (cufftComplex *)R, (cufftReal *)u));
+                // v-subproblem, multipliers, residuals
+                if (sizeof(T) == 4 && o.tv == 1) {
+                    grad_shrink_norms_k<T><<<gs, b, 0, ctx->stream>>>(v[nxt], v[cur], lmb[lc ^ 1], lmb[lc], u, d, ihx,
+                                                                      ihy, ihz, (T)o.alpha, ctl, -ihx, -ihy, -ihz,
+                                                                      part);
+                    lc ^= 1;
+                    fold_k<<<1, TV_BLOCK, 0, ctx->stream>>>(sums, part, TV_NSUM, GS_GRID, 0, 0);
+                } else {
+                    if (o.tv == 1)
+                        grad_shrink_k<T, false><<<gs, b, 0, ctx->stream>>>(v[nxt], v[cur], lmb[lc], u, d, ihx, ihy,
+                                                                           ihz, (T)o.alpha, ctl, part);
+                    else
+                        grad_shrink_k<T, true><<<gs, b, 0, ctx->stream>>>(v[nxt], v[cur], lmb[lc], u, d, ihx, ihy,
+                                                                          ihz, (T)o.alpha, ctl, part);
+                    adj_norms_k<T><<<g, b, 0, ctx->stream>>>(v[nxt], v[cur], lmb[lc], d, -ihx, -ihy, -ihz, ctl,
+                                                             part + 3 * GS_GRID);
+                    fold_k<<<1, TV_BLOCK, 0, ctx->stream>>>(sums, part, 3, GS_GRID, 2, TV_GRID);
+                }
+                tv_ctl_k<<<1, 1, 0, ctx->stream>>>(ctl, sums, co, ii);
+                QSM_STEP(cuda_st(ctx, cudaGetLastError(), "launch"));
+                cur = nxt;
+            }
+            last = ii - 1;
+            QSM_STEP(cuda_st(ctx, cudaMemcpyAsync(hc, ctl, C_N * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "copy"));
+            QSM_STEP(cuda_st(ctx, cudaStreamSynchronize(ctx->stream), "sync"));
+            done = hc[C_DONE] != 0.0;
+            if (o.verbose)
+                printf("%3d/%d\t\t%.4e\t%.4e\t%.4e\t%.4e\n", (int)hc[C_IT], o.maxit, hc[C_NR], hc[C_EP], hc[C_NS],
+                       hc[C_ED]);
         }
-        QSM_STEP(cuda_st(ctx, cudaGetLastError(), "launch"));
-        QSM_STEP(cuda_st(ctx, cudaMemcpyAsync(hs, sums, TV_NSUM * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "copy"));
-        QSM_STEP(cuda_st(ctx, cudaStreamSynchronize(ctx->stream), "sync"));
-        cur = nxt;
-        nr_ = nr;
-        nr = hs[0];
-        na = hs[1];
-        nb = hs[2];
-        ns = sqrt(hs[3]);
-        ep = atolp + o.rtol * std::max(na, nb);
-        ed = atold + o.rtol * sqrt(hs[4]);
-        if (o.verbose) printf("%3d/%d\t\t%.4e\t%.4e\t%.4e\t%.4e\n", ii, o.maxit, nr, ep, ns, ed);
-        if (nr < ep && ns < ed) break;
-        // rho update (tv.m:247-268)
-        if (nr > o.stau * ns || (nr > o.rtau * nr_ && flag < 3)) {
-            rho = o.gamma * rho;
-            irho = 1.0 / rho;
-            if (flag > 5) flag = 0;
-        } else if (nr < ns / o.stau) {
-            rho = rho / (o.gamma * o.gamma);
-            irho = 1.0 / rho;
-            flag = flag + 1;
-        }
+        it = done ? (uint32_t)hc[C_IT] : (uint32_t)last;
+        from_save = done && (int)hc[C_IT] < last;
     }
     if (o.verbose) printf("\n");
     QSM_STEP(cuda_st(ctx, cudaEventRecord(e1, ctx->stream), "event"));
-    mask_out_k<T, S><<<g, b, 0, ctx->stream>>>(xout, u, mask, N);
+    mask_out_k<T, S><<<g, b, 0, ctx->stream>>>(xout, from_save ? usave : u, mask, N);
     QSM_STEP(cuda_st(ctx, cudaGetLastError(), "launch"));
     QSM_STEP(cuda_st(ctx, cudaStreamSynchronize(ctx->stream), "sync"));
     if (info) {
         float ms = 0.f;
         cudaEventElapsedTime(&ms, e0, e1);
         info->iters = it;
-        info->rho = rho;
-        info->nr = nr;
-        info->eps_pri = ep;
-        info->ns = ns;
-        info->eps_dual = ed;
+        info->rho = hc[C_RHO];
+        info->nr = hc[C_NR];
+        info->eps_pri = hc[C_EP];
+        info->ns = hc[C_NS];
+        info->eps_dual = hc[C_ED];
         info->seconds = ms * 1e-3;
     }
 done:

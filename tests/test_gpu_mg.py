@@ -154,6 +154,24 @@ def test_coarse_grid_solver_vs_oracle(gpu_ctx, qsm, port, dt):
     assert bits_equal(a, port.mg_mex(v0, f, m, [1, 1, 1], 1e-6, 2, 1, 2, 2, 2, 2))
 
 
+@pytest.mark.parametrize("dt", ("float64", "float32"))
+def test_mgpcg_256_lbv_options_bitexact(gpu_ctx, qsm, port, dt):
+    """The benchmark's Poisson problem at full size (256^3, LBV options, 5
+    levels: 16-CTA cluster coarsest solve, list passes, fused PCG steps):
+    bit-for-bit against the oracle, same iteration count."""
+    import qsm_gb300.synthetic as S
+
+    f, m, _ = S.config1(seed=1)
+    f = f.astype(dt)
+    v0 = np.zeros(f.shape, dtype=dt, order="F")
+    oi, gi = {}, {}
+    b = port.mgpcg_mex(v0, f, m, [1, 1, 1], 1e-8, 40, -1.0, 2, 1, 2, 2, 2, 5, info=oi)
+    a = qsm.mgpcg_mex(v0, f, m, [1, 1, 1], 1e-8, 40, -1.0, 2, 1, 2, 2, 2, 5, info=gi)
+    assert gi["iters"] == oi["iters"] == 10
+    assert gi["coarse_ctas"] >= 2
+    assert bits_equal(a, b), first_diff(a, b)
+
+
 def test_mixed_pcg_cluster_coarse(gpu_ctx, qsm, port):
     """FP64 PCG with the FP32 V-cycle (FP32 coarsest solve on the cluster):
     same stopping rule, error against the FP64 oracle."""
