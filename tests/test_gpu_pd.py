@@ -120,10 +120,28 @@ def test_pd_errors(gpu_ctx, qsm):
         qsm.pd_tgv_mex(np.zeros((4, 4, 4), np.int32), np.ones((4, 4, 4), np.uint8), [1, 1, 1], 0.003, 2.0, 0.0, 5)
 
 
+def _active_voxels(m, tile):
+    """Interior voxels of the tiles that hold a voxel of m or of the dual mask
+    mi (all six neighbours in m), each tile clipped to the interior."""
+    mm = m != 0
+    mi = np.zeros_like(mm)
+    mi[1:-1, 1:-1, 1:-1] = (mm[:-2, 1:-1, 1:-1] & mm[2:, 1:-1, 1:-1] & mm[1:-1, :-2, 1:-1] & mm[1:-1, 2:, 1:-1] &
+                            mm[1:-1, 1:-1, :-2] & mm[1:-1, 1:-1, 2:])
+    act = (mm | mi)[1:-1, 1:-1, 1:-1]
+    tx, ty, tz = tile
+    tot = 0
+    for a in range(0, act.shape[0], tx):
+        for b in range(0, act.shape[1], ty):
+            for c in range(0, act.shape[2], tz):
+                blk = act[a:a + tx, b:b + ty, c:c + tz]
+                tot += blk.size if blk.any() else 0
+    return tot
+
+
 @pytest.mark.parametrize("shape", [(77, 41, 23), (70, 30, 75)])
-@pytest.mark.parametrize("variant", list(range(10)))
+@pytest.mark.parametrize("variant", list(range(16)))
 def test_fused_tile_variants_bitexact(gpu_ctx, qsm, port, variant, shape, monkeypatch):
-    """Every compiled tile shape (3-D tiles 0-3, z-streaming column tiles 4-9)
+    """Every tile variant (3-D tiles 0-3, z-streaming column tiles 4-15)
     gives the reference's FP32 result (partial tiles and chunks, odd extents,
     a mask that leaves whole tiles inactive)."""
     monkeypatch.setenv("QSM_FUSED_VARIANT", str(variant))
@@ -137,9 +155,8 @@ def test_fused_tile_variants_bitexact(gpu_ctx, qsm, port, variant, shape, monkey
     a = qsm.pd_tgv_mex(d2f, m, [1, 1, 1], 0.003, 2.0, 0.0, 30, fused=True, info=info)
     b = port.pd_tgv_mex(d2f, m, [1, 1, 1], 0.003, 2.0, 0.0, 30)
     assert bits_equal(a, b), first_diff(a, b)
-    interior = (shape[0] - 2) * (shape[1] - 2) * (shape[2] - 2)
-    if 8 * int(np.prod(info["tile"])) <= interior:  # small tiles: some miss the mask and are skipped
-        assert info["active_voxels"] < interior
+    # tiles that miss the mask are skipped: the launched voxels are exactly those of the active tiles
+    assert info["active_voxels"] == _active_voxels(m, tuple(info["tile"]))
     a = qsm.pd_tv_mex(d2f, m, [1, 1, 1], 0.003, 0.0, 30, fused=True)
     b = port.pd_tv_mex(d2f, m, [1, 1, 1], 0.003, 0.0, 30)
     assert bits_equal(a, b), first_diff(a, b)
