@@ -1275,11 +1275,6 @@ static void plan_coarse_grid(qsm_ctx *ctx, Hier<T> &H)
         return;
     }
     H.cg_ctas = sms;
-    // QSM_COARSE_GRID_CTAS overrides the CTA count (1 .. SMs), for tuning
-    if (const char *e = getenv("QSM_COARSE_GRID_CTAS")) {
-        const int want = atoi(e);
-        if (want >= 1 && want <= sms) H.cg_ctas = want;
-    }
 }
 
 // Colour lists of every level's G and boundary band B (counted, then filled
