@@ -56,7 +56,7 @@ ALG_BYTES_FP32 = 166  # algorithmic bytes per voxel-iteration of fused FP32 TGV
 # DRAM bytes (read + write) per launch of the fused kernel on the headline workload, by
 # tile (tx, ty, z-chunk), from one ncu capture each (profiles/tgv_224x224x128_launch_list.md);
 # None for other shapes and tiles
-NCU_TRAFFIC_224x224x128 = {(28, 12, 16): 272.5e6, (28, 16, 16): 276.5e6, (28, 16, 17): 278.3e6}
+NCU_TRAFFIC_224x224x128 = {(28, 12, 16): 272.5e6, (28, 16, 16): 276.5e6}
 WORKLOAD = "TGV-QSM 224x224x128, 1 mm isotropic, B0 along z, 1000 iterations, tol 0"
 
 

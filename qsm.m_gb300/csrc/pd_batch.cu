@@ -178,10 +178,7 @@ static BatchKernel batch_kernel(int v, bool tgv)
     case 2: return tgv ? tile_kernel<32, 4, 4, 8, true>() : tile_kernel<32, 4, 4, 8, false>();
     case 3: return tgv ? tile_kernel<32, 16, 2, 2, true>() : tile_kernel<32, 16, 2, 2, false>();
     case 8:
-    case 9:
-    case 10:
-    case 11:
-    case 12: return tgv ? column_kernel<28, 16, true>() : column_kernel<28, 16, false>();
+    case 9: return tgv ? column_kernel<28, 16, true>() : column_kernel<28, 16, false>();
     default: return tgv ? column_kernel<28, 12, true>() : column_kernel<28, 12, false>();
     }
 }

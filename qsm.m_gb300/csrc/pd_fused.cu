@@ -120,9 +120,7 @@ tv_fused_k(FusedArgs s, DualC<float> dc, PrimalC<float> pc, Dims d, double tol, 
 static const Variant kVariants[kNumVariants] = {{32, 8, 4, false}, {32, 8, 2, false}, {32, 4, 4, false},
                                                 {32, 16, 2, false}, {28, 12, 8, true},  {28, 12, 16, true},
                                                 {28, 12, 32, true},  {28, 12, 64, true}, {28, 16, 16, true},
-                                                {28, 16, 32, true},  {28, 16, 9, true},  {28, 16, 12, true},
-                                                {28, 16, 17, true},  {28, 12, 13, true}, {28, 12, 17, true},
-                                                {28, 12, 24, true}};
+                                                {28, 16, 32, true}};
 
 const Variant &variant(int v) { return kVariants[v]; }
 

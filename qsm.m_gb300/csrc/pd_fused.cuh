@@ -185,7 +185,7 @@ struct Variant {
     int tx, ty, tz;   // tile of interior voxels (z: chunk of planes for the column kernel)
     bool stream;      // column-streaming kernel, else the 3-D tile kernel
 };
-constexpr int kNumVariants = 16;
+constexpr int kNumVariants = 10;
 const Variant &variant(int v);
 size_t variant_smem(int v, bool tgv);
 int variant_threads(int v);

@@ -139,9 +139,9 @@ def _active_voxels(m, tile):
 
 
 @pytest.mark.parametrize("shape", [(77, 41, 23), (70, 30, 75)])
-@pytest.mark.parametrize("variant", list(range(16)))
+@pytest.mark.parametrize("variant", list(range(10)))
 def test_fused_tile_variants_bitexact(gpu_ctx, qsm, port, variant, shape, monkeypatch):
-    """Every tile variant (3-D tiles 0-3, z-streaming column tiles 4-15)
+    """Every tile variant (3-D tiles 0-3, z-streaming column tiles 4-9)
     gives the reference's FP32 result (partial tiles and chunks, odd extents,
     a mask that leaves whole tiles inactive)."""
     monkeypatch.setenv("QSM_FUSED_VARIANT", str(variant))
