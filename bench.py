@@ -567,6 +567,12 @@ def next_rows_arm(qsm_gb300, ctx, torch, peak, cpu=True, parts="tv64,tv32,pdf,vs
         out["lbv"] = {"workload": "lbv.m defaults, 4 echoes FP64, host arrays", "seconds": sec,
                       "pcg_iters": [i["iters"] for i in infos], "solve_s": [i["seconds"] for i in infos],
                       "coarse_ctas": infos[0]["coarse_ctas"], "coarse_outer": [i["coarse_outer"] for i in infos]}
+        # the same with the FP32 V-cycle (FP64 PCG recurrence, same stopping rule)
+        mi = []
+        sec_m, flm = timed(lambda: qsm_gb300.lbv(f4, mask, [1, 1, 1], mixed=True, infos=mi, ctx=ctx), reps=1)
+        fl64 = qsm_gb300.lbv(f4, mask, [1, 1, 1], ctx=ctx)
+        out["lbv"]["mixed"] = {"seconds": sec_m, "pcg_iters": [i["iters"] for i in mi],
+                               "rel_l2_vs_fp64": float(np.linalg.norm(flm - fl64) / np.linalg.norm(fl64))}
     return out
 
 

@@ -469,7 +469,7 @@ __device__ __forceinline__ void column_pd(const FusedArgs &s, const DualC<float>
             const float zs_ = nu_m2 + v[0];
             const float cn = pcur[0], en = pcur[1];
             const float e1 = pc.tau1 * (en - pc.lhh * nu0 - pc.lhx * xs - pc.lhy * ys - pc.lhz * zs_);
-            const float *P1 = Sm + NT, *P2 = Sm + 2 * NT, *P3 = Sm + 3 * NT;
+            const float *P1 = Sm + NT, *P2 = Sm + 2 * NT;  // p3's z-neighbour comes from registers
             const float c1 = cn + (pc.hx * (vp[1] - P1[tid - 1]) + pc.hy * (vp[2] - P2[tid - WX]) +
                                    pc.hz * (vp[3] - p3_m2) +
                                    (pc.whh * nu0 + pc.whx * xs + pc.why * ys + pc.whz * zs_));
@@ -478,7 +478,7 @@ __device__ __forceinline__ void column_pd(const FusedArgs &s, const DualC<float>
             pv[1] = e1;
             if (TGV) {
                 const float *Q1 = Sm + 4 * NT, *Q2 = Sm + 5 * NT, *Q3 = Sm + 6 * NT, *Q4 = Sm + 7 * NT,
-                            *Q5 = Sm + 8 * NT, *Q6 = Sm + 9 * NT;
+                            *Q5 = Sm + 8 * NT;  // q6 is only read along z (registers)
                 const float u1 = pcur[2] + (pc.tt * vp[1] + pc.hx * (vp[4] - Q1[tid - 1] + vp[5] - Q2[tid - WX] +
                                                                       vp[6] - q3_m2));
                 const float u2 = pcur[3] + (pc.tt * vp[2] + pc.hy * (vp[5] - Q2[tid - 1] + vp[7] - Q4[tid - WX] +
