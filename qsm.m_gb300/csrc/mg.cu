@@ -397,6 +397,14 @@ __global__ void gs_list_k(T *v, const T *__restrict__ f, const uint32_t *__restr
 // ---------------------------------------------------------------------------
 
 constexpr int SW_THREADS = 256;
+enum { SW_LAUNCH = 0, SW_CLUSTER = 1, SW_GRID = 2 };
+// per-colour list sizes: up to SW_CLUSTER_MAX on one cluster, up to SW_GRID_MAX
+// over the whole GPU with a grid barrier, else a launch per pass.  Measured per
+// pass (FP64, 256^3 hierarchy): cluster 2.1 us at 1.8k voxels, 3.5 us at 5-7k;
+// grid 3.1 us at 7.4k, 3.6 us at 31k, 8.6 us at 126k (a thread then walks
+// several entries one after another); launches 4.7 us at 31k, 7.8 us at 126k,
+// 11 us at 334k.  So the grid takes lists of up to about one entry per thread.
+constexpr unsigned SW_CLUSTER_MAX = 2500, SW_GRID_MAX = 45000;
 
 // A thread's share of one list: at most SW_PER entries (longer lists keep one
 // launch per pass), loaded once with their f values, since neither changes
@@ -663,6 +671,26 @@ __global__ void __launch_bounds__(CG_THREADS) coarse_grid_k(T *v, const T *__res
         if (rn < reltol) break;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0 && outer_out) *outer_out += outer;
+}
+
+// iter sweeps (colour-a pass over la, colour-b pass over lb skipping the
+// entries flagged skipb) over the whole GPU with a grid barrier between
+// passes: for lists too large for one cluster's 16 SMs but small enough that
+// a launch per pass costs more than the barrier (~2.5 us).
+template <typename T>
+__global__ void __launch_bounds__(CG_THREADS) sweeps_grid_k(T *v, const T *__restrict__ f,
+                                                            const uint32_t *__restrict__ la, unsigned ca,
+                                                            const uint32_t *__restrict__ lb, unsigned cb,
+                                                            uint32_t skipb, int32_t iter, GsC<T> c, size_t nx,
+                                                            size_t nxny, GridBar gb)
+{
+    unsigned bk = 0;
+    for (int32_t s = 0; s < iter; ++s) {
+        grid_pass(v, f, la, ca, 0u, c, nx, nxny);
+        if (!grid_bar(gb, bk)) return;
+        grid_pass(v, f, lb, cb, skipb, c, nx, nxny);
+        if (!grid_bar(gb, bk)) return;
+    }
 }
 
 __global__ void bmask_l1_init_k(uint8_t *B, uint8_t *GL, const uint8_t *__restrict__ G, Dims d)
@@ -1100,7 +1128,7 @@ struct Level {
     unsigned bn[2];
     uint32_t *gl[2];     // G voxels of each colour (null: full-grid passes)
     unsigned gn[2];
-    bool bcl, gcl;       // B / G passes of a smoothing call run on one cluster launch
+    uint8_t bmode, gmode;  // how a smoothing call runs the B / G passes (SW_LAUNCH, SW_CLUSTER, SW_GRID)
 };
 
 template <typename T>
@@ -1114,6 +1142,7 @@ struct Hier {
     size_t coarse_smem;
     void *lists;         // the levels' colour lists (one allocation)
     int sw_ctas;         // cluster size of the list passes (0: not available)
+    int sg_ctas;         // CTAs of the whole-GPU list passes (0: not available)
     int host_outer;      // outer iterations of the host-driven coarsest solve
     int cg_ctas;         // > 0: the coarsest level runs on this many CTAs, cooperatively (wins over the cluster)
     GridBar gb;          // their barrier words (arrival count, error flag)
@@ -1255,6 +1284,22 @@ static qsm_status hier_init(qsm_ctx *ctx, Hier<T> &H, int nl, const Dims &dp, co
     return QSM_OK;
 }
 
+// CTAs of the whole-GPU list passes: one per SM when cooperative launch is
+// available, else 0.
+template <typename T>
+static int grid_sweep_ctas(qsm_ctx *ctx)
+{
+    int coop = 0, sms = 0, per_sm = 0;
+    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device) != cudaSuccess || !coop ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweeps_grid_k<T>, CG_THREADS, 0) != cudaSuccess ||
+        per_sm < 1) {
+        cudaGetLastError();
+        return 0;
+    }
+    return sms;
+}
+
 // The whole-GPU coarsest solver: for large colour passes, or where neither a
 // cluster nor one CTA holds the grid; needs the coarsest level's G lists and
 // cooperative launch.  cg_ctas = one CTA per SM, else 0.
@@ -1278,7 +1323,7 @@ static void plan_coarse_grid(qsm_ctx *ctx, Hier<T> &H)
 }
 
 // Colour lists of every level's G and boundary band B (counted, then filled
-// into one allocation); small levels run their passes on one cluster launch.
+// into one allocation), and how each list's passes run (by its size).
 // Grids of 2^30 voxels or more keep the full-grid passes.
 template <typename T>
 static qsm_status boundary_lists(qsm_ctx *ctx, Hier<T> &H)
@@ -1299,12 +1344,18 @@ static qsm_status boundary_lists(qsm_ctx *ctx, Hier<T> &H)
     QSM_CUDA(cudaMemcpyAsync(hc, cnt, 4 * H.nl * sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
     QSM_CUDA(cudaStreamSynchronize(ctx->stream));
     size_t tot = 0;
+    H.sg_ctas = grid_sweep_ctas<T>(ctx);
+    auto mode = [&](unsigned c0, unsigned c1) -> uint8_t {
+        const unsigned c = c0 > c1 ? c0 : c1;
+        const unsigned cap = (unsigned)cn * SW_THREADS * SW_PER;
+        if (cn > 0 && c <= cap && c <= SW_CLUSTER_MAX) return SW_CLUSTER;
+        if (H.sg_ctas > 0 && c <= SW_GRID_MAX) return SW_GRID;
+        return SW_LAUNCH;
+    };
     for (int i = 0; i < H.nl; ++i) {
         Level<T> &L = H.L[i];
-        const unsigned cap = (unsigned)cn * SW_THREADS * SW_PER;
-        const bool small_g = i > 0 && cn > 0 && hc[4 * i + 2] <= cap && hc[4 * i + 3] <= cap;
-        L.bcl = i > 0 && cn > 0 && hc[4 * i] <= cap && hc[4 * i + 1] <= cap;
-        L.gcl = small_g;
+        L.bmode = mode(hc[4 * i], hc[4 * i + 1]);
+        L.gmode = mode(hc[4 * i + 2], hc[4 * i + 3]);
         for (int p = 0; p < 2; ++p)
             tot += al256((size_t)hc[4 * i + p] * sizeof(uint32_t)) + al256((size_t)hc[4 * i + 2 + p] * sizeof(uint32_t));
     }
@@ -1357,6 +1408,27 @@ static qsm_status list_sweeps(qsm_ctx *ctx, T *v, const T *f, uint32_t *const li
     return QSM_OK;
 }
 
+template <typename T>
+static qsm_status sweeps_grid(qsm_ctx *ctx, const Hier<T> &H, T *v, const T *f, uint32_t *const lists[2],
+                              const unsigned cnt[2], const double *h, const Dims &d, int32_t iter, bool rev)
+{
+    const int par0 = rev ? (int)((d.nx + 1) & 1) : 0;
+    T *vv = v;
+    const T *ff = f;
+    const uint32_t *la = lists[par0], *lb = lists[par0 ^ 1];
+    unsigned ca = cnt[par0], cb = cnt[par0 ^ 1];
+    uint32_t skipb = rev ? BL_INX2 : BL_I1;
+    int32_t it = iter;
+    GsC<T> gc = gs_consts<T>(h);
+    size_t nx = d.nx, nxny = d.nxny();
+    GridBar gb = H.gb;
+    void *args[] = {&vv, &ff, &la, &ca, &lb, &cb, &skipb, &it, &gc, &nx, &nxny, &gb};
+    QSM_CUDA(cudaMemsetAsync(H.gb.count, 0, sizeof(unsigned), ctx->stream));
+    QSM_CUDA(cudaLaunchCooperativeKernel((const void *)sweeps_grid_k<T>, dim3((unsigned)H.sg_ctas), dim3(CG_THREADS),
+                                         args, 0, ctx->stream));
+    return QSM_OK;
+}
+
 // `iter` colour-pass pairs over a level's G (gauss_seidel over G): one
 // cluster launch on small levels, else one launch per pass over the colour
 // lists (full-grid passes only where there are no lists).
@@ -1365,7 +1437,8 @@ static qsm_status smooth(qsm_ctx *ctx, const Hier<T> &H, Level<T> &L, int32_t it
 {
     if (!L.gl[0]) return gauss_seidel<T>(ctx, L.v, L.f, L.G, L.h, L.d, iter, rev);
     if (L.d.nx < 3 || L.d.ny < 3 || L.d.nz < 3 || iter <= 0) return QSM_OK;
-    if (L.gcl) return sweeps_cluster<T>(ctx, H.sw_ctas, L.v, L.f, L.gl, L.gn, L.h, L.d, iter, rev);
+    if (L.gmode == SW_CLUSTER) return sweeps_cluster<T>(ctx, H.sw_ctas, L.v, L.f, L.gl, L.gn, L.h, L.d, iter, rev);
+    if (L.gmode == SW_GRID) return sweeps_grid<T>(ctx, H, L.v, L.f, L.gl, L.gn, L.h, L.d, iter, rev);
     return list_sweeps<T>(ctx, L.v, L.f, L.gl, L.gn, L.h, L.d, iter, rev);
 }
 
@@ -1399,7 +1472,8 @@ static qsm_status boundary_sweeps(qsm_ctx *ctx, const Hier<T> &H, Level<T> &L, i
 {
     if (!L.bl[0]) return gauss_seidel<T>(ctx, L.v, L.f, L.B, L.h, L.d, iter, rev);
     if (L.d.nx < 3 || L.d.ny < 3 || L.d.nz < 3 || iter <= 0) return QSM_OK;
-    if (L.bcl) return sweeps_cluster<T>(ctx, H.sw_ctas, L.v, L.f, L.bl, L.bn, L.h, L.d, iter, rev);
+    if (L.bmode == SW_CLUSTER) return sweeps_cluster<T>(ctx, H.sw_ctas, L.v, L.f, L.bl, L.bn, L.h, L.d, iter, rev);
+    if (L.bmode == SW_GRID) return sweeps_grid<T>(ctx, H, L.v, L.f, L.bl, L.bn, L.h, L.d, iter, rev);
     return list_sweeps<T>(ctx, L.v, L.f, L.bl, L.bn, L.h, L.d, iter, rev);
 }
 
@@ -1736,11 +1810,11 @@ __global__ void __launch_bounds__(RED_BLOCK) pcg_xr_k(TP *__restrict__ x, const 
 template <typename T>
 static qsm_status coarse_report(qsm_ctx *ctx, const Hier<T> &H, qsm_mg_info *info)
 {
-    if (H.cg_ctas > 0) {
+    if (H.cg_ctas > 0 || H.sg_ctas > 0) {
         int err = 0;
         QSM_CUDA(cudaMemcpy(&err, H.gb.err, sizeof(int), cudaMemcpyDeviceToHost));
         if (err) {
-            set_error(ctx, "coarsest-level solve: a grid barrier timed out");
+            set_error(ctx, "multigrid: a grid barrier timed out");
             return QSM_ERR_TIMEOUT;
         }
     }
