@@ -1348,7 +1348,8 @@ static qsm_status boundary_lists(qsm_ctx *ctx, Hier<T> &H)
     auto mode = [&](unsigned c0, unsigned c1) -> uint8_t {
         const unsigned c = c0 > c1 ? c0 : c1;
         const unsigned cap = (unsigned)cn * SW_THREADS * SW_PER;
-        if (cn > 0 && c <= cap && c <= SW_CLUSTER_MAX) return SW_CLUSTER;
+        // FP32 passes are not bound by 16 SMs' arithmetic: a cluster takes lists up to its capacity
+        if (cn > 0 && c <= cap && (sizeof(T) == 4 || c <= SW_CLUSTER_MAX)) return SW_CLUSTER;
         if (H.sg_ctas > 0 && c <= SW_GRID_MAX) return SW_GRID;
         return SW_LAUNCH;
     };
