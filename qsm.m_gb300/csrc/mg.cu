@@ -7,15 +7,24 @@
 // common.cu, as does the oracle's BLAS shim, so whole PCG solves are
 // reproducible bit-for-bit.
 //
-//   red-black Gauss-Seidel  one launch per colour pass; a pass only reads the
-//                           other colour, so its voxels are independent
-//   coarsest level          one CTA keeps v, f and G in shared memory and
-//                           runs the reference's <= 1024 x (128 reverse +
-//                           128 forward sweeps + residual + norm) loop,
-//                           including the lane-order norm, with block
-//                           barriers only (no host round trips)
-//   PCG scalars             stay on the device; the host reads ||r|| once
-//                           per iteration for the stopping test
+//   red-black Gauss-Seidel  a pass only reads the other colour, so its voxels
+//                           are independent and may run in any order.  Every
+//                           level keeps its G voxels and its boundary band B
+//                           as per-colour lists; a smoothing call runs its
+//                           passes as one launch per pass (large lists), in
+//                           one cooperative whole-GPU launch with a grid
+//                           barrier per pass (mid-size), or in one cluster
+//                           launch (small); full-grid passes remain for the
+//                           public gauss_seidel_mex and grids without lists
+//   coarsest level          the reference's <= 1024 x (128 reverse + 128
+//                           forward sweeps + residual + norm) loop in one
+//                           launch: z-slabs over a 16-CTA cluster in shared
+//                           memory (small grids), over every SM with a grid
+//                           barrier (large passes), or in one CTA; the norm
+//                           keeps the lane order; no host round trips
+//   PCG                     the BLAS-1 steps fused into four kernels on the
+//                           lane-dot grid; scalars stay on the device and the
+//                           host reads ||r|| once per iteration
 #include <math.h>
 #include <stdlib.h>
 #include <mutex>
