@@ -1041,8 +1041,10 @@ template <typename T>
 __global__ void __launch_bounds__(CC_THREADS) coarse_cluster_k(T *gv, const T *__restrict__ gf,
                                                                const uint8_t *__restrict__ gG, T *gr, Dims d,
                                                                GsC<T> gc, LapC<T> lc, double tol, int npmax,
-                                                               int *outer_out)
+                                                               int *outer_out, int sweeps, int rev)
 {
+    // sweeps > 0: no coarsest solve, only that many sweeps (reverse when rev)
+    // over the voxels of gG (a boundary band), then v is written back
     extern __shared__ __align__(16) unsigned char smraw[];
     const int nx = (int)d.nx, ny = (int)d.ny, nz = (int)d.nz, nxny = nx * ny, n = nxny * nz;
     const uint32_t c = cl_rank(), cn = cl_size();
@@ -1084,13 +1086,27 @@ __global__ void __launch_bounds__(CC_THREADS) coarse_cluster_k(T *gv, const T *_
     const uint32_t offdn = (uint32_t)(nxny * (k0 - kp)), offup = (uint32_t)(nxny * np);
     const int n0 = cnt[0], n1 = cnt[1];
     const uint32_t *list0 = list, *list1 = list + cap;
+    const int rpar0 = (nx + 1) & 1;
+    const uint32_t *lr0 = rpar0 ? list1 : list0, *lr1 = rpar0 ? list0 : list1;
+    const int cr0 = rpar0 ? n1 : n0, cr1 = rpar0 ? n0 : n1;
+    if (sweeps > 0) {
+        for (int s = 0; s < sweeps; ++s) {
+            if (rev) {
+                cc_pass<T>(v, f, lr0, cr0, 0u, gc, nx, nxny, vdn, offdn, vup, offup);
+                cc_pass<T>(v, f, lr1, cr1, CC_INX2, gc, nx, nxny, vdn, offdn, vup, offup);
+            } else {
+                cc_pass<T>(v, f, list0, n0, 0u, gc, nx, nxny, vdn, offdn, vup, offup);
+                cc_pass<T>(v, f, list1, n1, CC_I1, gc, nx, nxny, vdn, offdn, vup, offup);
+            }
+        }
+        for (int t = tid; t < np * nxny; t += CC_THREADS) gv[base + nxny + t] = v[nxny + t];
+        cl_sync();
+        return;
+    }
 
     const T ff = cl_lane_sum<T>(gf, n, red, blk, bc, c, cn);
     const double fn = sizeof(T) == 4 ? (double)sqrtf((float)ff) : sqrt((double)ff);
     const double reltol = tol * fn;
-    const int rpar0 = (nx + 1) & 1;
-    const uint32_t *lr0 = rpar0 ? list1 : list0, *lr1 = rpar0 ? list0 : list1;
-    const int cr0 = rpar0 ? n1 : n0, cr1 = rpar0 ? n0 : n1;
     int outer = 0;
     for (int it = 0; it < 1024; ++it) {
         outer = it + 1;
@@ -1138,6 +1154,8 @@ struct Level {
     uint32_t *gl[2];     // G voxels of each colour (null: full-grid passes)
     unsigned gn[2];
     uint8_t bmode, gmode;  // how a smoothing call runs the B / G passes (SW_LAUNCH, SW_CLUSTER, SW_GRID)
+    int dsm_cn, dsm_npmax;  // > 0: long band sweeps run on z-slabs in a cluster's shared memory
+    size_t dsm_smem;
 };
 
 template <typename T>
@@ -1229,13 +1247,12 @@ static bool cluster_fits(int cn, size_t smem)
     return nclusters >= 1;
 }
 
-// Cluster shape of the coarsest level: up to 16 CTAs, at least one interior
-// plane each, within the shared-memory limit; cc_ctas = 0 if no cluster fits.
+// Cluster shape for a grid held in z-slabs over up to 16 CTAs (at least one
+// interior plane each) within the shared-memory limit; cn = 0 if none fits.
 template <typename T>
-static void plan_cluster(qsm_ctx *ctx, Hier<T> &H, int maxsm)
+static void plan_slabs(qsm_ctx *ctx, const Dims &dc, int maxsm, int *cn_out, int *npmax_out, size_t *smem_out)
 {
-    H.cc_ctas = 0;
-    const Dims dc = H.L[H.nl - 1].d;
+    *cn_out = 0;
     const int P = (int)dc.nz - 2;
     if (dc.nx < 3 || dc.ny < 3 || P < 2 || dc.n() >= (1u << 27)) return;
     const size_t lim = cluster_smem_limit<T>(ctx, maxsm);
@@ -1243,11 +1260,18 @@ static void plan_cluster(qsm_ctx *ctx, Hier<T> &H, int maxsm)
         const int npmax = (P + cn - 1) / cn;
         const CcLayout lay(dc.nxny(), npmax, sizeof(T));
         if (lay.bytes > lim || !cluster_fits<T>(cn, lay.bytes)) continue;
-        H.cc_ctas = cn;
-        H.cc_npmax = npmax;
-        H.cc_smem = lay.bytes;
+        *cn_out = cn;
+        *npmax_out = npmax;
+        *smem_out = lay.bytes;
         return;
     }
+}
+
+// Cluster shape of the coarsest level.
+template <typename T>
+static void plan_cluster(qsm_ctx *ctx, Hier<T> &H, int maxsm)
+{
+    plan_slabs<T>(ctx, H.L[H.nl - 1].d, maxsm, &H.cc_ctas, &H.cc_npmax, &H.cc_smem);
 }
 
 template <typename T>
@@ -1290,6 +1314,9 @@ static qsm_status hier_init(qsm_ctx *ctx, Hier<T> &H, int nl, const Dims &dp, co
     H.coarse_in_smem = H.coarse_smem <= (size_t)maxsm && nc < (1u << 18);
     if (H.coarse_in_smem) QSM_TRY(coarse_smem_limit<T>(ctx, maxsm));
     plan_cluster<T>(ctx, H, maxsm);
+    // levels whose long band sweeps can run on z-slabs in a cluster
+    for (int i = 0; i + 1 < nl; ++i)
+        plan_slabs<T>(ctx, H.L[i].d, maxsm, &H.L[i].dsm_cn, &H.L[i].dsm_npmax, &H.L[i].dsm_smem);
     return QSM_OK;
 }
 
@@ -1476,12 +1503,33 @@ static qsm_status level_residual(qsm_ctx *ctx, Level<T> &L)
     return QSM_OK;
 }
 
-// `iter` colour-pass pairs over a level's boundary band (gauss_seidel over B).
+// `iter` colour-pass pairs over a level's boundary band (gauss_seidel over B):
+// long sweeps (8 or more) on levels that fit run on z-slabs in a cluster's
+// shared memory (coarse_cluster_k's sweep mode, ~0.7 us per pass instead of
+// ~2 us with the level in L2); otherwise by list size.
 template <typename T>
 static qsm_status boundary_sweeps(qsm_ctx *ctx, const Hier<T> &H, Level<T> &L, int32_t iter, bool rev)
 {
     if (!L.bl[0]) return gauss_seidel<T>(ctx, L.v, L.f, L.B, L.h, L.d, iter, rev);
     if (L.d.nx < 3 || L.d.ny < 3 || L.d.nz < 3 || iter <= 0) return QSM_OK;
+    if (L.dsm_cn > 0 && iter >= 8) {
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = (unsigned)L.dsm_cn;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.gridDim = dim3((unsigned)L.dsm_cn);
+        cfg.blockDim = dim3(CC_THREADS);
+        cfg.dynamicSmemBytes = L.dsm_smem;
+        cfg.stream = ctx->stream;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        QSM_CUDA(cudaLaunchKernelEx(&cfg, coarse_cluster_k<T>, L.v, (const T *)L.f, (const uint8_t *)L.B, L.r, L.d,
+                                    gs_consts<T>(L.h), lap_consts<T>(L.h), 0.0, L.dsm_npmax, (int *)nullptr,
+                                    (int)iter, rev ? 1 : 0));
+        return QSM_OK;
+    }
     if (L.bmode == SW_CLUSTER) return sweeps_cluster<T>(ctx, H.sw_ctas, L.v, L.f, L.bl, L.bn, L.h, L.d, iter, rev);
     if (L.bmode == SW_GRID) return sweeps_grid<T>(ctx, H, L.v, L.f, L.bl, L.bn, L.h, L.d, iter, rev);
     return list_sweeps<T>(ctx, L.v, L.f, L.bl, L.bn, L.h, L.d, iter, rev);
@@ -1546,7 +1594,7 @@ static qsm_status coarse_solve(qsm_ctx *ctx, Hier<T> &H, int l, double *scal_dev
         cfg.attrs = at;
         cfg.numAttrs = 1;
         QSM_CUDA(cudaLaunchKernelEx(&cfg, coarse_cluster_k<T>, L.v, (const T *)L.f, (const uint8_t *)L.G, L.r, L.d,
-                                    gs_consts<T>(L.h), lap_consts<T>(L.h), tol, H.cc_npmax, H.counters));
+                                    gs_consts<T>(L.h), lap_consts<T>(L.h), tol, H.cc_npmax, H.counters, 0, 0));
         return QSM_OK;
     }
     if (H.coarse_in_smem) {
