@@ -223,7 +223,9 @@ __global__ void restrict_k(T *x2, const T *__restrict__ x, const uint8_t *__rest
 // the two fine voxels i = 2 i2 - 1 (a = 0) and 2 i2 (a = 1) of one coarse
 // column, so the case (b, c) is uniform across a warp (one x row) and the
 // FP64 pipe never runs two cases' instructions for one warp.
-template <typename T, bool ADD>
+// CLEAN (with ADD): x is +0 outside G, where the correction adds +0 and leaves
+// it +0; those voxels are not touched.
+template <typename T, bool ADD, bool CLEAN>
 __global__ void prolong_k(T *x, const T *__restrict__ x2, const uint8_t *__restrict__ G, Dims d, Dims d2)
 {
     const size_t i2 = 1 + (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -236,6 +238,7 @@ __global__ void prolong_k(T *x, const T *__restrict__ x2, const uint8_t *__restr
 #pragma unroll
     for (int a = 0; a < 2; ++a) {
         const size_t lf = (2 * i2 - 1 + a) + d.nx * j + d.nxny() * k;
+        if (ADD && CLEAN && !G[lf]) continue;
         T val = (T)0;
         if (G[lf]) {
             const T c0 = x2[l2];
@@ -267,13 +270,15 @@ static qsm_status restrict_(qsm_ctx *ctx, T *x2, const T *x, const uint8_t *G2, 
 }
 
 template <typename T>
-static qsm_status prolong(qsm_ctx *ctx, T *x, const T *x2, const uint8_t *G, const Dims &d, const Dims &d2, bool add)
+static qsm_status prolong(qsm_ctx *ctx, T *x, const T *x2, const uint8_t *G, const Dims &d, const Dims &d2, bool add,
+                          bool clean = false)
 {
     if (d2.nx < 3 || d2.ny < 3 || d2.nz < 3) return QSM_OK;
     const Dims e{d2.nx - 2, 2 * (d2.ny - 2), 2 * (d2.nz - 2)};
     const dim3 g = vox_grid(e);
-    if (add) prolong_k<T, true><<<g, vox_block(), 0, ctx->stream>>>(x, x2, G, d, d2);
-    else prolong_k<T, false><<<g, vox_block(), 0, ctx->stream>>>(x, x2, G, d, d2);
+    if (add && clean) prolong_k<T, true, true><<<g, vox_block(), 0, ctx->stream>>>(x, x2, G, d, d2);
+    else if (add) prolong_k<T, true, false><<<g, vox_block(), 0, ctx->stream>>>(x, x2, G, d, d2);
+    else prolong_k<T, false, false><<<g, vox_block(), 0, ctx->stream>>>(x, x2, G, d, d2);
     QSM_CUDA(cudaGetLastError());
     return QSM_OK;
 }
@@ -1170,6 +1175,7 @@ struct Hier {
     void *lists;         // the levels' colour lists (one allocation)
     int sw_ctas;         // cluster size of the list passes (0: not available)
     int sg_ctas;         // CTAs of the whole-GPU list passes (0: not available)
+    bool v0_zero_outside; // level 0's v is +0 outside G whenever a cycle corrects it
     int host_outer;      // outer iterations of the host-driven coarsest solve
     int cg_ctas;         // > 0: the coarsest level runs on this many CTAs, cooperatively (wins over the cluster)
     GridBar gb;          // their barrier words (arrival count, error flag)
@@ -1635,7 +1641,8 @@ static qsm_status cycle(qsm_ctx *ctx, Hier<T> &H, int l, int mu, int pre, int po
             QSM_TRY(cycle<T>(ctx, H, l + 1, mu, pre, post, nb, sc));
             if (l + 1 == H.nl - 1) break;
         }
-        QSM_TRY(prolong<T>(ctx, L.v, C.v, L.G, L.d, C.d, true));
+        // every level below the top is zeroed before its cycle; the PCG's top level too
+        QSM_TRY(prolong<T>(ctx, L.v, C.v, L.G, L.d, C.d, true, l > 0 || H.v0_zero_outside));
         QSM_TRY(boundary_sweeps<T>(ctx, H, L, bs, false));
         QSM_TRY(smooth<T>(ctx, H, L, post, false));
         return QSM_OK;
@@ -1896,6 +1903,7 @@ static qsm_status pcg(qsm_ctx *ctx, const Dims &d, const TP *v0, const TP *f, co
     const size_t n = dp.n();
     Hier<TM> H;
     QSM_TRY(hier_init<TM>(ctx, H, nl, dp, h));
+    H.v0_zero_outside = true;  // the preconditioner starts from v = 0 every time
     const bool same = sizeof(TP) == sizeof(TM);
     // PCG vectors: x, p (and r, q when the V-cycle runs in another precision)
     void *pv = nullptr;
