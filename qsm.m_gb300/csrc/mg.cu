@@ -1497,6 +1497,41 @@ __global__ void residual_list_k(T *r, const T *__restrict__ f, const T *__restri
     r[l] = f[l] + (c.hh * x[l] + c.hx * (x[l - 1] + x[l + 1]) + c.hy * (x[l - nx] + x[l + nx]) + c.hz * (x[l - nxny] + x[l + nxny]));
 }
 
+// restriction onto the coarse level's G voxels from its colour lists
+// (restrict_k without its zero writes: the coarse f outside G is zeroed at
+// set-up and nothing writes anything else there)
+template <typename T>
+__global__ void restrict_list_k(T *x2, const T *__restrict__ x, const uint32_t *__restrict__ l0, unsigned c0,
+                                const uint32_t *__restrict__ l1, unsigned c1, uint32_t nx2, uint32_t nxny2, Dims d)
+{
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= c0 + c1) return;
+    const uint32_t l2 = (t < c0 ? l0[t] : l1[t - c0]) & BL_IDX;
+    const uint32_t k2 = l2 / nxny2, rem = l2 - k2 * nxny2, j2 = rem / nx2, i2 = rem - j2 * nx2;
+    const size_t nx = d.nx, nxny = d.nxny();
+    const size_t l = (2 * (size_t)i2 - 1) + nx * (2 * (size_t)j2 - 1) + nxny * (2 * (size_t)k2 - 1);
+#define X(a, b, c) x[(ptrdiff_t)l + (a) + (b) * (ptrdiff_t)nx + (c) * (ptrdiff_t)nxny]
+    const T A = X(-1, -1, -1) + X(1, -1, -1) + X(-1, 1, -1) + X(1, 1, -1) + X(-1, -1, 1) + X(1, -1, 1) + X(-1, 1, 1) + X(1, 1, 1);
+    const T B = X(0, -1, -1) + X(-1, 0, -1) + X(1, 0, -1) + X(0, 1, -1) + X(1, -1, 0) + X(-1, -1, 0) + X(-1, 1, 0) +
+                X(1, 1, 0) + X(0, -1, 1) + X(-1, 0, 1) + X(1, 0, 1) + X(0, 1, 1);
+    const T C = X(0, 0, -1) + X(0, -1, 0) + X(-1, 0, 0) + X(1, 0, 0) + X(0, 1, 0) + X(0, 0, 1);
+#undef X
+    x2[l2] = (T)0.015625 * A + (T)0.03125 * B + (T)0.0625 * C + (T)0.125 * x[l];
+}
+
+// the V-cycle's restriction of level l's residual onto level l + 1
+template <typename T>
+static qsm_status level_restrict(qsm_ctx *ctx, Level<T> &C, const Level<T> &L)
+{
+    if (!C.gl[0]) return restrict_<T>(ctx, C.f, L.r, C.G, C.d, L.d);
+    const unsigned n = C.gn[0] + C.gn[1];
+    if (n == 0 || C.d.nx < 3 || C.d.ny < 3 || C.d.nz < 3) return QSM_OK;
+    restrict_list_k<T><<<(n + 255) / 256, 256, 0, ctx->stream>>>(C.f, L.r, C.gl[0], C.gn[0], C.gl[1], C.gn[1],
+                                                                 (uint32_t)C.d.nx, (uint32_t)C.d.nxny(), L.d);
+    QSM_CUDA(cudaGetLastError());
+    return QSM_OK;
+}
+
 template <typename T>
 static qsm_status level_residual(qsm_ctx *ctx, Level<T> &L)
 {
@@ -1635,7 +1670,7 @@ static qsm_status cycle(qsm_ctx *ctx, Hier<T> &H, int l, int mu, int pre, int po
         QSM_TRY(smooth<T>(ctx, H, L, pre, true));
         QSM_TRY(boundary_sweeps<T>(ctx, H, L, bs, true));
         QSM_TRY(level_residual<T>(ctx, L));
-        QSM_TRY(restrict_<T>(ctx, C.f, L.r, C.G, C.d, L.d));
+        QSM_TRY(level_restrict<T>(ctx, C, L));
         QSM_CUDA(cudaMemsetAsync(C.v, 0, C.n * sizeof(T), ctx->stream));
         for (int i = 0; i < mu; ++i) {
             QSM_TRY(cycle<T>(ctx, H, l + 1, mu, pre, post, nb, sc));
