@@ -250,7 +250,11 @@ qsm_status qsm_norm2(qsm_ctx *ctx, qsm_dtype dtype, size_t n, const void *x,
  *     1..QSM_NORM2_NOALLOC_MAX_N, otherwise QSM_ERR_DIMS;
  *   - all calls share that array: calls that overlap on the GPU race;
  *   - the first call on each device looks up the array's address with that
- *     device current; make that first call before any stream capture. */
+ *     device current; make that first call before any stream capture;
+ *   - a device reset (cudaDeviceReset; MATLAB's reset(gpuDevice)) replaces
+ *     the device's context and unloads the array: the next call notices the
+ *     new context and looks the address up again, so it is a first call
+ *     too and also belongs before any stream capture. */
 qsm_status qsm_norm2_noalloc(qsm_dtype dtype, size_t n, const void *x, const uint8_t *G,
                              double *out, void *stream);
 

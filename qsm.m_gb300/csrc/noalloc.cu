@@ -19,8 +19,14 @@
 //     to start at zero); calls that overlap on the GPU -- on two streams, or
 //     from two host threads -- race on it;
 //   - the first call on each device looks up the array's device address
-//     (cudaGetSymbolAddress, with that device current) and caches it; make
-//     that first call before any stream capture.
+//     (cudaGetSymbolAddress, with that device current) and caches it with
+//     the id of the CUDA context that was current; make that first call
+//     before any stream capture.  A device reset (cudaDeviceReset, MATLAB's
+//     reset(gpuDevice)) destroys the context and unloads the array, so the
+//     next call sees a new context id and looks the address up again: the
+//     first call after a reset is a set-up call too, and also belongs
+//     outside stream capture.
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <mutex>
 #include <stdint.h>
@@ -37,9 +43,43 @@ constexpr int kMaxDevices = 64;
 // Per-leaf partial sums (doubles; FP32 sums use the first half as floats).
 static __device__ __align__(256) double g_norm2_leaf_sums[kMaxLeaves];
 
-// Device address of g_norm2_leaf_sums per device, looked up once.
-double *g_scratch[kMaxDevices];
+// Device address of g_norm2_leaf_sums per device, with the id of the
+// context it was looked up in (0: not looked up yet).
+struct ScratchSlot {
+    unsigned long long ctx_id;
+    double *ptr;
+};
+ScratchSlot g_scratch[kMaxDevices];
 std::mutex g_scratch_mu;
+
+// The driver's context queries, reached through the runtime (the library
+// does not link libcuda itself).
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long *);
+
+// Id of the calling thread's current CUDA context; 0 when none is current
+// yet.  False when the driver does not offer the queries.
+bool current_ctx_id(unsigned long long &id)
+{
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    if (!get_current || !get_id) {
+        void *a = nullptr, *b = nullptr;
+        cudaDriverEntryPointQueryResult ra, rb;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 4000, cudaEnableDefault, &ra) != cudaSuccess ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &rb) != cudaSuccess ||
+            ra != cudaDriverEntryPointSuccess || rb != cudaDriverEntryPointSuccess || !a || !b) {
+            cudaGetLastError();
+            return false;
+        }
+        get_current = (CtxGetCurrentFn)a;
+        get_id = (CtxGetIdFn)b;
+    }
+    CUcontext c = nullptr;
+    if (get_current(&c) != CUDA_SUCCESS) return false;
+    id = 0;
+    return !c || get_id(c, &id) == CUDA_SUCCESS;
+}
 
 // (L(a), L(a+1)): leaf counts of the pairwise tree for sizes a and a+1.
 // A node of size s > 128 splits into s/2 (rounded down) and the rest.
@@ -165,15 +205,22 @@ extern "C" qsm_status qsm_norm2_noalloc(qsm_dtype dtype, size_t n, const void *x
     double *scratch;
     {
         std::lock_guard<std::mutex> lock(g_scratch_mu);
-        if (!g_scratch[dev]) {
+        unsigned long long id = 0;
+        if (!current_ctx_id(id)) return QSM_ERR_CUDA;
+        ScratchSlot &slot = g_scratch[dev];
+        if (id == 0 || slot.ctx_id != id || !slot.ptr) {
+            // set-up for this device and context: look the array up (this
+            // also creates the context when the runtime has not yet)
             void *p = nullptr;
             if (cudaGetSymbolAddress(&p, g_norm2_leaf_sums) != cudaSuccess || !p) {
                 cudaGetLastError();
                 return QSM_ERR_CUDA;
             }
-            g_scratch[dev] = (double *)p;
+            if (!current_ctx_id(id) || id == 0) return QSM_ERR_CUDA;
+            slot.ctx_id = id;
+            slot.ptr = (double *)p;
         }
-        scratch = g_scratch[dev];
+        scratch = slot.ptr;
     }
     const cudaStream_t s = (cudaStream_t)stream;
     const size_t nleaf = leaf_count(n);
