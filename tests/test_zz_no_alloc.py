@@ -46,6 +46,11 @@ def capi():
 
 
 def _existing(L, ctx, dt, x, g):
+    # qsm_norm2 runs on the context's own stream: torch's writes of x and g
+    # must be complete first
+    import torch
+
+    torch.cuda.current_stream().synchronize()
     out = ctypes.c_double()
     st = L.qsm_norm2(ctx, dt, x.numel(), ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(g.data_ptr()),
                      ctypes.byref(out))
