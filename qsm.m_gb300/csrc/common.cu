@@ -150,6 +150,42 @@ qsm_status read_double(qsm_ctx *ctx, const double *d, double *h)
     return QSM_OK;
 }
 
+namespace {
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+}  // namespace
+
+qsm_status tma_encode_3d(qsm_ctx *ctx, CUtensorMap *map, CUtensorMapDataType dt, const void *base,
+                         const uint64_t dims[3], const uint64_t strides[2], const uint32_t box[3])
+{
+    static EncodeTiledFn encode = nullptr;
+    if (!encode) {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        QSM_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
+        if (q != cudaDriverEntryPointSuccess || !fn) {
+            set_error(ctx, "cuTensorMapEncodeTiled is not available from the driver");
+            return QSM_ERR_CUDA;
+        }
+        encode = (EncodeTiledFn)fn;
+    }
+    const cuuint64_t gd[3] = {dims[0], dims[1], dims[2]};
+    const cuuint64_t gs[2] = {strides[0], strides[1]};
+    const cuuint32_t bx[3] = {box[0], box[1], box[2]};
+    const cuuint32_t es[3] = {1, 1, 1};
+    const CUresult r = encode(map, dt, 3, const_cast<void *>(base), gd, gs, bx, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error(ctx, "cuTensorMapEncodeTiled failed (%d): dims %llu %llu %llu box %u %u %u", (int)r,
+                  (unsigned long long)dims[0], (unsigned long long)dims[1], (unsigned long long)dims[2], box[0],
+                  box[1], box[2]);
+        return QSM_ERR_ARG;
+    }
+    return QSM_OK;
+}
+
 }  // namespace qsm
 
 // ---------------------------------------------------------------------------

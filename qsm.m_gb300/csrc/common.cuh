@@ -4,6 +4,7 @@
 // and the deterministic "lane order" reductions.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stddef.h>
@@ -172,5 +173,12 @@ qsm_status lane_dot(qsm_ctx *ctx, const T *x, const T *y, size_t n, double *dout
 
 // Reads back one device double (synchronises the stream).
 qsm_status read_double(qsm_ctx *ctx, const double *d, double *h);
+
+// A tiled TMA tensor map of a 3-D array (tma.cuh): element type dt, extents
+// dims[0..2] (dims[0] fastest), byte strides of dims 1 and 2 (multiples of
+// 16), box extents box[0..2]; zeros are read outside the extents.  Fails
+// with QSM_ERR_ARG where the driver refuses the description.
+qsm_status tma_encode_3d(qsm_ctx *ctx, CUtensorMap *map, CUtensorMapDataType dt, const void *base,
+                         const uint64_t dims[3], const uint64_t strides[2], const uint32_t box[3]);
 
 }  // namespace qsm

@@ -13,6 +13,7 @@ struct PdCtl {
     uint32_t iters;        // iteration count at which it passed
     uint32_t checks;       // checks performed
     uint32_t nonfinite;    // a monitor was NaN/Inf
+    uint32_t stalled;      // a bounded wait on a TMA load gave up (QSM_ERR_TIMEOUT)
 };
 
 // Device pointers of the plain path's state (component-major fields).

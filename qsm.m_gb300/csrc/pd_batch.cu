@@ -178,7 +178,10 @@ static BatchKernel batch_kernel(int v, bool tgv)
     case 2: return tgv ? tile_kernel<32, 4, 4, 8, true>() : tile_kernel<32, 4, 4, 8, false>();
     case 3: return tgv ? tile_kernel<32, 16, 2, 2, true>() : tile_kernel<32, 16, 2, 2, false>();
     case 8:
-    case 9: return tgv ? column_kernel<28, 16, true>() : column_kernel<28, 16, false>();
+    case 9:
+    case 10:  // TMA variants are packed with their register-prefetch stand-in
+    case 11:
+    case 12: return tgv ? column_kernel<28, 16, true>() : column_kernel<28, 16, false>();
     default: return tgv ? column_kernel<28, 12, true>() : column_kernel<28, 12, false>();
     }
 }
@@ -457,7 +460,8 @@ qsm_status rebuild(qsm_session *s)
             a.gbase = s->d_gbase;
             a.start = j->start;
             a.maxiter = j->maxiter;
-            if (pd_volume_launch(ctx, st, j->v, ((i + 1) % 10) == 0, a, j->tol, i) != QSM_OK) ce = cudaErrorLaunchFailure;
+            if (pd_volume_launch(ctx, st, j->v, ((i + 1) % 10) == 0, a, j->tol, i, i % kPhases) != QSM_OK)
+                ce = cudaErrorLaunchFailure;
         }
     }
     // join every stream used (branches sharing a stream are already ordered)
@@ -491,6 +495,7 @@ qsm_status set_batch_smem(qsm_ctx *ctx)
 {
     for (int v = 0; v < kNumVariants; ++v)
         for (int tg = 0; tg < 2; ++tg) {
+            if (variant(v).tma) continue;  // never packed (admission switches them to kTmaFallback)
             const BatchKernel bk = batch_kernel(v, tg != 0);
             const int sm = (int)variant_smem(v, tg != 0);
             for (int c = 0; c < 2; ++c)
@@ -633,6 +638,8 @@ qsm_status qsm_session_submit_pd(qsm_session *s, int32_t tgv, qsm_dtype dt, cons
     std::unique_ptr<PdJob> j(new PdJob());
     qsm_status st = pd_volume_init(ctx, &j->v, tgv != 0, d, dt, sf.dev, (const uint8_t *)sm.dev, vsz, lam, alpha);
     if (st == QSM_OK) st = pd_volume_tune(ctx, &j->v, maxiter);
+    // a volume small enough to be packed runs the packed kernels, which have no TMA form
+    if (st == QSM_OK && variant(j->v.var).tma && j->v.tl[j->v.var].nact < s->solo_tiles) j->v.var = kTmaFallback;
     stage_out(ctx, sf, false);
     stage_out(ctx, sm, false);
     if (st != QSM_OK) {
@@ -748,7 +755,10 @@ qsm_status qsm_session_step(qsm_session *s, uint32_t iters)
         j->ctl = s->h_ctl[k];
         j->seconds += ms * 1e-3;
         const uint32_t done_it = s->gbase - j->start;
-        if (j->ctl.done) {
+        if (j->ctl.stalled) {  // a bounded TMA wait gave up: the job ends with QSM_ERR_TIMEOUT
+            j->finished = true;
+            j->iters = std::min(done_it, j->maxiter);
+        } else if (j->ctl.done) {
             j->finished = true;
             j->iters = j->ctl.iters;
         } else if (done_it >= j->maxiter) {
@@ -768,6 +778,7 @@ qsm_status qsm_session_poll(qsm_session *s, uint64_t id, int32_t *finished, qsm_
     if (ip != s->pd.end()) {
         *finished = ip->second->finished ? 1 : 0;
         fill_pd_info(*ip->second, pd_info);
+        if (ip->second->ctl.stalled) return fail(s, QSM_ERR_TIMEOUT, "a bounded wait on a TMA load gave up");
         return QSM_OK;
     }
     auto im = s->mg.find(id);
@@ -794,6 +805,7 @@ qsm_status qsm_session_fetch(qsm_session *s, uint64_t id, void *out)
     if (ip != s->pd.end()) {
         PdJob &j = *ip->second;
         if (!j.finished) return fail(s, QSM_ERR_BUSY, "job still running");
+        if (j.ctl.stalled) return fail(s, QSM_ERR_TIMEOUT, "a bounded wait on a TMA load gave up");
         const size_t es = j.dt == QSM_F32 ? 4 : 8;
         Staged so;
         QSM_TRY(stage_in(ctx, so, out, j.v.d.n() * es, false));

@@ -116,11 +116,13 @@ tv_fused_k(FusedArgs s, DualC<float> dc, PrimalC<float> pc, Dims d, double tol, 
 // variants, launch, autotuning
 // ---------------------------------------------------------------------------
 
-// 3-D tiles: threads = tx * ty; streaming: threads = (tx + 4) * (ty + 4)
-static const Variant kVariants[kNumVariants] = {{32, 8, 4, false}, {32, 8, 2, false}, {32, 4, 4, false},
-                                                {32, 16, 2, false}, {28, 12, 8, true},  {28, 12, 16, true},
-                                                {28, 12, 32, true},  {28, 12, 64, true}, {28, 16, 16, true},
-                                                {28, 16, 32, true}};
+// 3-D tiles: threads = tx * ty; streaming: threads = (tx + 4) * (ty + 4);
+// 10-12: TMA-staged column kernels (TGV)
+static const Variant kVariants[kNumVariants] = {
+    {32, 8, 4, false, false},  {32, 8, 2, false, false},  {32, 4, 4, false, false},  {32, 16, 2, false, false},
+    {28, 12, 8, true, false},  {28, 12, 16, true, false}, {28, 12, 32, true, false}, {28, 12, 64, true, false},
+    {28, 16, 16, true, false}, {28, 16, 32, true, false}, {28, 16, 16, true, true},  {28, 20, 16, true, true},
+    {28, 24, 16, true, true}};
 
 const Variant &variant(int v) { return kVariants[v]; }
 
@@ -133,6 +135,7 @@ int variant_threads(int v)
 size_t variant_smem(int v, bool tgv)
 {
     const Variant &x = kVariants[v];
+    if (x.tma && tgv) return stream_tma_smem(x.tx, x.ty);
     if (x.stream) return stream_smem(x.tx, x.ty, tgv);
     const size_t bn = (size_t)(x.tx + 2) * (x.ty + 2) * (x.tz + 2);
     const size_t dual = (tgv ? 10 : 4) * bn * sizeof(float);
@@ -163,14 +166,21 @@ static qsm_status set_smem_t(qsm_ctx *ctx, size_t tgv_smem, size_t tv_smem)
     return QSM_OK;
 }
 
+bool variant_ok(const PdVolume &v, int var)
+{
+    return var >= 0 && var < kNumVariants && (!kVariants[var].tma || (v.tgv && !v.maps.empty()));
+}
+
+// tm: the volume's TMA maps of this iteration (TMA variants)
 static qsm_status launch_variant(qsm_ctx *ctx, cudaStream_t st, int v, bool tgv, bool chk, unsigned nact,
                                  const FusedArgs &s, const DualC<float> &dc, const PrimalC<float> &pc, const Dims &d,
-                                 double tol, uint32_t it)
+                                 double tol, uint32_t it, const TmaMaps *tm)
 {
     const size_t sm = variant_smem(v, tgv);
+    if (kVariants[v].tma && !tm) return QSM_ERR_ARG;
     if (kVariants[v].stream)
         return stream_launch(ctx, st, kVariants[v].tx, kVariants[v].ty, kVariants[v].tz, tgv, chk, nact, s, dc, pc, d,
-                             tol, it);
+                             tol, it, kVariants[v].tma ? tm : nullptr);
     switch (v) {
     case 0: launch_t<32, 8, 4, 4>(st, tgv, chk, nact, s, dc, pc, d, tol, it, sm); break;
     case 1: launch_t<32, 8, 2, 4>(st, tgv, chk, nact, s, dc, pc, d, tol, it, sm); break;
@@ -182,10 +192,18 @@ static qsm_status launch_variant(qsm_ctx *ctx, cudaStream_t st, int v, bool tgv,
     return QSM_OK;
 }
 
-qsm_status pd_volume_launch(qsm_ctx *ctx, cudaStream_t st, const PdVolume &v, bool chk, const FusedArgs &s,
-                            double tol, uint32_t it)
+// the TMA maps of variant var for the iteration whose arguments are pd_volume_args(v, var, rot)
+static const TmaMaps *volume_maps(const PdVolume &v, int var, uint32_t rot)
 {
-    return launch_variant(ctx, st, v.var, v.tgv, chk, v.tl[v.var].nact, s, v.dc, v.pc, v.d, tol, it);
+    if (!kVariants[var].tma || v.maps.empty()) return nullptr;
+    return &v.maps[(size_t)var * 3 + rot % 3];
+}
+
+qsm_status pd_volume_launch(qsm_ctx *ctx, cudaStream_t st, const PdVolume &v, bool chk, const FusedArgs &s,
+                            double tol, uint32_t it, uint32_t rot)
+{
+    return launch_variant(ctx, st, v.var, v.tgv, chk, v.tl[v.var].nact, s, v.dc, v.pc, v.d, tol, it,
+                          volume_maps(v, v.var, rot));
 }
 
 static qsm_status set_all_smem(qsm_ctx *ctx)
@@ -356,6 +374,32 @@ qsm_status pd_volume_init(qsm_ctx *ctx, PdVolume *v, bool tgv, const Dims &d, qs
     v->dc = tgv ? make_dual_c<float>(sigma, h, alpha * lam, lam) : make_dual_c<float>(sigma, h, 0.0, lam);
     v->pc = make_primal_c<float>(tau, h);
     v->var = 0;
+    // TMA variants: tensor maps of every primal buffer, per tile shape and iterate rotation.
+    // Family B's rows must be 16-byte strides: nx a multiple of 4.
+    v->maps.clear();
+    if (tgv && d.nx % 4 == 0 && d.nx >= 4) {
+        std::vector<TmaMaps> maps((size_t)kNumVariants * 3);
+        const uint64_t da[3] = {4 * d.nx, d.ny, d.nz}, sa[2] = {16 * d.nx, 16 * d.nx * d.ny};
+        const uint64_t db[3] = {d.nx, d.ny, d.nz}, sb[2] = {4 * d.nx, 4 * d.nx * d.ny};
+        for (int k = 0; k < kNumVariants; ++k) {
+            if (!kVariants[k].tma) continue;
+            const uint32_t wx = (uint32_t)kVariants[k].tx + 4, wy = (uint32_t)kVariants[k].ty + 4;
+            const uint32_t ba[3] = {4 * wx, wy, 1}, bb[3] = {wx + 4, wy, 1};
+            CUtensorMap A[3], Bm[3];
+            for (int b = 0; b < 3; ++b) {
+                QSM_TRY(tma_encode_3d(ctx, &A[b], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, v->PA[b], da, sa, ba));
+                QSM_TRY(tma_encode_3d(ctx, &Bm[b], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, v->PB[b], db, sb, bb));
+            }
+            for (uint32_t r = 0; r < 3; ++r) {  // the rotation of pd_volume_args
+                TmaMaps &m = maps[(size_t)k * 3 + r];
+                m.ac = A[r % 3];
+                m.ap = A[(r + 2) % 3];
+                m.bc = Bm[r % 3];
+                m.bp = Bm[(r + 2) % 3];
+            }
+        }
+        v->maps.swap(maps);
+    }
     return QSM_OK;
 }
 
@@ -392,6 +436,7 @@ qsm_status pd_volume_tune(qsm_ctx *ctx, PdVolume *v, uint32_t maxiter)
     const char *force = getenv("QSM_FUSED_VARIANT");
     if (force && *force) {
         v->var = std::min(std::max(atoi(force), 0), kNumVariants - 1);
+        if (!variant_ok(*v, v->var)) v->var = kTmaFallback;
         return QSM_OK;
     }
     const TuneKey key((int)v->tgv, v->d.nx, v->d.ny, v->d.nz);
@@ -399,7 +444,7 @@ qsm_status pd_volume_tune(qsm_ctx *ctx, PdVolume *v, uint32_t maxiter)
         std::lock_guard<std::mutex> lock(g_tune_mu);
         tune_load_locked();
         auto itk = g_tuned.find(key);
-        if (itk != g_tuned.end()) {
+        if (itk != g_tuned.end() && variant_ok(*v, itk->second)) {
             v->var = itk->second;
             return QSM_OK;
         }
@@ -412,13 +457,14 @@ qsm_status pd_volume_tune(qsm_ctx *ctx, PdVolume *v, uint32_t maxiter)
     QSM_CUDA(cudaEventCreate(&t1));
     float best = 1e30f;
     for (int k = 0; k < kNumVariants; ++k) {
+        if (!variant_ok(*v, k)) continue;
         for (uint32_t it = 0; it < 2; ++it)
             QSM_TRY(launch_variant(ctx, ctx->stream, k, v->tgv, false, v->tl[k].nact, pd_volume_args(*v, k, it),
-                                   v->dc, v->pc, v->d, 0.0, it + 1));
+                                   v->dc, v->pc, v->d, 0.0, it + 1, volume_maps(*v, k, it)));
         QSM_CUDA(cudaEventRecord(t0, ctx->stream));
         for (uint32_t it = 2; it < 8; ++it)
             QSM_TRY(launch_variant(ctx, ctx->stream, k, v->tgv, false, v->tl[k].nact, pd_volume_args(*v, k, it),
-                                   v->dc, v->pc, v->d, 0.0, it + 1));
+                                   v->dc, v->pc, v->d, 0.0, it + 1, volume_maps(*v, k, it)));
         QSM_CUDA(cudaEventRecord(t1, ctx->stream));
         QSM_CUDA(cudaEventSynchronize(t1));
         float ms = 0.f;
@@ -499,7 +545,7 @@ qsm_status pd_fused(qsm_ctx *ctx, bool tgv, const Dims &d, qsm_dtype dt, const v
         const bool chk = ((it + 1) % 10) == 0;
         if (!empty)
             QSM_TRY(launch_variant(ctx, ctx->stream, var, tgv, chk, nact, pd_volume_args(v, var, it), v.dc, v.pc, d,
-                                   tol, it + 1));
+                                   tol, it + 1, volume_maps(v, var, it)));
         enq = it + 1;
         const bool print = verbose && (it == 0 || it == maxiter - 1 || ((it + 1) % pmod) == 0);
         if (print || (chk && ((it + 1) % 100) == 0)) {
@@ -515,6 +561,13 @@ qsm_status pd_fused(qsm_ctx *ctx, bool tgv, const Dims &d, qsm_dtype dt, const v
     QSM_CUDA(cudaMemcpyAsync(&hctl, v.ctl, sizeof(PdCtl), cudaMemcpyDeviceToHost, ctx->stream));
     QSM_CUDA(cudaStreamSynchronize(ctx->stream));
     const uint32_t iters = hctl.done ? hctl.iters : enq;
+    if (hctl.stalled) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        pd_volume_free(ctx, &v);
+        set_error(ctx, "fused solve: a bounded wait on a TMA load gave up");
+        return QSM_ERR_TIMEOUT;
+    }
     QSM_TRY(pd_volume_result(ctx, v, iters, dt, chi_out));
     QSM_CUDA(cudaStreamSynchronize(ctx->stream));
     float ms = 0.f;

@@ -2,6 +2,8 @@
 // 3-D tiles; pd_stream.cu: z-streaming column tiles).
 #pragma once
 
+#include <vector>
+
 #include "common.cuh"
 #include "pd.cuh"
 
@@ -170,11 +172,21 @@ __device__ __forceinline__ void monitor_reduce(const FusedArgs &s, double *red, 
     monitor_fold<THREADS>(s.part, s.count, s.ctl, gridDim.x, blockIdx.x, red, acc, tol, it);
 }
 
+// Tensor maps of the TGV primal families at iterates n (c) and n-1 (p) for
+// the TMA column kernel (pd_tma.cuh): family A as floats (4 nx, ny, nz)
+// with a (4 (TX+4), TY+4, 1) box, family B as (nx, ny, nz) with a
+// (TX+8, TY+4, 1) box.
+struct TmaMaps {
+    CUtensorMap ac, ap, bc, bp;
+};
+
 size_t stream_smem(int tx, int ty, bool tgv);
+size_t stream_tma_smem(int tx, int ty);
 qsm_status stream_set_smem(qsm_ctx *ctx);
+// tm: the TMA column kernel (TGV) with these maps; null: the register-prefetch one
 qsm_status stream_launch(qsm_ctx *ctx, cudaStream_t st, int tx, int ty, int cz, bool tgv, bool chk, unsigned nact,
                          const FusedArgs &s, const DualC<float> &dc, const PrimalC<float> &pc, const Dims &d,
-                         double tol, uint32_t it);
+                         double tol, uint32_t it, const TmaMaps *tm);
 
 // ---------------------------------------------------------------------------
 // Tile variants and the device state of one fused solve (pd_fused.cu), shared
@@ -184,8 +196,13 @@ qsm_status stream_launch(qsm_ctx *ctx, cudaStream_t st, int tx, int ty, int cz, 
 struct Variant {
     int tx, ty, tz;   // tile of interior voxels (z: chunk of planes for the column kernel)
     bool stream;      // column-streaming kernel, else the 3-D tile kernel
+    bool tma;         // column kernel with TMA-staged primal iterates (TGV, nx a multiple of 4)
 };
-constexpr int kNumVariants = 10;
+constexpr int kNumVariants = 13;
+// register-prefetch column variant (28 x 16, 16 planes) that stands in for a
+// TMA variant where that cannot run (TV, nx not a multiple of 4, packed
+// many-volume launches)
+constexpr int kTmaFallback = 8;
 const Variant &variant(int v);
 size_t variant_smem(int v, bool tgv);
 int variant_threads(int v);
@@ -218,7 +235,13 @@ struct PdVolume {
     DualC<float> dc{};
     PrimalC<float> pc{};
     int var = 0;                 // chosen tile variant
+    // TMA maps per (variant, iterate rotation it % 3), filled for the TMA
+    // variants; empty when they cannot run on this volume
+    std::vector<TmaMaps> maps;
 };
+
+// Whether variant var can run on this volume.
+bool variant_ok(const PdVolume &v, int var);
 
 // Device bytes one solve holds (the allocation pd_volume_init makes).
 size_t pd_volume_bytes(bool tgv, const Dims &d);
@@ -230,9 +253,10 @@ FusedArgs pd_volume_args(const PdVolume &v, int var, uint32_t it);
 // Picks v->var: QSM_FUSED_VARIANT, the tuning table, or timing each variant
 // on this volume for a few iterations (the state is zeroed again after).
 qsm_status pd_volume_tune(qsm_ctx *ctx, PdVolume *v, uint32_t maxiter);
-// One iteration of variant v->var on stream st (the one-volume kernels).
+// One iteration of variant v->var on stream st (the one-volume kernels); s
+// from pd_volume_args(v, v.var, rot), it the kernel's iteration argument.
 qsm_status pd_volume_launch(qsm_ctx *ctx, cudaStream_t st, const PdVolume &v, bool chk, const FusedArgs &s,
-                            double tol, uint32_t it);
+                            double tol, uint32_t it, uint32_t rot);
 // chi after `iters` iterations, converted to dt.
 qsm_status pd_volume_result(qsm_ctx *ctx, const PdVolume &v, uint32_t iters, qsm_dtype dt, void *chi);
 qsm_status pd_volume_free(qsm_ctx *ctx, PdVolume *v);

@@ -1,7 +1,9 @@
 // Primal-dual TGV / TV, mixed-precision fused path: the one-volume
-// z-streaming kernel.  A CTA owns a TX x TY column tile of the interior and
-// a chunk of planes; the column body (column_pd) is in pd_tile.cuh.
+// z-streaming kernels.  A CTA owns a TX x TY column tile of the interior and
+// a chunk of planes; the column bodies are column_pd (pd_tile.cuh: register
+// prefetch) and column_tma (pd_tma.cuh: TMA-staged primal iterates, TGV).
 #include "pd_tile.cuh"
+#include "pd_tma.cuh"
 
 namespace qsm {
 
@@ -17,6 +19,22 @@ stream_k(FusedArgs s, DualC<float> dc, PrimalC<float> pc, Dims d, int cz, double
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
     column_pd<TX, TY, TGV>(s, dc, pc, d, cz, s.tiles[blockIdx.x], CHECK, (float *)smem_raw, acc);
     if (CHECK) monitor_reduce<(TX + 4) * (TY + 4)>(s, smem_raw, acc, tol, itn);
+}
+
+template <int TX, int TY, bool CHECK>
+__global__ void __launch_bounds__((TX + 4) * (TY + 4), 1)
+stream_tma_k(const __grid_constant__ TmaMaps tm, FusedArgs s, DualC<float> dc, PrimalC<float> pc, Dims d, int cz,
+             double tol, uint32_t it)
+{
+    extern __shared__ __align__(16) unsigned char smem_tma[];
+    if (s.ctl->done) return;
+    const uint32_t itn = launch_iter(s, it);
+    if (!itn) return;
+    char *base = tma_smem_base(smem_tma);
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    column_tma<TX, TY>(tm, s, dc, pc, d, cz, s.tiles[blockIdx.x], CHECK, base, acc);
+    // the monitor fold reuses shared memory past the plane barriers
+    if (CHECK) monitor_reduce<(TX + 4) * (TY + 4)>(s, (double *)(base + 128), acc, tol, itn);
 }
 
 size_t stream_smem(int tx, int ty, bool tgv)
@@ -37,11 +55,42 @@ static qsm_status set_t(qsm_ctx *ctx)
     return QSM_OK;
 }
 
+size_t stream_tma_smem(int tx, int ty)
+{
+    if (tx == 28 && ty == 16) return TmaLayout<28, 16>::REQUEST;
+    if (tx == 28 && ty == 20) return TmaLayout<28, 20>::REQUEST;
+    if (tx == 28 && ty == 24) return TmaLayout<28, 24>::REQUEST;
+    return 0;
+}
+
+template <int TX, int TY>
+static qsm_status set_tma_t(qsm_ctx *ctx)
+{
+    const int b = (int)TmaLayout<TX, TY>::REQUEST;
+    QSM_CUDA(cudaFuncSetAttribute(stream_tma_k<TX, TY, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    QSM_CUDA(cudaFuncSetAttribute(stream_tma_k<TX, TY, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    return QSM_OK;
+}
+
 qsm_status stream_set_smem(qsm_ctx *ctx)
 {
     QSM_TRY((set_t<28, 12>(ctx)));
     QSM_TRY((set_t<28, 16>(ctx)));
+    QSM_TRY((set_tma_t<28, 16>(ctx)));
+    QSM_TRY((set_tma_t<28, 20>(ctx)));
+    QSM_TRY((set_tma_t<28, 24>(ctx)));
     return QSM_OK;
+}
+
+template <int TX, int TY>
+static void launch_tma_t(cudaStream_t st, bool chk, unsigned nact, const TmaMaps &tm, const FusedArgs &s,
+                         const DualC<float> &dc, const PrimalC<float> &pc, const Dims &d, int cz, double tol,
+                         uint32_t it)
+{
+    const size_t sm = TmaLayout<TX, TY>::REQUEST;
+    const int nt = (TX + 4) * (TY + 4);
+    if (chk) stream_tma_k<TX, TY, true><<<nact, nt, sm, st>>>(tm, s, dc, pc, d, cz, tol, it);
+    else stream_tma_k<TX, TY, false><<<nact, nt, sm, st>>>(tm, s, dc, pc, d, cz, tol, it);
 }
 
 template <int TX, int TY>
@@ -61,8 +110,17 @@ static void launch_t(cudaStream_t st, bool tgv, bool chk, unsigned nact, const F
 
 qsm_status stream_launch(qsm_ctx *ctx, cudaStream_t st, int tx, int ty, int cz, bool tgv, bool chk, unsigned nact,
                          const FusedArgs &s, const DualC<float> &dc, const PrimalC<float> &pc, const Dims &d,
-                         double tol, uint32_t it)
+                         double tol, uint32_t it, const TmaMaps *tm)
 {
+    if (tm) {
+        if (!tgv) return QSM_ERR_ARG;
+        if (tx == 28 && ty == 16) launch_tma_t<28, 16>(st, chk, nact, *tm, s, dc, pc, d, cz, tol, it);
+        else if (tx == 28 && ty == 20) launch_tma_t<28, 20>(st, chk, nact, *tm, s, dc, pc, d, cz, tol, it);
+        else if (tx == 28 && ty == 24) launch_tma_t<28, 24>(st, chk, nact, *tm, s, dc, pc, d, cz, tol, it);
+        else return QSM_ERR_ARG;
+        QSM_CUDA(cudaGetLastError());
+        return QSM_OK;
+    }
     if (tx == 28 && ty == 12) launch_t<28, 12>(st, tgv, chk, nact, s, dc, pc, d, cz, tol, it);
     else if (tx == 28 && ty == 16) launch_t<28, 16>(st, tgv, chk, nact, s, dc, pc, d, cz, tol, it);
     else return QSM_ERR_ARG;

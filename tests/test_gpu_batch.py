@@ -27,7 +27,7 @@ LAUNCH = {"packed": "4294967295", "solo": "0"}  # QSM_BATCH_SOLO_TILES
 
 
 @pytest.mark.parametrize("launch", ["packed", "solo"])
-@pytest.mark.parametrize("variant", list(range(10)))
+@pytest.mark.parametrize("variant", list(range(13)))
 def test_batch_matches_oracle_every_variant(gpu_ctx, qsm, port, variant, launch, monkeypatch):
     """Uneven volumes, 40 iterations (not a multiple of the 30-iteration
     graph), packed into persistent launches or each in its own graph branch:

@@ -139,11 +139,12 @@ def _active_voxels(m, tile):
 
 
 @pytest.mark.parametrize("shape", [(77, 41, 23), (70, 30, 75)])
-@pytest.mark.parametrize("variant", list(range(10)))
+@pytest.mark.parametrize("variant", list(range(13)))
 def test_fused_tile_variants_bitexact(gpu_ctx, qsm, port, variant, shape, monkeypatch):
-    """Every tile variant (3-D tiles 0-3, z-streaming column tiles 4-9)
-    gives the reference's FP32 result (partial tiles and chunks, odd extents,
-    a mask that leaves whole tiles inactive)."""
+    """Every tile variant (3-D tiles 0-3, z-streaming column tiles 4-9, TMA
+    column tiles 10-12, which stand down to variant 8 where nx is not a
+    multiple of 4 and for TV) gives the reference's FP32 result (partial
+    tiles and chunks, odd extents, a mask that leaves whole tiles inactive)."""
     monkeypatch.setenv("QSM_FUSED_VARIANT", str(variant))
     rng = np.random.default_rng(40 + variant)
     d2f = np.asfortranarray((rng.standard_normal(shape) * 0.05).astype(np.float32))
@@ -160,6 +161,57 @@ def test_fused_tile_variants_bitexact(gpu_ctx, qsm, port, variant, shape, monkey
     a = qsm.pd_tv_mex(d2f, m, [1, 1, 1], 0.003, 0.0, 30, fused=True)
     b = port.pd_tv_mex(d2f, m, [1, 1, 1], 0.003, 0.0, 30)
     assert bits_equal(a, b), first_diff(a, b)
+
+
+TMA_TILES = {10: (28, 16, 16), 11: (28, 20, 16), 12: (28, 24, 16)}
+
+
+def _ellipsoid_case(shape, seed, fill=0.42):
+    rng = np.random.default_rng(seed)
+    d2f = np.asfortranarray((rng.standard_normal(shape) * 0.05).astype(np.float32))
+    g = np.indices(shape).astype(float)
+    c = [(n - 1) / 2 for n in shape]
+    q = sum(((g[i] - c[i]) / (fill * shape[i])) ** 2 for i in range(3))
+    return d2f, np.asfortranarray((q <= 1).astype(np.uint8))
+
+
+@pytest.mark.parametrize("shape", [(76, 41, 23), (72, 30, 75), (60, 64, 40), (32, 24, 18)])
+@pytest.mark.parametrize("variant", [10, 11, 12])
+def test_fused_tma_variants_bitexact(gpu_ctx, qsm, port, variant, shape, monkeypatch):
+    """The TMA-staged column kernels (nx a multiple of 4) give the reference's
+    FP32 TGV result bit for bit: partial tiles and z-chunks, plane boxes that
+    reach outside the volume on every side (read as the TMA's zero fill), a
+    grid smaller than one tile, anisotropic voxels."""
+    monkeypatch.setenv("QSM_FUSED_VARIANT", str(variant))
+    d2f, m = _ellipsoid_case(shape, 70 + variant)
+    for vsz in ([1, 1, 1], [1, 0.9, 1.2]):
+        info = {}
+        a = qsm.pd_tgv_mex(d2f, m, vsz, 0.003, 2.0, 0.0, 30, fused=True, info=info)
+        assert tuple(info["tile"]) == TMA_TILES[variant]
+        b = port.pd_tgv_mex(d2f, m, vsz, 0.003, 2.0, 0.0, 30)
+        assert bits_equal(a, b), first_diff(a, b)
+        assert info["active_voxels"] == _active_voxels(m, tuple(info["tile"]))
+
+
+def test_fused_tma_monitors_equal_register_path(gpu_ctx, qsm, monkeypatch):
+    """Same tile (28 x 16): the TMA kernel's in-kernel monitors and stopping
+    iteration equal the register-prefetch kernel's (every thread sums the
+    same voxels in the same order)."""
+    rng = np.random.default_rng(3)
+    shape = (24, 22, 20)  # the stopping-rule case above (nx a multiple of 4)
+    d2f = np.asfortranarray((rng.standard_normal(shape) * 0.01).astype(np.float32))
+    g = np.indices(shape).astype(float)
+    m = np.asfortranarray((sum((g[i] - 11) ** 2 for i in range(3)) < 64).astype(np.uint8))
+    out = {}
+    for variant in (8, 10):
+        monkeypatch.setenv("QSM_FUSED_VARIANT", str(variant))
+        info = {}
+        chi = qsm.pd_tgv_mex(d2f, m, [1, 1, 1], 0.003, 2.0, 5e-3, 2000, fused=True, info=info)
+        out[variant] = (chi, info)
+    (c8, i8), (c10, i10) = out[8], out[10]
+    assert i8["iters"] == i10["iters"] < 2000
+    assert i8["monitors"] == i10["monitors"]
+    assert bits_equal(c8, c10), first_diff(c8, c10)
 
 
 def test_autotuned_solve_is_reset(gpu_ctx, qsm, port, monkeypatch):
