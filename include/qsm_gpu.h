@@ -60,6 +60,15 @@ typedef struct qsm_ctx qsm_ctx;
 
 /* ---------------- context ---------------- */
 
+/* Test hook (no counterpart in the reference).  QSM_DEBUG_GRID_BARRIER_TIMEOUT
+ * makes every grid barrier of the whole-GPU multigrid kernels (the coarsest
+ * solve and list sweeps on cooperative launches) wait for one arrival more
+ * than the grid makes, with a short poll limit, so that their bounded wait
+ * runs out: the solve then returns QSM_ERR_TIMEOUT and the context stays
+ * usable.  flags = 0 restores normal operation. */
+#define QSM_DEBUG_GRID_BARRIER_TIMEOUT 1u
+qsm_status qsm_ctx_set_debug(qsm_ctx *ctx, uint32_t flags);
+
 /* Creates a context on `device` with its own non-blocking stream and a
  * stream-ordered memory pool. */
 qsm_status qsm_ctx_create(int device, qsm_ctx **ctx);

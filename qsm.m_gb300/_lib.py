@@ -174,6 +174,8 @@ def lib() -> ctypes.CDLL:
     L.qsm_ctx_get_stream.restype = P
     L.qsm_ctx_set_verbose.argtypes = [CTX, ctypes.c_int]
     L.qsm_ctx_set_verbose.restype = STATUS
+    L.qsm_ctx_set_debug.argtypes = [CTX, ctypes.c_uint32]
+    L.qsm_ctx_set_debug.restype = STATUS
     L.qsm_last_error.argtypes = [CTX]
     L.qsm_last_error.restype = ctypes.c_char_p
     L.qsm_status_string.argtypes = [ctypes.c_int]
@@ -202,7 +204,7 @@ def lib() -> ctypes.CDLL:
 def exported_symbols() -> list[str]:
     """Names of every function include/qsm_gpu.h declares."""
     return sorted(list(SIGNATURES) + list(SESSION_SIGNATURES) + list(HOST_SIGNATURES) + ["qsm_ctx_create", "qsm_ctx_destroy", "qsm_ctx_set_stream",
-                                      "qsm_ctx_get_stream", "qsm_ctx_set_verbose", "qsm_last_error",
+                                      "qsm_ctx_get_stream", "qsm_ctx_set_verbose", "qsm_ctx_set_debug", "qsm_last_error",
                                       "qsm_status_string", "qsm_abi_version", "qsm_norm2_noalloc",
                                       "qsm_fp_pipe_rate"])
 

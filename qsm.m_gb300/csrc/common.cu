@@ -255,6 +255,14 @@ qsm_status qsm_ctx_create(int device, qsm_ctx **out)
     return QSM_OK;
 }
 
+qsm_status qsm_ctx_set_debug(qsm_ctx *ctx, uint32_t flags)
+{
+    if (!ctx) return QSM_ERR_ARG;
+    if (flags & ~(uint32_t)QSM_DEBUG_GRID_BARRIER_TIMEOUT) return QSM_ERR_ARG;
+    ctx->debug = flags;
+    return QSM_OK;
+}
+
 qsm_status qsm_ctx_destroy(qsm_ctx *ctx)
 {
     if (!ctx) return QSM_OK;

@@ -97,6 +97,7 @@ struct qsm_ctx {
     double *red_out;       // 8 doubles
     unsigned int *red_count;
     double *host_out;      // pinned, 8 doubles
+    uint32_t debug;        // QSM_DEBUG_* test hooks (qsm_ctx_set_debug)
 };
 
 namespace qsm {

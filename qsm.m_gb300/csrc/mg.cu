@@ -562,6 +562,8 @@ constexpr unsigned CG_MIN_PASS = 6000;          // per-colour G count from which
 struct GridBar {
     unsigned *count;  // arrivals since the launch (zeroed by the host before it)
     int *err;
+    unsigned extra;   // arrivals required beyond the grid's (0; 1 under QSM_DEBUG_GRID_BARRIER_TIMEOUT)
+    long long limit;  // polls before a wait gives up
 };
 
 // Barrier number k (1, 2, ...) of the grid: each CTA adds one arrival with
@@ -573,7 +575,7 @@ __device__ __forceinline__ bool grid_bar(const GridBar &g, unsigned &k)
     __shared__ int bad;
     __syncthreads();
     if (threadIdx.x == 0) {
-        const unsigned target = ++k * gridDim.x;
+        const unsigned target = ++k * gridDim.x + g.extra;
         __threadfence();
         asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(g.count) : "memory");
         long long spins = 0;
@@ -582,7 +584,7 @@ __device__ __forceinline__ bool grid_bar(const GridBar &g, unsigned &k)
             asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(g.count) : "memory");
             if ((int)(cur - target) >= 0) break;
             if ((++spins & 1023) == 0 && *(volatile int *)g.err != 0) break;
-            if (spins > CG_SPIN_LIMIT) {
+            if (spins > g.limit) {
                 atomicExch(g.err, 1);
                 break;
             }
@@ -1313,6 +1315,10 @@ static qsm_status hier_init(qsm_ctx *ctx, Hier<T> &H, int nl, const Dims &dp, co
     c += al256((RED_NBLK + 1) * sizeof(double));
     H.gb.count = (unsigned *)c;
     H.gb.err = (int *)c + 1;
+    // test hook: barriers that can never complete, with a short wait, so the bounded wait runs out
+    const bool short_bar = (ctx->debug & QSM_DEBUG_GRID_BARRIER_TIMEOUT) != 0;
+    H.gb.extra = short_bar ? 1u : 0u;
+    H.gb.limit = short_bar ? (1ll << 12) : CG_SPIN_LIMIT;
     const size_t nc = H.L[nl - 1].n;
     H.coarse_smem = nc * (3 * sizeof(T) + 1) + RED_NBLK * sizeof(T) + 64;
     int maxsm = 0;
@@ -2011,9 +2017,10 @@ static qsm_status pcg(qsm_ctx *ctx, const Dims &d, const TP *v0, const TP *f, co
         info->resnorm = res;
         info->seconds = ms * 1e-3;
     }
-    QSM_TRY(coarse_report(ctx, H, info));
+    const qsm_status rep = coarse_report(ctx, H, info);  // a timed-out solve still frees its state
     QSM_TRY(dfree(ctx, pv));
-    return hier_free(ctx, H);
+    QSM_TRY(hier_free(ctx, H));
+    return rep;
 }
 
 template <typename T>
@@ -2073,9 +2080,10 @@ static qsm_status mg_solve(qsm_ctx *ctx, const Dims &d, const T *v0, const T *f,
         info->resnorm = 0.0;
         info->seconds = ms * 1e-3;
     }
-    QSM_TRY(coarse_report(ctx, H, info));
+    const qsm_status rep = coarse_report(ctx, H, info);  // a timed-out solve still frees its state
     QSM_TRY(dfree(ctx, sv));
-    return hier_free(ctx, H);
+    QSM_TRY(hier_free(ctx, H));
+    return rep;
 }
 
 // ---------------------------------------------------------------------------

@@ -154,6 +154,42 @@ def test_coarse_grid_solver_vs_oracle(gpu_ctx, qsm, port, dt):
     assert bits_equal(a, port.mg_mex(v0, f, m, [1, 1, 1], 1e-6, 2, 1, 2, 2, 2, 2))
 
 
+def test_grid_barrier_wait_runs_out(gpu_ctx, qsm, port):
+    """The grid barrier of the whole-GPU multigrid kernels waits a bounded
+    number of polls.  With the context's test hook every barrier waits for
+    one arrival more than the grid makes, so each wait runs out: the solve
+    must return QSM_ERR_TIMEOUT within seconds (no hang), and the same
+    context must then solve normally, bit for bit against the oracle."""
+    import time
+
+    import qsm_gb300._lib as _lib
+    import qsm_gb300.synthetic as S
+
+    f, m, _ = S.poisson_case((96, 88, 80), 9, semi=(30.0, 40.0))
+    v0 = np.zeros(f.shape, dtype=f.dtype, order="F")
+    L = _lib.lib()
+    assert L.qsm_ctx_set_debug(gpu_ctx.handle, 1) == 0
+    try:
+        t0 = time.perf_counter()
+        gi = {}
+        with pytest.raises(_lib.QsmError) as ei:
+            qsm.mgpcg_mex(v0, f, m, [1, 1, 1], 1e-8, 30, -1.0, 1, 1, 2, 2, 2, 2, info=gi, ctx=gpu_ctx)
+        assert ei.value.status == 9  # QSM_ERR_TIMEOUT
+        assert time.perf_counter() - t0 < 60
+        with pytest.raises(_lib.QsmError) as ei:
+            qsm.mg_mex(v0, f, m, [1, 1, 1], 1e-6, 2, 1, 2, 2, 2, 2, ctx=gpu_ctx)
+        assert ei.value.status == 9
+    finally:
+        assert L.qsm_ctx_set_debug(gpu_ctx.handle, 0) == 0
+    assert L.qsm_ctx_set_debug(gpu_ctx.handle, 2) == 1  # unknown flags are refused (QSM_ERR_ARG)
+    oi, gi = {}, {}
+    b = port.mgpcg_mex(v0, f, m, [1, 1, 1], 1e-8, 30, -1.0, 1, 1, 2, 2, 2, 2, info=oi)
+    a = qsm.mgpcg_mex(v0, f, m, [1, 1, 1], 1e-8, 30, -1.0, 1, 1, 2, 2, 2, 2, info=gi, ctx=gpu_ctx)
+    assert gi["coarse_ctas"] < 0  # the whole-GPU solver ran again, its barriers completing
+    assert gi["iters"] == oi["iters"]
+    assert bits_equal(a, b), first_diff(a, b)
+
+
 @pytest.mark.parametrize("dt", ("float64", "float32"))
 def test_mgpcg_256_lbv_options_bitexact(gpu_ctx, qsm, port, dt):
     """The benchmark's Poisson problem at full size (256^3, LBV options, 5
