@@ -17,11 +17,15 @@ Arms (JSON line on rank 0):
                 to the reference MEX), for the mixed-vs-FP64 ratio; the
                 mixed result's relative L2 error is taken against it.
   roofline      the fused kernel: algorithmic bytes per launch (166 B per
-                voxel-iteration x voxels) / average launch time measured with
-                CUDA events on the library's stream; peak from
-                MEASURED_PEAKS.json.
-  cpu_baseline  the CPU oracle (a C restatement of the reference MEX, FP64,
-                OpenMP on all host cores) on a bounded number of iterations.
+                voxel-iteration x the mask voxels of the interior, whose state
+                the kernel reads and writes) / average launch time measured
+                with CUDA events on the library's stream; peak from
+                MEASURED_PEAKS.json; beside it the DRAM bytes an ncu capture
+                of this kernel build measured per launch and their fraction.
+  cpu_baseline  the CPU oracle (a C restatement of the reference MEX,
+                bit-exact with it; OpenMP on all host cores): its FP32 path on
+                a bounded iteration sample, and its FP64 path for all 1000
+                iterations, whose chi the mixed result is compared against.
   poisson, batch, served, next_rows
                 the MG-PCG solve, batched TV, served requests, and the widened
                 rows (TV ADMM, PDF, V-SHARP, whole sstgv/lbv wrappers), each
@@ -53,10 +57,23 @@ METRIC = "TGV voxel-iter/s & HBM GB/s, mixed vs FP64 GPU at ≤1e-4 rel err; ser
 ITERS = 1000
 LAM, ALPHA = 0.003, 2.0
 ALG_BYTES_FP32 = 166  # algorithmic bytes per voxel-iteration of fused FP32 TGV
-# DRAM bytes (read + write) per launch of the fused kernel on the headline workload, by
-# tile (tx, ty, z-chunk), from one ncu capture each (profiles/tgv_224x224x128_launch_list.md);
-# None for other shapes and tiles
-NCU_TRAFFIC_224x224x128 = {(28, 12, 16): 272.5e6, (28, 16, 16): 276.5e6}
+# DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) per launch of the fused
+# kernel on the headline workload, from one single-pass ncu capture per kernel build and
+# tile (profiles/tgv_224x224x128_launch_list.md).  Keyed by a digest of the kernel's source
+# files, so a kernel changed since its capture reports no traffic rather than a stale one.
+KERNEL_SOURCES = ("qsm.m_gb300/csrc/pd_tile.cuh", "qsm.m_gb300/csrc/pd_fused.cuh", "qsm.m_gb300/csrc/pd_stream.cu",
+                  "qsm.m_gb300/csrc/pd_tma.cuh")
+NCU_TRAFFIC_224x224x128 = {}  # (digest, tx, ty, z-chunk) -> bytes per launch
+
+
+def kernel_digest() -> str:
+    import hashlib
+
+    h = hashlib.sha256()
+    for rel in KERNEL_SOURCES:
+        with open(os.path.join(ROOT, rel), "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()[:16]
 WORKLOAD = "TGV-QSM 224x224x128, 1 mm isotropic, B0 along z, 1000 iterations, tol 0"
 
 
@@ -183,31 +200,59 @@ def _cpu_model() -> str:
     return f"{name or platform.processor() or 'unknown'} ({platform.machine()}, {os.cpu_count()} cores)"
 
 
-def cpu_baseline(d2f, mask, budget_s=15.0):
-    """The CPU oracle (FP64, OpenMP on every host core) on a bounded sample."""
+def _port():
+    """The CPU oracle (oracle/liborc.so, built here if needed): only the CPU legs use it."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
     import port
 
-    cores = os.cpu_count() or 1
-    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
-    n = d2f.size
-    # per-iteration cost from two probes (their difference drops the set-up cost)
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+    return port
+
+
+def _cores() -> int:
+    return int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+
+
+def _tgv_sample(port, d2f, mask, budget_s):
+    """A bounded iteration sample of the TGV inversion on the CPU oracle:
+    (iterations, seconds), the count sized from two probes so the sample
+    takes about budget_s."""
     t = time.perf_counter()
     port.pd_tgv_mex(d2f, mask, [1, 1, 1], LAM, ALPHA, 0.0, 5)
     t5 = time.perf_counter() - t
     t = time.perf_counter()
     port.pd_tgv_mex(d2f, mask, [1, 1, 1], LAM, ALPHA, 0.0, 15)
     t15 = time.perf_counter() - t
-    per_iter = max((t15 - t5) / 10, t15 / 15 / 4, 1e-6)
-    iters = int(max(10, min(1000, budget_s / per_iter)))
+    per_iter = max((t15 - t5) / 10, t15 / 15 / 4, 1e-6)  # the difference drops the set-up cost
+    iters = int(max(10, min(ITERS, budget_s / per_iter)))
     iters -= iters % 10
     t = time.perf_counter()
     port.pd_tgv_mex(d2f, mask, [1, 1, 1], LAM, ALPHA, 0.0, iters)
-    dt = time.perf_counter() - t
-    return {"value": n * iters / dt, "unit": "voxel-iter/s", "cores": int(os.environ.get("OMP_NUM_THREADS", cores)),
-            "kind": "port", "seconds": dt, "cpu": _cpu_model(),
-            "sample": f"{iters} FP64 iterations of the same 224x224x128 TGV inversion (CPU oracle, OpenMP)"}
+    return iters, time.perf_counter() - t
+
+
+def cpu_baseline(d2f, mask, budget_s=12.0):
+    """The CPU oracle (a C restatement of the reference MEX, bit-exact with it;
+    OpenMP on every host core) on the headline inversion.  Its FP32 path
+    (mx_pdf, the algorithm the fused kernel reproduces bit for bit) on a
+    bounded iteration sample is the like-for-like baseline; its FP64 path
+    (mx_pdd) runs all 1000 iterations, and that chi is the FP64 oracle the
+    mixed result's error is measured against.  Returns (record, chi64)."""
+    port = _port()
+    n = d2f.size
+    d32 = np.asfortranarray(d2f.astype(np.float32))
+    it32, s32 = _tgv_sample(port, d32, mask, budget_s)
+    t = time.perf_counter()
+    chi64 = port.pd_tgv_mex(d2f, mask, [1, 1, 1], LAM, ALPHA, 0.0, ITERS)
+    s64 = time.perf_counter() - t
+    rec = {"value": n * it32 / s32, "unit": "voxel-iter/s", "cores": _cores(), "kind": "port", "dtype": "f32",
+           "seconds": s32, "cpu": _cpu_model(),
+           "sample": f"{it32} of the {ITERS} FP32 iterations (mx_pdf) of the same 224x224x128 TGV inversion "
+                     "(CPU oracle, OpenMP)",
+           "fp64": {"value": n * ITERS / s64, "unit": "voxel-iter/s", "seconds": s64,
+                    "sample": f"all {ITERS} FP64 iterations (mx_pdd), the FP64 oracle chi"}}
+    return rec, chi64
 
 
 def _coarsen(G):
@@ -283,11 +328,12 @@ def mgpcg_fp64_ops(mask, nlevels=5, maxitmg=2, npre=2, npost=2, nb=2, coarse_out
     return maxitmg * vcycle + 12 * n + 10 * float(G.sum())
 
 
-def poisson_arm(qsm_gb300, ctx, torch):
+def poisson_arm(qsm_gb300, ctx, torch, cpu=False):
     """256^3 MG-PCG Poisson solve with LBV's options (src/bgremove/lbv.m:58-75):
     FP64 PCG with an FP64 V-cycle (bit-identical to the oracle) beside FP64 PCG
     with an FP32 V-cycle; iterations, device time, error of the mixed solution
-    against the FP64 one."""
+    against the FP64 one.  cpu: the same FP64 solve on the CPU oracle (OpenMP),
+    timed, and the GPU FP64 solution compared with it bit for bit."""
     import qsm_gb300.synthetic as S
 
     f, mask, _ = S.config1(seed=1)
@@ -323,6 +369,20 @@ def poisson_arm(qsm_gb300, ctx, torch):
     out["rel_l2_fp32_vcycle_vs_fp64"] = float(torch.linalg.vector_norm(sols["fp32_vcycle"] - sols["fp64"]) /
                                               torch.linalg.vector_norm(sols["fp64"]))
     out["speedup_fp32_vcycle"] = out["fp64"]["seconds"] / out["fp32_vcycle"]["seconds"]
+    if cpu:
+        port = _port()
+        oi = {}
+        t = time.perf_counter()
+        vh = port.mgpcg_mex(np.zeros_like(f, order="F"), f, mask, [1, 1, 1], 1e-8, maxit, -1.0, 2, 1, 2, 2, 2, 5,
+                            info=oi)
+        s = time.perf_counter() - t
+        g64 = sols["fp64"].cpu().numpy().transpose(2, 1, 0)
+        out["cpu_oracle"] = {"seconds": s, "iters": int(oi["iters"]), "cores": _cores(), "kind": "port",
+                             "dtype": "f64", "cpu": _cpu_model(),
+                             "sample": "the whole FP64 solve (FP64 V-cycle, same options), CPU oracle, OpenMP"}
+        out["fp64"]["bitexact_vs_cpu_oracle"] = bool(np.array_equal(g64, vh))
+        out["speedup_fp64_vs_cpu_oracle"] = s / out["fp64"]["seconds"]
+        out["speedup_fp32_vcycle_vs_cpu_oracle"] = s / out["fp32_vcycle"]["seconds"]
     return out
 
 
@@ -348,14 +408,17 @@ def _batch_case(b, shape):
     return np.asfortranarray(d2f.astype(np.float32)), mask
 
 
-def batch_arm(qsm_gb300, ctx, torch, count=32, iters=500):
+def batch_arm(qsm_gb300, ctx, torch, count=32, iters=500, cpu=False):
     """Batched TV: 32 volumes of uneven size (each axis from {96..256} x
     {96..256} x {64..176} in steps of 16), lam 1e-3, 500 iterations each,
     FP32 stencils, FP64-folded monitors, all volumes in one persistent launch
     per tile shape and iteration replayed from a captured CUDA graph.  The
     tile shape per grid size comes from the autotuner (a short batch of the
     same sizes runs first and fills its table).  Against: the same volumes
-    solved one after another through the one-volume fused call."""
+    solved one after another through the one-volume fused call.  cpu: the
+    CPU oracle's FP32 TV (mx_pdf of pd_tv_mex) on two of the volumes, one
+    after another, timed over a 20-iteration sample each; the whole batch's
+    CPU time is extrapolated from that rate."""
     import qsm_gb300.synthetic as S
 
     sizes = S.config3_sizes(seed=3, count=count)
@@ -385,7 +448,20 @@ def batch_arm(qsm_gb300, ctx, torch, count=32, iters=500):
                                                                           inf["seconds"] / 1e9, 1)])
         same = same and bool(torch.equal(chi, outs[b]))
     tiles = sorted({tuple(i["tile"]) for i in infos})
-    return {"workload": f"{count} TV volumes, sizes from {{96..256}}x{{96..256}}x{{64..176}} step 16, lam 1e-3, "
+    cpu_rec = None
+    if cpu:
+        port = _port()
+        nsample, it_s = 2, 20
+        t = time.perf_counter()
+        for b in range(nsample):
+            port.pd_tv_mex(cases[b][0], cases[b][1], [1, 1, 1], 1e-3, 0.0, it_s)
+        s = time.perf_counter() - t
+        rate = sum(int(np.prod(sizes[b])) for b in range(nsample)) * it_s / s
+        cpu_rec = {"value": rate, "unit": "voxel-iter/s", "seconds": s, "batch_s_estimate": vox * iters / rate,
+                   "cores": _cores(), "kind": "port", "dtype": "f32", "cpu": _cpu_model(),
+                   "sample": f"volumes 0-{nsample - 1} ({', '.join('x'.join(map(str, sizes[b])) for b in range(nsample))}),"
+                             f" {it_s} FP32 TV iterations each, one after another (CPU oracle, OpenMP)"}
+    return {"cpu_oracle": cpu_rec,"workload": f"{count} TV volumes, sizes from {{96..256}}x{{96..256}}x{{64..176}} step 16, lam 1e-3, "
                         f"{iters} iterations, tol 0",
             "voxels": vox, "active_voxels": active, "iterations": iters,
             "value": vox * iters / dev_s, "unit": "voxel-iter/s",
@@ -635,28 +711,40 @@ def serve_arm(qsm_gb300, ctx, seconds=30.0, rate=4.0, per_kind=6, budget=160 * 1
     return summ
 
 
+def _config(ws):
+    return {"workload": WORKLOAD, "volume": [224, 224, 128], "iterations": ITERS, "lam": LAM, "alpha": ALPHA,
+            "l2": "inputs larger than L2 (solver state ~0.93 GB per volume)", "parallelism": f"replicas x{ws}"}
+
+
 def run_reference(args):
+    """The reference's algorithm on the host cores: the CPU oracle (bit-exact
+    with QSM.m's MEX in FP32 and FP64; the MEX files themselves need MATLAB
+    and are not shipped to the GPU host) in FP32, like this benchmark's
+    arm, each step a bounded iteration sample of the 1000-iteration
+    inversion; one FP64 sample beside it."""
     ws, rank, _ = _dist()
     if rank != 0:
         return
     d2f, mask = _case()
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
-    import port
-
+    port = _port()
+    d32 = np.asfortranarray(d2f.astype(np.float32))
     for _ in range(args.warmup):
-        port.pd_tgv_mex(d2f, mask, [1, 1, 1], LAM, ALPHA, 0.0, 2)
-    vals = []
-    for _ in range(args.steps):
-        vals.append(cpu_baseline(d2f, mask, budget_s=max(5.0, 60.0 / max(1, args.steps))))
-    v = float(np.median([x["value"] for x in vals]))
-    cb = dict(vals[0])
-    cb["value"] = v
+        port.pd_tgv_mex(d32, mask, [1, 1, 1], LAM, ALPHA, 0.0, 2)
+    budget = max(5.0, 60.0 / max(1, args.steps))
+    runs = [_tgv_sample(port, d32, mask, budget) for _ in range(args.steps)]
+    rates = [d2f.size * it / sec for it, sec in runs]
+    v = float(np.median(rates))
+    it64, s64 = _tgv_sample(port, d2f, mask, budget)
+    cb = {"value": v, "unit": "voxel-iter/s", "cores": _cores(), "kind": "port", "dtype": "f32", "cpu": _cpu_model(),
+          "sample": f"{runs[0][0]} of the {ITERS} FP32 iterations (mx_pdf) per step, CPU oracle, OpenMP",
+          "fp64": {"value": d2f.size * it64 / s64, "unit": "voxel-iter/s",
+                   "sample": f"{it64} FP64 iterations (mx_pdd), CPU oracle, OpenMP"}}
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "voxel-iter/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.median([x["seconds"] for x in vals])),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "volume": [224, 224, 128], "note": "bounded iteration sample per step"},
-            "cpu_baseline": cb, "e2e": {"value": v, "unit": "voxel-iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * float(np.median([sec * ITERS / it for it, sec in runs])),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": _config(ws), "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": "voxel-iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
 
@@ -676,9 +764,9 @@ def run_ours(args):
     stream = torch.cuda.ExternalStream(qsm_gb300.lib().qsm_ctx_get_stream(ctx.handle))
     if args.only in ("batch", "serve", "next", "poisson"):
         if args.only == "batch":
-            out = batch_arm(qsm_gb300, ctx, torch)
+            out = batch_arm(qsm_gb300, ctx, torch, cpu=not args.no_cpu and rank == 0)
         elif args.only == "poisson":
-            out = poisson_arm(qsm_gb300, ctx, torch)
+            out = poisson_arm(qsm_gb300, ctx, torch, cpu=not args.no_cpu and rank == 0)
         elif args.only == "serve":
             out = serve_arm(qsm_gb300, ctx, seconds=args.serve_seconds)
         else:
@@ -729,11 +817,16 @@ def run_ours(args):
                               "active_voxels": int(info["active_voxels"])}))
         return
 
-    # fused-kernel roofline: average launch time from the library's loop events
+    # fused-kernel roofline: average launch time from the library's loop events; the
+    # algorithmic bytes are charged on the mask voxels of the interior (the voxels whose state
+    # the kernel reads and writes: outside the mask it moves none)
     peak, peak_kind = _peaks()
     t_launch = loop_s / info["iters"]
     active = int(info["active_voxels"])  # voxels of the launched (mask-holding) tiles
-    achieved = ALG_BYTES_FP32 * active / t_launch / 1e9
+    mask_vox = int(np.count_nonzero(mask[1:-1, 1:-1, 1:-1]))
+    achieved = ALG_BYTES_FP32 * mask_vox / t_launch / 1e9
+    digest = kernel_digest()
+    traffic = None if args.shape else NCU_TRAFFIC_224x224x128.get((digest,) + tuple(info["tile"]))
 
     # plain FP64 path (reference structure, bit-exact with the reference MEX)
     d2f64_dev = d2f_dev
@@ -768,8 +861,9 @@ def run_ours(args):
     e2e_s = max_over_ranks(time.perf_counter() - t0, dist, "cuda")
     e2e_value = whole_job_rate(N * ITERS * args.steps, ws, e2e_s)
 
-    poisson = None if args.no_poisson else poisson_arm(qsm_gb300, ctx, torch)
-    batch = None if args.no_batch else batch_arm(qsm_gb300, ctx, torch)
+    cpu_rank0 = not args.no_cpu and rank == 0
+    poisson = None if args.no_poisson else poisson_arm(qsm_gb300, ctx, torch, cpu=cpu_rank0)
+    batch = None if args.no_batch else batch_arm(qsm_gb300, ctx, torch, cpu=cpu_rank0)
     served = None if args.no_serve else serve_arm(qsm_gb300, ctx, seconds=args.serve_seconds)
     nxt = None if args.no_next else next_rows_arm(qsm_gb300, ctx, torch, peak, cpu=not args.no_cpu and rank == 0)
 
@@ -777,25 +871,34 @@ def run_ours(args):
         if dist is not None:
             dist.destroy_process_group()
         return
-    cb = cpu_baseline(d2f, mask) if (ws == 1 or rank == 0) and not args.no_cpu else None
+    cb, rel_oracle = None, None
+    if not args.no_cpu:
+        cb, chi_oracle = cpu_baseline(d2f, mask)
+        cm = chi_mixed.cpu().numpy().transpose(2, 1, 0)
+        rel_oracle = float(np.linalg.norm(cm - chi_oracle) / np.linalg.norm(chi_oracle))
     line = {
         "metric": METRIC, "value": value, "unit": "voxel-iter/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 (FP64-folded monitors)", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "volume": [224, 224, 128], "iterations": ITERS, "lam": LAM, "alpha": ALPHA,
-                   "l2": "inputs larger than L2 (solver state ~0.93 GB per volume)", "parallelism": f"replicas x{ws}"},
+        "config": _config(ws),
         "fp64_plain": {"value": value64, "unit": "voxel-iter/s", "ms_per_step": ms64 / max(1, min(2, args.steps))},
         "speedup_vs_fp64": value / value64, "rel_l2_vs_fp64": rel,
+        # the FP64 oracle's own chi (CPU, all 1000 iterations); the plain FP64 GPU path is bit-identical to it
+        "rel_l2_vs_fp64_oracle": rel_oracle,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": (NCU_TRAFFIC_224x224x128[tuple(info["tile"])] / 1e9
-                                 if not args.shape and tuple(info["tile"]) in NCU_TRAFFIC_224x224x128 else None),
+                     "bytes_per_voxel_iter": ALG_BYTES_FP32, "charged_voxels": mask_vox,
+                     "charged_voxels_rule": "mask voxels of the interior (state read and written there only)",
+                     "traffic": traffic / 1e9 if traffic else None,
                      "traffic_unit": "GB per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
+                     "frac_dram": traffic / t_launch / 1e9 / peak if traffic else None,
+                     "traffic_note": None if traffic else
+                     f"no ncu capture recorded for this kernel build (digest {digest}) and tile",
+                     "kernel_digest": digest,
                      "kernel": ("stream_k<%d,%d,TGV> z-chunk %d" if info["tile"][0] == 28 else "tgv_fused_k<%d,%d,%d>")
                                % tuple(info["tile"]),
-                     "bytes_per_voxel_iter": ALG_BYTES_FP32,
-                     "avg_launch_us": t_launch * 1e6, "peak_source": peak_kind, "active_voxels": active,
-                     "tile": list(info["tile"]),
-                     "dense_voxels": N},
+                     "avg_launch_us": t_launch * 1e6, "peak_source": peak_kind,
+                     "achieved_launched_tiles": ALG_BYTES_FP32 * active / t_launch / 1e9,
+                     "launched_tile_voxels": active, "tile": list(info["tile"]), "dense_voxels": N},
         "cpu_baseline": cb,
         "e2e": {"value": e2e_value, "unit": "voxel-iter/s", "h2d_bytes_per_step": int(N * 8 + N),
                 "d2h_bytes_per_step": int(N * 8)},

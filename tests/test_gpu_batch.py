@@ -49,6 +49,23 @@ def test_batch_matches_oracle_every_variant(gpu_ctx, qsm, port, variant, launch,
         assert inf["iters"] == 40
 
 
+def test_batch_c3_sized_volume_vs_oracle(gpu_ctx, qsm, port, monkeypatch):
+    """A volume at the batched configuration's sizes (240 x 240 x 128, tile
+    shapes from the autotuner, its own graph branch) batched with a small
+    one: TV and TGV chi bit-identical to the oracle's FP32 result."""
+    monkeypatch.delenv("QSM_FUSED_VARIANT", raising=False)
+    monkeypatch.delenv("QSM_BATCH_SOLO_TILES", raising=False)
+    cases = [_case((240, 240, 128), 300), _case((56, 44, 31), 301)]
+    out = qsm.pd_tv_batch([c[0] for c in cases], [c[1] for c in cases], [1, 1, 1], 1e-3, 0.0, 40)
+    for (d2f, m), chi in zip(cases, out):
+        ref = port.pd_tv_mex(d2f, m, [1, 1, 1], 1e-3, 0.0, 40)
+        assert bits_equal(chi, ref), first_diff(chi, ref)
+    out = qsm.pd_tgv_batch([c[0] for c in cases], [c[1] for c in cases], [1, 1, 1], 0.003, 2.0, 0.0, 40)
+    for (d2f, m), chi in zip(cases, out):
+        ref = port.pd_tgv_mex(d2f, m, [1, 1, 1], 0.003, 2.0, 0.0, 40)
+        assert bits_equal(chi, ref), first_diff(chi, ref)
+
+
 def test_batch_equals_alone_autotuned(gpu_ctx, qsm, monkeypatch):
     """Tile shapes from the autotuner (tuned per grid size at admission): each
     volume's chi and monitors equal its one-volume fused solve."""
