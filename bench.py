@@ -63,7 +63,9 @@ ALG_BYTES_FP32 = 166  # algorithmic bytes per voxel-iteration of fused FP32 TGV
 # files, so a kernel changed since its capture reports no traffic rather than a stale one.
 KERNEL_SOURCES = ("qsm.m_gb300/csrc/pd_tile.cuh", "qsm.m_gb300/csrc/pd_fused.cuh", "qsm.m_gb300/csrc/pd_stream.cu",
                   "qsm.m_gb300/csrc/pd_tma.cuh")
-NCU_TRAFFIC_224x224x128 = {}  # (digest, tx, ty, z-chunk) -> bytes per launch
+NCU_TRAFFIC_224x224x128 = {  # (digest, tx, ty, z-chunk) -> bytes per launch
+    ("b5587692fbd9d68d", 28, 16, 16): 276.3e6,  # median of 5 launches: read 191.5 MB + write 84.8 MB
+}
 
 
 def kernel_digest() -> str:
