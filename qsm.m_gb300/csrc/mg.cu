@@ -1778,12 +1778,39 @@ __device__ __forceinline__ bool lane_fold(T *sm, T acc, T *part, unsigned *count
     return true;
 }
 
+// Voxels outside G in the PCG steps (sk: the level-0 mask, when the solve
+// runs its masked form).  That form runs when the initial residual and
+// iterate are exactly +0 outside G (pcg_zero_outside_k checks it per solve,
+// after r = f - A x0); then r, p and x stay +0 there and q holds +-0, every
+// update there leaves the value it had, and every product added to an
+// inner product there is +-0.  A
+// running sum that starts at +0 is never -0 in round-to-nearest, so adding
+// +-0 to it changes nothing: skipping those voxels gives the same bits.
+__device__ __forceinline__ bool pcg_on(const uint8_t *__restrict__ sk, size_t l) { return !sk || sk[l]; }
+
+// flag = 1 if some voxel outside G holds a value other than +0 in a or b
+template <typename T>
+__global__ void pcg_zero_outside_k(const T *__restrict__ a, const T *__restrict__ b, const uint8_t *__restrict__ G,
+                                   size_t n, int *flag)
+{
+    int bad = 0;
+    for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
+        if (G[l]) continue;
+        if (sizeof(T) == 8) {
+            bad |= __double_as_longlong((double)a[l]) != 0 || (b && __double_as_longlong((double)b[l]) != 0);
+        } else {
+            bad |= __float_as_int((float)a[l]) != 0 || (b && __float_as_int((float)b[l]) != 0);
+        }
+    }
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicExch(flag, 1);
+}
+
 // rho = r . q (q widened from the V-cycle's vm first when it runs in another
 // precision); prevrho = old rho; beta = rho / prevrho
 template <typename TP, typename TM>
 __global__ void __launch_bounds__(RED_BLOCK) pcg_rho_k(const TP *__restrict__ r, TP *__restrict__ q,
-                                                       const TM *__restrict__ vm, size_t n, TP *part,
-                                                       unsigned *count, double *sc)
+                                                       const TM *__restrict__ vm, const uint8_t *__restrict__ sk,
+                                                       size_t n, TP *part, unsigned *count, double *sc)
 {
     __shared__ TP sm[RED_BLOCK];
     const size_t L = RED_LANES;
@@ -1791,18 +1818,24 @@ __global__ void __launch_bounds__(RED_BLOCK) pcg_rho_k(const TP *__restrict__ r,
     TP acc = (TP)0;
     for (; l + 3 * L < n; l += 4 * L) {
         TP a[4], b[4];
+        bool on[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-            a[u] = r[l + u * L];
-            b[u] = vm ? (TP)vm[l + u * L] : q[l + u * L];
+            on[u] = pcg_on(sk, l + u * L);
+            if (on[u]) {
+                a[u] = r[l + u * L];
+                b[u] = vm ? (TP)vm[l + u * L] : q[l + u * L];
+            }
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
+            if (!on[u]) continue;
             if (vm) q[l + u * L] = b[u];
             acc = acc + a[u] * b[u];
         }
     }
     for (; l < n; l += L) {
+        if (!pcg_on(sk, l)) continue;
         const TP b = vm ? (TP)vm[l] : q[l];
         if (vm) q[l] = b;
         acc = acc + r[l] * b;
@@ -1818,19 +1851,20 @@ __global__ void __launch_bounds__(RED_BLOCK) pcg_rho_k(const TP *__restrict__ r,
 
 // p = beta * p, then p = p + 1 * q
 template <typename T>
-__global__ void pcg_p_k(T *__restrict__ p, const T *__restrict__ q, size_t n, const double *sc)
+__global__ void pcg_p_k(T *__restrict__ p, const T *__restrict__ q, const uint8_t *__restrict__ sk, size_t n,
+                        const double *sc)
 {
     const T beta = (T)sc[S_BETA];
     for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x)
-        p[l] = beta * p[l] + q[l];
+        if (pcg_on(sk, l)) p[l] = beta * p[l] + q[l];
 }
 
 // q = lapmg(p) on G (interior), then q = -1 * q everywhere; pq = p . q;
 // alpha = rho / pq
 template <typename T>
 __global__ void __launch_bounds__(RED_BLOCK) pcg_q_k(T *__restrict__ q, const T *__restrict__ p,
-                                                     const uint8_t *__restrict__ G, LapC<T> c, Dims d, T *part,
-                                                     unsigned *count, double *sc)
+                                                     const uint8_t *__restrict__ G, const uint8_t *__restrict__ sk,
+                                                     LapC<T> c, Dims d, T *part, unsigned *count, double *sc)
 {
     __shared__ T sm[RED_BLOCK];
     const size_t nx = d.nx, ny = d.ny, nxny = d.nxny(), n = d.n();
@@ -1840,15 +1874,18 @@ __global__ void __launch_bounds__(RED_BLOCK) pcg_q_k(T *__restrict__ q, const T 
     const size_t Lk = RED_LANES / nxny, Lj = (RED_LANES - Lk * nxny) / nx, Li = RED_LANES - Lk * nxny - Lj * nx;
     T acc = (T)0;
     for (size_t l = t; l < n; l += RED_LANES) {
-        const T pl = p[l];
-        T qv;
-        if (i >= 1 && j >= 1 && k >= 1 && i + 1 < nx && j + 1 < d.ny && k + 1 < d.nz && G[l])
-            qv = c.hh * pl + c.hx * (p[l - 1] + p[l + 1]) + c.hy * (p[l - nx] + p[l + nx]) + c.hz * (p[l - nxny] + p[l + nxny]);
-        else
-            qv = q[l];
-        qv = neg_bits(qv);
-        q[l] = qv;
-        acc = acc + pl * qv;
+        if (pcg_on(sk, l)) {
+            const T pl = p[l];
+            T qv;
+            if (i >= 1 && j >= 1 && k >= 1 && i + 1 < nx && j + 1 < d.ny && k + 1 < d.nz && G[l])
+                qv = c.hh * pl + c.hx * (p[l - 1] + p[l + 1]) + c.hy * (p[l - nx] + p[l + nx]) +
+                     c.hz * (p[l - nxny] + p[l + nxny]);
+            else
+                qv = q[l];
+            qv = neg_bits(qv);
+            q[l] = qv;
+            acc = acc + pl * qv;
+        }
         i += Li;
         const size_t cj = i >= nx;
         i -= cj * nx;
@@ -1870,8 +1907,8 @@ __global__ void __launch_bounds__(RED_BLOCK) pcg_q_k(T *__restrict__ q, const T 
 template <typename TP, typename TM>
 __global__ void __launch_bounds__(RED_BLOCK) pcg_xr_k(TP *__restrict__ x, const TP *__restrict__ p,
                                                       TP *__restrict__ r, const TP *__restrict__ q,
-                                                      TM *__restrict__ rm, size_t n, TP *part, unsigned *count,
-                                                      double *sc)
+                                                      TM *__restrict__ rm, const uint8_t *__restrict__ sk, size_t n,
+                                                      TP *part, unsigned *count, double *sc)
 {
     __shared__ TP sm[RED_BLOCK];
     const TP a = (TP)sc[S_A], na = (TP)(-sc[S_A]);
@@ -1880,15 +1917,20 @@ __global__ void __launch_bounds__(RED_BLOCK) pcg_xr_k(TP *__restrict__ x, const 
     TP acc = (TP)0;
     for (; l + 3 * L < n; l += 4 * L) {
         TP xv[4], pv[4], rv[4], qv[4];
+        bool on[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-            xv[u] = x[l + u * L];
-            pv[u] = p[l + u * L];
-            rv[u] = r[l + u * L];
-            qv[u] = q[l + u * L];
+            on[u] = pcg_on(sk, l + u * L);
+            if (on[u]) {
+                xv[u] = x[l + u * L];
+                pv[u] = p[l + u * L];
+                rv[u] = r[l + u * L];
+                qv[u] = q[l + u * L];
+            }
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
+            if (!on[u]) continue;
             x[l + u * L] = xv[u] + a * pv[u];
             const TP rn = rv[u] + na * qv[u];
             r[l + u * L] = rn;
@@ -1897,6 +1939,7 @@ __global__ void __launch_bounds__(RED_BLOCK) pcg_xr_k(TP *__restrict__ x, const 
         }
     }
     for (; l < n; l += L) {
+        if (!pcg_on(sk, l)) continue;
         x[l] = x[l] + a * p[l];
         const TP rn = r[l] + na * q[l];
         r[l] = rn;
@@ -1977,8 +2020,17 @@ static qsm_status pcg(qsm_ctx *ctx, const Dims &d, const TP *v0, const TP *f, co
     QSM_TRY(lapmg<TP>(ctx, q, x, H.L[0].G, h, dp));
     QSM_TRY(scal<TP>(ctx, q, n, sc, -1, false, -1.0));
     QSM_TRY(axpy<TP>(ctx, r, q, n, sc, -1, false, -1.0));
+    // The PCG steps skip the voxels outside G when the residual and the iterate are +0
+    // there (f +-0 outside G becomes +0 in r = f - A x0, as -0 + +0 is +0).
+    int *zflag = (int *)((char *)pv + (same ? 2 : 4) * vb + S_N * sizeof(double));
+    pcg_zero_outside_k<TP><<<1216, 256, 0, ctx->stream>>>(r, x, H.L[0].G, n, zflag);
+    QSM_CUDA(cudaGetLastError());
     QSM_TRY(nrm2<TP>(ctx, r, n, sc + S_RES));
     QSM_TRY(read_double(ctx, sc + S_RES, &res));
+    int hz = 1;
+    QSM_CUDA(cudaMemcpyAsync(&hz, zflag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+    const uint8_t *sk = hz ? nullptr : H.L[0].G;
     if (verbose) printf("\niter%6s\tresidual\n", "");
     int32_t it = 0;
     TP *part = (TP *)ctx->red_partial;
@@ -1992,11 +2044,11 @@ static qsm_status pcg(qsm_ctx *ctx, const Dims &d, const TP *v0, const TP *f, co
         else
             QSM_CUDA(cudaMemsetAsync(H.L[0].v, 0, n * sizeof(TM), ctx->stream));
         QSM_TRY(mg_run<TM>(ctx, H, tolmg, maxitmg, mu, npre, npost, nb, sc, nullptr));
-        pcg_rho_k<TP, TM><<<RED_NBLK, RED_BLOCK, 0, ctx->stream>>>(r, q, same ? nullptr : H.L[0].v, n, part,
+        pcg_rho_k<TP, TM><<<RED_NBLK, RED_BLOCK, 0, ctx->stream>>>(r, q, same ? nullptr : H.L[0].v, sk, n, part,
                                                                    ctx->red_count, sc);
-        pcg_p_k<TP><<<1216, 256, 0, ctx->stream>>>(p, q, n, sc);
-        pcg_q_k<TP><<<RED_NBLK, RED_BLOCK, 0, ctx->stream>>>(q, p, H.L[0].G, lc, dp, part, ctx->red_count, sc);
-        pcg_xr_k<TP, TM><<<RED_NBLK, RED_BLOCK, 0, ctx->stream>>>(x, p, r, q, same ? nullptr : H.L[0].f, n, part,
+        pcg_p_k<TP><<<1216, 256, 0, ctx->stream>>>(p, q, sk, n, sc);
+        pcg_q_k<TP><<<RED_NBLK, RED_BLOCK, 0, ctx->stream>>>(q, p, H.L[0].G, sk, lc, dp, part, ctx->red_count, sc);
+        pcg_xr_k<TP, TM><<<RED_NBLK, RED_BLOCK, 0, ctx->stream>>>(x, p, r, q, same ? nullptr : H.L[0].f, sk, n, part,
                                                                   ctx->red_count, sc);
         QSM_CUDA(cudaGetLastError());
         QSM_TRY(read_double(ctx, sc + S_RES, &res));
