@@ -1134,6 +1134,7 @@ qsm_status qsm_vsharp(qsm_ctx *ctx, qsm_dtype dt, const size_t dims[4], const vo
                       const double vsz[3], const double *radii, int32_t nradii, double thr, void *fl,
                       uint8_t *mask_out)
 {
+    Range nvtx_range("vsharp");
     if (!vsz) return QSM_ERR_ARG;
     std::vector<double> rs;
     if (nradii > 0) {
@@ -1179,6 +1180,7 @@ qsm_status qsm_pdf(qsm_ctx *ctx, qsm_dtype dt, const size_t dims[4], const void 
                    const void *w, const double vsz[3], const double bdir[3], double lambda, double tol,
                    int32_t maxit, int32_t verbose, void *fl, int32_t *iters)
 {
+    Range nvtx_range("pdf");
     if (!ctx || !dims || !f || !mask || !vsz || !bdir || !fl) return QSM_ERR_ARG;
     if (dt != QSM_F32 && dt != QSM_F64) return QSM_ERR_DTYPE;
     if (!dims[0] || !dims[1] || !dims[2] || !dims[3]) return QSM_ERR_DIMS;

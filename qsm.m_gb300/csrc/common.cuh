@@ -13,6 +13,8 @@
 
 #include "../../include/qsm_gpu.h"
 
+#include <nvtx3/nvToolsExt.h>
+
 namespace qsm {
 
 // ---------------------------------------------------------------------------
@@ -40,6 +42,16 @@ void set_error(qsm_ctx *ctx, const char *fmt, ...);
 // ---------------------------------------------------------------------------
 // geometry
 // ---------------------------------------------------------------------------
+
+// A named NVTX range over a scope, shown by profilers (Nsight Systems,
+// Nsight Compute's range filters); with no profiler attached a push/pop is a
+// call through an unset function pointer.
+struct Range {
+    explicit Range(const char *name) { nvtxRangePushA(name); }
+    ~Range() { nvtxRangePop(); }
+    Range(const Range &) = delete;
+    Range &operator=(const Range &) = delete;
+};
 
 struct Dims {
     size_t nx, ny, nz;

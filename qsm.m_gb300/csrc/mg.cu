@@ -1983,6 +1983,7 @@ static qsm_status pcg(qsm_ctx *ctx, const Dims &d, const TP *v0, const TP *f, co
                       double tolcg, int32_t maxitcg, double tolmg, int32_t maxitmg, int32_t mu, int32_t npre,
                       int32_t npost, int32_t nb, int32_t nl, int32_t verbose, TP *vout, qsm_mg_info *info)
 {
+    Range nvtx_range("mgpcg");
     const Dims dp{d.nx + 2, d.ny + 2, d.nz + 2};
     const size_t n = dp.n();
     Hier<TM> H;
@@ -2043,7 +2044,10 @@ static qsm_status pcg(qsm_ctx *ctx, const Dims &d, const TP *v0, const TP *f, co
             QSM_CUDA(cudaMemsetAsync(q, 0, n * sizeof(TP), ctx->stream));
         else
             QSM_CUDA(cudaMemsetAsync(H.L[0].v, 0, n * sizeof(TM), ctx->stream));
-        QSM_TRY(mg_run<TM>(ctx, H, tolmg, maxitmg, mu, npre, npost, nb, sc, nullptr));
+        {
+            Range cyc("mgpcg/preconditioner");
+            QSM_TRY(mg_run<TM>(ctx, H, tolmg, maxitmg, mu, npre, npost, nb, sc, nullptr));
+        }
         pcg_rho_k<TP, TM><<<RED_NBLK, RED_BLOCK, 0, ctx->stream>>>(r, q, same ? nullptr : H.L[0].v, sk, n, part,
                                                                    ctx->red_count, sc);
         pcg_p_k<TP><<<1216, 256, 0, ctx->stream>>>(p, q, sk, n, sc);
@@ -2080,6 +2084,7 @@ static qsm_status mg_solve(qsm_ctx *ctx, const Dims &d, const T *v0, const T *f,
                            double tol, int32_t maxit, int32_t mu, int32_t npre, int32_t npost, int32_t nb, int32_t nl,
                            T *vout, qsm_mg_info *info, bool full)
 {
+    Range nvtx_range("mg");
     const Dims dp{d.nx + 2, d.ny + 2, d.nz + 2};
     Hier<T> H;
     QSM_TRY(hier_init<T>(ctx, H, nl, dp, h));

@@ -510,6 +510,7 @@ size_t qsm_nifti_payload_bytes(const qsm_nifti_hdr *h)
 qsm_status qsm_nifti_decode(qsm_ctx *ctx, const qsm_nifti_hdr *h, const void *payload, int32_t out_datatype,
                             void *img)
 {
+    Range nvtx_range("nifti_decode");
     if (!ctx || !h || !payload || !img) return QSM_ERR_ARG;
     const int sdt = h->stored_datatype, eb = elem_bytes(sdt);
     if (!eb) return set_error(ctx, "datatype %d (bit, complex or RGB) is not decoded", sdt), QSM_ERR_DTYPE;

@@ -353,6 +353,7 @@ static qsm_status pd_plain(qsm_ctx *ctx, bool tgv, const Dims &d, const void *d2
                            const double *h, double lam, double alpha, double tol, uint32_t maxiter,
                            uint32_t verbose, T *chi_out, qsm_pd_info *info)
 {
+    Range nvtx_range("pd_plain");
     const size_t N = d.n();
     const int narr = tgv ? 23 : 11;
     void *blk = nullptr;

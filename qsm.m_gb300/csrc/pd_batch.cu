@@ -339,6 +339,7 @@ void worker_main(qsm_session *s, int w)
 // Rebuilds the device work lists and re-captures the 30-iteration graph.
 qsm_status rebuild(qsm_session *s)
 {
+    Range nvtx_range("session/rebuild");
     qsm_ctx *ctx = s->ctx;
     s->running.clear();
     for (auto &kv : s->pd)
@@ -728,6 +729,7 @@ qsm_status qsm_session_submit_mgpcg(qsm_session *s, const size_t dims[3], const 
 
 qsm_status qsm_session_step(qsm_session *s, uint32_t iters)
 {
+    Range nvtx_range("session/step");
     if (!s) return QSM_ERR_ARG;
     qsm_ctx *ctx = s->ctx;
     cudaSetDevice(ctx->device);
@@ -874,6 +876,7 @@ qsm_status qsm_pd_tv_batch(qsm_ctx *ctx, qsm_dtype dt, uint32_t count, const siz
                            const uint8_t *const *mask, const double vsz[3], double lam, double tol, uint32_t maxiter,
                            void *const *chi, qsm_pd_info *info)
 {
+    Range nvtx_range("pd_tv_batch");
     return pd_batch(ctx, false, dt, count, dims, d2f, mask, vsz, lam, 0.0, tol, maxiter, chi, info);
 }
 
@@ -881,6 +884,7 @@ qsm_status qsm_pd_tgv_batch(qsm_ctx *ctx, qsm_dtype dt, uint32_t count, const si
                             const uint8_t *const *mask, const double vsz[3], double lam, double alpha, double tol,
                             uint32_t maxiter, void *const *chi, qsm_pd_info *info)
 {
+    Range nvtx_range("pd_tgv_batch");
     return pd_batch(ctx, true, dt, count, dims, d2f, mask, vsz, lam, alpha, tol, maxiter, chi, info);
 }
 

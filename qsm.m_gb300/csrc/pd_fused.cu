@@ -433,6 +433,7 @@ FusedArgs pd_volume_args(const PdVolume &v, int var, uint32_t it)
 
 qsm_status pd_volume_tune(qsm_ctx *ctx, PdVolume *v, uint32_t maxiter)
 {
+    Range nvtx_range("pd_fused/autotune");
     const char *force = getenv("QSM_FUSED_VARIANT");
     if (force && *force) {
         v->var = std::min(std::max(atoi(force), 0), kNumVariants - 1);
@@ -521,6 +522,7 @@ qsm_status pd_fused(qsm_ctx *ctx, bool tgv, const Dims &d, qsm_dtype dt, const v
                     const double *h, double lam, double alpha, double tol, uint32_t maxiter, uint32_t verbose,
                     void *chi_out, qsm_pd_info *info)
 {
+    Range nvtx_range("pd_fused");
     PdVolume v;
     QSM_TRY(pd_volume_init(ctx, &v, tgv, d, dt, d2f, mask, h, lam, alpha));
     qsm_status st = pd_volume_tune(ctx, &v, maxiter);

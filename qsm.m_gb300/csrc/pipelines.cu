@@ -310,6 +310,7 @@ qsm_status qsm_sstgv(qsm_ctx *ctx, qsm_dtype dt, const size_t dims[4], const voi
                      const double vsz[3], double lambda, double alpha, double tol, uint32_t maxit, uint32_t verbose,
                      int32_t fused, void *x, qsm_pd_info *info)
 {
+    Range nvtx_range("sstgv");
     if (!ctx || !phas || !mask || !vsz || !x) return QSM_ERR_ARG;
     if (dt != QSM_F32 && dt != QSM_F64) return QSM_ERR_DTYPE;
     if (!check_dims4(dims)) return QSM_ERR_DIMS;
@@ -376,6 +377,7 @@ qsm_status qsm_lbv(qsm_ctx *ctx, qsm_dtype dt, const size_t dims[4], const void 
                    const double vsz[3], double tol, int32_t maxit, int32_t mg_maxit, int32_t npre, int32_t npost,
                    int32_t nboundary, int32_t verbose, int32_t mixed, void *fl, qsm_mg_info *info)
 {
+    Range nvtx_range("lbv");
     if (dims && maxit <= 0)  // lbv.m:60: ceil(sqrt(numel(mask))) of the full mask
         maxit = (int32_t)std::ceil(std::sqrt((double)dims[0] * (double)dims[1] * (double)dims[2]));
     return poisson_entry(ctx, false, dt, dims, f, mask, vsz, tol, maxit, mg_maxit, npre, npost, nboundary, verbose,

@@ -693,6 +693,7 @@ extern "C" qsm_status qsm_tv_admm(qsm_ctx *ctx, qsm_dtype dt, const size_t dims[
                                   double atol, int32_t maxit, double rho, double alpha, double rtau, double stau,
                                   double gamma, int32_t verbose, void *x, qsm_tv_info *info)
 {
+    Range nvtx_range("tv_admm");
     if (!ctx || !dims || !f || !mask || !vsz || !bdir || !x) return QSM_ERR_ARG;
     if (dt != QSM_F32 && dt != QSM_F64) return QSM_ERR_DTYPE;
     if (tv != 1 && tv != 2) return QSM_ERR_ARG;
