@@ -770,7 +770,8 @@ def run_ours(args):
         elif args.only == "poisson":
             out = poisson_arm(qsm_gb300, ctx, torch, cpu=not args.no_cpu and rank == 0)
         elif args.only == "serve":
-            out = serve_arm(qsm_gb300, ctx, seconds=args.serve_seconds)
+            out = serve_arm(qsm_gb300, ctx, seconds=args.serve_seconds, rate=args.serve_rate,
+                                per_kind=args.serve_pool, budget=int(args.serve_budget_gb * 1e9))
         else:
             out = next_rows_arm(qsm_gb300, ctx, torch, _peaks()[0], cpu=not args.no_cpu, parts=args.next_parts)
         if rank == 0:
@@ -866,7 +867,8 @@ def run_ours(args):
     cpu_rank0 = not args.no_cpu and rank == 0
     poisson = None if args.no_poisson else poisson_arm(qsm_gb300, ctx, torch, cpu=cpu_rank0)
     batch = None if args.no_batch else batch_arm(qsm_gb300, ctx, torch, cpu=cpu_rank0)
-    served = None if args.no_serve else serve_arm(qsm_gb300, ctx, seconds=args.serve_seconds)
+    served = None if args.no_serve else serve_arm(qsm_gb300, ctx, seconds=args.serve_seconds, rate=args.serve_rate,
+                                per_kind=args.serve_pool, budget=int(args.serve_budget_gb * 1e9))
     nxt = None if args.no_next else next_rows_arm(qsm_gb300, ctx, torch, peak, cpu=not args.no_cpu and rank == 0)
 
     if rank != 0:
@@ -931,6 +933,9 @@ def main():
     ap.add_argument("--next-parts", default="tv64,tv32,pdf,vsharp,sstgv,lbv,nifti",
                     help="parts of the next-rows arm with --only next (profiling aid)")
     ap.add_argument("--serve-seconds", type=float, default=30.0, help="arrival window of the served arm")
+    ap.add_argument("--serve-rate", type=float, default=4.0, help="arrivals per second of the served arm")
+    ap.add_argument("--serve-pool", type=int, default=6, help="seeded input cases per request kind (served arm)")
+    ap.add_argument("--serve-budget-gb", type=float, default=160.0, help="device byte budget of the served arm")
     ap.add_argument("--shape", default="", help="nx,ny,nz of a reduced volume (profiler captures)")
     ap.add_argument("--iters", type=int, default=ITERS, help="iterations per inversion (profiler captures)")
     ap.add_argument("--only", default="all", choices=["all", "fused", "batch", "serve", "next", "poisson"],
