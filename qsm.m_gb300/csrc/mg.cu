@@ -1154,6 +1154,10 @@ struct Level {
     Dims d;
     size_t n;
     T *v, *f, *r;
+    // Invariant: on levels whose G is held as colour lists, f is +0 outside G from set-up
+    // on (hier_init zeroes it, restrictions write only G): restrict_list_k writes f on G
+    // only and relies on it, which is restrict_mex's result there.  Nothing may use a
+    // coarse f as scratch outside G.
     uint8_t *G, *B;
     double h[3];
     uint32_t *bl[2];     // B voxels of each colour (null: full-grid passes over B)
