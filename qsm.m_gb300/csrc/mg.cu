@@ -890,19 +890,59 @@ __device__ void cta_gs(T *v, const T *f, const uint8_t *G, GsC<T> c, Dims d, int
     __syncthreads();
 }
 
+// One CTA's coarsest solve: list entries (v index, flags)
+constexpr uint32_t CS_IDX = 0x0FFFFFFFu;
+constexpr uint32_t CS_I1 = 1u << 28;    // i == 1
+constexpr uint32_t CS_INX2 = 1u << 29;  // i == nx - 2
+
+// Shared memory of coarse_solve_k for an n-voxel grid: v, f, sq (n each),
+// the lane-order block sums, G (n bytes), two colour lists of (n + 1) / 2
+// entries.
+__host__ __device__ inline size_t cs_smem(size_t n, size_t es)
+{
+    const size_t g = 3 * n * es + (size_t)RED_NBLK * es;
+    return ((g + n + 15) & ~(size_t)15) + 2 * ((n + 1) / 2) * sizeof(uint32_t);
+}
+
+// one colour pass of the one-CTA solver over a colour list (entries with a
+// `skip` flag are left alone): the expression of cta_gs, in any order
+template <typename T>
+__device__ __forceinline__ void cs_pass(T *v, const T *f, const uint32_t *list, int cnt, uint32_t skip, GsC<T> c,
+                                        int nx, int nxny)
+{
+    for (int m = threadIdx.x; m < cnt; m += CS_THREADS) {
+        const uint32_t e = list[m];
+        if (e & skip) continue;
+        const int l = (int)(e & CS_IDX);
+        v[l] = c.hh * (f[l] + (c.hx * (v[l - 1] + v[l + 1]) + c.hy * (v[l - nx] + v[l + nx]) +
+                               c.hz * (v[l - nxny] + v[l + nxny])));
+    }
+    __syncthreads();
+}
+
+// The coarsest solve (mgpcg_mex.c:265-275) of a grid one CTA holds in shared
+// memory.  The colour passes run from two lists of the interior G voxels
+// built once per call (a pass reads only the other colour, so the order of
+// its updates does not matter: the reference's result bit for bit), which
+// leaves no index arithmetic in the 512 passes of an outer iteration.
 template <typename T>
 __global__ void __launch_bounds__(CS_THREADS) coarse_solve_k(T *gv, const T *__restrict__ gf, const uint8_t *__restrict__ gG,
                                                              T *gr, Dims d, GsC<T> gc, LapC<T> lc, double tol,
                                                              int *outer_out)
 {
-    extern __shared__ unsigned char smraw[];
+    extern __shared__ __align__(16) unsigned char smraw[];
     const int n = (int)d.n();
     T *v = (T *)smraw;
     T *f = v + n;
     T *sq = f + n;
     T *blk = sq + n;
     uint8_t *G = (uint8_t *)(blk + RED_NBLK);
+    const int cap = (n + 1) / 2;
+    uint32_t *list = (uint32_t *)(smraw + (((size_t)3 * n * sizeof(T) + (size_t)RED_NBLK * sizeof(T) + n + 15) & ~(size_t)15));
+    __shared__ int cnt[2];
     const int tid = threadIdx.x;
+    const int nx = (int)d.nx, ny = (int)d.ny, nz = (int)d.nz, nxny = nx * ny;
+    if (tid < 2) cnt[tid] = 0;
     for (int l = tid; l < n; l += CS_THREADS) {
         v[l] = gv[l];
         f[l] = gf[l];
@@ -910,23 +950,35 @@ __global__ void __launch_bounds__(CS_THREADS) coarse_solve_k(T *gv, const T *__r
         sq[l] = f[l] * f[l];
     }
     __syncthreads();
+    for (int l = tid; l < n; l += CS_THREADS) {
+        const int k = l / nxny, j = (l / nx) % ny, i = l % nx;
+        if (i < 1 || i > nx - 2 || j < 1 || j > ny - 2 || k < 1 || k > nz - 2 || !G[l]) continue;
+        const int par = (i + j + k) & 1;
+        uint32_t e = (uint32_t)l;
+        if (i == 1) e |= CS_I1;
+        if (i == nx - 2) e |= CS_INX2;
+        list[par * cap + atomicAdd(&cnt[par], 1)] = e;
+    }
     // reltol = tol * nrm2(f)
     const T ff = cta_lane_sum<T>(sq, blk, n);
     const double fn = sizeof(T) == 4 ? (double)sqrtf((float)ff) : sqrt((double)ff);
     const double reltol = tol * fn;
     __syncthreads();
-    const int nx = (int)d.nx, ny = (int)d.ny, nz = (int)d.nz, nxny = nx * ny;
+    const int n0 = cnt[0], n1 = cnt[1];
+    const uint32_t *list0 = list, *list1 = list + cap;
     const int rpar0 = (nx + 1) & 1;
+    const uint32_t *lr0 = rpar0 ? list1 : list0, *lr1 = rpar0 ? list0 : list1;
+    const int cr0 = rpar0 ? n1 : n0, cr1 = rpar0 ? n0 : n1;
     int outer = 0;
     for (int it = 0; it < 1024; ++it) {
         outer = it + 1;
         for (int s = 0; s < 128; ++s) {  // reverse sweeps
-            cta_gs<T>(v, f, G, gc, d, rpar0, -1);
-            cta_gs<T>(v, f, G, gc, d, rpar0 ^ 1, nx - 2);
+            cs_pass<T>(v, f, lr0, cr0, 0u, gc, nx, nxny);
+            cs_pass<T>(v, f, lr1, cr1, CS_INX2, gc, nx, nxny);
         }
         for (int s = 0; s < 128; ++s) {  // forward sweeps
-            cta_gs<T>(v, f, G, gc, d, 0, -1);
-            cta_gs<T>(v, f, G, gc, d, 1, 1);
+            cs_pass<T>(v, f, list0, n0, 0u, gc, nx, nxny);
+            cs_pass<T>(v, f, list1, n1, CS_I1, gc, nx, nxny);
         }
         // residual into r (global copy kept like the reference) and its norm
         for (int l = tid; l < n; l += CS_THREADS) {
@@ -1324,7 +1376,7 @@ static qsm_status hier_init(qsm_ctx *ctx, Hier<T> &H, int nl, const Dims &dp, co
     H.gb.extra = short_bar ? 1u : 0u;
     H.gb.limit = short_bar ? (1ll << 12) : CG_SPIN_LIMIT;
     const size_t nc = H.L[nl - 1].n;
-    H.coarse_smem = nc * (3 * sizeof(T) + 1) + RED_NBLK * sizeof(T) + 64;
+    H.coarse_smem = cs_smem(nc, sizeof(T)) + 64;
     int maxsm = 0;
     cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
     H.coarse_in_smem = H.coarse_smem <= (size_t)maxsm && nc < (1u << 18);
