@@ -1248,15 +1248,26 @@ static inline size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
 // The coarse solver's dynamic shared-memory limit is a process-wide function
 // attribute: raise it once per device to the opt-in maximum, so concurrent
 // solves on several host threads never lower it under each other's launch.
+// The limit is the opt-in maximum less the kernel's static shared memory; it
+// is returned in *lim (0: the attribute could not be read).
 template <typename T>
-static qsm_status coarse_smem_limit(qsm_ctx *ctx, int maxsm)
+static qsm_status coarse_smem_limit(qsm_ctx *ctx, int maxsm, size_t *lim)
 {
     static std::mutex mu;
     static std::set<int> done;
+    *lim = 0;
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, coarse_solve_k<T>) != cudaSuccess || (size_t)maxsm <= fa.sharedSizeBytes) {
+        cudaGetLastError();
+        return QSM_OK;
+    }
+    const size_t l = (size_t)maxsm - fa.sharedSizeBytes;
     std::lock_guard<std::mutex> lock(mu);
-    if (done.count(ctx->device)) return QSM_OK;
-    QSM_CUDA(cudaFuncSetAttribute(coarse_solve_k<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm));
-    done.insert(ctx->device);
+    if (!done.count(ctx->device)) {
+        QSM_CUDA(cudaFuncSetAttribute(coarse_solve_k<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)l));
+        done.insert(ctx->device);
+    }
+    *lim = l;
     return QSM_OK;
 }
 
@@ -1379,9 +1390,15 @@ static qsm_status hier_init(qsm_ctx *ctx, Hier<T> &H, int nl, const Dims &dp, co
     H.coarse_smem = cs_smem(nc, sizeof(T)) + 64;
     int maxsm = 0;
     cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
-    H.coarse_in_smem = H.coarse_smem <= (size_t)maxsm && nc < (1u << 18);
-    if (H.coarse_in_smem) QSM_TRY(coarse_smem_limit<T>(ctx, maxsm));
+    size_t cs_lim = 0;
+    QSM_TRY(coarse_smem_limit<T>(ctx, maxsm, &cs_lim));
+    H.coarse_in_smem = H.coarse_smem <= cs_lim && nc < (1u << 18);
     plan_cluster<T>(ctx, H, maxsm);
+    // In FP32 one SM's FP32 rate keeps a colour pass of a small coarsest grid
+    // under the cluster barrier's cost (157 against 214 us per 512-pass call
+    // at 18^3): one CTA from colour lists, where it holds the grid.  FP64
+    // passes need the cluster's 16 FP64 pipes.
+    if (sizeof(T) == 4 && H.coarse_in_smem) H.cc_ctas = 0;
     // levels whose long band sweeps can run on z-slabs in a cluster
     for (int i = 0; i + 1 < nl; ++i)
         plan_slabs<T>(ctx, H.L[i].d, maxsm, &H.L[i].dsm_cn, &H.L[i].dsm_npmax, &H.L[i].dsm_smem);

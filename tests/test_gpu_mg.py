@@ -111,10 +111,11 @@ def test_mgpcg_lbv_options_vs_oracle(gpu_ctx, qsm, port):
                                       ((28, 24, 16), 1), ((26, 22, 13), 1)])
 def test_coarse_levels_vs_oracle(gpu_ctx, qsm, port, dt, shape, nl):
     """Coarsest grids from 5 to 31 interior planes: solved on a thread-block
-    cluster (one slab of planes per CTA, uneven slabs included), including
-    grids too large for one CTA's shared memory; the boundary-band sweeps run
-    from voxel lists.  Bit-for-bit against the oracle for the PCG, the plain
-    V-cycle iteration and FMG."""
+    cluster (one slab of planes per CTA, uneven slabs included) in FP64, and
+    in FP32 on one CTA from colour lists where its shared memory holds the
+    grid, else on the cluster; the boundary-band sweeps run from voxel lists.
+    Bit-for-bit against the oracle for the PCG, the plain V-cycle iteration
+    and FMG."""
     import qsm_gb300.synthetic as S
 
     f, m, _ = S.poisson_case(shape, 7 + nl, semi=(8.0, 30.0))
@@ -124,7 +125,7 @@ def test_coarse_levels_vs_oracle(gpu_ctx, qsm, port, dt, shape, nl):
     b = port.mgpcg_mex(v0, f, m, [1, 1, 1], 1e-8, 30, -1.0, 2, 1, 2, 2, 2, nl, info=oi)
     a = qsm.mgpcg_mex(v0, f, m, [1, 1, 1], 1e-8, 30, -1.0, 2, 1, 2, 2, 2, nl, info=gi)
     assert gi["iters"] == oi["iters"]
-    assert gi["coarse_ctas"] >= 2, gi  # the cluster solver ran
+    assert gi["coarse_ctas"] >= (1 if dt == "float32" else 2), gi  # one CTA (FP32) or the cluster
     assert bits_equal(a, b), first_diff(a, b)
     a = qsm.mg_mex(v0, f, m, [1, 1, 1], 1e-6, 3, 1, 2, 2, 2, nl)
     assert bits_equal(a, port.mg_mex(v0, f, m, [1, 1, 1], 1e-6, 3, 1, 2, 2, 2, nl))
@@ -227,7 +228,7 @@ def test_grid_barrier_wait_runs_out(gpu_ctx, qsm, port):
 @pytest.mark.parametrize("dt", ("float64", "float32"))
 def test_mgpcg_256_lbv_options_bitexact(gpu_ctx, qsm, port, dt):
     """The benchmark's Poisson problem at full size (256^3, LBV options, 5
-    levels: 16-CTA cluster coarsest solve, list passes, fused PCG steps):
+    levels: 16-CTA cluster coarsest solve in FP64, one CTA in FP32, list passes, fused PCG steps):
     bit-for-bit against the oracle, same iteration count."""
     import qsm_gb300.synthetic as S
 
@@ -238,13 +239,13 @@ def test_mgpcg_256_lbv_options_bitexact(gpu_ctx, qsm, port, dt):
     b = port.mgpcg_mex(v0, f, m, [1, 1, 1], 1e-8, 40, -1.0, 2, 1, 2, 2, 2, 5, info=oi)
     a = qsm.mgpcg_mex(v0, f, m, [1, 1, 1], 1e-8, 40, -1.0, 2, 1, 2, 2, 2, 5, info=gi)
     assert gi["iters"] == oi["iters"] == 10
-    assert gi["coarse_ctas"] >= 2
+    assert gi["coarse_ctas"] == (1 if dt == "float32" else 16)
     assert bits_equal(a, b), first_diff(a, b)
 
 
 def test_mixed_pcg_cluster_coarse(gpu_ctx, qsm, port):
-    """FP64 PCG with the FP32 V-cycle (FP32 coarsest solve on the cluster):
-    same stopping rule, error against the FP64 oracle."""
+    """FP64 PCG with the FP32 V-cycle (FP32 coarsest solve on one CTA from
+    colour lists): same stopping rule, error against the FP64 oracle."""
     import qsm_gb300.synthetic as S
 
     f, m, _ = S.poisson_case((70, 64, 58), 5, semi=(20.0, 30.0))
@@ -252,7 +253,7 @@ def test_mixed_pcg_cluster_coarse(gpu_ctx, qsm, port):
     oi, mi = {}, {}
     b = port.mgpcg_mex(v0, f, m, [1, 1, 1], 1e-8, 100, -1.0, 2, 1, 2, 2, 2, 3, info=oi)
     c = qsm.mgpcg_mex(v0, f, m, [1, 1, 1], 1e-8, 100, -1.0, 2, 1, 2, 2, 2, 3, mixed=True, info=mi)
-    assert mi["coarse_ctas"] >= 2, mi
+    assert mi["coarse_ctas"] >= 1, mi
     assert np.linalg.norm(c - b) / np.linalg.norm(b) < 1e-6
     assert mi["iters"] <= oi["iters"] + 3
 
