@@ -963,6 +963,19 @@ __global__ void __launch_bounds__(CS_THREADS) coarse_solve_k(T *gv, const T *__r
     const T ff = cta_lane_sum<T>(sq, blk, n);
     const double fn = sizeof(T) == 4 ? (double)sqrtf((float)ff) : sqrt((double)ff);
     const double reltol = tol * fn;
+    // An idle solve: no G voxel to update, or f and v all +0.  Its sweeps then
+    // leave every value as it is (hh * (+0 + ...) is +0), so after the first
+    // outer iteration (which writes the residual) every later one repeats it
+    // exactly; the reference runs them all when its tolerance cannot be met
+    // (tol * ||f|| = 0), and their result is that of the first.
+    int nz_bits = 0;
+    for (int l = tid; l < n; l += CS_THREADS) {
+        if (sizeof(T) == 8)
+            nz_bits |= (__double_as_longlong((double)v[l]) | __double_as_longlong((double)f[l])) != 0;
+        else
+            nz_bits |= (__float_as_int((float)v[l]) | __float_as_int((float)f[l])) != 0;
+    }
+    const bool idle = !__syncthreads_or(nz_bits) || (cnt[0] + cnt[1] == 0);
     __syncthreads();
     const int n0 = cnt[0], n1 = cnt[1];
     const uint32_t *list0 = list, *list1 = list + cap;
@@ -996,6 +1009,10 @@ __global__ void __launch_bounds__(CS_THREADS) coarse_solve_k(T *gv, const T *__r
         const double rn = sizeof(T) == 4 ? (double)sqrtf((float)rr) : sqrt((double)rr);
         __syncthreads();
         if (rn < reltol) break;
+        if (idle) {
+            outer = 1024;
+            break;
+        }
     }
     for (int l = tid; l < n; l += CS_THREADS) gv[l] = v[l];
     if (tid == 0 && outer_out) *outer_out += outer;

@@ -189,6 +189,28 @@ def test_mgpcg_masked_steps_bitexact(gpu_ctx, qsm, port, outside, dt):
         assert np.linalg.norm(c - a) <= 1e-10 * np.linalg.norm(a)
 
 
+def test_coarsest_idle_solve_bitexact(gpu_ctx, qsm, port):
+    """A thin volume with five levels leaves a coarsest grid whose mask and
+    right-hand side are empty: the reference's coarsest loop cannot meet
+    tol * ||f|| = 0 and runs all 1024 outer iterations without changing a
+    value.  The one-CTA FP32 solver stops after the first with the same
+    result, still reports the 1024 outer iterations of each call, and the
+    whole solve stays bit-identical to the oracle (which takes ~20 s here)."""
+    import qsm_gb300.synthetic as S
+
+    f, m, _ = S.poisson_case((48, 48, 16), 3, semi=(6.0, 20.0))
+    f = np.asfortranarray(f.astype(np.float32))
+    v0 = np.zeros(f.shape, dtype=np.float32, order="F")
+    oi, gi = {}, {}
+    b = port.mgpcg_mex(v0, f, m, [1, 1, 1], 1e-8, 50, -1.0, 2, 1, 2, 2, 2, 5, info=oi)
+    a = qsm.mgpcg_mex(v0, f, m, [1, 1, 1], 1e-8, 50, -1.0, 2, 1, 2, 2, 2, 5, info=gi)
+    assert gi["iters"] == oi["iters"]
+    assert bits_equal(a, b), first_diff(a, b)
+    assert gi["coarse_ctas"] == 1
+    assert gi["coarse_outer"] == 1024 * 2 * gi["iters"]  # every call idle, counted as the reference runs it
+    assert gi["seconds"] < 0.5, gi["seconds"]
+
+
 def test_grid_barrier_wait_runs_out(gpu_ctx, qsm, port):
     """The grid barrier of the whole-GPU multigrid kernels waits a bounded
     number of polls.  With the context's test hook every barrier waits for
