@@ -64,6 +64,7 @@ class Record:
     t_done: float
     digest: str          # sha256 of the result bytes
     iters: int
+    device_s: float = 0.0  # the solve's device time as the session reports it (see summarize)
 
     @property
     def latency(self) -> float:
@@ -218,7 +219,7 @@ class ServeLoop:
                 t_done = self.clock() - t0
                 case = self.pool[r.kind][r.case]
                 self.records.append(Record(r.rid, r.kind, r.case, tuple(case["shape"]), r.t_arrive, t_admit, t_done,
-                                           digest(out), int(info.get("iters", 0))))
+                                           digest(out), int(info.get("iters", 0)), float(info.get("seconds", 0.0))))
                 if self.keep_results and (r.kind, r.case) not in self.results:
                     self.results[(r.kind, r.case)] = out
             if not pd_running:
@@ -242,5 +243,9 @@ def summarize(records: list[Record], duration: float) -> dict:
     for k in KINDS:
         lk = np.array([r.latency for r in records if r.kind == k]) * 1e3
         if lk.size:
-            out[k] = dict(n=int(lk.size), p50_ms=float(np.percentile(lk, 50)), p99_ms=float(np.percentile(lk, 99)))
+            # device_s: Poisson jobs, the solve's span on its worker stream; primal-dual jobs, the
+            # batched steps they took part in (shared with the other jobs of those steps)
+            dev = float(sum(r.device_s for r in records if r.kind == k))
+            out[k] = dict(n=int(lk.size), p50_ms=float(np.percentile(lk, 50)), p99_ms=float(np.percentile(lk, 99)),
+                          device_s=dev, device_share_of_span=dev / span)
     return out
