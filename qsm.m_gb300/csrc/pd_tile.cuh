@@ -50,6 +50,7 @@
 #include "common.cuh"
 #include "pd.cuh"
 #include "pd_fused.cuh"
+#include "tma.cuh"
 
 namespace qsm {
 
@@ -273,8 +274,18 @@ __device__ __forceinline__ void tile_tv(const FusedArgs &s, const DualC<float> &
 
 // One TX x TY column tile, planes [zs, zs + cz) of the interior, of the
 // fused TGV (TGV) or TV iteration with (TX+4)(TY+4) threads; smem holds
-// 2 x (NB + ND) planes of (TX+4)(TY+4) floats.  acc receives this thread's
-// monitor sums when check is set.
+// 3 x (NB + ND) planes of (TX+4)(TY+4) floats and three mbarriers.  acc
+// receives this thread's monitor sums when check is set.
+//
+// Steps are ordered by split arrive/wait barriers instead of one barrier per
+// plane: step k publishes the extragradient point of plane j+1 and the dual
+// of plane j, arrives on barrier k % 3 and then runs the primal of plane
+// j-1, which reads only what step k-1 published; step k+1 starts by waiting
+// for every thread's step-k arrival.  A warp may so run up to a step ahead
+// of the others.  The exchange planes are triple-buffered: a fast warp at
+// step k+1 writes the buffers step k-1 read, and its wait for step k proves
+// that every thread is done with step k-1.
+constexpr uint32_t kColumnWaitLimit = 1u << 22;
 template <int TX, int TY, bool TGV>
 __device__ __forceinline__ void column_pd(const FusedArgs &s, const DualC<float> &dc, const PrimalC<float> &pc,
                                           const Dims &d, int cz, unsigned tile, bool check, float *smem, double *acc)
@@ -282,8 +293,9 @@ __device__ __forceinline__ void column_pd(const FusedArgs &s, const DualC<float>
     constexpr int WX = TX + 4, WY = TY + 4, NT = WX * WY;
     constexpr int NB = TGV ? 5 : 2;   // extragradient arrays: chi_, eta_, w1_, w2_, w3_
     constexpr int ND = TGV ? 10 : 4;  // dual arrays: nu, p1..3, q1..6
-    float *B = smem;                  // [2][NB][NT]  extragradient point of one plane
-    float *S = B + 2 * NB * NT;       // [2][ND][NT]  dual of one plane
+    float *B = smem;                  // [3][NB][NT]  extragradient point of one plane
+    float *S = B + 3 * NB * NT;       // [3][ND][NT]  dual of one plane
+    uint64_t *sbar = (uint64_t *)(S + 3 * ND * NT);  // [3] step barriers
     const long x0 = 1 + (long)(tile % s.gx) * TX, y0 = 1 + (long)((tile / s.gx) % s.gy) * TY;
     const long zs = 1 + (long)(tile / (s.gx * s.gy)) * cz;
     const long ze = min(zs + (long)cz, (long)d.nz - 1);
@@ -363,11 +375,10 @@ __device__ __forceinline__ void column_pd(const FusedArgs &s, const DualC<float>
     make_bars(bm);
     fetch_bars(zs - 1, mr & 0xffu);
     make_bars(b0);
-    {
-        float *Bw = B + ((zs - 1) & 1) * NB * NT;
 #pragma unroll
-        for (int q = 0; q < NB; ++q) Bw[q * NT + tid] = b0[q];
-    }
+    for (int q = 0; q < NB; ++q) B[q * NT + tid] = b0[q];  // plane zs - 1: buffer of step 0
+    if (tid == 0)
+        for (int q = 0; q < 3; ++q) mbar_init(sbar + q, NT);
     fetch_bars(zs, (mr >> 8) & 0xffu);
     fetch_dual(zs - 1, mr & 0xffu);
     // own dual of planes j-1 (vp) and j-2 (the z-1 neighbours of the primal
@@ -377,20 +388,26 @@ __device__ __forceinline__ void column_pd(const FusedArgs &s, const DualC<float>
 #pragma unroll
     for (int q = 0; q < ND; ++q) vp[q] = 0.0f;
     float nu_m2 = 0.f, p3_m2 = 0.f, q3_m2 = 0.f, q5_m2 = 0.f, q6_m2 = 0.f;
+    bool waited = true;
     __syncthreads();
 
     for (long j = zs - 1; j <= ze; ++j) {
-        float *Bj = B + (j & 1) * NB * NT;              // extragradient of plane j (written last step)
-        float *Bn = B + ((j + 1) & 1) * NB * NT;        // plane j+1 (written now)
-        float *Sj = S + (j & 1) * ND * NT;              // dual of plane j (written now; held plane j-2)
-        const float *Sm = S + ((j + 1) & 1) * ND * NT;  // dual of plane j-1
+        const int k = (int)(j - (zs - 1));                      // step
+        float *Bj = B + (k % 3) * NB * NT;                      // extragradient of plane j (step k-1)
+        float *Bn = B + ((k + 1) % 3) * NB * NT;                // plane j+1 (written now)
+        float *Sj = S + (k % 3) * ND * NT;                      // dual of plane j (written now)
+        const float *Sm = S + ((k + 2) % 3) * ND * NT;          // dual of plane j-1 (step k-1)
 
-        // (a) extragradient point of plane j+1 (fetched last step); fetch plane j+2
+        // (a) extragradient point of plane j+1 (fetched last step); fetch plane j+2.  Its buffer
+        // was last read by step k-2, which every thread finished before step k-1's arrival.
         make_bars(bp);
 #pragma unroll
         for (int q = 0; q < NB; ++q) Bn[q * NT + tid] = bp[q];
         const unsigned mfar = mask_at(j + 5);
         fetch_bars(j + 2, (mr >> 16) & 0xffu);
+        // the x/y neighbours of plane j come from step k-1
+        if (k > 0 && !mbar_wait(sbar + (k - 1) % 3, (uint32_t)(((k - 1) / 3) & 1), kColumnWaitLimit))
+            waited = false;
 
         // (b) dual at plane j from the state fetched last step; fetch plane j+1
         float v[ND];
@@ -459,6 +476,7 @@ __device__ __forceinline__ void column_pd(const FusedArgs &s, const DualC<float>
         }
 #pragma unroll
         for (int q = 0; q < ND; ++q) Sj[q * NT + tid] = v[q];
+        mbar_arrive(sbar + k % 3);
 
         // (c) primal + extragradient at plane j-1
         if (do_primal) {
@@ -513,8 +531,14 @@ __device__ __forceinline__ void column_pd(const FusedArgs &s, const DualC<float>
         for (int q = 0; q < ND; ++q) vp[q] = v[q];
         mr = (mr >> 8) | (mnext << 24);
         mnext = mfar;
-        __syncthreads();
     }
+    if (!waited) atomicOr(&s.ctl->stalled, 1u);
+    // every thread's last arrival is in: the barriers are retired before the
+    // shared memory is used again
+    __syncthreads();
+    if (tid == 0)
+        for (int q = 0; q < 3; ++q) mbar_inval(sbar + q);
+    __syncthreads();
     if (check)
 #pragma unroll
         for (int q = 0; q < 4; ++q) acc[q] += mon[q].get();

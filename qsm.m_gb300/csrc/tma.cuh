@@ -32,6 +32,13 @@ __device__ __forceinline__ void mbar_inval(uint64_t *bar)
     asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
 
+// one thread's arrival (its earlier shared-memory writes are released to the
+// threads that then complete a wait on this phase)
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
 // the arrival of the issuing thread, announcing `bytes` of TMA traffic
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes)
 {
