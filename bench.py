@@ -65,6 +65,7 @@ KERNEL_SOURCES = ("qsm.m_gb300/csrc/pd_tile.cuh", "qsm.m_gb300/csrc/pd_fused.cuh
                   "qsm.m_gb300/csrc/pd_tma.cuh")
 NCU_TRAFFIC_224x224x128 = {  # (digest, tx, ty, z-chunk) -> bytes per launch
     ("b5587692fbd9d68d", 28, 16, 16): 276.3e6,  # median of 5 launches: read 191.5 MB + write 84.8 MB
+    ("f8d62df05796e322", 28, 16, 16): 275.6e6,  # split step barriers: read 191.1 MB + write 84.5 MB
 }
 
 

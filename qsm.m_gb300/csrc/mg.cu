@@ -98,6 +98,11 @@ __device__ __forceinline__ void cl_st(uint32_t a, float v)
 {
     asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(a), "f"(v) : "memory");
 }
+// bitwise OR into a word of a CTA of the cluster (visible after the next cl_sync)
+__device__ __forceinline__ void cl_or(uint32_t a, uint32_t v)
+{
+    asm volatile("red.relaxed.cluster.shared::cluster.or.b32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
+}
 
 // ---------------------------------------------------------------------------
 // Gauss-Seidel colour pass (gauss_seidel_mex.c:138-190 / :256-308)
@@ -1134,8 +1139,10 @@ __global__ void __launch_bounds__(CC_THREADS) coarse_cluster_k(T *gv, const T *_
     uint32_t *list = (uint32_t *)(smraw + lay.list);
     const int cap = npmax * nxny;
     __shared__ int cnt[2];
+    __shared__ unsigned cflag;  // OR over the cluster: 1 = some G voxel to update, 2 = some v or f bit set
     const int tid = threadIdx.x;
     if (tid < 2) cnt[tid] = 0;
+    if (tid == 0) cflag = 0u;
     for (int t = tid; t < RED_NBLK; t += CC_THREADS) blk[t] = (T)0;
     const size_t base = (size_t)(k0 - 1) * nxny;
     for (int t = tid; t < (np + 2) * nxny; t += CC_THREADS) v[t] = gv[base + t];
@@ -1180,9 +1187,23 @@ __global__ void __launch_bounds__(CC_THREADS) coarse_cluster_k(T *gv, const T *_
         return;
     }
 
+    // An idle solve (no G voxel to update anywhere, or every v and f bit clear):
+    // its sweeps change nothing, so after the first outer iteration every
+    // later one repeats it exactly (see coarse_solve_k).  The slab flags are
+    // ORed into every CTA; the lane sum's cluster barriers make them visible.
+    {
+        int nzb = 0;
+        for (int t = tid; t < (np + 2) * nxny; t += CC_THREADS)
+            nzb |= sizeof(T) == 8 ? __double_as_longlong((double)v[t]) != 0 : __float_as_int((float)v[t]) != 0;
+        for (int t = tid; t < np * nxny; t += CC_THREADS)
+            nzb |= sizeof(T) == 8 ? __double_as_longlong((double)f[t]) != 0 : __float_as_int((float)f[t]) != 0;
+        const unsigned bits = (cnt[0] + cnt[1] > 0 ? 1u : 0u) | (__syncthreads_or(nzb) ? 2u : 0u);
+        if (tid < (int)cn && bits) cl_or(cl_map(&cflag, (uint32_t)tid), bits);
+    }
     const T ff = cl_lane_sum<T>(gf, n, red, blk, bc, c, cn);
     const double fn = sizeof(T) == 4 ? (double)sqrtf((float)ff) : sqrt((double)ff);
     const double reltol = tol * fn;
+    const bool idle = (cflag & 1u) == 0 || (cflag & 2u) == 0;
     int outer = 0;
     for (int it = 0; it < 1024; ++it) {
         outer = it + 1;
@@ -1208,6 +1229,10 @@ __global__ void __launch_bounds__(CC_THREADS) coarse_cluster_k(T *gv, const T *_
         const T rr = cl_lane_sum<T>(gr, n, red, blk, bc, c, cn);
         const double rn = sizeof(T) == 4 ? (double)sqrtf((float)rr) : sqrt((double)rr);
         if (rn < reltol) break;
+        if (idle) {
+            outer = 1024;
+            break;
+        }
     }
     for (int t = tid; t < np * nxny; t += CC_THREADS) gv[base + nxny + t] = v[nxny + t];
     if (c == 0 && tid == 0 && outer_out) *outer_out += outer;

@@ -202,12 +202,35 @@ def test_coarsest_idle_solve_bitexact(gpu_ctx, qsm, port):
     f = np.asfortranarray(f.astype(np.float32))
     v0 = np.zeros(f.shape, dtype=np.float32, order="F")
     oi, gi = {}, {}
-    b = port.mgpcg_mex(v0, f, m, [1, 1, 1], 1e-8, 50, -1.0, 2, 1, 2, 2, 2, 5, info=oi)
-    a = qsm.mgpcg_mex(v0, f, m, [1, 1, 1], 1e-8, 50, -1.0, 2, 1, 2, 2, 2, 5, info=gi)
+    b = port.mgpcg_mex(v0, f, m, [1, 1, 1], 1e-8, 3, -1.0, 2, 1, 2, 2, 2, 5, info=oi)
+    a = qsm.mgpcg_mex(v0, f, m, [1, 1, 1], 1e-8, 3, -1.0, 2, 1, 2, 2, 2, 5, info=gi)
     assert gi["iters"] == oi["iters"]
     assert bits_equal(a, b), first_diff(a, b)
     assert gi["coarse_ctas"] == 1
     assert gi["coarse_outer"] == 1024 * 2 * gi["iters"]  # every call idle, counted as the reference runs it
+    assert gi["seconds"] < 0.5, gi["seconds"]
+
+
+def test_coarsest_idle_cluster_solve_bitexact(gpu_ctx, qsm, port):
+    """The same idle coarsest loop in FP64 on the thread-block cluster: a mask
+    a few planes thick in a 64 x 64 x 40 grid leaves the 6 x 6 x 4 coarsest
+    grid without mask voxels; the cluster solver stops each idle call after
+    one outer iteration, reports 1024, and matches the oracle bit for bit."""
+    import qsm_gb300.synthetic as S
+
+    rng = np.random.default_rng(8)
+    shape = (64, 64, 40)
+    m = S.ellipsoid_mask(shape, (24.0, 20.0, 3.0))
+    u = np.asfortranarray(rng.standard_normal(shape))
+    f = np.asfortranarray(-S.lap7(u, m, (1.0, 1.0, 1.0)))
+    v0 = np.zeros(shape, order="F")
+    oi, gi = {}, {}
+    b = port.mgpcg_mex(v0, f, m, [1, 1, 1], 1e-8, 3, -1.0, 2, 1, 2, 2, 2, 5, info=oi)
+    a = qsm.mgpcg_mex(v0, f, m, [1, 1, 1], 1e-8, 3, -1.0, 2, 1, 2, 2, 2, 5, info=gi)
+    assert gi["iters"] == oi["iters"]
+    assert bits_equal(a, b), first_diff(a, b)
+    assert gi["coarse_ctas"] >= 2  # the cluster solver
+    assert gi["coarse_outer"] == 1024 * 2 * gi["iters"]
     assert gi["seconds"] < 0.5, gi["seconds"]
 
 
