@@ -690,6 +690,10 @@ __global__ void __launch_bounds__(CG_THREADS) coarse_grid_k(T *v, const T *__res
         if (!grid_lane_sum(r, n, part, red, gb, bk, &rr)) return;
         const double rn = sizeof(T) == 4 ? (double)sqrtf((float)rr) : sqrt((double)rr);
         if (rn < reltol) break;
+        if (c0 + c1 == 0) {  // no G voxel: every later outer iteration repeats this one exactly
+            outer = 1024;
+            break;
+        }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0 && outer_out) *outer_out += outer;
 }
