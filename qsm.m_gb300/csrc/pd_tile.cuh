@@ -25,7 +25,9 @@
 //            (c) the primal + extragradient at plane j-1 (tile threads), from
 //                the dual of planes j-2 (registers), j-1 (shared memory, x/y
 //                neighbours) and j (own value)
-//            one __syncthreads
+//            (b) ends with an arrival on the step's mbarrier; step j+1 waits
+//            for every thread's arrival before it reads plane j+1's shared
+//            values (triple-buffered planes, see column_pd)
 //
 // so every input value of a plane is read from HBM once per CTA (the ring
 // re-reads neighbouring tiles' edges, mostly from L2) and the dual is
