@@ -113,66 +113,6 @@ tv_fused_k(FusedArgs s, DualC<float> dc, PrimalC<float> pc, Dims d, double tol, 
 }
 
 // ---------------------------------------------------------------------------
-// monitors of the one-volume path
-// ---------------------------------------------------------------------------
-
-// Monitor sums of a fused iteration from the stored iterates n+1 (An) and n
-// (Ao) over the interior mask voxels (those whose primal the iteration
-// updated): x^2, e^2, (x - x0)^2, (e - e0)^2 in FP32 per voxel -- the terms
-// the kernels' monitor form sums -- added per thread with compensation and
-// folded in FP64 across threads and blocks in a fixed order, then the
-// stopping test.  The one-volume driver runs it after a check iteration's
-// plain kernel: the kernels' monitor form needs more registers than 640
-// threads per SM leave and spilled (a check iteration cost 1.4 plain ones).
-// Block b takes the interior rows b, b + gridDim.x, ...; STRIDE is the
-// floats per voxel of family A (TGV 4, TV 2).
-constexpr int MON_THREADS = 256;
-
-template <int STRIDE>
-__global__ void __launch_bounds__(MON_THREADS) fused_monitor_k(const float *__restrict__ An, const float *__restrict__ Ao,
-                                                               const uint8_t *__restrict__ mm, Dims d, double *part,
-                                                               unsigned *count, PdCtl *ctl, double tol, uint32_t it)
-{
-    __shared__ double red[4 * MON_THREADS];
-    if (ctl->done) return;
-    PartialSum<float> mon[4];
-    const size_t nx = d.nx, nxny = d.nxny(), ry = d.ny - 2, rows = ry * (d.nz - 2);
-    for (size_t row = blockIdx.x; row < rows; row += gridDim.x) {
-        const size_t k = 1 + row / ry, j = 1 + row % ry;
-        const size_t base = nx * j + nxny * k;
-        for (size_t i = 1 + threadIdx.x; i + 1 < nx; i += MON_THREADS) {
-            const size_t l = base + i;
-            if (!(__ldg(mm + l) & 1u)) continue;
-            const float2 a = __ldg((const float2 *)(An + STRIDE * l)), b = __ldg((const float2 *)(Ao + STRIDE * l));
-            mon[0].add(a.x * a.x);
-            mon[1].add(a.y * a.y);
-            mon[2].add((a.x - b.x) * (a.x - b.x));
-            mon[3].add((a.y - b.y) * (a.y - b.y));
-        }
-    }
-    double acc[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) acc[q] = mon[q].get();
-    monitor_fold<MON_THREADS>(part, count, ctl, gridDim.x, blockIdx.x, red, acc, tol, it);
-}
-
-static qsm_status launch_monitor(qsm_ctx *ctx, cudaStream_t st, const PdVolume &v, uint32_t it, double tol)
-{
-    const Dims &d = v.d;
-    if (d.nx < 3 || d.ny < 3 || d.nz < 3) return QSM_OK;
-    const size_t rows = (d.ny - 2) * (d.nz - 2);
-    const unsigned grid = (unsigned)std::min<size_t>(std::min<size_t>(rows, 1216), v.nblk_max);
-    // iteration `it` read iterate it % 3 and wrote iterate (it + 1) % 3 (pd_volume_args)
-    const float *An = (const float *)v.PA[(it + 1) % 3], *Ao = (const float *)v.PA[it % 3];
-    if (v.tgv)
-        fused_monitor_k<4><<<grid, MON_THREADS, 0, st>>>(An, Ao, v.mm, d, v.part, v.count, v.ctl, tol, it + 1);
-    else
-        fused_monitor_k<2><<<grid, MON_THREADS, 0, st>>>(An, Ao, v.mm, d, v.part, v.count, v.ctl, tol, it + 1);
-    QSM_CUDA(cudaGetLastError());
-    return QSM_OK;
-}
-
-// ---------------------------------------------------------------------------
 // variants, launch, autotuning
 // ---------------------------------------------------------------------------
 
@@ -385,7 +325,6 @@ qsm_status pd_volume_init(qsm_ctx *ctx, PdVolume *v, bool tgv, const Dims &d, qs
     v->count = (unsigned *)c;
     v->ctl = (PdCtl *)(c + 256);
     v->state_bytes = 3 * (L.pa + L.pb) + 2 * (L.da + L.db + L.dc);
-    v->nblk_max = (unsigned)L.nblk_max;
 
     double tau, sigma;
     pd_steps(h, &tau, &sigma);
@@ -606,11 +545,9 @@ qsm_status pd_fused(qsm_ctx *ctx, bool tgv, const Dims &d, qsm_dtype dt, const v
     uint32_t enq = 0;
     for (uint32_t it = 0; it < maxiter; ++it) {
         const bool chk = ((it + 1) % 10) == 0;
-        if (!empty) {
-            QSM_TRY(launch_variant(ctx, ctx->stream, var, tgv, false, nact, pd_volume_args(v, var, it), v.dc, v.pc, d,
+        if (!empty)
+            QSM_TRY(launch_variant(ctx, ctx->stream, var, tgv, chk, nact, pd_volume_args(v, var, it), v.dc, v.pc, d,
                                    tol, it + 1, volume_maps(v, var, it)));
-            if (chk) QSM_TRY(launch_monitor(ctx, ctx->stream, v, it, tol));
-        }
         enq = it + 1;
         const bool print = verbose && (it == 0 || it == maxiter - 1 || ((it + 1) % pmod) == 0);
         if (print || (chk && ((it + 1) % 100) == 0)) {

@@ -229,7 +229,6 @@ struct PdVolume {
     uint8_t *mm = nullptr;       // bit 0 m, bit 1 mi
     TileList tl[kNumVariants];
     double *part = nullptr;      // 4 x (max tiles) monitor partials
-    unsigned nblk_max = 0;       // entries of part per sum (the most tiles of any variant)
     unsigned *count = nullptr;   // arrival counter of the monitor fold
     PdCtl *ctl = nullptr;
     size_t state_bytes = 0;      // primal + dual buffers (from PA[0])
