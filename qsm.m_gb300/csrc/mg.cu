@@ -1907,6 +1907,53 @@ __device__ __forceinline__ bool lane_fold(T *sm, T acc, T *part, unsigned *count
 // +-0 to it changes nothing: skipping those voxels gives the same bits.
 __device__ __forceinline__ bool pcg_on(const uint8_t *__restrict__ sk, size_t l) { return !sk || sk[l]; }
 
+// Segments of the lane grid for the masked PCG steps.  Warp w of the lane
+// grid (lanes 32 w .. 32 w + 31) visits the elements l = 32 w + lane +
+// k RED_LANES, k = 0, 1, ...; segment (w, k) is those 32 elements.
+// k[j * SEG_NW + w], j < cnt[w], lists in increasing k the segments that
+// hold a voxel of G, and the masked steps visit only those: a warp whose 32
+// elements all lie outside G then issues no FP64 instruction at all, where
+// a per-element test leaves FP64 instructions with every lane predicated
+// off, and those still take their slot in the FP64 pipe.  Each lane still
+// visits its own elements of G in increasing k, so inner products keep
+// the lane order and their bits.
+constexpr uint32_t SEG_NW = (uint32_t)(RED_LANES / 32);
+
+struct Segs {
+    const uint32_t *k;    // nullptr: every element is visited
+    const uint32_t *cnt;
+};
+
+static size_t seg_entries(size_t n) { return (n + RED_LANES - 1) / RED_LANES * SEG_NW; }
+
+__global__ void __launch_bounds__(RED_BLOCK) pcg_segs_k(const uint8_t *__restrict__ sk, size_t n, uint32_t *segk,
+                                                        uint32_t *segcnt)
+{
+    const size_t t = (size_t)blockIdx.x * RED_BLOCK + threadIdx.x;
+    const uint32_t w = (uint32_t)(t >> 5);
+    const bool lead = (threadIdx.x & 31) == 0;
+    uint32_t c = 0;
+    // k * RED_LANES < n is the same for the whole warp: every lane votes
+    for (size_t k = 0, l = t; k * RED_LANES < n; ++k, l += RED_LANES) {
+        const bool on = l < n && sk[l];
+        if (__ballot_sync(0xffffffffu, on)) {
+            if (lead) segk[(size_t)c * SEG_NW + w] = (uint32_t)k;
+            ++c;
+        }
+    }
+    if (lead) segcnt[w] = c;
+}
+
+// element indices of this warp's listed segments j .. j + 3 (n past the list
+// end; the last segment may reach past n as well)
+__device__ __forceinline__ void seg_group(const Segs &sg, size_t t, uint32_t w, uint32_t j, uint32_t c, size_t n,
+                                          size_t *l)
+{
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+        l[u] = j + u < c ? t + (size_t)sg.k[(size_t)(j + u) * SEG_NW + w] * RED_LANES : n;
+}
+
 // flag = 1 if some voxel outside G holds a value other than +0 in a or b
 template <typename T>
 __global__ void pcg_zero_outside_k(const T *__restrict__ a, const T *__restrict__ b, const uint8_t *__restrict__ G,
@@ -1929,12 +1976,36 @@ __global__ void pcg_zero_outside_k(const T *__restrict__ a, const T *__restrict_
 template <typename TP, typename TM>
 __global__ void __launch_bounds__(RED_BLOCK) pcg_rho_k(const TP *__restrict__ r, TP *__restrict__ q,
                                                        const TM *__restrict__ vm, const uint8_t *__restrict__ sk,
-                                                       size_t n, TP *part, unsigned *count, double *sc)
+                                                       Segs sg, size_t n, TP *part, unsigned *count, double *sc)
 {
     __shared__ TP sm[RED_BLOCK];
     const size_t L = RED_LANES;
     size_t l = (size_t)blockIdx.x * RED_BLOCK + threadIdx.x;
     TP acc = (TP)0;
+    if (sg.k) {
+        const uint32_t w = (uint32_t)(l >> 5), c = sg.cnt[w];
+        for (uint32_t j = 0; j < c; j += 4) {
+            size_t e[4];
+            seg_group(sg, l, w, j, c, n, e);
+            TP a[4] = {}, b[4] = {};
+            bool on[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                on[u] = e[u] < n && sk[e[u]];
+                if (e[u] < n) {
+                    a[u] = r[e[u]];
+                    b[u] = vm ? (TP)vm[e[u]] : q[e[u]];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (!on[u]) continue;
+                if (vm) q[e[u]] = b[u];
+                acc = acc + a[u] * b[u];
+            }
+        }
+        l = n;
+    }
     for (; l + 3 * L < n; l += 4 * L) {
         TP a[4], b[4];
         bool on[4];
@@ -1968,12 +2039,34 @@ __global__ void __launch_bounds__(RED_BLOCK) pcg_rho_k(const TP *__restrict__ r,
     }
 }
 
-// p = beta * p, then p = p + 1 * q
+// p = beta * p, then p = p + 1 * q (with segments: on the lane grid)
 template <typename T>
-__global__ void pcg_p_k(T *__restrict__ p, const T *__restrict__ q, const uint8_t *__restrict__ sk, size_t n,
-                        const double *sc)
+__global__ void pcg_p_k(T *__restrict__ p, const T *__restrict__ q, const uint8_t *__restrict__ sk, Segs sg,
+                        size_t n, const double *sc)
 {
     const T beta = (T)sc[S_BETA];
+    if (sg.k) {
+        const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+        const uint32_t w = (uint32_t)(t >> 5), c = sg.cnt[w];
+        for (uint32_t j = 0; j < c; j += 4) {
+            size_t e[4];
+            seg_group(sg, t, w, j, c, n, e);
+            T pv[4] = {}, qv[4] = {};
+            bool on[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                on[u] = e[u] < n && sk[e[u]];
+                if (e[u] < n) {
+                    pv[u] = p[e[u]];
+                    qv[u] = q[e[u]];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (on[u]) p[e[u]] = beta * pv[u] + qv[u];
+        }
+        return;
+    }
     for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x)
         if (pcg_on(sk, l)) p[l] = beta * p[l] + q[l];
 }
@@ -1983,15 +2076,43 @@ __global__ void pcg_p_k(T *__restrict__ p, const T *__restrict__ q, const uint8_
 template <typename T>
 __global__ void __launch_bounds__(RED_BLOCK) pcg_q_k(T *__restrict__ q, const T *__restrict__ p,
                                                      const uint8_t *__restrict__ G, const uint8_t *__restrict__ sk,
-                                                     LapC<T> c, Dims d, T *part, unsigned *count, double *sc)
+                                                     Segs sg, LapC<T> c, Dims d, T *part, unsigned *count, double *sc)
 {
     __shared__ T sm[RED_BLOCK];
     const size_t nx = d.nx, ny = d.ny, nxny = d.nxny(), n = d.n();
-    // (i, j, k) of l, then advanced by the lane stride in mixed radix (no division per element)
     const size_t t = (size_t)blockIdx.x * RED_BLOCK + threadIdx.x;
+    T acc = (T)0;
+    if (sg.k) {
+        // sk is G here, whose one-voxel frame is 0: a voxel of G is interior and takes the stencil
+        const uint32_t w = (uint32_t)(t >> 5), cn = sg.cnt[w];
+        for (uint32_t jj = 0; jj < cn; jj += 4) {
+            size_t e[4];
+            seg_group(sg, t, w, jj, cn, n, e);
+            bool on[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) on[u] = e[u] < n && sk[e[u]];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (!on[u]) continue;
+                const size_t l = e[u];
+                const T pl = p[l];
+                const T qv = neg_bits(c.hh * pl + c.hx * (p[l - 1] + p[l + 1]) + c.hy * (p[l - nx] + p[l + nx]) +
+                                      c.hz * (p[l - nxny] + p[l + nxny]));
+                q[l] = qv;
+                acc = acc + pl * qv;
+            }
+        }
+        T tot;
+        if (lane_fold(sm, acc, part, count, &tot) && threadIdx.x == 0) {
+            sc[S_PQ] = (double)tot;
+            sc[S_A] = sc[S_RHO] / sc[S_PQ];
+            *count = 0;
+        }
+        return;
+    }
+    // (i, j, k) of l, then advanced by the lane stride in mixed radix (no division per element)
     size_t k = t / nxny, j = (t - k * nxny) / nx, i = t - k * nxny - j * nx;
     const size_t Lk = RED_LANES / nxny, Lj = (RED_LANES - Lk * nxny) / nx, Li = RED_LANES - Lk * nxny - Lj * nx;
-    T acc = (T)0;
     for (size_t l = t; l < n; l += RED_LANES) {
         if (pcg_on(sk, l)) {
             const T pl = p[l];
@@ -2026,14 +2147,43 @@ __global__ void __launch_bounds__(RED_BLOCK) pcg_q_k(T *__restrict__ q, const T 
 template <typename TP, typename TM>
 __global__ void __launch_bounds__(RED_BLOCK) pcg_xr_k(TP *__restrict__ x, const TP *__restrict__ p,
                                                       TP *__restrict__ r, const TP *__restrict__ q,
-                                                      TM *__restrict__ rm, const uint8_t *__restrict__ sk, size_t n,
-                                                      TP *part, unsigned *count, double *sc)
+                                                      TM *__restrict__ rm, const uint8_t *__restrict__ sk, Segs sg,
+                                                      size_t n, TP *part, unsigned *count, double *sc)
 {
     __shared__ TP sm[RED_BLOCK];
     const TP a = (TP)sc[S_A], na = (TP)(-sc[S_A]);
     const size_t L = RED_LANES;
     size_t l = (size_t)blockIdx.x * RED_BLOCK + threadIdx.x;
     TP acc = (TP)0;
+    if (sg.k) {
+        const uint32_t w = (uint32_t)(l >> 5), c = sg.cnt[w];
+        for (uint32_t j = 0; j < c; j += 4) {
+            size_t e[4];
+            seg_group(sg, l, w, j, c, n, e);
+            TP xv[4] = {}, pv[4] = {}, rv[4] = {}, qv[4] = {};
+            bool on[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                on[u] = e[u] < n && sk[e[u]];
+                if (e[u] < n) {
+                    xv[u] = x[e[u]];
+                    pv[u] = p[e[u]];
+                    rv[u] = r[e[u]];
+                    qv[u] = q[e[u]];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (!on[u]) continue;
+                x[e[u]] = xv[u] + a * pv[u];
+                const TP rn = rv[u] + na * qv[u];
+                r[e[u]] = rn;
+                if (rm) rm[e[u]] = (TM)rn;
+                acc = acc + rn * rn;
+            }
+        }
+        l = n;
+    }
     for (; l + 3 * L < n; l += 4 * L) {
         TP xv[4], pv[4], rv[4], qv[4];
         bool on[4];
@@ -2111,9 +2261,11 @@ static qsm_status pcg(qsm_ctx *ctx, const Dims &d, const TP *v0, const TP *f, co
     const bool same = sizeof(TP) == sizeof(TM);
     // PCG vectors: x, p (and r, q when the V-cycle runs in another precision)
     void *pv = nullptr;
-    const size_t vb = al256(n * sizeof(TP));
-    QSM_TRY(dalloc(ctx, &pv, (same ? 2 : 4) * vb + S_N * sizeof(double) + 256));
-    QSM_CUDA(cudaMemsetAsync(pv, 0, (same ? 2 : 4) * vb + S_N * sizeof(double) + 256, ctx->stream));
+    const size_t vb = al256(n * sizeof(TP)), scb = al256(S_N * sizeof(double) + 256);
+    // + the lane-grid segment lists of the masked steps (built below when that form runs)
+    QSM_TRY(dalloc(ctx, &pv, (same ? 2 : 4) * vb + scb + al256(seg_entries(n) * sizeof(uint32_t)) +
+                                 SEG_NW * sizeof(uint32_t)));
+    QSM_CUDA(cudaMemsetAsync(pv, 0, (same ? 2 : 4) * vb + scb, ctx->stream));
     TP *x = (TP *)pv, *p = (TP *)((char *)pv + vb);
     TP *r = same ? (TP *)H.L[0].f : (TP *)((char *)pv + 2 * vb);
     TP *q = same ? (TP *)H.L[0].v : (TP *)((char *)pv + 3 * vb);
@@ -2151,6 +2303,14 @@ static qsm_status pcg(qsm_ctx *ctx, const Dims &d, const TP *v0, const TP *f, co
     QSM_CUDA(cudaMemcpyAsync(&hz, zflag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     QSM_CUDA(cudaStreamSynchronize(ctx->stream));
     const uint8_t *sk = hz ? nullptr : H.L[0].G;
+    Segs sg{nullptr, nullptr};
+    if (sk) {
+        uint32_t *segk = (uint32_t *)((char *)pv + (same ? 2 : 4) * vb + scb);
+        uint32_t *segcnt = (uint32_t *)((char *)segk + al256(seg_entries(n) * sizeof(uint32_t)));
+        pcg_segs_k<<<RED_NBLK, RED_BLOCK, 0, ctx->stream>>>(sk, n, segk, segcnt);
+        QSM_CUDA(cudaGetLastError());
+        sg = Segs{segk, segcnt};
+    }
     if (verbose) printf("\niter%6s\tresidual\n", "");
     int32_t it = 0;
     TP *part = (TP *)ctx->red_partial;
@@ -2167,12 +2327,14 @@ static qsm_status pcg(qsm_ctx *ctx, const Dims &d, const TP *v0, const TP *f, co
             Range cyc("mgpcg/preconditioner");
             QSM_TRY(mg_run<TM>(ctx, H, tolmg, maxitmg, mu, npre, npost, nb, sc, nullptr));
         }
-        pcg_rho_k<TP, TM><<<RED_NBLK, RED_BLOCK, 0, ctx->stream>>>(r, q, same ? nullptr : H.L[0].v, sk, n, part,
-                                                                   ctx->red_count, sc);
-        pcg_p_k<TP><<<1216, 256, 0, ctx->stream>>>(p, q, sk, n, sc);
-        pcg_q_k<TP><<<RED_NBLK, RED_BLOCK, 0, ctx->stream>>>(q, p, H.L[0].G, sk, lc, dp, part, ctx->red_count, sc);
-        pcg_xr_k<TP, TM><<<RED_NBLK, RED_BLOCK, 0, ctx->stream>>>(x, p, r, q, same ? nullptr : H.L[0].f, sk, n, part,
-                                                                  ctx->red_count, sc);
+        pcg_rho_k<TP, TM><<<RED_NBLK, RED_BLOCK, 0, ctx->stream>>>(r, q, same ? nullptr : H.L[0].v, sk, sg, n,
+                                                                   part, ctx->red_count, sc);
+        // with segments pcg_p_k runs on the lane grid
+        pcg_p_k<TP><<<sg.k ? RED_NBLK : 1216, RED_BLOCK, 0, ctx->stream>>>(p, q, sk, sg, n, sc);
+        pcg_q_k<TP><<<RED_NBLK, RED_BLOCK, 0, ctx->stream>>>(q, p, H.L[0].G, sk, sg, lc, dp, part, ctx->red_count,
+                                                             sc);
+        pcg_xr_k<TP, TM><<<RED_NBLK, RED_BLOCK, 0, ctx->stream>>>(x, p, r, q, same ? nullptr : H.L[0].f, sk, sg, n,
+                                                                  part, ctx->red_count, sc);
         QSM_CUDA(cudaGetLastError());
         QSM_TRY(read_double(ctx, sc + S_RES, &res));
         if (info && info->resnorm_hist) info->resnorm_hist[i] = res;
