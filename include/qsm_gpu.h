@@ -296,7 +296,10 @@ qsm_status qsm_mgpcg(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3],
 /* Mixed-precision variant: FP64 PCG recurrence (residual update, inner
  * products, step lengths) preconditioned by an FP32 V-cycle (FP32 smoother,
  * residual, transfer operators, coarse solve with the reference's FP32
- * coarse tolerance 1e-4).  v0/f/v_out are FP64.  Same arguments otherwise. */
+ * coarse tolerance 1e-4).  The recurrence's multiply-adds are FP64 fused
+ * multiply-adds (one rounding each), so its result is not bit-identical to
+ * the FP64 solve's; it is reproducible run to run.  v0/f/v_out are FP64.
+ * Same arguments otherwise. */
 qsm_status qsm_mgpcg_mixed(qsm_ctx *ctx, const size_t dims[3],
                            const double *v0, const double *f, const uint8_t *mask,
                            const double vsz[3], double tolcg, int32_t maxitcg, double tolmg,
@@ -557,6 +560,13 @@ qsm_status qsm_dot(qsm_ctx *ctx, qsm_dtype dtype, size_t n, const void *x, const
  * timed with events on the context's stream (best of three launches).  The
  * FP64 figure is the roofline of the bit-exact FP64 solvers. */
 qsm_status qsm_fp_pipe_rate(qsm_ctx *ctx, qsm_dtype dtype, double *ops_per_s);
+
+/* *mismatches = the number of inputs on which the library's integer-arithmetic
+ * FP32 <-> FP64 conversions (the mixed-precision PCG's, which keep them off the
+ * FP64 pipe) differ from the device's own conversions: all 2^32 floats, and
+ * 2^30 doubles, most aimed at rounding ties, subnormal and overflowing float
+ * results.  0 on every correct build. */
+qsm_status qsm_fp_convert_check(qsm_ctx *ctx, unsigned long long *mismatches);
 
 #ifdef __cplusplus
 }

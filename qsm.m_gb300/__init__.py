@@ -331,6 +331,14 @@ def fp_pipe_rate(dtype="float64", *, ctx=None) -> float:
     return out.value
 
 
+def fp_convert_check(*, ctx=None) -> int:
+    """Inputs on which the library's integer FP32 <-> FP64 conversions differ
+    from the device's (all floats, 2^30 chosen doubles): 0 on a correct build."""
+    out = ctypes.c_ulonglong(0)
+    _ctx(ctx).call("qsm_fp_convert_check", ctypes.byref(out))
+    return out.value
+
+
 # ---------------------------------------------------------------------------
 # Poisson solvers
 # ---------------------------------------------------------------------------

@@ -187,6 +187,8 @@ def lib() -> ctypes.CDLL:
                               "rebuild it with `python qsm.m_gb300/build.py`")
     L.qsm_fp_pipe_rate.argtypes = [CTX, I32, ctypes.POINTER(DBL)]
     L.qsm_fp_pipe_rate.restype = STATUS
+    L.qsm_fp_convert_check.argtypes = [CTX, ctypes.POINTER(ctypes.c_ulonglong)]
+    L.qsm_fp_convert_check.restype = STATUS
     L.qsm_norm2_noalloc.argtypes = [I32, ctypes.c_size_t, P, U8, P, P]
     L.qsm_norm2_noalloc.restype = STATUS
     for name, args in SIGNATURES.items():
@@ -206,7 +208,7 @@ def exported_symbols() -> list[str]:
     return sorted(list(SIGNATURES) + list(SESSION_SIGNATURES) + list(HOST_SIGNATURES) + ["qsm_ctx_create", "qsm_ctx_destroy", "qsm_ctx_set_stream",
                                       "qsm_ctx_get_stream", "qsm_ctx_set_verbose", "qsm_ctx_set_debug", "qsm_last_error",
                                       "qsm_status_string", "qsm_abi_version", "qsm_norm2_noalloc",
-                                      "qsm_fp_pipe_rate"])
+                                      "qsm_fp_pipe_rate", "qsm_fp_convert_check"])
 
 
 class Context:

@@ -94,6 +94,55 @@ __global__ void __launch_bounds__(256) fp_rate_k(T *out, T m, T c, int iters)
     if (s == (T)-1) out[0] = s;  // keeps the chains live; never true for these inputs
 }
 
+// f32_to_f64 / f64_to_f32 against the device's conversions: every float
+// (base .. base + count), and `count` doubles from a 64-bit mix of the index,
+// one in eight drawn at random and the rest aimed at the cases that need
+// care (float rounding ties, the float exponent range and its edges,
+// subnormal and overflowing results).
+__device__ __forceinline__ uint64_t cvt_mix(uint64_t z)
+{
+    z += 0x9e3779b97f4a7c15ull;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
+__global__ void cvt_check_k(unsigned long long nfloat, unsigned long long ndouble, unsigned long long *bad)
+{
+    unsigned long long nb = 0;
+    const unsigned long long st = (unsigned long long)gridDim.x * blockDim.x;
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < nfloat; i += st) {
+        const float f = __uint_as_float((uint32_t)i);
+        nb += __double_as_longlong((double)f) != __double_as_longlong(f32_to_f64(f));
+    }
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < ndouble; i += st) {
+        uint64_t u = cvt_mix(i);
+        const uint64_t sign = u & 0x8000000000000000ull, ex = cvt_mix(i ^ 0x5bd1e995ull);
+        switch (i & 7) {
+        case 1:  // exponents around the float range
+            u = (u & 0x800fffffffffffffull) | ((860 + ex % 300) << 52);
+            break;
+        case 2:  // exact ties between two floats
+            u = (u & 0xfff0000000000000ull) | (((u >> 12) & 0x7fffffull) << 29) | (1ull << 28);
+            break;
+        case 3:  // ties or float-exact values near the subnormal and overflow edges
+            u = sign | ((860 + ex % 300) << 52) | (((u >> 20) & 0x7fffffull) << 29) | ((ex >> 40) & 1 ? (1ull << 28) : 0);
+            break;
+        case 4:  // next to 2^128
+            u = (u & 0x800fffffffffffffull) | ((1140 + ex % 20) << 52);
+            break;
+        case 5:  // double subnormals and tiny normals
+            u = (u & 0x800fffffffffffffull) | ((ex % 40) << 52);
+            break;
+        default:
+            break;
+        }
+        const double d = __longlong_as_double((long long)u);
+        nb += __float_as_uint((float)d) != __float_as_uint(f64_to_f32(d));
+    }
+    if (nb) atomicAdd(bad, nb);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(RED_BLOCK) lane_dot_kernel(const T *__restrict__ x, const T *__restrict__ y,
                                                              size_t n, T *part, unsigned int *count, double *out)
@@ -325,6 +374,22 @@ qsm_status qsm_fp_pipe_rate(qsm_ctx *ctx, qsm_dtype dtype, double *ops_per_s)
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     *ops_per_s = (double)grid.x * block.x * 16.0 * iters / (best * 1e-3);
+    return QSM_OK;
+}
+
+qsm_status qsm_fp_convert_check(qsm_ctx *ctx, unsigned long long *mismatches)
+{
+    if (!ctx || !mismatches) return QSM_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    int sms = 0;
+    QSM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    unsigned long long *bad = (unsigned long long *)ctx->red_out;
+    QSM_CUDA(cudaMemsetAsync(bad, 0, sizeof(unsigned long long), ctx->stream));
+    cvt_check_k<<<(unsigned)sms * 8, 256, 0, ctx->stream>>>(1ull << 32, 1ull << 30, bad);
+    QSM_CUDA(cudaGetLastError());
+    QSM_CUDA(cudaMemcpyAsync(ctx->host_out, bad, sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
+    QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+    *mismatches = *(unsigned long long *)ctx->host_out;
     return QSM_OK;
 }
 

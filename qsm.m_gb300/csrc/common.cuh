@@ -178,6 +178,61 @@ __device__ __forceinline__ T halve_partials(T *sm, int tid, const T *part)
     return halve_block(sm, tid, v);
 }
 
+// FP32 -> FP64 (exact) and FP64 -> FP32 (round to nearest, ties to even)
+// in integer arithmetic, from the IEEE 754 binary32 / binary64 encodings:
+// the bits of the device's own conversions (a NaN keeps its payload and is
+// made quiet), but issued on the integer pipes rather than the FP64 pipe,
+// which this GPU runs at 1/64 of the FP32 rate.  qsm_fp_convert_check
+// compares them with the device's conversions.
+__device__ __forceinline__ double f32_to_f64(float f)
+{
+    const uint32_t u = __float_as_uint(f);
+    const uint64_t s = (uint64_t)(u >> 31) << 63;
+    const uint32_t e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+    uint64_t r;
+    if (e == 0xffu) {  // infinity, NaN (quiet bit set)
+        r = s | (0x7ffull << 52) | ((uint64_t)m << 29) | (m ? (1ull << 51) : 0ull);
+    } else if (e == 0u) {  // zero, or a subnormal made normal: its leading 1 moves to bit 23
+        if (m == 0u) {
+            r = s;
+        } else {
+            const int sh = __clz(m) - 8;
+            r = s | ((uint64_t)(897 - sh) << 52) | ((uint64_t)((m << sh) & 0x7fffffu) << 29);
+        }
+    } else {  // exponent bias 127 -> 1023
+        r = s | ((uint64_t)(e + 896u) << 52) | ((uint64_t)m << 29);
+    }
+    return __longlong_as_double((long long)r);
+}
+
+__device__ __forceinline__ float f64_to_f32(double d)
+{
+    const uint64_t u = (uint64_t)__double_as_longlong(d);
+    const uint32_t s = (uint32_t)(u >> 63) << 31;
+    const int e = (int)((u >> 52) & 0x7ffu);
+    const uint64_t m = u & ((1ull << 52) - 1);
+    uint32_t r;
+    if (e == 0x7ff) {  // infinity, NaN (quiet bit set, top payload bits kept)
+        r = m ? (0x7fc00000u | (uint32_t)(m >> 29)) : 0x7f800000u;
+    } else if (e >= 1151) {  // 2^128 or more: infinity
+        r = 0x7f800000u;
+    } else if (e >= 897) {  // a normal float: keep 23 fraction bits, round on the other 29
+        const uint32_t hi = (uint32_t)(m >> 29), rem = (uint32_t)(m & ((1u << 29) - 1));
+        const uint32_t up = rem > (1u << 28) || (rem == (1u << 28) && (hi & 1u));
+        r = (((uint32_t)(e - 896) << 23) | hi) + up;  // a carry moves into the exponent (up to infinity)
+    } else {  // a subnormal float or zero: the significand in units of 2^-149, rounded
+        const int sh = 926 - e;
+        if (sh >= 54) {
+            r = 0u;  // below half the smallest subnormal
+        } else {
+            const uint64_t M = e ? (m | (1ull << 52)) : m;
+            const uint64_t q = M >> sh, rem = M & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+            r = (uint32_t)q + (uint32_t)(rem > half || (rem == half && (q & 1)));
+        }
+    }
+    return __uint_as_float(s | r);
+}
+
 // out[0] = dot(x, y) (or sum x*x when y == x) in lane order, on ctx->stream,
 // written to device memory `dout`.  T in {float, double}; FP32 inputs
 // accumulate in FP32 like sdot and the result is widened.

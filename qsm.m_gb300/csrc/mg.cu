@@ -24,7 +24,11 @@
 //                           keeps the lane order; no host round trips
 //   PCG                     the BLAS-1 steps fused into four kernels on the
 //                           lane-dot grid; scalars stay on the device and the
-//                           host reads ||r|| once per iteration
+//                           host reads ||r|| once per iteration; where the
+//                           iterate and residual are +0 outside G, warps visit
+//                           only their lane-grid segments that hold G.  The
+//                           mixed solver (FP32 V-cycle) contracts the FP64
+//                           recurrence's multiply-adds into FMAs
 #include <math.h>
 #include <stdlib.h>
 #include <mutex>
@@ -402,6 +406,44 @@ __global__ void gs_list_k(T *v, const T *__restrict__ f, const uint32_t *__restr
     if (e & skip) return;
     const size_t l = e & BL_IDX;
     v[l] = c.hh * (f[l] + (c.hx * (v[l - 1] + v[l + 1]) + c.hy * (v[l - nx] + v[l + nx]) + c.hz * (v[l - nxny] + v[l + nxny])));
+}
+
+// gs_list_k for FP32 passes, which are bound by load latency rather than by
+// arithmetic: a thread takes GS_PER entries at a stride of the grid and issues
+// all their loads before its first store.  A pass reads only the other
+// colour, so the order of its updates does not change a bit.
+constexpr int GS_PER = 4;
+template <typename T>
+__global__ void gs_list_ilp_k(T *v, const T *__restrict__ f, const uint32_t *__restrict__ list, unsigned cnt,
+                              uint32_t skip, GsC<T> c, size_t nx, size_t nxny)
+{
+    const unsigned t0 = blockIdx.x * blockDim.x + threadIdx.x, st = gridDim.x * blockDim.x;
+    size_t l[GS_PER];
+    bool on[GS_PER];
+#pragma unroll
+    for (int u = 0; u < GS_PER; ++u) {
+        const unsigned m = t0 + u * st;
+        const uint32_t e = m < cnt ? list[m] : 0u;
+        on[u] = m < cnt && !(e & skip);
+        l[u] = e & BL_IDX;
+    }
+    T fv[GS_PER], a[GS_PER][6];
+#pragma unroll
+    for (int u = 0; u < GS_PER; ++u) {
+        if (!on[u]) continue;
+        const size_t q = l[u];
+        fv[u] = f[q];
+        a[u][0] = v[q - 1];
+        a[u][1] = v[q + 1];
+        a[u][2] = v[q - nx];
+        a[u][3] = v[q + nx];
+        a[u][4] = v[q - nxny];
+        a[u][5] = v[q + nxny];
+    }
+#pragma unroll
+    for (int u = 0; u < GS_PER; ++u)
+        if (on[u])
+            v[l[u]] = c.hh * (fv[u] + (c.hx * (a[u][0] + a[u][1]) + c.hy * (a[u][2] + a[u][3]) + c.hz * (a[u][4] + a[u][5])));
 }
 
 // ---------------------------------------------------------------------------
@@ -903,6 +945,7 @@ __device__ void cta_gs(T *v, const T *f, const uint8_t *G, GsC<T> c, Dims d, int
 constexpr uint32_t CS_IDX = 0x0FFFFFFFu;
 constexpr uint32_t CS_I1 = 1u << 28;    // i == 1
 constexpr uint32_t CS_INX2 = 1u << 29;  // i == nx - 2
+constexpr uint32_t CS_ABSENT = 1u << 30; // no entry (register-held shares)
 
 // Shared memory of coarse_solve_k for an n-voxel grid: v, f, sq (n each),
 // the lane-order block sums, G (n bytes), two colour lists of (n + 1) / 2
@@ -927,6 +970,51 @@ __device__ __forceinline__ void cs_pass(T *v, const T *f, const uint32_t *list, 
                                c.hz * (v[l - nxny] + v[l + nxny])));
     }
     __syncthreads();
+}
+
+// A thread's entries of one colour list, held in registers through the
+// 512 passes of an outer iteration (the lists and f do not change during a
+// call): at most CS_PER entries each, taken at a stride of the CTA.
+constexpr int CS_PER = 2;
+template <typename T>
+struct CsShare {
+    int l[CS_PER];
+    T f[CS_PER];
+    uint32_t fl[CS_PER];
+    __device__ __forceinline__ void load(const uint32_t *list, int cnt, const T *fs)
+    {
+#pragma unroll
+        for (int u = 0; u < CS_PER; ++u) {
+            const int m = threadIdx.x + u * CS_THREADS;
+            const uint32_t e = m < cnt ? list[m] : CS_ABSENT;
+            l[u] = (int)(e & CS_IDX);
+            fl[u] = e & ~CS_IDX;
+            f[u] = m < cnt ? fs[l[u]] : (T)0;
+        }
+    }
+    // one colour pass (entries flagged `skip` or absent are left alone), then the barrier
+    __device__ __forceinline__ void pass(T *v, uint32_t skip, GsC<T> c, int nx, int nxny) const
+    {
+#pragma unroll
+        for (int u = 0; u < CS_PER; ++u) {
+            if (fl[u] & (skip | CS_ABSENT)) continue;
+            const int q = l[u];
+            v[q] = c.hh * (f[u] + (c.hx * (v[q - 1] + v[q + 1]) + c.hy * (v[q - nx] + v[q + nx]) +
+                                   c.hz * (v[q - nxny] + v[q + nxny])));
+        }
+        __syncthreads();
+    }
+};
+
+// 128 sweeps of (pass over a, pass over b skipping the entries flagged skipb)
+template <typename T>
+__device__ __forceinline__ void cs_sweeps(T *v, const CsShare<T> &a, const CsShare<T> &b, uint32_t skipb, GsC<T> c,
+                                          int nx, int nxny)
+{
+    for (int s = 0; s < 128; ++s) {
+        a.pass(v, 0u, c, nx, nxny);
+        b.pass(v, skipb, c, nx, nxny);
+    }
 }
 
 // The coarsest solve (mgpcg_mex.c:265-275) of a grid one CTA holds in shared
@@ -991,16 +1079,32 @@ __global__ void __launch_bounds__(CS_THREADS) coarse_solve_k(T *gv, const T *__r
     const int rpar0 = (nx + 1) & 1;
     const uint32_t *lr0 = rpar0 ? list1 : list0, *lr1 = rpar0 ? list0 : list1;
     const int cr0 = rpar0 ? n1 : n0, cr1 = rpar0 ? n0 : n1;
+    // lists that fit are held in registers (both colours, CS_PER entries per thread)
+    const bool regs = n0 <= CS_PER * CS_THREADS && n1 <= CS_PER * CS_THREADS;
+    CsShare<T> s0, s1;
+    if (regs) {
+        s0.load(list0, n0, f);
+        s1.load(list1, n1, f);
+    }
     int outer = 0;
     for (int it = 0; it < 1024; ++it) {
         outer = it + 1;
-        for (int s = 0; s < 128; ++s) {  // reverse sweeps
-            cs_pass<T>(v, f, lr0, cr0, 0u, gc, nx, nxny);
-            cs_pass<T>(v, f, lr1, cr1, CS_INX2, gc, nx, nxny);
-        }
-        for (int s = 0; s < 128; ++s) {  // forward sweeps
-            cs_pass<T>(v, f, list0, n0, 0u, gc, nx, nxny);
-            cs_pass<T>(v, f, list1, n1, CS_I1, gc, nx, nxny);
+        if (regs) {
+            if (rpar0) {  // reverse sweeps, then forward sweeps
+                cs_sweeps<T>(v, s1, s0, CS_INX2, gc, nx, nxny);
+            } else {
+                cs_sweeps<T>(v, s0, s1, CS_INX2, gc, nx, nxny);
+            }
+            cs_sweeps<T>(v, s0, s1, CS_I1, gc, nx, nxny);
+        } else {
+            for (int s = 0; s < 128; ++s) {  // reverse sweeps
+                cs_pass<T>(v, f, lr0, cr0, 0u, gc, nx, nxny);
+                cs_pass<T>(v, f, lr1, cr1, CS_INX2, gc, nx, nxny);
+            }
+            for (int s = 0; s < 128; ++s) {  // forward sweeps
+                cs_pass<T>(v, f, list0, n0, 0u, gc, nx, nxny);
+                cs_pass<T>(v, f, list1, n1, CS_I1, gc, nx, nxny);
+            }
         }
         // residual into r (global copy kept like the reference) and its norm
         for (int l = tid; l < n; l += CS_THREADS) {
@@ -1569,8 +1673,12 @@ static qsm_status list_sweeps(qsm_ctx *ctx, T *v, const T *f, uint32_t *const li
         for (int q = 0; q < 2; ++q) {
             const int par = par0 ^ q;
             if (!cnt[par]) continue;
-            gs_list_k<T><<<(cnt[par] + 255) / 256, 256, 0, ctx->stream>>>(v, f, lists[par], cnt[par], q ? skip : 0u, c,
-                                                                         d.nx, d.nxny());
+            if (sizeof(T) == 4)
+                gs_list_ilp_k<T><<<(cnt[par] + 256 * GS_PER - 1) / (256 * GS_PER), 256, 0, ctx->stream>>>(
+                    v, f, lists[par], cnt[par], q ? skip : 0u, c, d.nx, d.nxny());
+            else
+                gs_list_k<T><<<(cnt[par] + 255) / 256, 256, 0, ctx->stream>>>(v, f, lists[par], cnt[par],
+                                                                             q ? skip : 0u, c, d.nx, d.nxny());
         }
     QSM_CUDA(cudaGetLastError());
     return QSM_OK;
@@ -1709,7 +1817,6 @@ static qsm_status hier_free(qsm_ctx *ctx, Hier<T> &H)
     return dfree(ctx, H.blk);
 }
 
-// masks of every level (mx_init): coarsen, boundary masks; FMG restricts f.
 template <typename T>
 static qsm_status hier_masks(qsm_ctx *ctx, Hier<T> &H, bool restrict_f)
 {
@@ -1897,6 +2004,36 @@ __device__ __forceinline__ bool lane_fold(T *sm, T acc, T *part, unsigned *count
     return true;
 }
 
+// The mixed solver's PCG (an FP64 recurrence around an FP32 V-cycle, FM)
+// contracts its multiply-adds into FP64 FMAs and converts between the two
+// precisions in integer arithmetic: on this GPU the FP64 pipe bounds these
+// steps, and that takes a third of their FP64 instructions off it.  The FP64
+// and FP32 solvers keep the reference's separate products and sums.
+template <bool FM, typename T>
+__device__ __forceinline__ T pmad(T x, T y, T z)
+{
+    if constexpr (FM)
+        return fma(x, y, z);
+    else
+        return x * y + z;
+}
+template <typename TP, typename TM>
+__device__ __forceinline__ TP widen(TM v)
+{
+    if constexpr (sizeof(TP) == 8 && sizeof(TM) == 4)
+        return f32_to_f64(v);
+    else
+        return (TP)v;
+}
+template <typename TM, typename TP>
+__device__ __forceinline__ TM narrow(TP v)
+{
+    if constexpr (sizeof(TP) == 8 && sizeof(TM) == 4)
+        return f64_to_f32(v);
+    else
+        return (TM)v;
+}
+
 // Voxels outside G in the PCG steps (sk: the level-0 mask, when the solve
 // runs its masked form).  That form runs when the initial residual and
 // iterate are exactly +0 outside G (pcg_zero_outside_k checks it per solve,
@@ -1978,6 +2115,7 @@ __global__ void __launch_bounds__(RED_BLOCK) pcg_rho_k(const TP *__restrict__ r,
                                                        const TM *__restrict__ vm, const uint8_t *__restrict__ sk,
                                                        Segs sg, size_t n, TP *part, unsigned *count, double *sc)
 {
+    constexpr bool FM = sizeof(TP) != sizeof(TM);
     __shared__ TP sm[RED_BLOCK];
     const size_t L = RED_LANES;
     size_t l = (size_t)blockIdx.x * RED_BLOCK + threadIdx.x;
@@ -1994,14 +2132,14 @@ __global__ void __launch_bounds__(RED_BLOCK) pcg_rho_k(const TP *__restrict__ r,
                 on[u] = e[u] < n && sk[e[u]];
                 if (e[u] < n) {
                     a[u] = r[e[u]];
-                    b[u] = vm ? (TP)vm[e[u]] : q[e[u]];
+                    b[u] = vm ? widen<TP, TM>(vm[e[u]]) : q[e[u]];
                 }
             }
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 if (!on[u]) continue;
                 if (vm) q[e[u]] = b[u];
-                acc = acc + a[u] * b[u];
+                acc = pmad<FM>(a[u], b[u], acc);
             }
         }
         l = n;
@@ -2014,21 +2152,21 @@ __global__ void __launch_bounds__(RED_BLOCK) pcg_rho_k(const TP *__restrict__ r,
             on[u] = pcg_on(sk, l + u * L);
             if (on[u]) {
                 a[u] = r[l + u * L];
-                b[u] = vm ? (TP)vm[l + u * L] : q[l + u * L];
+                b[u] = vm ? widen<TP, TM>(vm[l + u * L]) : q[l + u * L];
             }
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             if (!on[u]) continue;
             if (vm) q[l + u * L] = b[u];
-            acc = acc + a[u] * b[u];
+            acc = pmad<FM>(a[u], b[u], acc);
         }
     }
     for (; l < n; l += L) {
         if (!pcg_on(sk, l)) continue;
-        const TP b = vm ? (TP)vm[l] : q[l];
+        const TP b = vm ? widen<TP, TM>(vm[l]) : q[l];
         if (vm) q[l] = b;
-        acc = acc + r[l] * b;
+        acc = pmad<FM>(r[l], b, acc);
     }
     TP tot;
     if (lane_fold(sm, acc, part, count, &tot) && threadIdx.x == 0) {
@@ -2040,7 +2178,7 @@ __global__ void __launch_bounds__(RED_BLOCK) pcg_rho_k(const TP *__restrict__ r,
 }
 
 // p = beta * p, then p = p + 1 * q (with segments: on the lane grid)
-template <typename T>
+template <typename T, bool FM>
 __global__ void pcg_p_k(T *__restrict__ p, const T *__restrict__ q, const uint8_t *__restrict__ sk, Segs sg,
                         size_t n, const double *sc)
 {
@@ -2063,17 +2201,27 @@ __global__ void pcg_p_k(T *__restrict__ p, const T *__restrict__ q, const uint8_
             }
 #pragma unroll
             for (int u = 0; u < 4; ++u)
-                if (on[u]) p[e[u]] = beta * pv[u] + qv[u];
+                if (on[u]) p[e[u]] = pmad<FM>(beta, pv[u], qv[u]);
         }
         return;
     }
     for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x)
-        if (pcg_on(sk, l)) p[l] = beta * p[l] + q[l];
+        if (pcg_on(sk, l)) p[l] = pmad<FM>(beta, p[l], q[l]);
 }
 
 // q = lapmg(p) on G (interior), then q = -1 * q everywhere; pq = p . q;
 // alpha = rho / pq
-template <typename T>
+template <typename T, bool FM>
+__device__ __forceinline__ T pcg_lap(const T *__restrict__ p, size_t l, size_t nx, size_t nxny, const LapC<T> &c, T pl)
+{
+    const T sx = p[l - 1] + p[l + 1], sy = p[l - nx] + p[l + nx], sz = p[l - nxny] + p[l + nxny];
+    if constexpr (FM)
+        return pmad<true>(c.hz, sz, pmad<true>(c.hy, sy, pmad<true>(c.hx, sx, c.hh * pl)));
+    else
+        return c.hh * pl + c.hx * sx + c.hy * sy + c.hz * sz;
+}
+
+template <typename T, bool FM>
 __global__ void __launch_bounds__(RED_BLOCK) pcg_q_k(T *__restrict__ q, const T *__restrict__ p,
                                                      const uint8_t *__restrict__ G, const uint8_t *__restrict__ sk,
                                                      Segs sg, LapC<T> c, Dims d, T *part, unsigned *count, double *sc)
@@ -2096,10 +2244,9 @@ __global__ void __launch_bounds__(RED_BLOCK) pcg_q_k(T *__restrict__ q, const T 
                 if (!on[u]) continue;
                 const size_t l = e[u];
                 const T pl = p[l];
-                const T qv = neg_bits(c.hh * pl + c.hx * (p[l - 1] + p[l + 1]) + c.hy * (p[l - nx] + p[l + nx]) +
-                                      c.hz * (p[l - nxny] + p[l + nxny]));
+                const T qv = neg_bits(pcg_lap<T, FM>(p, l, nx, nxny, c, pl));
                 q[l] = qv;
-                acc = acc + pl * qv;
+                acc = pmad<FM>(pl, qv, acc);
             }
         }
         T tot;
@@ -2118,13 +2265,12 @@ __global__ void __launch_bounds__(RED_BLOCK) pcg_q_k(T *__restrict__ q, const T 
             const T pl = p[l];
             T qv;
             if (i >= 1 && j >= 1 && k >= 1 && i + 1 < nx && j + 1 < d.ny && k + 1 < d.nz && G[l])
-                qv = c.hh * pl + c.hx * (p[l - 1] + p[l + 1]) + c.hy * (p[l - nx] + p[l + nx]) +
-                     c.hz * (p[l - nxny] + p[l + nxny]);
+                qv = pcg_lap<T, FM>(p, l, nx, nxny, c, pl);
             else
                 qv = q[l];
             qv = neg_bits(qv);
             q[l] = qv;
-            acc = acc + pl * qv;
+            acc = pmad<FM>(pl, qv, acc);
         }
         i += Li;
         const size_t cj = i >= nx;
@@ -2150,6 +2296,7 @@ __global__ void __launch_bounds__(RED_BLOCK) pcg_xr_k(TP *__restrict__ x, const 
                                                       TM *__restrict__ rm, const uint8_t *__restrict__ sk, Segs sg,
                                                       size_t n, TP *part, unsigned *count, double *sc)
 {
+    constexpr bool FM = sizeof(TP) != sizeof(TM);
     __shared__ TP sm[RED_BLOCK];
     const TP a = (TP)sc[S_A], na = (TP)(-sc[S_A]);
     const size_t L = RED_LANES;
@@ -2175,11 +2322,11 @@ __global__ void __launch_bounds__(RED_BLOCK) pcg_xr_k(TP *__restrict__ x, const 
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 if (!on[u]) continue;
-                x[e[u]] = xv[u] + a * pv[u];
-                const TP rn = rv[u] + na * qv[u];
+                x[e[u]] = pmad<FM>(a, pv[u], xv[u]);
+                const TP rn = pmad<FM>(na, qv[u], rv[u]);
                 r[e[u]] = rn;
-                if (rm) rm[e[u]] = (TM)rn;
-                acc = acc + rn * rn;
+                if (rm) rm[e[u]] = narrow<TM, TP>(rn);
+                acc = pmad<FM>(rn, rn, acc);
             }
         }
         l = n;
@@ -2200,20 +2347,20 @@ __global__ void __launch_bounds__(RED_BLOCK) pcg_xr_k(TP *__restrict__ x, const 
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             if (!on[u]) continue;
-            x[l + u * L] = xv[u] + a * pv[u];
-            const TP rn = rv[u] + na * qv[u];
+            x[l + u * L] = pmad<FM>(a, pv[u], xv[u]);
+            const TP rn = pmad<FM>(na, qv[u], rv[u]);
             r[l + u * L] = rn;
-            if (rm) rm[l + u * L] = (TM)rn;
-            acc = acc + rn * rn;
+            if (rm) rm[l + u * L] = narrow<TM, TP>(rn);
+            acc = pmad<FM>(rn, rn, acc);
         }
     }
     for (; l < n; l += L) {
         if (!pcg_on(sk, l)) continue;
-        x[l] = x[l] + a * p[l];
-        const TP rn = r[l] + na * q[l];
+        x[l] = pmad<FM>(a, p[l], x[l]);
+        const TP rn = pmad<FM>(na, q[l], r[l]);
         r[l] = rn;
-        if (rm) rm[l] = (TM)rn;
-        acc = acc + rn * rn;
+        if (rm) rm[l] = narrow<TM, TP>(rn);
+        acc = pmad<FM>(rn, rn, acc);
     }
     TP tot;
     if (lane_fold(sm, acc, part, count, &tot) && threadIdx.x == 0) {
@@ -2258,7 +2405,7 @@ static qsm_status pcg(qsm_ctx *ctx, const Dims &d, const TP *v0, const TP *f, co
     Hier<TM> H;
     QSM_TRY(hier_init<TM>(ctx, H, nl, dp, h));
     H.v0_zero_outside = true;  // the preconditioner starts from v = 0 every time
-    const bool same = sizeof(TP) == sizeof(TM);
+    constexpr bool same = sizeof(TP) == sizeof(TM);
     // PCG vectors: x, p (and r, q when the V-cycle runs in another precision)
     void *pv = nullptr;
     const size_t vb = al256(n * sizeof(TP)), scb = al256(S_N * sizeof(double) + 256);
@@ -2330,9 +2477,9 @@ static qsm_status pcg(qsm_ctx *ctx, const Dims &d, const TP *v0, const TP *f, co
         pcg_rho_k<TP, TM><<<RED_NBLK, RED_BLOCK, 0, ctx->stream>>>(r, q, same ? nullptr : H.L[0].v, sk, sg, n,
                                                                    part, ctx->red_count, sc);
         // with segments pcg_p_k runs on the lane grid
-        pcg_p_k<TP><<<sg.k ? RED_NBLK : 1216, RED_BLOCK, 0, ctx->stream>>>(p, q, sk, sg, n, sc);
-        pcg_q_k<TP><<<RED_NBLK, RED_BLOCK, 0, ctx->stream>>>(q, p, H.L[0].G, sk, sg, lc, dp, part, ctx->red_count,
-                                                             sc);
+        pcg_p_k<TP, !same><<<sg.k ? RED_NBLK : 1216, RED_BLOCK, 0, ctx->stream>>>(p, q, sk, sg, n, sc);
+        pcg_q_k<TP, !same><<<RED_NBLK, RED_BLOCK, 0, ctx->stream>>>(q, p, H.L[0].G, sk, sg, lc, dp, part,
+                                                                    ctx->red_count, sc);
         pcg_xr_k<TP, TM><<<RED_NBLK, RED_BLOCK, 0, ctx->stream>>>(x, p, r, q, same ? nullptr : H.L[0].f, sk, sg, n,
                                                                   part, ctx->red_count, sc);
         QSM_CUDA(cudaGetLastError());

@@ -309,3 +309,10 @@ def test_mg_errors(gpu_ctx, qsm):
         qsm.mgpcg_mex(f, f, np.ones((8, 8, 8), np.uint8), [1, 1, 1], 1e-8, 5, -1.0, 1, 1, 1, 1, 2, 17)
     with pytest.raises(qsm.QsmError, match="DIMS"):
         qsm.restrict_mex(np.zeros((9, 9, 9), order="F"), np.zeros((8, 8, 8), order="F"), np.ones((9, 9, 9), np.uint8))
+
+
+def test_fp_convert_exact(gpu_ctx, qsm):
+    """The mixed solver's integer-arithmetic FP32 <-> FP64 conversions give
+    the device's own conversion bits on every float and on 2^30 doubles aimed
+    at rounding ties, subnormal and overflowing results."""
+    assert qsm.fp_convert_check(ctx=gpu_ctx) == 0
