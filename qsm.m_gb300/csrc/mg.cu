@@ -974,8 +974,9 @@ __device__ __forceinline__ void cs_pass(T *v, const T *f, const uint32_t *list, 
 
 // A thread's entries of one colour list, held in registers through the
 // 512 passes of an outer iteration (the lists and f do not change during a
-// call): at most CS_PER entries each, taken at a stride of the CTA.
-constexpr int CS_PER = 2;
+// call): at most CS_PER entries each, taken at a stride of the CTA, so lists
+// of up to 2048 entries per colour are held.
+constexpr int CS_PER = 2048 / CS_THREADS;
 template <typename T>
 struct CsShare {
     int l[CS_PER];
@@ -1730,6 +1731,94 @@ __global__ void residual_list_k(T *r, const T *__restrict__ f, const T *__restri
     r[l] = f[l] + (c.hh * x[l] + c.hx * (x[l - 1] + x[l + 1]) + c.hy * (x[l - nx] + x[l + nx]) + c.hz * (x[l - nxny] + x[l + nxny]));
 }
 
+// residual_list_k for FP32 levels (bound by load latency): GS_PER entries
+// per thread at a stride of the grid, every load issued before a store.
+template <typename T>
+__global__ void residual_list_ilp_k(T *r, const T *__restrict__ f, const T *__restrict__ x,
+                                    const uint32_t *__restrict__ l0, unsigned c0, const uint32_t *__restrict__ l1,
+                                    unsigned c1, LapC<T> c, size_t nx, size_t nxny)
+{
+    const unsigned t0 = blockIdx.x * blockDim.x + threadIdx.x, st = gridDim.x * blockDim.x;
+    size_t l[GS_PER];
+    bool on[GS_PER];
+#pragma unroll
+    for (int u = 0; u < GS_PER; ++u) {
+        const unsigned m = t0 + u * st;
+        on[u] = m < c0 + c1;
+        l[u] = on[u] ? ((m < c0 ? l0[m] : l1[m - c0]) & BL_IDX) : 0;
+    }
+    T fv[GS_PER], a[GS_PER][7];
+#pragma unroll
+    for (int u = 0; u < GS_PER; ++u) {
+        if (!on[u]) continue;
+        const size_t q = l[u];
+        fv[u] = f[q];
+        a[u][0] = x[q];
+        a[u][1] = x[q - 1];
+        a[u][2] = x[q + 1];
+        a[u][3] = x[q - nx];
+        a[u][4] = x[q + nx];
+        a[u][5] = x[q - nxny];
+        a[u][6] = x[q + nxny];
+    }
+#pragma unroll
+    for (int u = 0; u < GS_PER; ++u)
+        if (on[u])
+            r[l[u]] = fv[u] + (c.hh * a[u][0] + c.hx * (a[u][1] + a[u][2]) + c.hy * (a[u][3] + a[u][4]) +
+                               c.hz * (a[u][5] + a[u][6]));
+}
+
+// The V-cycle's correction of an FP32 level whose v is +0 outside G
+// (prolong_k<T, true, true>) from its G lists: x += the interpolated coarse
+// value on each G voxel, GS_PER entries per thread.  The fine voxel
+// (i, j, k) takes coarse parent i2 = (i + 1) / 2 and case bit (i + 1) mod 2
+// per axis, as in prolong_k; the voxels of one colour in one x row share
+// their case, so a warp's lanes mostly run one case.
+template <typename T>
+__global__ void correct_list_k(T *x, const T *__restrict__ x2, const uint32_t *__restrict__ l0, unsigned c0,
+                               const uint32_t *__restrict__ l1, unsigned c1, uint32_t nx, uint32_t nxny,
+                               uint32_t nx2, uint32_t nxny2)
+{
+    const unsigned t0 = blockIdx.x * blockDim.x + threadIdx.x, st = gridDim.x * blockDim.x;
+    uint32_t l[GS_PER], l2[GS_PER];
+    int cs[GS_PER];
+    bool on[GS_PER];
+#pragma unroll
+    for (int u = 0; u < GS_PER; ++u) {
+        const unsigned m = t0 + u * st;
+        on[u] = m < c0 + c1;
+        const uint32_t q = on[u] ? ((m < c0 ? l0[m] : l1[m - c0]) & BL_IDX) : 0u;
+        const uint32_t k = q / nxny, rem = q - k * nxny, j = rem / nx, i = rem - j * nx;
+        l[u] = q;
+        l2[u] = (i + 1) / 2 + nx2 * ((j + 1) / 2) + nxny2 * ((k + 1) / 2);
+        cs[u] = (int)(((i + 1) & 1) + 2 * ((j + 1) & 1) + 4 * ((k + 1) & 1));
+    }
+    T val[GS_PER], xv[GS_PER];
+    const uint32_t ox = 1, oy = nx2, oz = nxny2;
+#pragma unroll
+    for (int u = 0; u < GS_PER; ++u) {
+        if (!on[u]) continue;
+        const uint32_t q2 = l2[u];
+        const T c0v = x2[q2];
+        xv[u] = x[l[u]];
+        switch (cs[u]) {
+        case 0: val[u] = c0v; break;
+        case 1: val[u] = (T)0.5 * (c0v + x2[q2 + ox]); break;
+        case 2: val[u] = (T)0.5 * (c0v + x2[q2 + oy]); break;
+        case 4: val[u] = (T)0.5 * (c0v + x2[q2 + oz]); break;
+        case 3: val[u] = (T)0.25 * (c0v + x2[q2 + ox] + x2[q2 + oy] + x2[q2 + ox + oy]); break;
+        case 5: val[u] = (T)0.25 * (c0v + x2[q2 + ox] + x2[q2 + oz] + x2[q2 + ox + oz]); break;
+        case 6: val[u] = (T)0.25 * (c0v + x2[q2 + oy] + x2[q2 + oz] + x2[q2 + oy + oz]); break;
+        default:
+            val[u] = (T)0.125 * (c0v + x2[q2 + ox] + x2[q2 + oy] + x2[q2 + oz] + x2[q2 + ox + oy] + x2[q2 + ox + oz] +
+                                 x2[q2 + oy + oz] + x2[q2 + ox + oy + oz]);
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < GS_PER; ++u)
+        if (on[u]) x[l[u]] = xv[u] + val[u];
+}
+
 // restriction onto the coarse level's G voxels from its colour lists
 // (restrict_k without its zero writes: the coarse f outside G is zeroed at
 // set-up and nothing writes anything else there)
@@ -1765,14 +1854,35 @@ static qsm_status level_restrict(qsm_ctx *ctx, Level<T> &C, const Level<T> &L)
     return QSM_OK;
 }
 
+// the V-cycle's correction of level l from level l + 1 (clean: v is +0 outside G)
+template <typename T>
+static qsm_status level_correct(qsm_ctx *ctx, Level<T> &L, const Level<T> &C, bool clean)
+{
+    // from lists where they are long (~36 against ~43 us for a 258^3 level's 5.5M G voxels);
+    // the grid kernel stays faster on small levels
+    const unsigned n = L.gl[0] ? L.gn[0] + L.gn[1] : 0;
+    if (sizeof(T) != 4 || !clean || n < (1u << 20) || L.n >= ((size_t)1 << 28) || C.d.nx < 3 || C.d.ny < 3 ||
+        C.d.nz < 3)
+        return prolong<T>(ctx, L.v, C.v, L.G, L.d, C.d, true, clean);
+    correct_list_k<T><<<(n + 256 * GS_PER - 1) / (256 * GS_PER), 256, 0, ctx->stream>>>(
+        L.v, C.v, L.gl[0], L.gn[0], L.gl[1], L.gn[1], (uint32_t)L.d.nx, (uint32_t)L.d.nxny(), (uint32_t)C.d.nx,
+        (uint32_t)C.d.nxny());
+    QSM_CUDA(cudaGetLastError());
+    return QSM_OK;
+}
+
 template <typename T>
 static qsm_status level_residual(qsm_ctx *ctx, Level<T> &L)
 {
     if (!L.gl[0]) return residual<T>(ctx, L.r, L.f, L.v, L.G, L.h, L.d);
     const unsigned n = L.gn[0] + L.gn[1];
     if (n == 0 || L.d.nx < 3 || L.d.ny < 3 || L.d.nz < 3) return QSM_OK;
-    residual_list_k<T><<<(n + 255) / 256, 256, 0, ctx->stream>>>(L.r, L.f, L.v, L.gl[0], L.gn[0], L.gl[1], L.gn[1],
-                                                                 lap_consts<T>(L.h), L.d.nx, L.d.nxny());
+    if (sizeof(T) == 4)
+        residual_list_ilp_k<T><<<(n + 256 * GS_PER - 1) / (256 * GS_PER), 256, 0, ctx->stream>>>(
+            L.r, L.f, L.v, L.gl[0], L.gn[0], L.gl[1], L.gn[1], lap_consts<T>(L.h), L.d.nx, L.d.nxny());
+    else
+        residual_list_k<T><<<(n + 255) / 256, 256, 0, ctx->stream>>>(L.r, L.f, L.v, L.gl[0], L.gn[0], L.gl[1],
+                                                                     L.gn[1], lap_consts<T>(L.h), L.d.nx, L.d.nxny());
     QSM_CUDA(cudaGetLastError());
     return QSM_OK;
 }
@@ -1909,7 +2019,7 @@ static qsm_status cycle(qsm_ctx *ctx, Hier<T> &H, int l, int mu, int pre, int po
             if (l + 1 == H.nl - 1) break;
         }
         // every level below the top is zeroed before its cycle; the PCG's top level too
-        QSM_TRY(prolong<T>(ctx, L.v, C.v, L.G, L.d, C.d, true, l > 0 || H.v0_zero_outside));
+        QSM_TRY(level_correct<T>(ctx, L, C, l > 0 || H.v0_zero_outside));
         QSM_TRY(boundary_sweeps<T>(ctx, H, L, bs, false));
         QSM_TRY(smooth<T>(ctx, H, L, post, false));
         return QSM_OK;
