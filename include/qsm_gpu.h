@@ -307,6 +307,23 @@ qsm_status qsm_mgpcg_mixed(qsm_ctx *ctx, const size_t dims[3],
                            int32_t nboundary, int32_t nlevels, int32_t verbose,
                            double *v_out, qsm_mg_info *info);
 
+/* Packed Poisson solves (no reference counterpart: the reference solves one
+ * volume per mgpcg_mex call): `count` solves with shared options, volume b of
+ * size dims[3b..3b+2] with FP64 arrays f[b], mask[b], v_out[b] (host or
+ * device) and initial guess v0[b] (v0 or v0[b] NULL: zeros).  mixed selects the
+ * FP32 V-cycle of qsm_mgpcg_mixed, else all FP64 as qsm_mgpcg.  Solves with a
+ * fixed number of V-cycles (tolmg <= 0, as lbv.m's options), voxel lists on
+ * every level and a coarsest grid one CTA holds advance together, up to 16 at
+ * a time: each PCG iteration launches each of its kernels once for all of
+ * them.  Any other solve runs by itself.  Every v_out[b] equals the solve
+ * alone bit for bit.  info: NULL or `count` entries. */
+qsm_status qsm_mgpcg_batch(qsm_ctx *ctx, int32_t mixed, uint32_t count, const size_t *dims,
+                           const double *const *v0, const double *const *f,
+                           const uint8_t *const *mask, const double vsz[3], double tolcg,
+                           int32_t maxitcg, double tolmg, int32_t maxitmg, int32_t mu,
+                           int32_t npre, int32_t npost, int32_t nboundary, int32_t nlevels,
+                           double *const *v_out, qsm_mg_info *info);
+
 /* v = mg_mex(v, f, mask, vsz, tol, maxit, mu, npre, npost, nboundary, nlevels)
  * Replaces src/utils/poisson_solver/mex/mg_mex.c:55-91. */
 qsm_status qsm_mg(qsm_ctx *ctx, qsm_dtype dtype, const size_t dims[3],

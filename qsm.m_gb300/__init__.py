@@ -643,6 +643,40 @@ def pd_tgv_batch(d2fs, masks, vsz, lam, alpha, tol, maxiter, *, infos=None, ctx=
                      infos=infos, ctx=ctx, outs=outs)
 
 
+def mgpcg_batch(v0s, fs, masks, vsz, tolcg, maxitcg, tolmg, maxitmg, mu, npre, npost, nboundary, nlevels, *,
+                mixed=True, infos=None, ctx=None, outs=None):
+    """[v_b] = mgpcg_mex(v0_b, f_b, mask_b, vsz, ...) for every volume b (FP64 arrays; v0s None or entries None
+    for zeros), packed: solves with tolmg <= 0 advance together, each kernel of a PCG iteration launched once
+    for up to 16 of them.  Each v_b equals the solve alone bit for bit; mixed selects the FP32 V-cycle."""
+    fa = [_Arr(a) for a in fs]
+    ms = [_Arr(a, mask=True) for a in masks]
+    if len(fa) != len(ms):
+        raise ValueError("one mask per volume")
+    if any(a.dt != _lib.QSM_F64 for a in fa):
+        raise TypeError("mgpcg_batch takes FP64 arrays")
+    n = len(fa)
+    v0a = [None if (v0s is None or v0s[b] is None) else _Arr(v0s[b]) for b in range(n)]
+    outs = [_zeros_like(a) for a in fa] if outs is None else list(outs)
+    oa = [_Arr(o, writable=True) for o in outs]
+    dims = (ctypes.c_size_t * (3 * max(n, 1)))(*[x for a in fa for x in a.dims])
+    p0 = (ctypes.c_void_p * max(n, 1))(*[(v.ptr.value if v is not None else None) for v in v0a])
+    pf = (ctypes.c_void_p * max(n, 1))(*[a.ptr.value for a in fa])
+    pm = (ctypes.c_void_p * max(n, 1))(*[m.ptr.value for m in ms])
+    po = (ctypes.c_void_p * max(n, 1))(*[o.ptr.value for o in oa])
+    mis = (MgInfo * max(n, 1))()
+    hists = [np.zeros(max(1, int(maxitcg)), dtype=np.float64) for _ in range(n)]
+    for b in range(n):
+        mis[b].resnorm_hist = hists[b].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    _sync_torch(*(fa + ms + oa + [v for v in v0a if v is not None]))
+    _ctx(ctx).call("qsm_mgpcg_batch", int(bool(mixed)), n, dims, p0, pf, pm, _h(vsz), float(tolcg), int(maxitcg),
+                   float(tolmg), int(maxitmg), int(mu), int(npre), int(npost), int(nboundary), int(nlevels), po, mis)
+    if infos is not None:
+        infos[:] = [dict(iters=mis[b].iters, resnorm=mis[b].resnorm, seconds=mis[b].seconds,
+                         resnorm_hist=hists[b][: mis[b].iters].copy(), coarse_ctas=mis[b].coarse_ctas,
+                         coarse_outer=mis[b].coarse_outer) for b in range(n)]
+    return outs
+
+
 def footprint(kind: str, dims, nlevels: int = 5) -> int:
     """Device bytes a resident job holds: kind in {"tv", "tgv", "mgpcg", "mgpcg_f64"}."""
     k = {"tv": _lib.QSM_JOB_TV, "tgv": _lib.QSM_JOB_TGV, "mgpcg": _lib.QSM_JOB_MGPCG,

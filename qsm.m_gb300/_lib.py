@@ -106,6 +106,7 @@ SIGNATURES = {
     "qsm_dot": [I32, ctypes.c_size_t, P, P, D3],
     "qsm_mgpcg": [I32, SZ3, P, P, U8, D3, DBL, I32, DBL, I32, I32, I32, I32, I32, I32, I32, P, ctypes.POINTER(MgInfo)],
     "qsm_mgpcg_mixed": [SZ3, P, P, U8, D3, DBL, I32, DBL, I32, I32, I32, I32, I32, I32, I32, P, ctypes.POINTER(MgInfo)],
+    "qsm_mgpcg_batch": [I32, U32, P, P, P, P, D3, DBL, I32, DBL, I32, I32, I32, I32, I32, I32, P, P],
     "qsm_mg": [I32, SZ3, P, P, U8, D3, DBL, I32, I32, I32, I32, I32, I32, P, ctypes.POINTER(MgInfo)],
     "qsm_fmg": [I32, SZ3, P, U8, D3, DBL, I32, I32, I32, I32, I32, I32, P, ctypes.POINTER(MgInfo)],
     "qsm_tv_admm": [I32, SZ3, P, U8, D3, D3, DBL, I32, DBL, DBL, I32, DBL, DBL, DBL, DBL, DBL, I32, P,

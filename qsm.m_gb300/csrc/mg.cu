@@ -31,6 +31,8 @@
 //                           recurrence's multiply-adds into FMAs
 #include <math.h>
 #include <stdlib.h>
+#include <algorithm>
+#include <memory>
 #include <mutex>
 #include <set>
 #include <vector>
@@ -414,10 +416,10 @@ __global__ void gs_list_k(T *v, const T *__restrict__ f, const uint32_t *__restr
 // colour, so the order of its updates does not change a bit.
 constexpr int GS_PER = 4;
 template <typename T>
-__global__ void gs_list_ilp_k(T *v, const T *__restrict__ f, const uint32_t *__restrict__ list, unsigned cnt,
-                              uint32_t skip, GsC<T> c, size_t nx, size_t nxny)
+__device__ __forceinline__ void gs_list_ilp_body(T *v, const T *__restrict__ f, const uint32_t *__restrict__ list, unsigned cnt,
+                              uint32_t skip, GsC<T> c, size_t nx, size_t nxny, unsigned blk, unsigned nblk)
 {
-    const unsigned t0 = blockIdx.x * blockDim.x + threadIdx.x, st = gridDim.x * blockDim.x;
+    const unsigned t0 = blk * blockDim.x + threadIdx.x, st = nblk * blockDim.x;
     size_t l[GS_PER];
     bool on[GS_PER];
 #pragma unroll
@@ -444,6 +446,13 @@ __global__ void gs_list_ilp_k(T *v, const T *__restrict__ f, const uint32_t *__r
     for (int u = 0; u < GS_PER; ++u)
         if (on[u])
             v[l[u]] = c.hh * (fv[u] + (c.hx * (a[u][0] + a[u][1]) + c.hy * (a[u][2] + a[u][3]) + c.hz * (a[u][4] + a[u][5])));
+}
+
+template <typename T>
+__global__ void gs_list_ilp_k(T *v, const T *__restrict__ f, const uint32_t *__restrict__ list, unsigned cnt,
+                              uint32_t skip, GsC<T> c, size_t nx, size_t nxny)
+{
+    gs_list_ilp_body<T>(v, f, list, cnt, skip, c, nx, nxny, blockIdx.x, gridDim.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -1024,7 +1033,7 @@ __device__ __forceinline__ void cs_sweeps(T *v, const CsShare<T> &a, const CsSha
 // its updates does not matter: the reference's result bit for bit), which
 // leaves no index arithmetic in the 512 passes of an outer iteration.
 template <typename T>
-__global__ void __launch_bounds__(CS_THREADS) coarse_solve_k(T *gv, const T *__restrict__ gf, const uint8_t *__restrict__ gG,
+__device__ __forceinline__ void coarse_solve_body(T *gv, const T *__restrict__ gf, const uint8_t *__restrict__ gG,
                                                              T *gr, Dims d, GsC<T> gc, LapC<T> lc, double tol,
                                                              int *outer_out)
 {
@@ -1130,6 +1139,14 @@ __global__ void __launch_bounds__(CS_THREADS) coarse_solve_k(T *gv, const T *__r
     }
     for (int l = tid; l < n; l += CS_THREADS) gv[l] = v[l];
     if (tid == 0 && outer_out) *outer_out += outer;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(CS_THREADS) coarse_solve_k(T *gv, const T *__restrict__ gf, const uint8_t *__restrict__ gG,
+                                                             T *gr, Dims d, GsC<T> gc, LapC<T> lc, double tol,
+                                                             int *outer_out)
+{
+    coarse_solve_body<T>(gv, gf, gG, gr, d, gc, lc, tol, outer_out);
 }
 
 // ---------------------------------------------------------------------------
@@ -1734,11 +1751,11 @@ __global__ void residual_list_k(T *r, const T *__restrict__ f, const T *__restri
 // residual_list_k for FP32 levels (bound by load latency): GS_PER entries
 // per thread at a stride of the grid, every load issued before a store.
 template <typename T>
-__global__ void residual_list_ilp_k(T *r, const T *__restrict__ f, const T *__restrict__ x,
+__device__ __forceinline__ void residual_list_ilp_body(T *r, const T *__restrict__ f, const T *__restrict__ x,
                                     const uint32_t *__restrict__ l0, unsigned c0, const uint32_t *__restrict__ l1,
-                                    unsigned c1, LapC<T> c, size_t nx, size_t nxny)
+                                    unsigned c1, LapC<T> c, size_t nx, size_t nxny, unsigned blk, unsigned nblk)
 {
-    const unsigned t0 = blockIdx.x * blockDim.x + threadIdx.x, st = gridDim.x * blockDim.x;
+    const unsigned t0 = blk * blockDim.x + threadIdx.x, st = nblk * blockDim.x;
     size_t l[GS_PER];
     bool on[GS_PER];
 #pragma unroll
@@ -1768,6 +1785,14 @@ __global__ void residual_list_ilp_k(T *r, const T *__restrict__ f, const T *__re
                                c.hz * (a[u][5] + a[u][6]));
 }
 
+template <typename T>
+__global__ void residual_list_ilp_k(T *r, const T *__restrict__ f, const T *__restrict__ x,
+                                    const uint32_t *__restrict__ l0, unsigned c0, const uint32_t *__restrict__ l1,
+                                    unsigned c1, LapC<T> c, size_t nx, size_t nxny)
+{
+    residual_list_ilp_body<T>(r, f, x, l0, c0, l1, c1, c, nx, nxny, blockIdx.x, gridDim.x);
+}
+
 // The V-cycle's correction of an FP32 level whose v is +0 outside G
 // (prolong_k<T, true, true>) from its G lists: x += the interpolated coarse
 // value on each G voxel, GS_PER entries per thread.  The fine voxel
@@ -1775,11 +1800,11 @@ __global__ void residual_list_ilp_k(T *r, const T *__restrict__ f, const T *__re
 // per axis, as in prolong_k; the voxels of one colour in one x row share
 // their case, so a warp's lanes mostly run one case.
 template <typename T>
-__global__ void correct_list_k(T *x, const T *__restrict__ x2, const uint32_t *__restrict__ l0, unsigned c0,
+__device__ __forceinline__ void correct_list_body(T *x, const T *__restrict__ x2, const uint32_t *__restrict__ l0, unsigned c0,
                                const uint32_t *__restrict__ l1, unsigned c1, uint32_t nx, uint32_t nxny,
-                               uint32_t nx2, uint32_t nxny2)
+                               uint32_t nx2, uint32_t nxny2, unsigned blk, unsigned nblk)
 {
-    const unsigned t0 = blockIdx.x * blockDim.x + threadIdx.x, st = gridDim.x * blockDim.x;
+    const unsigned t0 = blk * blockDim.x + threadIdx.x, st = nblk * blockDim.x;
     uint32_t l[GS_PER], l2[GS_PER];
     int cs[GS_PER];
     bool on[GS_PER];
@@ -1819,14 +1844,22 @@ __global__ void correct_list_k(T *x, const T *__restrict__ x2, const uint32_t *_
         if (on[u]) x[l[u]] = xv[u] + val[u];
 }
 
+template <typename T>
+__global__ void correct_list_k(T *x, const T *__restrict__ x2, const uint32_t *__restrict__ l0, unsigned c0,
+                               const uint32_t *__restrict__ l1, unsigned c1, uint32_t nx, uint32_t nxny,
+                               uint32_t nx2, uint32_t nxny2)
+{
+    correct_list_body<T>(x, x2, l0, c0, l1, c1, nx, nxny, nx2, nxny2, blockIdx.x, gridDim.x);
+}
+
 // restriction onto the coarse level's G voxels from its colour lists
 // (restrict_k without its zero writes: the coarse f outside G is zeroed at
 // set-up and nothing writes anything else there)
 template <typename T>
-__global__ void restrict_list_k(T *x2, const T *__restrict__ x, const uint32_t *__restrict__ l0, unsigned c0,
-                                const uint32_t *__restrict__ l1, unsigned c1, uint32_t nx2, uint32_t nxny2, Dims d)
+__device__ __forceinline__ void restrict_list_body(T *x2, const T *__restrict__ x, const uint32_t *__restrict__ l0, unsigned c0,
+                                const uint32_t *__restrict__ l1, unsigned c1, uint32_t nx2, uint32_t nxny2, Dims d, unsigned blk)
 {
-    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned t = blk * blockDim.x + threadIdx.x;
     if (t >= c0 + c1) return;
     const uint32_t l2 = (t < c0 ? l0[t] : l1[t - c0]) & BL_IDX;
     const uint32_t k2 = l2 / nxny2, rem = l2 - k2 * nxny2, j2 = rem / nx2, i2 = rem - j2 * nx2;
@@ -1839,6 +1872,13 @@ __global__ void restrict_list_k(T *x2, const T *__restrict__ x, const uint32_t *
     const T C = X(0, 0, -1) + X(0, -1, 0) + X(-1, 0, 0) + X(1, 0, 0) + X(0, 1, 0) + X(0, 0, 1);
 #undef X
     x2[l2] = (T)0.015625 * A + (T)0.03125 * B + (T)0.0625 * C + (T)0.125 * x[l];
+}
+
+template <typename T>
+__global__ void restrict_list_k(T *x2, const T *__restrict__ x, const uint32_t *__restrict__ l0, unsigned c0,
+                                const uint32_t *__restrict__ l1, unsigned c1, uint32_t nx2, uint32_t nxny2, Dims d)
+{
+    restrict_list_body<T>(x2, x, l0, c0, l1, c1, nx2, nxny2, d, blockIdx.x);
 }
 
 // the V-cycle's restriction of level l's residual onto level l + 1
@@ -2097,13 +2137,13 @@ __device__ __forceinline__ T neg_bits(T x)
 
 // true in the last block to finish (all its threads), with the lane-order total
 template <typename T>
-__device__ __forceinline__ bool lane_fold(T *sm, T acc, T *part, unsigned *count, T *tot)
+__device__ __forceinline__ bool lane_fold(T *sm, T acc, T *part, unsigned *count, T *tot, unsigned blk)
 {
     __shared__ bool last;
     const int tid = threadIdx.x;
     const T b = halve_block(sm, tid, acc);
     if (tid == 0) {
-        part[blockIdx.x] = b;
+        part[blk] = b;
         __threadfence();
         last = atomicAdd(count, 1u) == RED_NBLK - 1;
     }
@@ -2221,14 +2261,14 @@ __global__ void pcg_zero_outside_k(const T *__restrict__ a, const T *__restrict_
 // rho = r . q (q widened from the V-cycle's vm first when it runs in another
 // precision); prevrho = old rho; beta = rho / prevrho
 template <typename TP, typename TM>
-__global__ void __launch_bounds__(RED_BLOCK) pcg_rho_k(const TP *__restrict__ r, TP *__restrict__ q,
+__device__ __forceinline__ void pcg_rho_body(const TP *__restrict__ r, TP *__restrict__ q,
                                                        const TM *__restrict__ vm, const uint8_t *__restrict__ sk,
-                                                       Segs sg, size_t n, TP *part, unsigned *count, double *sc)
+                                                       Segs sg, size_t n, TP *part, unsigned *count, double *sc, unsigned blk)
 {
     constexpr bool FM = sizeof(TP) != sizeof(TM);
     __shared__ TP sm[RED_BLOCK];
     const size_t L = RED_LANES;
-    size_t l = (size_t)blockIdx.x * RED_BLOCK + threadIdx.x;
+    size_t l = (size_t)blk * RED_BLOCK + threadIdx.x;
     TP acc = (TP)0;
     if (sg.k) {
         const uint32_t w = (uint32_t)(l >> 5), c = sg.cnt[w];
@@ -2279,7 +2319,7 @@ __global__ void __launch_bounds__(RED_BLOCK) pcg_rho_k(const TP *__restrict__ r,
         acc = pmad<FM>(r[l], b, acc);
     }
     TP tot;
-    if (lane_fold(sm, acc, part, count, &tot) && threadIdx.x == 0) {
+    if (lane_fold(sm, acc, part, count, &tot, blk) && threadIdx.x == 0) {
         sc[S_PREV] = sc[S_RHO];
         sc[S_RHO] = (double)tot;
         sc[S_BETA] = sc[S_RHO] / sc[S_PREV];
@@ -2287,14 +2327,22 @@ __global__ void __launch_bounds__(RED_BLOCK) pcg_rho_k(const TP *__restrict__ r,
     }
 }
 
+template <typename TP, typename TM>
+__global__ void __launch_bounds__(RED_BLOCK) pcg_rho_k(const TP *__restrict__ r, TP *__restrict__ q,
+                                                       const TM *__restrict__ vm, const uint8_t *__restrict__ sk,
+                                                       Segs sg, size_t n, TP *part, unsigned *count, double *sc)
+{
+    pcg_rho_body<TP, TM>(r, q, vm, sk, sg, n, part, count, sc, blockIdx.x);
+}
+
 // p = beta * p, then p = p + 1 * q (with segments: on the lane grid)
 template <typename T, bool FM>
-__global__ void pcg_p_k(T *__restrict__ p, const T *__restrict__ q, const uint8_t *__restrict__ sk, Segs sg,
-                        size_t n, const double *sc)
+__device__ __forceinline__ void pcg_p_body(T *__restrict__ p, const T *__restrict__ q, const uint8_t *__restrict__ sk, Segs sg,
+                        size_t n, const double *sc, unsigned blk, unsigned nblk)
 {
     const T beta = (T)sc[S_BETA];
     if (sg.k) {
-        const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+        const size_t t = (size_t)blk * blockDim.x + threadIdx.x;
         const uint32_t w = (uint32_t)(t >> 5), c = sg.cnt[w];
         for (uint32_t j = 0; j < c; j += 4) {
             size_t e[4];
@@ -2315,8 +2363,15 @@ __global__ void pcg_p_k(T *__restrict__ p, const T *__restrict__ q, const uint8_
         }
         return;
     }
-    for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x)
+    for (size_t l = (size_t)blk * blockDim.x + threadIdx.x; l < n; l += (size_t)nblk * blockDim.x)
         if (pcg_on(sk, l)) p[l] = pmad<FM>(beta, p[l], q[l]);
+}
+
+template <typename T, bool FM>
+__global__ void pcg_p_k(T *__restrict__ p, const T *__restrict__ q, const uint8_t *__restrict__ sk, Segs sg,
+                        size_t n, const double *sc)
+{
+    pcg_p_body<T, FM>(p, q, sk, sg, n, sc, blockIdx.x, gridDim.x);
 }
 
 // q = lapmg(p) on G (interior), then q = -1 * q everywhere; pq = p . q;
@@ -2332,13 +2387,13 @@ __device__ __forceinline__ T pcg_lap(const T *__restrict__ p, size_t l, size_t n
 }
 
 template <typename T, bool FM>
-__global__ void __launch_bounds__(RED_BLOCK) pcg_q_k(T *__restrict__ q, const T *__restrict__ p,
+__device__ __forceinline__ void pcg_q_body(T *__restrict__ q, const T *__restrict__ p,
                                                      const uint8_t *__restrict__ G, const uint8_t *__restrict__ sk,
-                                                     Segs sg, LapC<T> c, Dims d, T *part, unsigned *count, double *sc)
+                                                     Segs sg, LapC<T> c, Dims d, T *part, unsigned *count, double *sc, unsigned blk)
 {
     __shared__ T sm[RED_BLOCK];
     const size_t nx = d.nx, ny = d.ny, nxny = d.nxny(), n = d.n();
-    const size_t t = (size_t)blockIdx.x * RED_BLOCK + threadIdx.x;
+    const size_t t = (size_t)blk * RED_BLOCK + threadIdx.x;
     T acc = (T)0;
     if (sg.k) {
         // sk is G here, whose one-voxel frame is 0: a voxel of G is interior and takes the stencil
@@ -2360,7 +2415,7 @@ __global__ void __launch_bounds__(RED_BLOCK) pcg_q_k(T *__restrict__ q, const T 
             }
         }
         T tot;
-        if (lane_fold(sm, acc, part, count, &tot) && threadIdx.x == 0) {
+        if (lane_fold(sm, acc, part, count, &tot, blk) && threadIdx.x == 0) {
             sc[S_PQ] = (double)tot;
             sc[S_A] = sc[S_RHO] / sc[S_PQ];
             *count = 0;
@@ -2391,26 +2446,34 @@ __global__ void __launch_bounds__(RED_BLOCK) pcg_q_k(T *__restrict__ q, const T 
         k += Lk + ck;
     }
     T tot;
-    if (lane_fold(sm, acc, part, count, &tot) && threadIdx.x == 0) {
+    if (lane_fold(sm, acc, part, count, &tot, blk) && threadIdx.x == 0) {
         sc[S_PQ] = (double)tot;
         sc[S_A] = sc[S_RHO] / sc[S_PQ];
         *count = 0;
     }
 }
 
+template <typename T, bool FM>
+__global__ void __launch_bounds__(RED_BLOCK) pcg_q_k(T *__restrict__ q, const T *__restrict__ p,
+                                                     const uint8_t *__restrict__ G, const uint8_t *__restrict__ sk,
+                                                     Segs sg, LapC<T> c, Dims d, T *part, unsigned *count, double *sc)
+{
+    pcg_q_body<T, FM>(q, p, G, sk, sg, c, d, part, count, sc, blockIdx.x);
+}
+
 // x = x + alpha * p; r = r + (-alpha) * q; ||r|| (and r in the V-cycle's
 // precision for the next cycle when that differs)
 template <typename TP, typename TM>
-__global__ void __launch_bounds__(RED_BLOCK) pcg_xr_k(TP *__restrict__ x, const TP *__restrict__ p,
+__device__ __forceinline__ void pcg_xr_body(TP *__restrict__ x, const TP *__restrict__ p,
                                                       TP *__restrict__ r, const TP *__restrict__ q,
                                                       TM *__restrict__ rm, const uint8_t *__restrict__ sk, Segs sg,
-                                                      size_t n, TP *part, unsigned *count, double *sc)
+                                                      size_t n, TP *part, unsigned *count, double *sc, unsigned blk)
 {
     constexpr bool FM = sizeof(TP) != sizeof(TM);
     __shared__ TP sm[RED_BLOCK];
     const TP a = (TP)sc[S_A], na = (TP)(-sc[S_A]);
     const size_t L = RED_LANES;
-    size_t l = (size_t)blockIdx.x * RED_BLOCK + threadIdx.x;
+    size_t l = (size_t)blk * RED_BLOCK + threadIdx.x;
     TP acc = (TP)0;
     if (sg.k) {
         const uint32_t w = (uint32_t)(l >> 5), c = sg.cnt[w];
@@ -2473,10 +2536,19 @@ __global__ void __launch_bounds__(RED_BLOCK) pcg_xr_k(TP *__restrict__ x, const 
         acc = pmad<FM>(rn, rn, acc);
     }
     TP tot;
-    if (lane_fold(sm, acc, part, count, &tot) && threadIdx.x == 0) {
+    if (lane_fold(sm, acc, part, count, &tot, blk) && threadIdx.x == 0) {
         sc[S_RES] = sizeof(TP) == 4 ? (double)sqrtf((float)tot) : sqrt((double)tot);
         *count = 0;
     }
+}
+
+template <typename TP, typename TM>
+__global__ void __launch_bounds__(RED_BLOCK) pcg_xr_k(TP *__restrict__ x, const TP *__restrict__ p,
+                                                      TP *__restrict__ r, const TP *__restrict__ q,
+                                                      TM *__restrict__ rm, const uint8_t *__restrict__ sk, Segs sg,
+                                                      size_t n, TP *part, unsigned *count, double *sc)
+{
+    pcg_xr_body<TP, TM>(x, p, r, q, rm, sk, sg, n, part, count, sc, blockIdx.x);
 }
 
 // Which coarsest-level solver ran and its outer iterations (after the stream
@@ -2504,117 +2576,657 @@ static qsm_status coarse_report(qsm_ctx *ctx, const Hier<T> &H, qsm_mg_info *inf
 // PCG (mx_pcg, mgpcg_mex.c:126-216).  TP = PCG precision, TM = V-cycle
 // precision.  With TP == TM the V-cycle's level-0 v/f are the PCG q/r (as in
 // the reference); with TM = float they are FP32 copies converted per call.
+// A solve's state between iterations: pcg_setup runs everything before the
+// loop, pcg_launch_iter enqueues one iteration (no host read), pcg_read_res
+// reads its residual norm, pcg_finish writes the solution and frees the
+// state.  pcg runs them in order; packed solves (pcg_pack_iter) advance
+// several states per launch.
 template <typename TP, typename TM>
-static qsm_status pcg(qsm_ctx *ctx, const Dims &d, const TP *v0, const TP *f, const uint8_t *mask, const double *h,
-                      double tolcg, int32_t maxitcg, double tolmg, int32_t maxitmg, int32_t mu, int32_t npre,
-                      int32_t npost, int32_t nb, int32_t nl, int32_t verbose, TP *vout, qsm_mg_info *info)
-{
-    Range nvtx_range("mgpcg");
-    const Dims dp{d.nx + 2, d.ny + 2, d.nz + 2};
-    const size_t n = dp.n();
+struct PcgState {
+    Dims d{}, dp{};
+    size_t n = 0;
     Hier<TM> H;
-    QSM_TRY(hier_init<TM>(ctx, H, nl, dp, h));
-    H.v0_zero_outside = true;  // the preconditioner starts from v = 0 every time
-    constexpr bool same = sizeof(TP) == sizeof(TM);
-    // PCG vectors: x, p (and r, q when the V-cycle runs in another precision)
     void *pv = nullptr;
+    TP *x = nullptr, *p = nullptr, *r = nullptr, *q = nullptr;
+    double *sc = nullptr;
+    TP *part = nullptr;         // RED_NBLK lane-order block sums of the fused steps
+    unsigned *count = nullptr;  // their last-block counter
+    const uint8_t *sk = nullptr;
+    Segs sg{nullptr, nullptr};
+    LapC<TP> lc{};
+    double res = 0.0, reltol = 0.0;
+    int32_t it = 0, maxitcg = 0;
+    double tolmg = 0.0;
+    int32_t maxitmg = 0, mu = 1, npre = 1, npost = 1, nb = 0;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    bool done() const { return it >= maxitcg || res <= reltol; }
+};
+
+template <typename TP, typename TM>
+static qsm_status pcg_setup(qsm_ctx *ctx, PcgState<TP, TM> &S, const Dims &d, const TP *v0, const TP *f,
+                            const uint8_t *mask, const double *h, double tolcg, int32_t maxitcg, double tolmg,
+                            int32_t maxitmg, int32_t mu, int32_t npre, int32_t npost, int32_t nb, int32_t nl)
+{
+    constexpr bool same = sizeof(TP) == sizeof(TM);
+    S.d = d;
+    S.dp = Dims{d.nx + 2, d.ny + 2, d.nz + 2};
+    const size_t n = S.n = S.dp.n();
+    S.maxitcg = maxitcg;
+    S.tolmg = tolmg;
+    S.maxitmg = maxitmg;
+    S.mu = mu;
+    S.npre = npre;
+    S.npost = npost;
+    S.nb = nb;
+    Hier<TM> &H = S.H;
+    QSM_TRY(hier_init<TM>(ctx, H, nl, S.dp, h));
+    H.v0_zero_outside = true;  // the preconditioner starts from v = 0 every time
+    // PCG vectors: x, p (and r, q when the V-cycle runs in another precision), scalars,
+    // the fused steps' block sums and counter, and the lane-grid segment lists of the
+    // masked steps (built below when that form runs)
     const size_t vb = al256(n * sizeof(TP)), scb = al256(S_N * sizeof(double) + 256);
-    // + the lane-grid segment lists of the masked steps (built below when that form runs)
-    QSM_TRY(dalloc(ctx, &pv, (same ? 2 : 4) * vb + scb + al256(seg_entries(n) * sizeof(uint32_t)) +
-                                 SEG_NW * sizeof(uint32_t)));
-    QSM_CUDA(cudaMemsetAsync(pv, 0, (same ? 2 : 4) * vb + scb, ctx->stream));
-    TP *x = (TP *)pv, *p = (TP *)((char *)pv + vb);
-    TP *r = same ? (TP *)H.L[0].f : (TP *)((char *)pv + 2 * vb);
-    TP *q = same ? (TP *)H.L[0].v : (TP *)((char *)pv + 3 * vb);
-    double *sc = (double *)((char *)pv + (same ? 2 : 4) * vb);
+    const size_t pb = al256(RED_NBLK * sizeof(TP)) + 256;
+    const size_t zb = (same ? 2 : 4) * vb + scb + pb;
+    QSM_TRY(dalloc(ctx, &S.pv, zb + al256(seg_entries(n) * sizeof(uint32_t)) + SEG_NW * sizeof(uint32_t)));
+    QSM_CUDA(cudaMemsetAsync(S.pv, 0, zb, ctx->stream));
+    char *pv = (char *)S.pv;
+    TP *x = S.x = (TP *)pv;
+    S.p = (TP *)(pv + vb);
+    TP *r = S.r = same ? (TP *)H.L[0].f : (TP *)(pv + 2 * vb);
+    TP *q = S.q = same ? (TP *)H.L[0].v : (TP *)(pv + 3 * vb);
+    double *sc = S.sc = (double *)(pv + (same ? 2 : 4) * vb);
+    S.part = (TP *)(pv + (same ? 2 : 4) * vb + scb);
+    S.count = (unsigned *)(pv + (same ? 2 : 4) * vb + scb + al256(RED_NBLK * sizeof(TP)));
 
     QSM_TRY(pad_mask(ctx, H.L[0].G, mask, d));
     QSM_TRY(hier_masks<TM>(ctx, H, false));
     if (v0) QSM_TRY(pad<TP>(ctx, x, v0, d));
     QSM_TRY(pad<TP>(ctx, r, f, d));
 
-    cudaEvent_t e0, e1;
-    QSM_CUDA(cudaEventCreate(&e0));
-    QSM_CUDA(cudaEventCreate(&e1));
-    QSM_CUDA(cudaEventRecord(e0, ctx->stream));
+    QSM_CUDA(cudaEventCreate(&S.e0));
+    QSM_CUDA(cudaEventCreate(&S.e1));
+    QSM_CUDA(cudaEventRecord(S.e0, ctx->stream));
     QSM_CUDA(cudaMemsetAsync(sc, 0, S_N * sizeof(double), ctx->stream));
     // rho = 1 initially (mgpcg_mex.c:135-138)
     const double one = 1.0;
     QSM_CUDA(cudaMemcpyAsync(sc + S_RHO, &one, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-    double res;
     QSM_TRY(nrm2<TP>(ctx, r, n, sc + S_RES));
-    QSM_TRY(read_double(ctx, sc + S_RES, &res));
-    const double reltol = tolcg * res;
+    QSM_TRY(read_double(ctx, sc + S_RES, &S.res));
+    S.reltol = tolcg * S.res;
     QSM_CUDA(cudaMemsetAsync(q, 0, n * sizeof(TP), ctx->stream));
-    QSM_TRY(lapmg<TP>(ctx, q, x, H.L[0].G, h, dp));
+    QSM_TRY(lapmg<TP>(ctx, q, x, H.L[0].G, h, S.dp));
     QSM_TRY(scal<TP>(ctx, q, n, sc, -1, false, -1.0));
     QSM_TRY(axpy<TP>(ctx, r, q, n, sc, -1, false, -1.0));
     // The PCG steps skip the voxels outside G when the residual and the iterate are +0
     // there (f +-0 outside G becomes +0 in r = f - A x0, as -0 + +0 is +0).
-    int *zflag = (int *)((char *)pv + (same ? 2 : 4) * vb + S_N * sizeof(double));
+    int *zflag = (int *)(pv + (same ? 2 : 4) * vb + S_N * sizeof(double));
     pcg_zero_outside_k<TP><<<1216, 256, 0, ctx->stream>>>(r, x, H.L[0].G, n, zflag);
     QSM_CUDA(cudaGetLastError());
     QSM_TRY(nrm2<TP>(ctx, r, n, sc + S_RES));
-    QSM_TRY(read_double(ctx, sc + S_RES, &res));
+    QSM_TRY(read_double(ctx, sc + S_RES, &S.res));
     int hz = 1;
     QSM_CUDA(cudaMemcpyAsync(&hz, zflag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     QSM_CUDA(cudaStreamSynchronize(ctx->stream));
-    const uint8_t *sk = hz ? nullptr : H.L[0].G;
-    Segs sg{nullptr, nullptr};
-    if (sk) {
-        uint32_t *segk = (uint32_t *)((char *)pv + (same ? 2 : 4) * vb + scb);
+    S.sk = hz ? nullptr : H.L[0].G;
+    if (S.sk) {
+        uint32_t *segk = (uint32_t *)(pv + zb);
         uint32_t *segcnt = (uint32_t *)((char *)segk + al256(seg_entries(n) * sizeof(uint32_t)));
-        pcg_segs_k<<<RED_NBLK, RED_BLOCK, 0, ctx->stream>>>(sk, n, segk, segcnt);
+        pcg_segs_k<<<RED_NBLK, RED_BLOCK, 0, ctx->stream>>>(S.sk, n, segk, segcnt);
         QSM_CUDA(cudaGetLastError());
-        sg = Segs{segk, segcnt};
+        S.sg = Segs{segk, segcnt};
     }
-    if (verbose) printf("\niter%6s\tresidual\n", "");
-    int32_t it = 0;
-    TP *part = (TP *)ctx->red_partial;
-    const LapC<TP> lc = lap_consts<TP>(h);
+    S.lc = lap_consts<TP>(h);
     // the V-cycle's right-hand side in its own precision; pcg_xr_k refreshes it
     if (!same) cvt_k<TM, TP><<<1216, 256, 0, ctx->stream>>>(H.L[0].f, r, n);
-    for (int32_t i = 0; i < maxitcg; ++i) {
-        if (res <= reltol) break;
-        if (same)
-            QSM_CUDA(cudaMemsetAsync(q, 0, n * sizeof(TP), ctx->stream));
-        else
-            QSM_CUDA(cudaMemsetAsync(H.L[0].v, 0, n * sizeof(TM), ctx->stream));
-        {
-            Range cyc("mgpcg/preconditioner");
-            QSM_TRY(mg_run<TM>(ctx, H, tolmg, maxitmg, mu, npre, npost, nb, sc, nullptr));
-        }
-        pcg_rho_k<TP, TM><<<RED_NBLK, RED_BLOCK, 0, ctx->stream>>>(r, q, same ? nullptr : H.L[0].v, sk, sg, n,
-                                                                   part, ctx->red_count, sc);
-        // with segments pcg_p_k runs on the lane grid
-        pcg_p_k<TP, !same><<<sg.k ? RED_NBLK : 1216, RED_BLOCK, 0, ctx->stream>>>(p, q, sk, sg, n, sc);
-        pcg_q_k<TP, !same><<<RED_NBLK, RED_BLOCK, 0, ctx->stream>>>(q, p, H.L[0].G, sk, sg, lc, dp, part,
-                                                                    ctx->red_count, sc);
-        pcg_xr_k<TP, TM><<<RED_NBLK, RED_BLOCK, 0, ctx->stream>>>(x, p, r, q, same ? nullptr : H.L[0].f, sk, sg, n,
-                                                                  part, ctx->red_count, sc);
-        QSM_CUDA(cudaGetLastError());
-        QSM_TRY(read_double(ctx, sc + S_RES, &res));
-        if (info && info->resnorm_hist) info->resnorm_hist[i] = res;
-        it += 1;
-        if (verbose) printf("%5d/%d\t%1.3e\n", i, maxitcg, res);
+    QSM_CUDA(cudaGetLastError());
+    return QSM_OK;
+}
+
+template <typename TP, typename TM>
+static qsm_status pcg_launch_iter(qsm_ctx *ctx, PcgState<TP, TM> &S)
+{
+    constexpr bool same = sizeof(TP) == sizeof(TM);
+    Hier<TM> &H = S.H;
+    const size_t n = S.n;
+    if (same)
+        QSM_CUDA(cudaMemsetAsync(S.q, 0, n * sizeof(TP), ctx->stream));
+    else
+        QSM_CUDA(cudaMemsetAsync(H.L[0].v, 0, n * sizeof(TM), ctx->stream));
+    {
+        Range cyc("mgpcg/preconditioner");
+        QSM_TRY(mg_run<TM>(ctx, H, S.tolmg, S.maxitmg, S.mu, S.npre, S.npost, S.nb, S.sc, nullptr));
     }
-    if (verbose) printf("\n");
-    QSM_CUDA(cudaEventRecord(e1, ctx->stream));
-    QSM_TRY(unpad<TP>(ctx, vout, x, d));
+    pcg_rho_k<TP, TM><<<RED_NBLK, RED_BLOCK, 0, ctx->stream>>>(S.r, S.q, same ? nullptr : H.L[0].v, S.sk, S.sg, n,
+                                                               S.part, S.count, S.sc);
+    // with segments pcg_p_k runs on the lane grid
+    pcg_p_k<TP, !same><<<S.sg.k ? RED_NBLK : 1216, RED_BLOCK, 0, ctx->stream>>>(S.p, S.q, S.sk, S.sg, n, S.sc);
+    pcg_q_k<TP, !same><<<RED_NBLK, RED_BLOCK, 0, ctx->stream>>>(S.q, S.p, H.L[0].G, S.sk, S.sg, S.lc, S.dp, S.part,
+                                                                S.count, S.sc);
+    pcg_xr_k<TP, TM><<<RED_NBLK, RED_BLOCK, 0, ctx->stream>>>(S.x, S.p, S.r, S.q, same ? nullptr : H.L[0].f, S.sk,
+                                                              S.sg, n, S.part, S.count, S.sc);
+    QSM_CUDA(cudaGetLastError());
+    return QSM_OK;
+}
+
+template <typename TP, typename TM>
+static qsm_status pcg_read_res(qsm_ctx *ctx, PcgState<TP, TM> &S)
+{
+    QSM_TRY(read_double(ctx, S.sc + S_RES, &S.res));
+    S.it += 1;
+    return QSM_OK;
+}
+
+// Writes the solution (vout: unpadded, device) and the statistics and frees the state.
+template <typename TP, typename TM>
+static qsm_status pcg_finish(qsm_ctx *ctx, PcgState<TP, TM> &S, TP *vout, qsm_mg_info *info)
+{
+    if (S.e1) QSM_CUDA(cudaEventRecord(S.e1, ctx->stream));
+    if (vout) QSM_TRY(unpad<TP>(ctx, vout, S.x, S.d));
     QSM_CUDA(cudaStreamSynchronize(ctx->stream));
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, e0, e1);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    if (S.e0 && S.e1) cudaEventElapsedTime(&ms, S.e0, S.e1);
+    if (S.e0) cudaEventDestroy(S.e0);
+    if (S.e1) cudaEventDestroy(S.e1);
+    S.e0 = S.e1 = nullptr;
     if (info) {
-        info->iters = it;
-        info->resnorm = res;
+        info->iters = S.it;
+        info->resnorm = S.res;
         info->seconds = ms * 1e-3;
     }
-    const qsm_status rep = coarse_report(ctx, H, info);  // a timed-out solve still frees its state
-    QSM_TRY(dfree(ctx, pv));
-    QSM_TRY(hier_free(ctx, H));
+    const qsm_status rep = coarse_report(ctx, S.H, info);  // a timed-out solve still frees its state
+    if (S.pv) QSM_TRY(dfree(ctx, S.pv));
+    S.pv = nullptr;
+    QSM_TRY(hier_free(ctx, S.H));
     return rep;
+}
+
+template <typename TP, typename TM>
+static qsm_status pcg(qsm_ctx *ctx, const Dims &d, const TP *v0, const TP *f, const uint8_t *mask, const double *h,
+                      double tolcg, int32_t maxitcg, double tolmg, int32_t maxitmg, int32_t mu, int32_t npre,
+                      int32_t npost, int32_t nb, int32_t nl, int32_t verbose, TP *vout, qsm_mg_info *info)
+{
+    Range nvtx_range("mgpcg");
+    PcgState<TP, TM> S;
+    QSM_TRY(pcg_setup(ctx, S, d, v0, f, mask, h, tolcg, maxitcg, tolmg, maxitmg, mu, npre, npost, nb, nl));
+    if (verbose) printf("\niter%6s\tresidual\n", "");
+    while (!S.done()) {
+        QSM_TRY(pcg_launch_iter(ctx, S));
+        QSM_TRY(pcg_read_res(ctx, S));
+        if (info && info->resnorm_hist) info->resnorm_hist[S.it - 1] = S.res;
+        if (verbose) printf("%5d/%d\t%1.3e\n", S.it - 1, maxitcg, S.res);
+    }
+    if (verbose) printf("\n");
+    return pcg_finish(ctx, S, vout, info);
+}
+
+// ---------------------------------------------------------------------------
+// Packed PCG solves (qsm_mgpcg_batch and session steps): up to MV_MAX solves
+// with the same multigrid options advance together, one PCG iteration at a
+// time, each kernel of the iteration launched once for all of them.  A
+// packed launch's descriptor set (one kernel parameter) gives each solve its
+// arrays, lists and block range; the bodies are those of the one-solve
+// kernels, so every solve's result is its solve alone bit for bit:
+// colour passes, residuals, restrictions and corrections from the levels'
+// voxel lists (any order within a pass or a level gives the same bits),
+// the coarsest level on one CTA per solve (the one-CTA solver, whose
+// results the cluster and whole-GPU solvers reproduce), and the four PCG
+// steps on one lane grid per solve with its own block sums.
+// ---------------------------------------------------------------------------
+constexpr int MV_MAX = 16;
+
+template <typename T>
+struct MvGs {  // one solve's share of a packed colour pass
+    T *v;
+    const T *f;
+    const uint32_t *list;
+    unsigned cnt, blk0, nblk;
+    uint32_t skip;
+    GsC<T> c;
+    size_t nx, nxny;
+};
+template <typename T>
+struct MvGsSet {
+    MvGs<T> m[MV_MAX];
+    int n;
+};
+
+template <typename T>
+struct MvLev {  // one solve's level l (residual, restriction onto l + 1, correction from l + 1)
+    T *v, *f, *r, *v2, *f2;
+    const uint32_t *l0, *l1, *c0l, *c1l;  // level l's and level l+1's G lists
+    unsigned n0, n1, m0, m1, blk0, nblk;
+    LapC<T> c;
+    uint32_t nx, nxny, nx2, nxny2;
+    Dims d;
+};
+template <typename T>
+struct MvLevSet {
+    MvLev<T> m[MV_MAX];
+    int n;
+};
+
+template <typename T>
+struct MvCs {  // one solve's coarsest level (CTA blockIdx.x)
+    T *v, *r;
+    const T *f;
+    const uint8_t *G;
+    Dims d;
+    GsC<T> gc;
+    LapC<T> lc;
+    double tol;
+    int *outer;
+};
+template <typename T>
+struct MvCsSet {
+    MvCs<T> m[MV_MAX];
+    int n;
+};
+
+template <typename TP, typename TM>
+struct MvPcg {  // one solve's PCG vectors and scratch (blocks k RED_NBLK .. (k + 1) RED_NBLK - 1)
+    TP *x, *p, *r, *q, *part;
+    TM *vm, *rm;  // the V-cycle's level-0 v and f in its precision (null when they are q and r)
+    const uint8_t *sk, *G;
+    Segs sg;
+    unsigned *count;
+    double *sc;
+    size_t n;
+    LapC<TP> lc;
+    Dims dp;
+};
+template <typename TP, typename TM>
+struct MvPcgSet {
+    MvPcg<TP, TM> m[MV_MAX];
+    int n;
+};
+
+// the solve that owns this block of a list launch: blk0 <= blockIdx.x < blk0 + nblk
+template <typename D>
+__device__ __forceinline__ const D &mv_of(const D *m, int n)
+{
+    int k = 0;
+    for (int q = 1; q < n; ++q)
+        if (m[q].blk0 <= blockIdx.x) k = q;
+    return m[k];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) gs_pack_k(const __grid_constant__ MvGsSet<T> P)
+{
+    const MvGs<T> &m = mv_of(P.m, P.n);
+    gs_list_ilp_body<T>(m.v, m.f, m.list, m.cnt, m.skip, m.c, m.nx, m.nxny, blockIdx.x - m.blk0, m.nblk);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) residual_pack_k(const __grid_constant__ MvLevSet<T> P)
+{
+    const MvLev<T> &m = mv_of(P.m, P.n);
+    residual_list_ilp_body<T>(m.r, m.f, m.v, m.l0, m.n0, m.l1, m.n1, m.c, m.nx, m.nxny, blockIdx.x - m.blk0,
+                              m.nblk);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) restrict_pack_k(const __grid_constant__ MvLevSet<T> P)
+{
+    const MvLev<T> &m = mv_of(P.m, P.n);
+    restrict_list_body<T>(m.f2, m.r, m.c0l, m.m0, m.c1l, m.m1, m.nx2, m.nxny2, m.d, blockIdx.x - m.blk0);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) correct_pack_k(const __grid_constant__ MvLevSet<T> P)
+{
+    const MvLev<T> &m = mv_of(P.m, P.n);
+    correct_list_body<T>(m.v, m.v2, m.l0, m.n0, m.l1, m.n1, m.nx, m.nxny, m.nx2, m.nxny2, blockIdx.x - m.blk0,
+                         m.nblk);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(CS_THREADS) coarse_pack_k(const __grid_constant__ MvCsSet<T> P)
+{
+    const MvCs<T> &m = P.m[blockIdx.x];
+    coarse_solve_body<T>(m.v, m.f, m.G, m.r, m.d, m.gc, m.lc, m.tol, m.outer);
+}
+
+template <typename TP, typename TM>
+__global__ void __launch_bounds__(RED_BLOCK) pcg_rho_pack_k(const __grid_constant__ MvPcgSet<TP, TM> P)
+{
+    const MvPcg<TP, TM> &m = P.m[blockIdx.x / RED_NBLK];
+    pcg_rho_body<TP, TM>(m.r, m.q, m.vm, m.sk, m.sg, m.n, m.part, m.count, m.sc, blockIdx.x % RED_NBLK);
+}
+
+template <typename TP, typename TM>
+__global__ void __launch_bounds__(RED_BLOCK) pcg_p_pack_k(const __grid_constant__ MvPcgSet<TP, TM> P)
+{
+    const MvPcg<TP, TM> &m = P.m[blockIdx.x / RED_NBLK];
+    pcg_p_body<TP, sizeof(TP) != sizeof(TM)>(m.p, m.q, m.sk, m.sg, m.n, m.sc, blockIdx.x % RED_NBLK, RED_NBLK);
+}
+
+template <typename TP, typename TM>
+__global__ void __launch_bounds__(RED_BLOCK) pcg_q_pack_k(const __grid_constant__ MvPcgSet<TP, TM> P)
+{
+    const MvPcg<TP, TM> &m = P.m[blockIdx.x / RED_NBLK];
+    pcg_q_body<TP, sizeof(TP) != sizeof(TM)>(m.q, m.p, m.G, m.sk, m.sg, m.lc, m.dp, m.part, m.count, m.sc,
+                                             blockIdx.x % RED_NBLK);
+}
+
+template <typename TP, typename TM>
+__global__ void __launch_bounds__(RED_BLOCK) pcg_xr_pack_k(const __grid_constant__ MvPcgSet<TP, TM> P)
+{
+    const MvPcg<TP, TM> &m = P.m[blockIdx.x / RED_NBLK];
+    pcg_xr_body<TP, TM>(m.x, m.p, m.r, m.q, m.rm, m.sk, m.sg, m.n, m.part, m.count, m.sc, blockIdx.x % RED_NBLK);
+}
+
+static unsigned blocks_for(unsigned entries, unsigned per_block) { return (entries + per_block - 1) / per_block; }
+
+// `iter` sweeps of one kind of list (G or the band B) on level l of every solve
+template <typename T>
+static qsm_status pack_sweeps(qsm_ctx *ctx, Hier<T> *const *H, int ns, int l, bool band, int32_t iter, bool rev)
+{
+    if (iter <= 0) return QSM_OK;
+    for (int32_t s = 0; s < iter; ++s)
+        for (int pass = 0; pass < 2; ++pass) {
+            MvGsSet<T> P;
+            P.n = 0;
+            unsigned blk = 0;
+            for (int k = 0; k < ns; ++k) {
+                const Level<T> &L = H[k]->L[l];
+                if (L.d.nx < 3 || L.d.ny < 3 || L.d.nz < 3) continue;
+                const int par = (rev ? (int)((L.d.nx + 1) & 1) : 0) ^ pass;
+                const unsigned cnt = band ? L.bn[par] : L.gn[par];
+                if (!cnt) continue;
+                MvGs<T> &m = P.m[P.n++];
+                m.v = L.v;
+                m.f = L.f;
+                m.list = band ? L.bl[par] : L.gl[par];
+                m.cnt = cnt;
+                m.skip = pass ? (rev ? BL_INX2 : BL_I1) : 0u;
+                m.c = gs_consts<T>(L.h);
+                m.nx = L.d.nx;
+                m.nxny = L.d.nxny();
+                m.blk0 = blk;
+                m.nblk = blocks_for(cnt, 256 * GS_PER);
+                blk += m.nblk;
+            }
+            if (!P.n) continue;
+            gs_pack_k<T><<<blk, 256, 0, ctx->stream>>>(P);
+        }
+    QSM_CUDA(cudaGetLastError());
+    return QSM_OK;
+}
+
+enum { MV_RESIDUAL, MV_RESTRICT, MV_CORRECT };
+
+// the residual of level l, its restriction onto level l + 1, or level l's correction from l + 1
+template <typename T>
+static qsm_status pack_level(qsm_ctx *ctx, Hier<T> *const *H, int ns, int l, int what)
+{
+    MvLevSet<T> P;
+    P.n = 0;
+    unsigned blk = 0;
+    for (int k = 0; k < ns; ++k) {
+        Level<T> &L = H[k]->L[l];
+        Level<T> &C = H[k]->L[l + 1];
+        if (L.d.nx < 3 || L.d.ny < 3 || L.d.nz < 3) continue;
+        if (what != MV_RESIDUAL && (C.d.nx < 3 || C.d.ny < 3 || C.d.nz < 3)) continue;
+        const unsigned nf = L.gn[0] + L.gn[1], nc = C.gn[0] + C.gn[1];
+        const unsigned work = what == MV_RESTRICT ? nc : nf;
+        if (!work) continue;
+        MvLev<T> &m = P.m[P.n++];
+        m.v = L.v;
+        m.f = L.f;
+        m.r = L.r;
+        m.v2 = C.v;
+        m.f2 = C.f;
+        m.l0 = L.gl[0];
+        m.l1 = L.gl[1];
+        m.n0 = L.gn[0];
+        m.n1 = L.gn[1];
+        m.c0l = C.gl[0];
+        m.c1l = C.gl[1];
+        m.m0 = C.gn[0];
+        m.m1 = C.gn[1];
+        m.c = lap_consts<T>(L.h);
+        m.nx = (uint32_t)L.d.nx;
+        m.nxny = (uint32_t)L.d.nxny();
+        m.nx2 = (uint32_t)C.d.nx;
+        m.nxny2 = (uint32_t)C.d.nxny();
+        m.d = L.d;
+        m.blk0 = blk;
+        m.nblk = blocks_for(work, what == MV_RESTRICT ? 256 : 256 * GS_PER);
+        blk += m.nblk;
+    }
+    if (!P.n) return QSM_OK;
+    if (what == MV_RESIDUAL)
+        residual_pack_k<T><<<blk, 256, 0, ctx->stream>>>(P);
+    else if (what == MV_RESTRICT)
+        restrict_pack_k<T><<<blk, 256, 0, ctx->stream>>>(P);
+    else
+        correct_pack_k<T><<<blk, 256, 0, ctx->stream>>>(P);
+    QSM_CUDA(cudaGetLastError());
+    return QSM_OK;
+}
+
+// The packed coarsest solve's dynamic shared-memory limit (as coarse_smem_limit).
+template <typename T>
+static qsm_status coarse_pack_smem_limit(qsm_ctx *ctx, size_t *lim)
+{
+    static std::mutex mu;
+    static std::set<int> done;
+    *lim = 0;
+    int maxsm = 0;
+    cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, coarse_pack_k<T>) != cudaSuccess || (size_t)maxsm <= fa.sharedSizeBytes) {
+        cudaGetLastError();
+        return QSM_OK;
+    }
+    const size_t l = (size_t)maxsm - fa.sharedSizeBytes;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!done.count(ctx->device)) {
+        QSM_CUDA(cudaFuncSetAttribute(coarse_pack_k<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)l));
+        done.insert(ctx->device);
+    }
+    *lim = l;
+    return QSM_OK;
+}
+
+template <typename T>
+static qsm_status pack_coarse(qsm_ctx *ctx, Hier<T> *const *H, int ns, int l)
+{
+    MvCsSet<T> P;
+    P.n = 0;
+    size_t smem = 0;
+    for (int k = 0; k < ns; ++k) {
+        Level<T> &L = H[k]->L[l];
+        MvCs<T> &m = P.m[P.n++];
+        m.v = L.v;
+        m.r = L.r;
+        m.f = L.f;
+        m.G = L.G;
+        m.d = L.d;
+        m.gc = gs_consts<T>(L.h);
+        m.lc = lap_consts<T>(L.h);
+        m.tol = sizeof(T) == 4 ? 1e-4 : 1e-8;
+        m.outer = H[k]->counters;
+        smem = std::max(smem, H[k]->coarse_smem);
+    }
+    if (!P.n) return QSM_OK;
+    coarse_pack_k<T><<<(unsigned)P.n, CS_THREADS, smem, ctx->stream>>>(P);
+    QSM_CUDA(cudaGetLastError());
+    return QSM_OK;
+}
+
+// The V-cycle (cycle) on level l of every solve
+template <typename T>
+static qsm_status cycle_pack(qsm_ctx *ctx, Hier<T> *const *H, int ns, int l, int mu, int pre, int post, int nb)
+{
+    const int nl = H[0]->nl;
+    if (l < nl - 1) {
+        const int32_t bs = (1 << l) * nb;
+        QSM_TRY(pack_sweeps<T>(ctx, H, ns, l, false, pre, true));
+        QSM_TRY(pack_sweeps<T>(ctx, H, ns, l, true, bs, true));
+        QSM_TRY(pack_level<T>(ctx, H, ns, l, MV_RESIDUAL));
+        QSM_TRY(pack_level<T>(ctx, H, ns, l, MV_RESTRICT));
+        for (int k = 0; k < ns; ++k)
+            QSM_CUDA(cudaMemsetAsync(H[k]->L[l + 1].v, 0, H[k]->L[l + 1].n * sizeof(T), ctx->stream));
+        for (int i = 0; i < mu; ++i) {
+            QSM_TRY(cycle_pack<T>(ctx, H, ns, l + 1, mu, pre, post, nb));
+            if (l + 1 == nl - 1) break;
+        }
+        QSM_TRY(pack_level<T>(ctx, H, ns, l, MV_CORRECT));
+        QSM_TRY(pack_sweeps<T>(ctx, H, ns, l, true, bs, false));
+        QSM_TRY(pack_sweeps<T>(ctx, H, ns, l, false, post, false));
+        return QSM_OK;
+    }
+    return pack_coarse<T>(ctx, H, ns, l);
+}
+
+// Whether a set-up solve can run packed: fixed V-cycle count (tolmg <= 0), voxel lists on
+// every level, and a coarsest grid one CTA holds.
+template <typename TP, typename TM>
+static bool pcg_packable(qsm_ctx *ctx, const PcgState<TP, TM> &S)
+{
+    if (S.tolmg > 0.0) return false;
+    for (int i = 0; i < S.H.nl; ++i)
+        if (!S.H.L[i].gl[0] || !S.H.L[i].bl[0]) return false;
+    size_t lim = 0;
+    if (coarse_pack_smem_limit<TM>(ctx, &lim) != QSM_OK || lim == 0) return false;
+    const Level<TM> &C = S.H.L[S.H.nl - 1];
+    return S.H.coarse_smem <= lim && C.n < (1u << 18);
+}
+
+// Packed solves must agree on the options that shape an iteration's launches.
+template <typename TP, typename TM>
+static bool pcg_same_shape(const PcgState<TP, TM> &a, const PcgState<TP, TM> &b)
+{
+    return a.H.nl == b.H.nl && a.mu == b.mu && a.npre == b.npre && a.npost == b.npost && a.nb == b.nb &&
+           a.maxitmg == b.maxitmg;
+}
+
+// One PCG iteration of ns (<= MV_MAX) packable solves of one shape that are not done;
+// their residual norms are read back (h_res: ns pinned doubles).
+template <typename TP, typename TM>
+static qsm_status pcg_pack_iter(qsm_ctx *ctx, PcgState<TP, TM> *const *S, int ns, double *h_res)
+{
+    constexpr bool same = sizeof(TP) == sizeof(TM);
+    if (ns <= 0) return QSM_OK;
+    if (ns > MV_MAX) return QSM_ERR_ARG;
+    Range nvtx_range("mgpcg/packed iteration");
+    Hier<TM> *H[MV_MAX];
+    for (int k = 0; k < ns; ++k) {
+        H[k] = &S[k]->H;
+        if (same)
+            QSM_CUDA(cudaMemsetAsync(S[k]->q, 0, S[k]->n * sizeof(TP), ctx->stream));
+        else
+            QSM_CUDA(cudaMemsetAsync(H[k]->L[0].v, 0, S[k]->n * sizeof(TM), ctx->stream));
+    }
+    for (int c = 0; c < S[0]->maxitmg; ++c)
+        QSM_TRY(cycle_pack<TM>(ctx, H, ns, 0, S[0]->mu, S[0]->npre, S[0]->npost, S[0]->nb));
+    MvPcgSet<TP, TM> P;
+    P.n = ns;
+    for (int k = 0; k < ns; ++k) {
+        PcgState<TP, TM> &s = *S[k];
+        MvPcg<TP, TM> &m = P.m[k];
+        m.x = s.x;
+        m.p = s.p;
+        m.r = s.r;
+        m.q = s.q;
+        m.part = s.part;
+        m.vm = same ? nullptr : H[k]->L[0].v;
+        m.rm = same ? nullptr : H[k]->L[0].f;
+        m.sk = s.sk;
+        m.G = H[k]->L[0].G;
+        m.sg = s.sg;
+        m.count = s.count;
+        m.sc = s.sc;
+        m.n = s.n;
+        m.lc = s.lc;
+        m.dp = s.dp;
+    }
+    const unsigned grid = (unsigned)ns * RED_NBLK;
+    pcg_rho_pack_k<TP, TM><<<grid, RED_BLOCK, 0, ctx->stream>>>(P);
+    pcg_p_pack_k<TP, TM><<<grid, RED_BLOCK, 0, ctx->stream>>>(P);
+    pcg_q_pack_k<TP, TM><<<grid, RED_BLOCK, 0, ctx->stream>>>(P);
+    pcg_xr_pack_k<TP, TM><<<grid, RED_BLOCK, 0, ctx->stream>>>(P);
+    QSM_CUDA(cudaGetLastError());
+    for (int k = 0; k < ns; ++k)
+        QSM_CUDA(cudaMemcpyAsync(h_res + k, S[k]->sc + S_RES, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (int k = 0; k < ns; ++k) {
+        S[k]->res = h_res[k];
+        S[k]->it += 1;
+    }
+    return QSM_OK;
+}
+
+// count solves with shared options: set up in groups of MV_MAX, the packable ones of a group
+// advanced together (pcg_pack_iter), any other one by itself; then each finished.
+template <typename TM>
+static qsm_status mgpcg_batch_t(qsm_ctx *ctx, uint32_t count, const Dims *d, const double *const *v0,
+                                const double *const *f, const uint8_t *const *mask, const double *h, double tolcg,
+                                int32_t maxitcg, double tolmg, int32_t maxitmg, int32_t mu, int32_t npre,
+                                int32_t npost, int32_t nb, int32_t nl, double *const *out, qsm_mg_info *info,
+                                double *h_res)
+{
+    using St = PcgState<double, TM>;
+    for (uint32_t g0 = 0; g0 < count; g0 += MV_MAX) {
+        const uint32_t g1 = std::min<uint32_t>(count, g0 + MV_MAX);
+        std::vector<std::unique_ptr<St>> st;
+        qsm_status err = QSM_OK;
+        auto release = [&]() {
+            for (auto &sp : st)
+                if (sp && sp->pv) pcg_finish(ctx, *sp, (double *)nullptr, (qsm_mg_info *)nullptr);
+        };
+        std::vector<St *> pack;
+        for (uint32_t b = g0; b < g1 && err == QSM_OK; ++b) {
+            st.emplace_back(new St());
+            St &S = *st.back();
+            err = pcg_setup(ctx, S, d[b], v0 ? v0[b] : nullptr, f[b], mask[b], h, tolcg, maxitcg, tolmg, maxitmg,
+                            mu, npre, npost, nb, nl);
+            if (err != QSM_OK) break;
+            if (pcg_packable(ctx, S) && (pack.empty() || pcg_same_shape(*pack[0], S))) {
+                // the one-CTA form reports its coarsest solver as such
+                S.H.cc_ctas = 0;
+                S.H.cg_ctas = 0;
+                pack.push_back(&S);
+                continue;
+            }
+            while (err == QSM_OK && !S.done()) {
+                err = pcg_launch_iter(ctx, S);
+                if (err == QSM_OK) err = pcg_read_res(ctx, S);
+                if (err == QSM_OK && info && info[b].resnorm_hist) info[b].resnorm_hist[S.it - 1] = S.res;
+            }
+        }
+        while (err == QSM_OK) {
+            St *act[MV_MAX];
+            int na = 0;
+            for (St *sp : pack)
+                if (!sp->done()) act[na++] = sp;
+            if (!na) break;
+            err = pcg_pack_iter(ctx, act, na, h_res);
+            if (err == QSM_OK && info)
+                for (int k = 0; k < na; ++k) {
+                    const uint32_t b = g0 + (uint32_t)(std::find_if(st.begin(), st.end(),
+                                                                    [&](const std::unique_ptr<St> &u) {
+                                                                        return u.get() == act[k];
+                                                                    }) - st.begin());
+                    if (info[b].resnorm_hist) info[b].resnorm_hist[act[k]->it - 1] = act[k]->res;
+                }
+        }
+        if (err != QSM_OK) {
+            release();
+            return err;
+        }
+        for (uint32_t b = g0; b < g1; ++b) {
+            const qsm_status fs = pcg_finish(ctx, *st[b - g0], out[b], info ? info + b : nullptr);
+            if (fs != QSM_OK && err == QSM_OK) err = fs;
+        }
+        if (err != QSM_OK) {
+            release();
+            return err;
+        }
+    }
+    return QSM_OK;
 }
 
 template <typename T>
@@ -3066,6 +3678,55 @@ qsm_status qsm_mgpcg_mixed(qsm_ctx *ctx, const size_t dims[3], const double *v0,
     QSM_TRY(stage_out(ctx, sf, false));
     QSM_TRY(stage_out(ctx, sm, false));
     QSM_TRY(stage_out(ctx, so, s == QSM_OK));
+    QSM_CUDA(cudaStreamSynchronize(ctx->stream));
+    return s;
+}
+
+qsm_status qsm_mgpcg_batch(qsm_ctx *ctx, int32_t mixed, uint32_t count, const size_t *dims, const double *const *v0,
+                           const double *const *f, const uint8_t *const *mask, const double vsz[3], double tolcg,
+                           int32_t maxitcg, double tolmg, int32_t maxitmg, int32_t mu, int32_t npre, int32_t npost,
+                           int32_t nboundary, int32_t nlevels, double *const *v_out, qsm_mg_info *info)
+{
+    if (!ctx || !dims || !f || !mask || !vsz || !v_out) return QSM_ERR_ARG;
+    if (count == 0) return QSM_OK;
+    for (uint32_t b = 0; b < count; ++b) {
+        if (!f[b] || !mask[b] || !v_out[b]) return QSM_ERR_ARG;
+        QSM_TRY(solver_checks(ctx, dims + 3 * b, nlevels));
+    }
+    cudaSetDevice(ctx->device);
+    std::vector<Dims> d(count);
+    std::vector<Staged> s0(count), sf(count), sm(count), so(count);
+    std::vector<const double *> pv0(count, nullptr), pf(count);
+    std::vector<const uint8_t *> pm(count);
+    std::vector<double *> po(count);
+    for (uint32_t b = 0; b < count; ++b) {
+        d[b] = make_dims(dims + 3 * b);
+        const size_t n = d[b].n();
+        if (v0 && v0[b]) {
+            QSM_TRY(stage_in(ctx, s0[b], v0[b], n * 8, true));
+            pv0[b] = (const double *)s0[b].dev;
+        }
+        QSM_TRY(stage_in(ctx, sf[b], f[b], n * 8, true));
+        QSM_TRY(stage_in(ctx, sm[b], mask[b], n, true));
+        QSM_TRY(stage_in(ctx, so[b], v_out[b], n * 8, false));
+        pf[b] = (const double *)sf[b].dev;
+        pm[b] = (const uint8_t *)sm[b].dev;
+        po[b] = (double *)so[b].dev;
+    }
+    double *h_res = nullptr;
+    QSM_CUDA(cudaMallocHost((void **)&h_res, MV_MAX * sizeof(double)));
+    const qsm_status s =
+        mixed ? mgpcg_batch_t<float>(ctx, count, d.data(), pv0.data(), pf.data(), pm.data(), vsz, tolcg, maxitcg, tolmg,
+                                     maxitmg, mu, npre, npost, nboundary, nlevels, po.data(), info, h_res)
+              : mgpcg_batch_t<double>(ctx, count, d.data(), pv0.data(), pf.data(), pm.data(), vsz, tolcg, maxitcg,
+                                      tolmg, maxitmg, mu, npre, npost, nboundary, nlevels, po.data(), info, h_res);
+    cudaFreeHost(h_res);
+    for (uint32_t b = 0; b < count; ++b) {
+        if (v0 && v0[b]) QSM_TRY(stage_out(ctx, s0[b], false));
+        QSM_TRY(stage_out(ctx, sf[b], false));
+        QSM_TRY(stage_out(ctx, sm[b], false));
+        QSM_TRY(stage_out(ctx, so[b], s == QSM_OK));
+    }
     QSM_CUDA(cudaStreamSynchronize(ctx->stream));
     return s;
 }

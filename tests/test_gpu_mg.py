@@ -316,3 +316,45 @@ def test_fp_convert_exact(gpu_ctx, qsm):
     the device's own conversion bits on every float and on 2^30 doubles aimed
     at rounding ties, subnormal and overflowing results."""
     assert qsm.fp_convert_check(ctx=gpu_ctx) == 0
+
+
+@pytest.mark.parametrize("mixed", [True, False])
+def test_mgpcg_batch_bitexact(gpu_ctx, qsm, mixed):
+    """Packed Poisson solves: volumes of different sizes (different
+    hierarchies and iteration counts; one with an initial guess that is -0
+    or nonzero outside the mask, so its PCG steps run over the whole array)
+    advance together, each kernel of a PCG iteration launched once for all.
+    Each result equals the same solve alone bit for bit."""
+    import qsm_gb300.synthetic as S
+
+    shapes = [(40, 36, 34), (58, 50, 44), (33, 61, 29), (70, 40, 52), (96, 88, 80)]
+    cases = [S.poisson_case(sh, 800 + k, semi=(10.0, 30.0))[:2] for k, sh in enumerate(shapes)]
+    fs = [c[0] for c in cases]
+    ms = [c[1] for c in cases]
+    v0s = [None] * len(cases)
+    v0s[1] = np.asfortranarray(0.01 * fs[1] - 0.0)
+    args = ([1, 1, 1], 1e-8, 60, -1.0, 2, 1, 2, 2, 2, 4)
+    infos = []
+    outs = qsm.mgpcg_batch(v0s, fs, ms, *args, mixed=mixed, infos=infos)
+    for b in range(len(cases)):
+        info = {}
+        ref = qsm.mgpcg_mex(v0s[b], fs[b], ms[b], *args, mixed=mixed, info=info)
+        assert infos[b]["iters"] == info["iters"], (b, infos[b], info)
+        assert infos[b]["coarse_ctas"] == 1  # one CTA per solve in the packed launches
+        assert np.array_equal(infos[b]["resnorm_hist"], info["resnorm_hist"])
+        assert bits_equal(outs[b], ref), (b, first_diff(outs[b], ref))
+
+
+def test_mgpcg_batch_groups(gpu_ctx, qsm):
+    """More solves than one packed launch takes (16): 18 small volumes in two
+    groups, each equal to its solve alone."""
+    import qsm_gb300.synthetic as S
+
+    rng = np.random.default_rng(5)
+    shapes = [tuple(int(x) for x in rng.integers(18, 34, 3)) for _ in range(18)]
+    cases = [S.poisson_case(sh, 900 + k, semi=(5.0, 14.0))[:2] for k, sh in enumerate(shapes)]
+    args = ([1, 1, 1], 1e-8, 40, -1.0, 2, 1, 2, 2, 2, 3)
+    outs = qsm.mgpcg_batch(None, [c[0] for c in cases], [c[1] for c in cases], *args, mixed=True)
+    for (f, m), out in zip(cases, outs):
+        ref = qsm.mgpcg_mex(None, f, m, *args, mixed=True)
+        assert bits_equal(out, ref), first_diff(out, ref)
