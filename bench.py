@@ -377,6 +377,7 @@ def poisson_arm(qsm_gb300, ctx, torch, cpu=False):
         out[key] = rec
     out["rel_l2_fp32_vcycle_vs_fp64"] = float(torch.linalg.vector_norm(sols["fp32_vcycle"] - sols["fp64"]) /
                                               torch.linalg.vector_norm(sols["fp64"]))
+    out["packed_16"] = packed_poisson(qsm_gb300, ctx, torch)
     out["speedup_fp32_vcycle"] = out["fp64"]["seconds"] / out["fp32_vcycle"]["seconds"]
     if cpu:
         port = _port()
@@ -393,6 +394,34 @@ def poisson_arm(qsm_gb300, ctx, torch, cpu=False):
         out["speedup_fp64_vs_cpu_oracle"] = s / out["fp64"]["seconds"]
         out["speedup_fp32_vcycle_vs_cpu_oracle"] = s / out["fp32_vcycle"]["seconds"]
     return out
+
+
+def packed_poisson(qsm_gb300, ctx, torch, count=16, lo=96, hi=127):
+    """qsm_mgpcg_batch: `count` seeded Poisson problems of lo..hi voxels per
+    axis with LBV's options and the FP32 V-cycle, packed (each PCG kernel
+    launched once for all), against the same solves one after another;
+    results compared bit for bit."""
+    import qsm_gb300.synthetic as S
+
+    rng = np.random.default_rng(3)
+    shapes = [tuple(int(x) for x in rng.integers(lo, hi + 1, 3)) for _ in range(count)]
+    cases = [S.poisson_case(sh, 50 + k, semi=(lo * 0.3, lo * 0.45))[:2] for k, sh in enumerate(shapes)]
+    fs = [torch.from_numpy(np.ascontiguousarray(f.transpose(2, 1, 0))).cuda() for f, _ in cases]
+    ms = [torch.from_numpy(np.ascontiguousarray(m.transpose(2, 1, 0))).cuda() for _, m in cases]
+    args = ([1, 1, 1], 1e-8, 200, -1.0, 2, 1, 2, 2, 2, 5)
+    qsm_gb300.mgpcg_batch(None, fs, ms, *args, mixed=True, ctx=ctx)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    outs = qsm_gb300.mgpcg_batch(None, fs, ms, *args, mixed=True, ctx=ctx)
+    torch.cuda.synchronize()
+    tp = time.perf_counter() - t
+    t = time.perf_counter()
+    refs = [qsm_gb300.mgpcg_mex(None, f, m, *args, mixed=True, ctx=ctx) for f, m in zip(fs, ms)]
+    torch.cuda.synchronize()
+    ts = time.perf_counter() - t
+    return {"workload": f"{count} Poisson problems {lo}..{hi} per axis (seeded), LBV options, FP32 V-cycle, 5 levels",
+            "packed_s": tp, "one_by_one_s": ts, "speedup": ts / tp,
+            "identical": all(bool(torch.equal(a, b)) for a, b in zip(outs, refs))}
 
 
 def _generate(fn, *cols):
@@ -664,12 +693,13 @@ def next_rows_arm(qsm_gb300, ctx, torch, peak, cpu=True, parts="tv64,tv32,pdf,vs
     return out
 
 
-def serve_arm(qsm_gb300, ctx, seconds=30.0, rate=4.0, per_kind=6, budget=160 * 10**9):
+def serve_arm(qsm_gb300, ctx, seconds=30.0, rate=4.0, per_kind=6, budget=160 * 10**9, poisson_workers=0):
     """Served reconstructions: Poisson arrivals at `rate`/s for `seconds`, 40%
     Poisson (LBV options), 30% TV (lam 1e-3, 500 iterations), 30% TGV (lam
     0.003, alpha 2, 1000 iterations), sizes as the batched configuration, a
     pool of `per_kind` seeded cases per kind, FIFO admission against a
-    160 GB device budget.  Every case is first solved alone (which also tunes
+    160 GB device budget; Poisson solves packed into the session's steps
+    (poisson_workers 0) or run whole on worker threads.  Every case is first solved alone (which also tunes
     its grid size); every served result must equal its case's alone result
     bit for bit.  Errors: FP32 results against the FP64 plain GPU path (bit-
     identical to the FP64 oracle)."""
@@ -702,7 +732,7 @@ def serve_arm(qsm_gb300, ctx, seconds=30.0, rate=4.0, per_kind=6, budget=160 * 1
             alone[(kind, c)] = serve.digest(out)
             err[kind].append(float(np.linalg.norm(out.astype(np.float64) - ref) / max(np.linalg.norm(ref), 1e-300)))
     reqs = serve.arrivals(rate, seconds, seed=4, pool_size=per_kind)
-    with qsm_gb300.Session(budget_bytes=budget, poisson_workers=2, ctx=ctx) as sess:
+    with qsm_gb300.Session(budget_bytes=budget, poisson_workers=poisson_workers, ctx=ctx) as sess:
         loop = serve.ServeLoop(sess, pool)
         recs = loop.run(reqs)
     summ = serve.summarize(recs, seconds)
@@ -711,6 +741,7 @@ def serve_arm(qsm_gb300, ctx, seconds=30.0, rate=4.0, per_kind=6, budget=160 * 1
         "workload": f"Poisson arrivals {rate}/s for {seconds:.0f} s (seed 4), 40% Poisson / 30% TV / 30% TGV, "
                     f"sizes from {{96..256}}x{{96..256}}x{{64..176}}, {per_kind} seeded cases per kind, "
                     f"budget {budget / 1e9:.0f} GB",
+        "poisson_mode": ("packed into the session steps" if poisson_workers == 0 else f"{poisson_workers} worker threads"),
         "arrived": len(reqs), "rejected": len(loop.rejected), "budget_refusals": loop.refusals,
         "max_resident": loop.max_resident, "max_queue": loop.max_queue, "steps": loop.steps,
         "same_alone_vs_mix": not mism, "mismatches": mism[:10],
@@ -781,7 +812,8 @@ def run_ours(args):
             out = poisson_arm(qsm_gb300, ctx, torch, cpu=not args.no_cpu and rank == 0)
         elif args.only == "serve":
             out = serve_arm(qsm_gb300, ctx, seconds=args.serve_seconds, rate=args.serve_rate,
-                                per_kind=args.serve_pool, budget=int(args.serve_budget_gb * 1e9))
+                                per_kind=args.serve_pool, budget=int(args.serve_budget_gb * 1e9),
+                                poisson_workers=args.serve_poisson_workers)
         else:
             out = next_rows_arm(qsm_gb300, ctx, torch, _peaks()[0], cpu=not args.no_cpu, parts=args.next_parts)
         if rank == 0:
@@ -878,7 +910,8 @@ def run_ours(args):
     poisson = None if args.no_poisson else poisson_arm(qsm_gb300, ctx, torch, cpu=cpu_rank0)
     batch = None if args.no_batch else batch_arm(qsm_gb300, ctx, torch, cpu=cpu_rank0)
     served = None if args.no_serve else serve_arm(qsm_gb300, ctx, seconds=args.serve_seconds, rate=args.serve_rate,
-                                per_kind=args.serve_pool, budget=int(args.serve_budget_gb * 1e9))
+                                per_kind=args.serve_pool, budget=int(args.serve_budget_gb * 1e9),
+                                poisson_workers=args.serve_poisson_workers)
     nxt = None if args.no_next else next_rows_arm(qsm_gb300, ctx, torch, peak, cpu=not args.no_cpu and rank == 0)
 
     if rank != 0:
@@ -946,6 +979,8 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=4.0, help="arrivals per second of the served arm")
     ap.add_argument("--serve-pool", type=int, default=6, help="seeded input cases per request kind (served arm)")
     ap.add_argument("--serve-budget-gb", type=float, default=160.0, help="device byte budget of the served arm")
+    ap.add_argument("--serve-poisson-workers", type=int, default=0,
+                    help="served arm: 0 packs Poisson solves into the session steps, N > 0 runs them on N threads")
     ap.add_argument("--shape", default="", help="nx,ny,nz of a reduced volume (profiler captures)")
     ap.add_argument("--iters", type=int, default=ITERS, help="iterations per inversion (profiler captures)")
     ap.add_argument("--only", default="all", choices=["all", "fused", "batch", "serve", "next", "poisson"],

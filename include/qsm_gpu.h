@@ -364,9 +364,13 @@ qsm_status qsm_pd_tgv_batch(qsm_ctx *ctx, qsm_dtype dtype, uint32_t count, const
 
 /* A session holds admitted solves resident in device memory until their
  * results are fetched.  Primal-dual solves advance together in
- * qsm_session_step (the batched launches above); Poisson solves run whole on
- * `poisson_workers` host threads, each with its own stream, concurrently
- * with the steps.  Admission: a submit whose footprint
+ * qsm_session_step (the batched launches above).  Poisson solves: with
+ * poisson_workers = 0 they stay resident too and advance in the same steps,
+ * packed as in qsm_mgpcg_batch, on a stream of their own beside the replays:
+ * at least one PCG iteration per 30 primal-dual iterations, and more while
+ * the step's replays are still running; with
+ * poisson_workers > 0 each runs whole on one of that many host threads, each
+ * with its own stream, concurrently with the steps.  Admission: a submit whose footprint
  * (qsm_session_footprint) does not fit in budget_bytes minus the bytes in
  * use fails with QSM_ERR_BUSY and changes nothing (budget 0 = no limit).
  * A session is driven from one host thread. */
@@ -393,15 +397,18 @@ qsm_status qsm_session_submit_pd(qsm_session *session, int32_t tgv, qsm_dtype dt
                                  const double vsz[3], double lam, double alpha, double tol,
                                  uint32_t maxiter, uint64_t *id);
 /* Admits an mgpcg_mex solve (FP64 arrays; v0 may be NULL for zeros; mixed
- * selects the FP32 V-cycle).  It runs on the next free Poisson worker. */
+ * selects the FP32 V-cycle).  It runs on the next free Poisson worker, or,
+ * without workers, is set up before the call returns and advances in the
+ * steps. */
 qsm_status qsm_session_submit_mgpcg(qsm_session *session, const size_t dims[3], const double *v0,
                                     const double *f, const uint8_t *mask, const double vsz[3],
                                     double tolcg, int32_t maxitcg, double tolmg, int32_t maxitmg,
                                     int32_t mu, int32_t npre, int32_t npost, int32_t nboundary,
                                     int32_t nlevels, int32_t mixed, uint64_t *id);
 /* Advances every running primal-dual solve by `iters` iterations (rounded up
- * to a multiple of 30; solves stop at their own maxiter or tolerance) and
- * returns when they are done. */
+ * to a multiple of 30; solves stop at their own maxiter or tolerance), and
+ * every resident Poisson solve by at least one PCG iteration per 30 of them
+ * (more while they run), and returns when they are done. */
 qsm_status qsm_session_step(qsm_session *session, uint32_t iters);
 /* *finished = 1 once the job's result can be fetched.  pd_info / mg_info
  * (either may be NULL) receive the job's statistics. */

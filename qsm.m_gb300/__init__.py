@@ -687,8 +687,11 @@ def footprint(kind: str, dims, nlevels: int = 5) -> int:
 class Session:
     """Resident solves on one GPU (qsm_session_* in include/qsm_gpu.h).
 
-    Primal-dual solves advance together in :meth:`step`; Poisson solves run
-    on ``poisson_workers`` worker streams concurrently.  A submit that does
+    Primal-dual solves advance together in :meth:`step`.  Poisson solves run
+    on ``poisson_workers`` worker streams concurrently, or, with
+    ``poisson_workers=0``, stay resident and advance in :meth:`step` (packed
+    launches; at least one PCG iteration per 30 primal-dual iterations, more
+    while the step's replays run).  A submit that does
     not fit in ``budget_bytes`` raises :class:`QsmError` with status
     QSM_ERR_BUSY and leaves the session unchanged.
     """
@@ -700,6 +703,7 @@ class Session:
                                              ctypes.byref(h)), "qsm_session_create")
         self.handle = h
         self._meta = {}
+        self.poisson_workers = int(poisson_workers)  # 0: Poisson solves advance in step()
 
     def _check(self, st, name):
         if st != 0:

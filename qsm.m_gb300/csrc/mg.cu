@@ -38,6 +38,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "mg_pack.cuh"
 
 namespace qsm {
 
@@ -3227,6 +3228,91 @@ static qsm_status mgpcg_batch_t(qsm_ctx *ctx, uint32_t count, const Dims *d, con
         }
     }
     return QSM_OK;
+}
+
+// Session interface (mg_pack.cuh): a solve is one PcgState in the precision
+// its V-cycle asks for.
+struct MgPackSolve {
+    bool mixed = true, packable = false;
+    PcgState<double, float> sm;
+    PcgState<double, double> sd;
+};
+
+qsm_status mgpack_setup(qsm_ctx *ctx, bool mixed, const Dims &d, const double *v0, const double *f,
+                        const uint8_t *mask, const double vsz[3], double tolcg, int32_t maxitcg, double tolmg,
+                        int32_t maxitmg, int32_t mu, int32_t npre, int32_t npost, int32_t nb, int32_t nl,
+                        MgPackSolve **out)
+{
+    *out = nullptr;
+    std::unique_ptr<MgPackSolve> p(new MgPackSolve());
+    p->mixed = mixed;
+    qsm_status st;
+    if (mixed) {
+        st = pcg_setup(ctx, p->sm, d, v0, f, mask, vsz, tolcg, maxitcg, tolmg, maxitmg, mu, npre, npost, nb, nl);
+        if (st == QSM_OK) p->packable = pcg_packable(ctx, p->sm);
+        if (p->packable) p->sm.H.cc_ctas = p->sm.H.cg_ctas = 0;
+    } else {
+        st = pcg_setup(ctx, p->sd, d, v0, f, mask, vsz, tolcg, maxitcg, tolmg, maxitmg, mu, npre, npost, nb, nl);
+        if (st == QSM_OK) p->packable = pcg_packable(ctx, p->sd);
+        if (p->packable) p->sd.H.cc_ctas = p->sd.H.cg_ctas = 0;
+    }
+    if (st != QSM_OK) {
+        if (p->sm.pv) pcg_finish(ctx, p->sm, (double *)nullptr, (qsm_mg_info *)nullptr);
+        if (p->sd.pv) pcg_finish(ctx, p->sd, (double *)nullptr, (qsm_mg_info *)nullptr);
+        return st;
+    }
+    *out = p.release();
+    return QSM_OK;
+}
+
+bool mgpack_done(const MgPackSolve *s) { return s->mixed ? s->sm.done() : s->sd.done(); }
+
+template <typename TM>
+static qsm_status mgpack_step_t(qsm_ctx *ctx, std::vector<PcgState<double, TM> *> &todo, double *h_res)
+{
+    while (!todo.empty()) {
+        PcgState<double, TM> *grp[MV_MAX];
+        int ng = 0;
+        std::vector<PcgState<double, TM> *> rest;
+        for (auto *sp : todo)
+            if (ng < MV_MAX && (ng == 0 || pcg_same_shape(*grp[0], *sp)))
+                grp[ng++] = sp;
+            else
+                rest.push_back(sp);
+        QSM_TRY(pcg_pack_iter(ctx, grp, ng, h_res));
+        todo.swap(rest);
+    }
+    return QSM_OK;
+}
+
+qsm_status mgpack_step(qsm_ctx *ctx, MgPackSolve *const *s, int n, double *h_res)
+{
+    std::vector<PcgState<double, float> *> pm;
+    std::vector<PcgState<double, double> *> pd;
+    for (int k = 0; k < n; ++k) {
+        MgPackSolve *p = s[k];
+        if (mgpack_done(p)) continue;
+        if (p->packable) {
+            if (p->mixed)
+                pm.push_back(&p->sm);
+            else
+                pd.push_back(&p->sd);
+        } else if (p->mixed) {
+            QSM_TRY(pcg_launch_iter(ctx, p->sm));
+            QSM_TRY(pcg_read_res(ctx, p->sm));
+        } else {
+            QSM_TRY(pcg_launch_iter(ctx, p->sd));
+            QSM_TRY(pcg_read_res(ctx, p->sd));
+        }
+    }
+    QSM_TRY(mgpack_step_t<float>(ctx, pm, h_res));
+    return mgpack_step_t<double>(ctx, pd, h_res);
+}
+
+qsm_status mgpack_finish(qsm_ctx *ctx, MgPackSolve *s, double *vout, qsm_mg_info *info)
+{
+    std::unique_ptr<MgPackSolve> p(s);
+    return p->mixed ? pcg_finish(ctx, p->sm, vout, info) : pcg_finish(ctx, p->sd, vout, info);
 }
 
 template <typename T>

@@ -27,8 +27,13 @@
 //     base (a multiple of 30), so its buffer phase and monitor iterations
 //     are the graph's; a volume whose monitors met tol, or that reached its
 //     maxiter, does nothing in later launches;
-//   * Poisson solves (mgpcg) run whole on worker threads, each with its own
-//     stream and context, concurrently with the primal-dual replays.
+//   * Poisson solves (mgpcg) either stay resident too and advance in the
+//     same steps, every kernel of a PCG iteration launched once for all
+//     solves of one multigrid shape (mg_pack.cuh), on a stream of their own
+//     that runs beside the replays: at least one PCG iteration per 30
+//     primal-dual iterations, and more while the replays run -- or, with
+//     worker threads, run whole on the workers' streams, concurrently with
+//     the replays.
 //
 // Admission is by device footprint against the session's byte budget.
 #include <math.h>
@@ -50,6 +55,7 @@
 #include "pd.cuh"
 #include "pd_fused.cuh"
 #include "pd_tile.cuh"
+#include "mg_pack.cuh"
 
 namespace qsm {
 
@@ -221,6 +227,7 @@ struct MgJob {
     double *v0 = nullptr, *f = nullptr, *out = nullptr;
     uint8_t *mask = nullptr;
     std::atomic<int> state{0};  // 0 queued, 1 running, 2 finished
+    MgPackSolve *ps = nullptr;  // resident solve state (packed sessions)
     qsm_status st = QSM_OK;
     char err[256] = {0};
     qsm_mg_info info{};
@@ -271,6 +278,11 @@ struct qsm_session {
     cudaGraphExec_t exec = nullptr;
     PdCtl *h_ctl = nullptr;  // pinned
     size_t h_ctl_cap = 0;
+
+    // packed Poisson solves: their context (own stream), scratch and the resident solves
+    qsm_ctx *pctx = nullptr;
+    double *h_res = nullptr;  // pinned
+    std::vector<MgJob *> packed;
 
     // Poisson workers
     std::vector<std::thread> workers;
@@ -528,7 +540,7 @@ extern "C" {
 
 qsm_status qsm_session_create(qsm_ctx *ctx, size_t budget_bytes, int32_t poisson_workers, qsm_session **out)
 {
-    if (!ctx || !out || poisson_workers < 0 || poisson_workers > 16) return QSM_ERR_ARG;
+    if (!ctx || !out || poisson_workers < 0 || poisson_workers > 16) return QSM_ERR_ARG;  // 0: packed Poisson solves
     *out = nullptr;
     cudaSetDevice(ctx->device);
     std::unique_ptr<qsm_session> s(new qsm_session());
@@ -582,6 +594,12 @@ qsm_status qsm_session_destroy(qsm_session *s)
     s->cv.notify_all();
     for (auto &t : s->workers) t.join();
     for (auto *wc : s->wctx) qsm_ctx_destroy(wc);
+    if (s->pctx) {
+        for (auto &kv : s->mg)
+            if (kv.second->ps) mgpack_finish(s->pctx, kv.second->ps, nullptr, nullptr);
+        qsm_ctx_destroy(s->pctx);
+    }
+    if (s->h_res) cudaFreeHost(s->h_res);
     qsm_ctx *ctx = s->ctx;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
@@ -676,7 +694,6 @@ qsm_status qsm_session_submit_mgpcg(qsm_session *s, const size_t dims[3], const 
                                     int32_t nboundary, int32_t nlevels, int32_t mixed, uint64_t *id)
 {
     if (!s || !dims || !f || !mask || !vsz || !id) return QSM_ERR_ARG;
-    if (s->workers.empty()) return fail(s, QSM_ERR_ARG, "session has no Poisson workers");
     if (nlevels < 1) return QSM_ERR_ARG;
     if (nlevels > 16) return QSM_ERR_DEPTH;
     qsm_ctx *ctx = s->ctx;
@@ -715,10 +732,29 @@ qsm_status qsm_session_submit_mgpcg(qsm_session *s, const size_t dims[3], const 
     j->mixed = mixed != 0;
     j->has_v0 = v0 != nullptr;
     j->bytes = bytes;
+    if (s->workers.empty()) {
+        // packed: set the solve up now; the steps advance it
+        if (!s->pctx) {
+            QSM_TRY(qsm_ctx_create(ctx->device, &s->pctx));
+            QSM_CUDA(cudaMallocHost((void **)&s->h_res, 16 * sizeof(double)));
+        }
+        const qsm_status st = mgpack_setup(s->pctx, j->mixed, d, j->has_v0 ? j->v0 : nullptr, j->f, j->mask, j->vsz,
+                                           tolcg, maxitcg, tolmg, maxitmg, mu, npre, npost, nboundary, nlevels, &j->ps);
+        if (st != QSM_OK) {
+            set_error(ctx, "%s", qsm_last_error(s->pctx));
+            dfree(ctx, j->blk);
+            return st;
+        }
+        j->state.store(1);
+    }
     *id = j->id;
     s->used += bytes;
     MgJob *raw = j.get();
     s->mg.emplace(j->id, std::move(j));
+    if (raw->ps) {
+        s->packed.push_back(raw);
+        return QSM_OK;
+    }
     {
         std::lock_guard<std::mutex> lock(s->mu);
         s->queue.push_back(raw);
@@ -734,11 +770,41 @@ qsm_status qsm_session_step(qsm_session *s, uint32_t iters)
     qsm_ctx *ctx = s->ctx;
     cudaSetDevice(ctx->device);
     if (s->dirty) QSM_TRY(rebuild(s));
-    if (s->running.empty()) return QSM_OK;
     const uint32_t reps = std::max<uint32_t>(1, (iters + kGraphIters - 1) / kGraphIters);
-    QSM_CUDA(cudaEventRecord(s->ev0, ctx->stream));
-    for (uint32_t r = 0; r < reps; ++r) QSM_CUDA(cudaGraphLaunch(s->exec, ctx->stream));
-    QSM_CUDA(cudaEventRecord(s->ev1, ctx->stream));
+    if (!s->running.empty()) {
+        QSM_CUDA(cudaEventRecord(s->ev0, ctx->stream));
+        for (uint32_t r = 0; r < reps; ++r) QSM_CUDA(cudaGraphLaunch(s->exec, ctx->stream));
+        QSM_CUDA(cudaEventRecord(s->ev1, ctx->stream));
+    }
+    // packed Poisson solves, on their own stream while the replays run: at least one PCG
+    // iteration per 30 primal-dual iterations, and more for as long as the replays have not
+    // finished
+    if (!s->packed.empty()) {
+        std::vector<MgPackSolve *> ps;
+        for (uint32_t r = 0;; ++r) {
+            if (r >= reps && (s->running.empty() || cudaEventQuery(s->ev1) != cudaErrorNotReady)) break;
+            ps.clear();
+            for (MgJob *j : s->packed)
+                if (!mgpack_done(j->ps)) ps.push_back(j->ps);
+            if (ps.empty()) break;
+            const qsm_status st = mgpack_step(s->pctx, ps.data(), (int)ps.size(), s->h_res);
+            if (st != QSM_OK) return fail(s, st, qsm_last_error(s->pctx));
+        }
+        cudaGetLastError();  // a not-ready event query leaves no error behind
+        std::vector<MgJob *> keep;
+        for (MgJob *j : s->packed) {
+            if (!mgpack_done(j->ps)) {
+                keep.push_back(j);
+                continue;
+            }
+            j->st = mgpack_finish(s->pctx, j->ps, j->out, &j->info);
+            j->ps = nullptr;
+            if (j->st != QSM_OK) snprintf(j->err, sizeof j->err, "%s", qsm_last_error(s->pctx));
+            j->state.store(2);
+        }
+        s->packed.swap(keep);
+    }
+    if (s->running.empty()) return QSM_OK;
     s->gbase += reps * kGraphIters;
     const size_t nv = s->running.size();
     if (nv > s->h_ctl_cap) {

@@ -6,9 +6,10 @@ admits the head whenever a slot is free and its device footprint fits in
 the session's byte budget (the session refuses a submit that does not fit
 with QSM_ERR_BUSY and the request waits).  Admitted solves stay resident on
 the device: primal-dual solves advance together in 30-iteration batched
-steps, Poisson solves run on worker streams at the same time, and a request
-that arrives while others are running joins the next step (continuous
-batching).  Finished results are fetched as soon as they are done; latency
+steps; Poisson solves advance in the same steps (packed launches, a session
+without Poisson workers) or run on worker streams at the same time; and a
+request that arrives while others are running joins the next step
+(continuous batching).  Finished results are fetched as soon as they are done; latency
 is arrival to fetched result.
 
 The session is any object with the :class:`qsm_gb300.Session` methods, and
@@ -205,7 +206,9 @@ class ServeLoop:
                 queue.popleft()
                 active[jid] = (r, self.clock() - t0)
             self.max_resident = max(self.max_resident, len(active))
-            pd_running = any(r.kind != "poisson" for r, _ in active.values())
+            # a session without Poisson workers advances its resident Poisson solves in its steps
+            steps_poisson = getattr(self.s, "poisson_workers", 1) == 0
+            pd_running = any(r.kind != "poisson" or steps_poisson for r, _ in active.values())
             if pd_running:
                 self.s.step(self.step_iters)
                 self.steps += 1

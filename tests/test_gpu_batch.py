@@ -190,10 +190,45 @@ def test_session_admission_budget(gpu_ctx, qsm):
         chi = s.fetch(ib)
         with pytest.raises(qsm.QsmError, match="ARG"):
             s.fetch(ib)  # already released
-        with pytest.raises(qsm.QsmError, match="ARG"):
-            s.submit_mgpcg(None, np.zeros((8, 8, 8)), np.ones((8, 8, 8), np.uint8), [1, 1, 1], *MG_ARGS)
     ref = qsm.pd_tv_mex(b[0], b[1], [1, 1, 1], 0.003, 0.0, 30, fused=True)
     assert bits_equal(chi, ref)
+
+
+def test_session_packed_poisson_in_mix(gpu_ctx, qsm):
+    """Packed Poisson solves (no worker threads): solves of different sizes
+    and both V-cycle precisions, admitted at different steps, stay resident
+    and advance one PCG iteration per 30 primal-dual iterations beside a TV
+    solve, each PCG kernel launched once for all solves of one shape.  Each
+    result equals its solve alone bit for bit, and so does the TV solve."""
+    cases = [_poisson(s, 1000 + k) for k, s in enumerate([(40, 36, 34), (58, 50, 44), (33, 61, 29), (70, 40, 52)])]
+    mixed = (True, False, True, True)
+    jb = _case((60, 38, 44), 501)
+    with qsm.Session(poisson_workers=0) as s:
+        ids = [s.submit_mgpcg(None, f, m, [1, 1, 1], *MG_ARGS, mixed=mx) for (f, m), mx in zip(cases[:2], mixed[:2])]
+        ib = s.submit_pd(jb[0], jb[1], [1, 1, 1], 0.003, 0.0, 0.0, 170, tgv=False)
+        s.step(30)
+        ids += [s.submit_mgpcg(None, f, m, [1, 1, 1], *MG_ARGS, mixed=mx) for (f, m), mx in zip(cases[2:], mixed[2:])]
+        steps = 1
+        while s.running():
+            s.step(30)
+            steps += 1
+        infos = []
+        for i in ids:
+            fin, inf = s.poll(i)
+            assert fin
+            infos.append(inf)
+        outs = [s.fetch(i) for i in ids]
+        chib = s.fetch(ib)
+        assert s.bytes_in_use() == 0
+    for (f, m), mx, out, inf in zip(cases, mixed, outs, infos):
+        info = {}
+        ref = qsm.mgpcg_mex(None, f, m, [1, 1, 1], *MG_ARGS, mixed=mx, info=info)
+        assert inf["iters"] == info["iters"]
+        assert bits_equal(out, ref), first_diff(out, ref)
+    # at least one PCG iteration per step (the TV solve needs 6 steps of 30)
+    assert steps <= max(max(i["iters"] for i in infos) + 1, 7)
+    refb = qsm.pd_tv_mex(jb[0], jb[1], [1, 1, 1], 0.003, 0.0, 170, fused=True)
+    assert bits_equal(chib, refb), first_diff(chib, refb)
 
 
 def test_session_concurrent_poisson_sizes(gpu_ctx, qsm):
