@@ -64,7 +64,7 @@ ALG_BYTES_FP32 = 166  # algorithmic bytes per voxel-iteration of fused FP32 TGV
 KERNEL_SOURCES = ("qsm.m_gb300/csrc/pd_tile.cuh", "qsm.m_gb300/csrc/pd_fused.cuh", "qsm.m_gb300/csrc/pd_stream.cu",
                   "qsm.m_gb300/csrc/pd_tma.cuh")
 NCU_TRAFFIC_224x224x128 = {  # (digest, tx, ty, z-chunk) -> bytes per launch
-    ("fc0e0dabdbc5f1b1", 28, 16, 16): 275.6e6,  # median of 5 launches: read 191.1 MB + write 84.5 MB
+    ("2e157d096d22f024", 28, 16, 16): 275.6e6,  # median of 5 launches: read 190.9 MB + write 84.7 MB
 }
 
 

@@ -40,8 +40,10 @@ stream_tma_k(const __grid_constant__ TmaMaps tm, FusedArgs s, DualC<float> dc, P
 size_t stream_smem(int tx, int ty, bool tgv)
 {
     const size_t nt = (size_t)(tx + 4) * (ty + 4);
-    // three exchange planes of (extragradient, dual) and three step barriers (column_pd)
-    const size_t planes = 3 * ((tgv ? 5 : 2) + (tgv ? 10 : 4)) * nt * sizeof(float) + 3 * sizeof(uint64_t);
+    // exchange planes of (extragradient, dual): three and three step barriers for TGV, two
+    // for TV (column_pd)
+    const size_t planes = tgv ? 3 * (5 + 10) * nt * sizeof(float) + 3 * sizeof(uint64_t)
+                              : 2 * (2 + 4) * nt * sizeof(float);
     return std::max(planes, 4 * nt * sizeof(double));
 }
 
