@@ -2841,6 +2841,48 @@ struct MvPcgSet {
     int n;
 };
 
+template <typename T>
+struct MvSw {  // one solve's smoothing call on a thread-block cluster of its own
+    T *v;
+    const T *f;
+    const uint32_t *la, *lb;
+    unsigned ca, cb;
+    uint32_t skipb;
+    GsC<T> c;
+    size_t nx, nxny;
+};
+template <typename T>
+struct MvSwSet {
+    MvSw<T> m[MV_MAX];
+    int n;
+};
+
+__device__ __forceinline__ uint32_t cl_id()
+{
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
+    return r;
+}
+
+// iter sweeps (pass over la, pass over lb skipping skipb) of solve `cluster id`
+// on its cluster: sweeps_cluster_k's body, each cluster on its own solve
+// (clusters never wait for one another)
+template <typename T>
+__global__ void __launch_bounds__(SW_THREADS) sweeps_pack_k(const __grid_constant__ MvSwSet<T> P, int32_t iter)
+{
+    const MvSw<T> &m = P.m[cl_id()];
+    const unsigned stride = cl_size() * SW_THREADS, t0 = cl_rank() * SW_THREADS + threadIdx.x;
+    SwShare<T> a, b;
+    a.load(m.la, m.ca, m.f, t0, stride);
+    b.load(m.lb, m.cb, m.f, t0, stride);
+    for (int32_t s = 0; s < iter; ++s) {
+        a.pass(m.v, 0u, m.c, m.nx, m.nxny);
+        cl_sync();
+        b.pass(m.v, m.skipb, m.c, m.nx, m.nxny);
+        cl_sync();
+    }
+}
+
 // the solve that owns this block of a list launch: blk0 <= blockIdx.x < blk0 + nblk
 template <typename D>
 __device__ __forceinline__ const D &mv_of(const D *m, int n)
@@ -2920,10 +2962,67 @@ __global__ void __launch_bounds__(RED_BLOCK) pcg_xr_pack_k(const __grid_constant
 static unsigned blocks_for(unsigned entries, unsigned per_block) { return (entries + per_block - 1) / per_block; }
 
 // `iter` sweeps of one kind of list (G or the band B) on level l of every solve
+// Clusters of the packed smoothing calls: 8 CTAs (portable), so that 16 solves' clusters
+// are resident at once.
+constexpr int MV_CLUSTER = 8;
+
+// The whole smoothing call on one cluster per solve, where every solve's lists of
+// that kind fit its cluster (as sweeps_cluster's capacity rule); false if not.
+template <typename T>
+static bool pack_sweeps_cluster(qsm_ctx *ctx, Hier<T> *const *H, int ns, int l, bool band, int32_t iter, bool rev,
+                                qsm_status *st)
+{
+    *st = QSM_OK;
+    const unsigned cap = MV_CLUSTER * SW_THREADS * SW_PER;
+    MvSwSet<T> P;
+    P.n = 0;
+    for (int k = 0; k < ns; ++k) {
+        const Level<T> &L = H[k]->L[l];
+        if (L.d.nx < 3 || L.d.ny < 3 || L.d.nz < 3) continue;
+        const int par0 = rev ? (int)((L.d.nx + 1) & 1) : 0;
+        const unsigned *cnt = band ? L.bn : L.gn;
+        uint32_t *const *lists = band ? L.bl : L.gl;
+        const unsigned c = std::max(cnt[0], cnt[1]);
+        if (c > cap || (sizeof(T) == 8 && c > SW_CLUSTER_MAX)) return false;
+        if (!cnt[0] && !cnt[1]) continue;
+        MvSw<T> &m = P.m[P.n++];
+        m.v = L.v;
+        m.f = L.f;
+        m.la = lists[par0];
+        m.ca = cnt[par0];
+        m.lb = lists[par0 ^ 1];
+        m.cb = cnt[par0 ^ 1];
+        m.skipb = rev ? BL_INX2 : BL_I1;
+        m.c = gs_consts<T>(L.h);
+        m.nx = L.d.nx;
+        m.nxny = L.d.nxny();
+    }
+    if (!P.n) return true;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = MV_CLUSTER;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3((unsigned)(P.n * MV_CLUSTER));
+    cfg.blockDim = dim3(SW_THREADS);
+    cfg.stream = ctx->stream;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, sweeps_pack_k<T>, P, iter);
+    if (e != cudaSuccess) {
+        set_error(ctx, "%s", cudaGetErrorString(e));
+        *st = QSM_ERR_CUDA;
+    }
+    return true;
+}
+
 template <typename T>
 static qsm_status pack_sweeps(qsm_ctx *ctx, Hier<T> *const *H, int ns, int l, bool band, int32_t iter, bool rev)
 {
     if (iter <= 0) return QSM_OK;
+    qsm_status cst;
+    if (pack_sweeps_cluster<T>(ctx, H, ns, l, band, iter, rev, &cst)) return cst;
     for (int32_t s = 0; s < iter; ++s)
         for (int pass = 0; pass < 2; ++pass) {
             MvGsSet<T> P;
