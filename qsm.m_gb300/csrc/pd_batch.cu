@@ -48,6 +48,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <chrono>
 #include <thread>
 #include <vector>
 
@@ -279,10 +280,16 @@ struct qsm_session {
     PdCtl *h_ctl = nullptr;  // pinned
     size_t h_ctl_cap = 0;
 
-    // packed Poisson solves: their context (own stream), scratch and the resident solves
-    qsm_ctx *pctx = nullptr;
+    // packed Poisson solves: their context (own stream), scratch and the resident solves;
+    // a set-up thread with a context of its own prepares admitted solves (submits return at
+    // once) and hands them to the steps through `ready`
+    qsm_ctx *pctx = nullptr, *sctx = nullptr;
     double *h_res = nullptr;  // pinned
     std::vector<MgJob *> packed;
+    std::thread setup;
+    std::deque<MgJob *> setup_queue, ready;
+    std::condition_variable ready_cv;  // a solve's set-up finished
+    int setting_up = 0;                 // submitted solves whose set-up has not finished
 
     // Poisson workers
     std::vector<std::thread> workers;
@@ -345,6 +352,38 @@ void worker_main(qsm_session *s, int w)
         j->st = st;
         if (st != QSM_OK) snprintf(j->err, sizeof j->err, "%s", qsm_last_error(ctx));
         j->state.store(2);
+    }
+}
+
+// Sets up admitted Poisson solves of a packed session on its set-up context.
+void setup_main(qsm_session *s)
+{
+    qsm_ctx *ctx = s->sctx;
+    cudaSetDevice(ctx->device);
+    for (;;) {
+        MgJob *j = nullptr;
+        {
+            std::unique_lock<std::mutex> lock(s->mu);
+            s->cv.wait(lock, [&] { return s->stop || !s->setup_queue.empty(); });
+            if (s->stop && s->setup_queue.empty()) return;
+            j = s->setup_queue.front();
+            s->setup_queue.pop_front();
+        }
+        const qsm_status st = mgpack_setup(ctx, j->mixed, j->d, j->has_v0 ? j->v0 : nullptr, j->f, j->mask, j->vsz,
+                                           j->tolcg, j->maxitcg, j->tolmg, j->maxitmg, j->mu, j->npre, j->npost, j->nb,
+                                           j->nl, &j->ps);
+        {
+            std::lock_guard<std::mutex> lock(s->mu);
+            --s->setting_up;
+            if (st != QSM_OK) {
+                j->st = st;
+                snprintf(j->err, sizeof j->err, "%s", qsm_last_error(ctx));
+                j->state.store(2);
+            } else {
+                s->ready.push_back(j);
+            }
+        }
+        s->ready_cv.notify_all();
     }
 }
 
@@ -593,12 +632,16 @@ qsm_status qsm_session_destroy(qsm_session *s)
     }
     s->cv.notify_all();
     for (auto &t : s->workers) t.join();
+    if (s->setup.joinable()) s->setup.join();
     for (auto *wc : s->wctx) qsm_ctx_destroy(wc);
+    if (s->sctx) cudaStreamSynchronize(s->sctx->stream);
     if (s->pctx) {
         for (auto &kv : s->mg)
             if (kv.second->ps) mgpack_finish(s->pctx, kv.second->ps, nullptr, nullptr);
+        cudaStreamSynchronize(s->pctx->stream);
         qsm_ctx_destroy(s->pctx);
     }
+    if (s->sctx) qsm_ctx_destroy(s->sctx);
     if (s->h_res) cudaFreeHost(s->h_res);
     qsm_ctx *ctx = s->ctx;
     cudaSetDevice(ctx->device);
@@ -732,34 +775,32 @@ qsm_status qsm_session_submit_mgpcg(qsm_session *s, const size_t dims[3], const 
     j->mixed = mixed != 0;
     j->has_v0 = v0 != nullptr;
     j->bytes = bytes;
-    if (s->workers.empty()) {
-        // packed: set the solve up now; the steps advance it
-        if (!s->pctx) {
-            QSM_TRY(qsm_ctx_create(ctx->device, &s->pctx));
-            QSM_CUDA(cudaMallocHost((void **)&s->h_res, 16 * sizeof(double)));
-        }
-        const qsm_status st = mgpack_setup(s->pctx, j->mixed, d, j->has_v0 ? j->v0 : nullptr, j->f, j->mask, j->vsz,
-                                           tolcg, maxitcg, tolmg, maxitmg, mu, npre, npost, nboundary, nlevels, &j->ps);
-        if (st != QSM_OK) {
-            set_error(ctx, "%s", qsm_last_error(s->pctx));
-            dfree(ctx, j->blk);
-            return st;
-        }
-        j->state.store(1);
+    const bool packed = s->workers.empty();
+    if (packed && !s->pctx) {
+        // packed: the steps' context, the set-up context and its thread, made on first use
+        QSM_TRY(qsm_ctx_create(ctx->device, &s->pctx));
+        QSM_TRY(qsm_ctx_create(ctx->device, &s->sctx));
+        QSM_CUDA(cudaMallocHost((void **)&s->h_res, 16 * sizeof(double)));
+        s->setup = std::thread(setup_main, s);
     }
     *id = j->id;
     s->used += bytes;
     MgJob *raw = j.get();
     s->mg.emplace(j->id, std::move(j));
-    if (raw->ps) {
-        s->packed.push_back(raw);
+    if (packed) {
+        {
+            std::lock_guard<std::mutex> lock(s->mu);
+            s->setup_queue.push_back(raw);
+            ++s->setting_up;
+        }
+        s->cv.notify_all();
         return QSM_OK;
     }
     {
         std::lock_guard<std::mutex> lock(s->mu);
         s->queue.push_back(raw);
     }
-    s->cv.notify_one();
+    s->cv.notify_all();
     return QSM_OK;
 }
 
@@ -775,6 +816,18 @@ qsm_status qsm_session_step(qsm_session *s, uint32_t iters)
         QSM_CUDA(cudaEventRecord(s->ev0, ctx->stream));
         for (uint32_t r = 0; r < reps; ++r) QSM_CUDA(cudaGraphLaunch(s->exec, ctx->stream));
         QSM_CUDA(cudaEventRecord(s->ev1, ctx->stream));
+    }
+    if (s->pctx) {
+        std::unique_lock<std::mutex> lock(s->mu);
+        // nothing else to advance while solves are being set up: wait for one (briefly)
+        if (s->running.empty() && s->packed.empty() && s->ready.empty() && s->setting_up > 0)
+            s->ready_cv.wait_for(lock, std::chrono::milliseconds(2),
+                                 [&] { return !s->ready.empty() || s->setting_up == 0; });
+        for (MgJob *j : s->ready) {
+            j->state.store(1);
+            s->packed.push_back(j);
+        }
+        s->ready.clear();
     }
     // packed Poisson solves, on their own stream while the replays run: at least one PCG
     // iteration per 30 primal-dual iterations, and more for as long as the replays have not

@@ -358,3 +358,31 @@ def test_mgpcg_batch_groups(gpu_ctx, qsm):
     for (f, m), out in zip(cases, outs):
         ref = qsm.mgpcg_mex(None, f, m, *args, mixed=True)
         assert bits_equal(out, ref), first_diff(out, ref)
+
+
+@pytest.mark.parametrize("dt_mixed", [False, True])
+def test_mgpcg_batch_tiny_grids_vs_oracle(gpu_ctx, qsm, port, dt_mixed):
+    """Packed solves of tiny grids (3 to 9 voxels per axis, odd and even, masks
+    filling the box or touching its faces, a single voxel): FP64 solves
+    against the oracle bit for bit; the FP32 V-cycle ones against their solves
+    alone."""
+    rng = np.random.default_rng(21)
+    shapes = [(3, 3, 3), (4, 5, 3), (7, 6, 9), (8, 8, 8), (9, 4, 6), (5, 9, 7)]
+    fs, ms = [], []
+    for k, sh in enumerate(shapes):
+        f = np.asfortranarray(rng.standard_normal(sh))
+        m = np.ones(sh, np.uint8, order="F") if k % 2 == 0 else np.asfortranarray(
+            (rng.random(sh) > 0.3).astype(np.uint8))
+        if k == 4:
+            m[:] = 0
+            m[2, 1, 3] = 1  # a single voxel
+        fs.append(np.asfortranarray(f * m))
+        ms.append(m)
+    args = ([1, 1, 1], 1e-8, 30, -1.0, 2, 1, 2, 2, 2, 2)
+    outs = qsm.mgpcg_batch(None, fs, ms, *args, mixed=dt_mixed)
+    for f, m, out in zip(fs, ms, outs):
+        if dt_mixed:
+            ref = qsm.mgpcg_mex(None, f, m, *args, mixed=True)
+        else:
+            ref = port.mgpcg_mex(np.zeros_like(f, order="F"), f, m, *args)
+        assert bits_equal(out, ref), (f.shape, first_diff(out, ref))
