@@ -397,9 +397,9 @@ qsm_status qsm_session_submit_pd(qsm_session *session, int32_t tgv, qsm_dtype dt
                                  const double vsz[3], double lam, double alpha, double tol,
                                  uint32_t maxiter, uint64_t *id);
 /* Admits an mgpcg_mex solve (FP64 arrays; v0 may be NULL for zeros; mixed
- * selects the FP32 V-cycle).  It runs on the next free Poisson worker, or,
- * without workers, is set up before the call returns and advances in the
- * steps. */
+ * selects the FP32 V-cycle).  Inputs are copied.  It runs on the next free
+ * Poisson worker, or, without workers, is set up on the session's set-up
+ * thread (the call returns at once) and advances in the steps from then on. */
 qsm_status qsm_session_submit_mgpcg(qsm_session *session, const size_t dims[3], const double *v0,
                                     const double *f, const uint8_t *mask, const double vsz[3],
                                     double tolcg, int32_t maxitcg, double tolmg, int32_t maxitmg,
