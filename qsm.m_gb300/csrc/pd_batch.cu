@@ -365,7 +365,7 @@ void setup_main(qsm_session *s)
         {
             std::unique_lock<std::mutex> lock(s->mu);
             s->cv.wait(lock, [&] { return s->stop || !s->setup_queue.empty(); });
-            if (s->stop && s->setup_queue.empty()) return;
+            if (s->stop) return;  // solves still queued are released with the session
             j = s->setup_queue.front();
             s->setup_queue.pop_front();
         }
