@@ -243,3 +243,23 @@ def test_session_concurrent_poisson_sizes(gpu_ctx, qsm):
     for (f, m), mixed, out in zip(cases, (True, False, True, True), outs):
         ref = qsm.mgpcg_mex(None, f, m, [1, 1, 1], *MG_ARGS, mixed=mixed)
         assert bits_equal(out, ref), first_diff(out, ref)
+
+
+def test_session_packed_destroy_while_resident(gpu_ctx, qsm):
+    """A packed session destroyed with Poisson solves still queued for set-up
+    or resident mid-solve releases them; a new session then solves as
+    before, bit for bit against the solve alone."""
+    cases = [_poisson(s, 1100 + k) for k, s in enumerate([(40, 36, 34), (33, 41, 29), (48, 30, 36)])]
+    with qsm.Session(poisson_workers=0) as s:
+        for f, m in cases:
+            s.submit_mgpcg(None, f, m, [1, 1, 1], *MG_ARGS, mixed=True)
+        s.step(30)
+    f, m = cases[1]
+    with qsm.Session(poisson_workers=0) as s:
+        i = s.submit_mgpcg(None, f, m, [1, 1, 1], *MG_ARGS, mixed=True)
+        while s.running():
+            s.step(30)
+        out = s.fetch(i)
+        assert s.bytes_in_use() == 0
+    ref = qsm.mgpcg_mex(None, f, m, [1, 1, 1], *MG_ARGS, mixed=True)
+    assert bits_equal(out, ref), first_diff(out, ref)
