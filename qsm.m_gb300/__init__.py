@@ -687,16 +687,16 @@ def footprint(kind: str, dims, nlevels: int = 5) -> int:
 class Session:
     """Resident solves on one GPU (qsm_session_* in include/qsm_gpu.h).
 
-    Primal-dual solves advance together in :meth:`step`.  Poisson solves run
-    on ``poisson_workers`` worker streams concurrently, or, with
-    ``poisson_workers=0``, stay resident and advance in :meth:`step` (packed
-    launches; at least one PCG iteration per 30 primal-dual iterations, more
-    while the step's replays run).  A submit that does
+    Primal-dual solves advance together in :meth:`step`.  Poisson solves
+    stay resident and advance in :meth:`step` too (``poisson_workers=0``, the
+    default: packed launches, at least one PCG iteration per 30 primal-dual
+    iterations, more while the step's replays run), or run whole on
+    ``poisson_workers`` worker streams concurrently.  A submit that does
     not fit in ``budget_bytes`` raises :class:`QsmError` with status
     QSM_ERR_BUSY and leaves the session unchanged.
     """
 
-    def __init__(self, budget_bytes: int = 0, poisson_workers: int = 2, *, ctx=None):
+    def __init__(self, budget_bytes: int = 0, poisson_workers: int = 0, *, ctx=None):
         self.ctx = _ctx(ctx)
         h = _lib.SES()
         self._check(lib().qsm_session_create(self.ctx.handle, int(budget_bytes), int(poisson_workers),
