@@ -368,34 +368,125 @@ static qsm_status boundary_mask(qsm_ctx *ctx, uint8_t *B, const uint8_t *G, cons
 
 constexpr uint32_t BL_I1 = 1u << 31, BL_INX2 = 1u << 30, BL_IDX = 0x3FFFFFFFu;
 
-// fill == 0: count the B voxels of each colour into cnt[0..1]; fill == 1:
-// also write them to list0 / list1 at positions taken from cnt (reset first).
-__global__ void blist_k(uint32_t *list0, uint32_t *list1, unsigned *cnt, const uint8_t *__restrict__ B, Dims d,
-                        int fill)
+// The lists are in increasing index order: a pass over one then walks its
+// level row by row, and the rows a warp's neighbours lie in are those the
+// warps before it have just read (on the 256^3 FP32-V-cycle solve this took
+// the solve from 19.7 to 17.9 ms against lists in atomic-append order).  Per
+// x-row segment of 32 voxels (one warp of the interior grid, blockDim.x ==
+// 32) the voxels of each colour are counted (COUNT: segc[p nseg + seg]), the
+// counts are scanned, and each segment writes its voxels at its offset
+// (segc then holds the offsets): the same lists every time, no atomics.
+struct SegLists {
+    uint32_t *l[4];  // B colour 0, B colour 1, G colour 0, G colour 1
+};
+
+template <bool FILL>
+__global__ void blist_seg_k(SegLists out, unsigned *seg, const uint8_t *__restrict__ B, const uint8_t *__restrict__ G,
+                            Dims d, size_t nseg)
 {
     const size_t i = 1 + (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const size_t j = 1 + (size_t)blockIdx.y * blockDim.y + threadIdx.y;
     const size_t k = 1 + (size_t)blockIdx.z * blockDim.z + threadIdx.z;
-    bool on = false;
+    if (j + 1 >= d.ny || k + 1 >= d.nz) return;  // the whole warp (one row)
+    bool onb = false, ong = false;
     int par = 0;
     uint32_t e = 0;
-    if (i + 1 < d.nx && j + 1 < d.ny && k + 1 < d.nz) {
+    if (i + 1 < d.nx) {
         const size_t l = i + d.nx * j + d.nxny() * k;
-        if (B[l]) {
-            on = true;
-            par = (int)((i + j + k) & 1);
-            e = (uint32_t)l | (i == 1 ? BL_I1 : 0u) | (i == d.nx - 2 ? BL_INX2 : 0u);
+        onb = B[l] != 0;
+        ong = G[l] != 0;
+        par = (int)((i + j + k) & 1);
+        e = (uint32_t)l | (i == 1 ? BL_I1 : 0u) | (i == d.nx - 2 ? BL_INX2 : 0u);
+    }
+    const int lane = threadIdx.x;
+    const size_t sg = blockIdx.x + (size_t)gridDim.x * ((j - 1) + (d.ny - 2) * (k - 1));
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const bool on = (q < 2 ? onb : ong) && par == (q & 1);
+        const unsigned m = __ballot_sync(0xffffffffu, on);
+        if (!FILL) {
+            if (lane == 0) seg[q * nseg + sg] = (unsigned)__popc(m);
+        } else if (on) {
+            // seg holds one exclusive scan over the four count arrays: rebase to array q
+            out.l[q][seg[q * nseg + sg] - seg[q * nseg] + __popc(m & ((1u << lane) - 1u))] = e;
         }
     }
-    const int lane = threadIdx.x & 31;  // blockDim.x == 32: a warp is one x row
-    for (int p = 0; p < 2; ++p) {
-        const unsigned m = __ballot_sync(0xffffffffu, on && par == p);
-        if (!m) continue;
-        const int leader = __ffs(m) - 1;
-        unsigned pos = 0;
-        if (lane == leader) pos = atomicAdd(cnt + p, (unsigned)__popc(m));
-        pos = __shfl_sync(0xffffffffu, pos, leader);
-        if (fill && on && par == p) (p ? list1 : list0)[pos + __popc(m & ((1u << lane) - 1u))] = e;
+}
+
+// exclusive scans of unsigned counts: blocks of SCAN_BLK elements scanned on
+// their own (their totals to bs), the totals scanned the same way, then added
+constexpr int SCAN_T = 256, SCAN_PER = 4, SCAN_BLK = SCAN_T * SCAN_PER;
+
+__global__ void __launch_bounds__(SCAN_T) scan_blocks_k(const unsigned *__restrict__ a, unsigned *o, size_t n,
+                                                        unsigned *bs)
+{
+    __shared__ unsigned sh[SCAN_T];
+    const int tid = threadIdx.x;
+    const size_t base = (size_t)blockIdx.x * SCAN_BLK + (size_t)tid * SCAN_PER;
+    unsigned v[SCAN_PER], s = 0;
+#pragma unroll
+    for (int u = 0; u < SCAN_PER; ++u) {
+        v[u] = base + u < n ? a[base + u] : 0u;
+        s += v[u];
+    }
+    sh[tid] = s;
+    __syncthreads();
+    for (int off = 1; off < SCAN_T; off <<= 1) {
+        const unsigned t = tid >= off ? sh[tid - off] : 0u;
+        __syncthreads();
+        sh[tid] += t;
+        __syncthreads();
+    }
+    unsigned run = sh[tid] - s;
+#pragma unroll
+    for (int u = 0; u < SCAN_PER; ++u) {
+        if (base + u < n) o[base + u] = run;
+        run += v[u];
+    }
+    if (bs && tid == SCAN_T - 1) bs[blockIdx.x] = sh[tid];
+}
+
+__global__ void scan_add_k(unsigned *o, size_t n, const unsigned *__restrict__ bo)
+{
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < n) o[e] += bo[e / SCAN_BLK];
+}
+
+// the scratch (unsigned) exclusive_scan needs for n elements
+static size_t scan_scratch(size_t n)
+{
+    size_t t = 0;
+    for (size_t m = n; m > SCAN_BLK;) {
+        const size_t nb = (m + SCAN_BLK - 1) / SCAN_BLK;
+        t += 2 * nb;
+        m = nb;
+    }
+    return t + 16;
+}
+
+static qsm_status exclusive_scan(qsm_ctx *ctx, const unsigned *a, unsigned *o, size_t n, unsigned *tmp)
+{
+    if (n == 0) return QSM_OK;
+    const size_t nb = (n + SCAN_BLK - 1) / SCAN_BLK;
+    scan_blocks_k<<<(unsigned)nb, SCAN_T, 0, ctx->stream>>>(a, o, n, nb > 1 ? tmp : nullptr);
+    QSM_CUDA(cudaGetLastError());
+    if (nb > 1) {
+        unsigned *bo = tmp + nb;  // the block totals' exclusive scan
+        QSM_TRY(exclusive_scan(ctx, tmp, bo, nb, bo + nb));
+        scan_add_k<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(o, n, bo);
+        QSM_CUDA(cudaGetLastError());
+    }
+    return QSM_OK;
+}
+
+// cnt[q] = the entries of list q (B colour 0, 1, G colour 0, 1) from the counts and their scan
+__global__ void blist_total_k(const unsigned *__restrict__ segc, const unsigned *__restrict__ off, size_t nseg,
+                              unsigned *cnt)
+{
+    const int q = threadIdx.x;
+    if (q < 4 && nseg) {
+        const size_t last = (size_t)(q + 1) * nseg - 1;
+        cnt[q] = off[last] + segc[last] - off[(size_t)q * nseg];
     }
 }
 
@@ -1622,12 +1713,26 @@ static qsm_status boundary_lists(qsm_ctx *ctx, Hier<T> &H)
     const int cn = sweeps_cluster_size<T>(ctx);
     unsigned *cnt = (unsigned *)H.counters + 8;  // B: 4i, 4i+1; G: 4i+2, 4i+3 (nl <= 16)
     QSM_CUDA(cudaMemsetAsync(cnt, 0, 4 * H.nl * sizeof(unsigned), ctx->stream));
+    // per level: segment counts of its four lists (B and G, two colours each) and their scan
+    size_t nseg[16] = {0}, tot_seg = 0, max_seg = 0;
     for (int i = 0; i < H.nl; ++i) {
+        const dim3 g = interior_grid3(H.L[i].d);
+        nseg[i] = (g.x && g.y && g.z) ? (size_t)g.x * (H.L[i].d.ny - 2) * (H.L[i].d.nz - 2) : 0;
+        tot_seg += 2 * 2 * nseg[i];
+        max_seg = std::max(max_seg, nseg[i]);
+    }
+    void *segblk = nullptr;
+    const size_t segbytes = (2 * tot_seg + scan_scratch(4 * max_seg)) * sizeof(unsigned);
+    QSM_TRY(dalloc(ctx, &segblk, segbytes));
+    unsigned *segc = (unsigned *)segblk, *segoff = segc + tot_seg, *scan_tmp = segoff + tot_seg;
+    for (size_t i = 0, o = 0; i < (size_t)H.nl; o += 4 * nseg[i], ++i) {
         const Level<T> &L = H.L[i];
+        if (!nseg[i]) continue;
         const dim3 g = interior_grid3(L.d);
-        if (!(g.x && g.y && g.z)) continue;
-        blist_k<<<g, vox_block(), 0, ctx->stream>>>(nullptr, nullptr, cnt + 4 * i, L.B, L.d, 0);
-        blist_k<<<g, vox_block(), 0, ctx->stream>>>(nullptr, nullptr, cnt + 4 * i + 2, L.G, L.d, 0);
+        blist_seg_k<false><<<g, vox_block(), 0, ctx->stream>>>(SegLists{}, segc + o, L.B, L.G, L.d, nseg[i]);
+        QSM_CUDA(cudaGetLastError());
+        QSM_TRY(exclusive_scan(ctx, segc + o, segoff + o, 4 * nseg[i], scan_tmp));
+        blist_total_k<<<1, 32, 0, ctx->stream>>>(segc + o, segoff + o, nseg[i], cnt + 4 * i);
     }
     QSM_CUDA(cudaGetLastError());
     unsigned hc[64];
@@ -1666,15 +1771,15 @@ static qsm_status boundary_lists(qsm_ctx *ctx, Hier<T> &H)
             c += al256((size_t)hc[4 * i + 2 + p] * sizeof(uint32_t));
         }
     }
-    QSM_CUDA(cudaMemsetAsync(cnt, 0, 4 * H.nl * sizeof(unsigned), ctx->stream));
-    for (int i = 0; i < H.nl; ++i) {
+    for (size_t i = 0, o = 0; i < (size_t)H.nl; o += 4 * nseg[i], ++i) {
         const Level<T> &L = H.L[i];
+        if (!nseg[i]) continue;
         const dim3 g = interior_grid3(L.d);
-        if (!(g.x && g.y && g.z)) continue;
-        blist_k<<<g, vox_block(), 0, ctx->stream>>>(L.bl[0], L.bl[1], cnt + 4 * i, L.B, L.d, 1);
-        blist_k<<<g, vox_block(), 0, ctx->stream>>>(L.gl[0], L.gl[1], cnt + 4 * i + 2, L.G, L.d, 1);
+        blist_seg_k<true><<<g, vox_block(), 0, ctx->stream>>>(SegLists{{L.bl[0], L.bl[1], L.gl[0], L.gl[1]}},
+                                                               segoff + o, L.B, L.G, L.d, nseg[i]);
     }
     QSM_CUDA(cudaGetLastError());
+    QSM_TRY(dfree(ctx, segblk));
     plan_coarse_grid<T>(ctx, H);
     return QSM_OK;
 }
