@@ -76,6 +76,34 @@ class FakeSession:
         return len(self.jobs)
 
 
+class PackedFakeSession(FakeSession):
+    """A session without Poisson workers: Poisson jobs advance only in
+    step(), one PCG iteration per step, `poisson_iters` in all."""
+
+    poisson_workers = 0
+
+    def __init__(self, clock, budget, poisson_iters=5, **kw):
+        super().__init__(clock, budget, **kw)
+        self.poisson_iters = poisson_iters
+
+    def submit_mgpcg(self, v, f, mask, vsz, *args, mixed=True):
+        return self._admit("poisson", f.shape, self.poisson_iters, f)
+
+    def step(self, iters):
+        super().step(iters)
+        for j in self.jobs.values():
+            if j["kind"] == "poisson" and j["left"] > 0:
+                j["left"] -= 1
+                j["iters"] += 1
+        self.clock.t += self.step_cost
+
+    def poll(self, jid):
+        j = self.jobs[jid]
+        if j["kind"] == "poisson":
+            return j["left"] <= 0, dict(iters=j["iters"])
+        return super().poll(jid)
+
+
 def _pool():
     rng = np.random.default_rng(0)
     pool = {}
@@ -178,3 +206,31 @@ def test_summarize():
     assert abs(out["p50_ms"] - 505.0) < 1e-6 and abs(out["p99_ms"] - 990.1) < 1e-6
     assert out["tv"]["n"] == 100 and "tgv" not in out
     assert abs(out["throughput_rps"] - 100.0) < 1e-9
+
+
+def test_loop_steps_packed_poisson_without_pd_jobs():
+    """A session without Poisson workers advances its Poisson solves only in
+    its steps: the loop steps whenever anything is resident, so a stream of
+    Poisson requests alone is served (and mixed with primal-dual ones)."""
+    clock = FakeClock()
+    pool = _pool()
+    s = PackedFakeSession(clock, 0, poisson_iters=7)
+    loop = serve.ServeLoop(s, pool, clock=clock, sleep=clock.sleep)
+    reqs = [serve.Request(i, 0.01 * i, "poisson", i % 2) for i in range(10)]
+    recs = loop.run(reqs)
+    assert len(recs) == 10 and all(r.iters == 7 for r in recs)
+    assert loop.steps >= 7 and not s.jobs
+    # mixed with primal-dual requests, every request still retires
+    clock = FakeClock()
+    s = PackedFakeSession(clock, 0, poisson_iters=4)
+    loop = serve.ServeLoop(s, {k: [dict(c) for c in v] for k, v in pool.items()}, clock=clock, sleep=clock.sleep)
+    reqs = serve.arrivals(40.0, 1.0, seed=2, pool_size=2)
+    saved = dict(serve.TV_ARGS), dict(serve.TGV_ARGS)
+    try:
+        serve.TV_ARGS["maxiter"], serve.TGV_ARGS["maxiter"] = 60, 90
+        recs = loop.run(reqs)
+    finally:
+        serve.TV_ARGS.update(saved[0])
+        serve.TGV_ARGS.update(saved[1])
+    assert len(recs) == len(reqs) and not s.jobs
+    assert all(r.iters == 4 for r in recs if r.kind == "poisson")
