@@ -49,3 +49,14 @@ def test_benchmark_operation_count(bench):
     # 12 per padded voxel and 10 per G voxel in the PCG steps, the rest in two V-cycles
     assert 1.0e9 < ops < 1.1e9
     assert bench.mgpcg_fp64_ops(mask, coarse_outer_per_cycle=2) > ops
+
+
+def test_recorded_traffic_matches_the_kernel_sources(bench):
+    """The DRAM traffic bench.py reports for the headline kernel was captured
+    from the current kernel sources: its key carries the digest of the
+    sources without comments, so an edited kernel needs a new capture (the
+    bench would otherwise report traffic null)."""
+    digest = bench.kernel_digest()
+    keys = [k for k in bench.NCU_TRAFFIC_224x224x128 if k[0] == digest]
+    assert keys, f"no ncu traffic recorded for kernel digest {digest}"
+    assert all(150e6 < bench.NCU_TRAFFIC_224x224x128[k] < 600e6 for k in keys)
