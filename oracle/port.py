@@ -21,7 +21,9 @@ import os
 import numpy as np
 
 _DIR = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_DIR, "liborc.so")
+# QSM_ORACLE_LIB: another build of the same sources (the sanitizer build of
+# tests/test_oracle_sanitized.py)
+LIB_PATH = os.environ.get("QSM_ORACLE_LIB") or os.path.join(_DIR, "liborc.so")
 _lib = None
 
 _P = ctypes.c_void_p
